@@ -1,0 +1,307 @@
+"""Benchmark of the batched forward-dynamics hot path on one GB300.
+
+Workload (default): the 32-Ball chain, 65,536 instances, realize(Stage::
+Acceleration) of every instance per step ("body-steps" = body-RHS
+evaluations). The headline value is the mixed-precision form (FP32 spatial
+recursions + compensated refinement, FP64 state); the plain FP64 form is timed
+on the same inputs and reported beside it with the relative udot error.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Timing: W untimed steps, then K steps bracketed by synchronisation, timed with
+CUDA events recorded on the batch's own stream. The working set (state,
+derivatives, per-body scratch) is larger than the 129 MB L2, so no flush is
+needed between steps. ``e2e`` times the same metric through the public C-ABI
+path with host buffers: per step a host->device state upload, the realize and
+a device->host copy of [qdot, udot] and the status words.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--instances", type=int, default=65536)
+    p.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU-baseline sample duration")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return rank, world
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    try:
+        d = json.loads(PEAKS_FILE.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_baseline(w, seconds: float, instances: int):
+    """The oracle (the reference's CPU algorithm restated, compiled -O2) timed
+    on this host's cores over a bounded sample of the same workload."""
+    from oracle import oracle as O
+
+    threads = O.hardware_threads()
+    n = min(instances, w.ninst)
+    sys_of = w.instance_system[:n]
+    y = w.y0[: int(w.y_offsets[n])]
+    off = w.y_offsets[: n + 1]
+    t1 = O.time_realize(w.systems, w.nsys, sys_of, off, y, nreps=1, nthreads=threads)
+    reps = max(1, int(seconds / max(t1, 1e-6)))
+    t = O.time_realize(w.systems, w.nsys, sys_of, off, y, nreps=reps, nthreads=threads)
+    nb = int(w.nbodies()[:n].sum())
+    return {"value": nb * reps / t, "unit": "body-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{n} instances x {reps} realize(Acceleration) passes, {t:.1f} s wall"}
+
+
+# ------------------------------------------------------------------ GPU arm
+def time_resident(b, steps: int, warmup: int):
+    import torch
+
+    stream = torch.cuda.ExternalStream(b.stream)
+    for _ in range(warmup):
+        b.realize_acceleration_async()
+    b.sync()
+    torch.cuda.synchronize()
+    n0 = b.launch_count
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        b.realize_acceleration_async()
+    end.record(stream)
+    end.synchronize()
+    torch.cuda.synchronize()
+    return start.elapsed_time(end) / steps, b.launch_count - n0
+
+
+def time_e2e(b, y0, steps: int, warmup: int):
+    for _ in range(warmup):
+        b.set_state(y0)
+        b.realize_acceleration()
+    t0 = time.perf_counter()
+    n0 = b.launch_count
+    for _ in range(steps):
+        b.set_state(y0)
+        ydot, st = b.realize_acceleration()
+    dt = (time.perf_counter() - t0) / steps
+    return dt * 1e3, b.launch_count - n0, ydot
+
+
+def udot_rel_err(d_mixed, d_64, b):
+    errs = np.empty(b.ninst)
+    for i in range(b.ninst):
+        s = slice(int(b.y_offsets[i] + b.nq[i]), int(b.y_offsets[i + 1]))
+        x, y = d_mixed[s], d_64[s]
+        errs[i] = np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300)
+    return errs
+
+
+def run_ours(args):
+    import torch
+
+    rank, world = _dist()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from simbody_gb300 import Workload, engine_batch
+    from simbody_gb300.build import build_all
+
+    build_all()
+    w = Workload(2, args.instances)
+    nb_total = int(w.nbodies().sum())
+
+    b64, y0 = engine_batch(w, "fp64")
+    bmx, _ = engine_batch(w, "mixed")
+    b64.set_state(y0)
+    bmx.set_state(y0)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        ms_mx, launches = time_resident(bmx, args.steps, args.warmup)
+        ms_64, _ = time_resident(b64, max(3, args.steps // 4), 1)
+    d64, st64 = b64.realize_acceleration()
+    dmx, stmx = bmx.realize_acceleration()
+    err = udot_rel_err(dmx, d64, bmx)
+    ms_e2e, e2e_launches, _ = time_e2e(bmx, y0, max(3, args.steps // 2), 1)
+
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms_mx], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_mx = float(t.item())
+    value = nb_total * world / (ms_mx * 1e-3)
+    value64 = nb_total / (ms_64 * 1e-3)
+    ny_total = b64.ny_total
+    alg_bytes = 2 * ny_total * 8  # read [q,u], write [qdot,udot]
+    peak, peak_kind = _peaks()
+    achieved = alg_bytes / (ms_mx * 1e-3) / 1e9
+    from oracle import oracle as O
+
+    flops_inst = sum(O.count_realize(w.systems, w.y0[w.instance_slice(0)]).values())
+    result = {
+        "metric": "body-steps/sec mixed vs FP64 on 1 GPU at <=1e-5 rel udot err",
+        "value": value,
+        "unit": "body-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_mx,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 recursions + f64 state",
+        "data": "synthetic (seeded: std::mt19937_64(2<<32|i) states, body params from seed 2)",
+        "config": {"workload": "32-Ball chain, 65,536 instances, realize(Stage::Acceleration) per step",
+                   "instances": w.ninst, "bodies_per_instance": 32, "dof_per_instance": 96,
+                   "l2": "working set (state 117 MB + derivatives + per-body scratch) larger than L2; no flush"},
+        "fp64": {"value": value64, "ms_per_step": ms_64, "speedup_mixed_over_fp64": value / value64},
+        "udot_rel_err": {"max": float(err.max()), "p99": float(np.quantile(err, 0.99)), "mean": float(err.mean()),
+                         "definition": "per instance ||udot_mixed - udot_fp64||_2 / ||udot_fp64||_2"},
+        "status_nonzero": int((stmx != 0).sum() + (st64 != 0).sum()),
+        "e2e": {"value": nb_total / (ms_e2e * 1e-3), "unit": "body-steps/s", "ms_per_step": ms_e2e,
+                "h2d_bytes_per_step": ny_total * 8, "d2h_bytes_per_step": ny_total * 8 + 4 * w.ninst},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_kind": peak_kind,
+                     "algorithmic_bytes": "16 B per state element: read [q,u] (f64), write [qdot,udot] (f64)"},
+        "fp_work": {"flops_per_instance_fp64_algorithm": flops_inst,
+                    "achieved_tflops": flops_inst * w.ninst / (ms_mx * 1e-3) / 1e12},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, min(args.instances, 65536))
+    if rank == 0:
+        print(json.dumps(result))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank, world = _dist()
+    if rank != 0:
+        return
+    from simbody_gb300 import Workload
+    from simbody_gb300.build import build_oracle, build_workloads
+
+    build_workloads()
+    build_oracle()
+    from oracle import oracle as O
+
+    w = Workload(2, args.instances)
+    threads = O.hardware_threads()
+    n = w.ninst
+    nb = int(w.nbodies().sum())
+    off = w.y_offsets
+    for _ in range(args.warmup):
+        O.time_realize(w.systems, w.nsys, w.instance_system, off, w.y0, nreps=1, nthreads=threads)
+    times = []
+    for _ in range(args.steps):
+        times.append(O.time_realize(w.systems, w.nsys, w.instance_system, off, w.y0, nreps=1, nthreads=threads))
+    t = float(np.mean(times))
+    v = nb / t
+    print(json.dumps({
+        "impl": "reference",
+        "metric": "body-steps/sec mixed vs FP64 on 1 GPU at <=1e-5 rel udot err",
+        "value": v, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (same seeded inputs as the GPU arm)",
+        "config": {"workload": "32-Ball chain, 65,536 instances, realize(Stage::Acceleration) per step",
+                   "instances": n},
+        "cpu_baseline": {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"the full {n}-instance batch per step, {args.steps} steps"},
+        "e2e": {"value": v, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+if __name__ == "__main__":
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

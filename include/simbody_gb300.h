@@ -1,0 +1,230 @@
+/* simbody_gb300.h -- C ABI of the GB300 batched forward-dynamics engine.
+ *
+ * This is the drop-in boundary for Simbody's O(n) articulated-body hot path:
+ * a batch of states of systems built from SimbodyMatterSubsystem,
+ * MobilizedBody::{Pin, Slider, Universal, Ball, Free}, Force::Gravity,
+ * Force::MobilityLinearSpring / MobilityLinearDamper (and Constraint::Ball loop
+ * closures) is realized through Stage::Acceleration and stepped with a
+ * fixed-step Runge-Kutta-Merson integrator, on one GPU.
+ *
+ * Simbody itself exposes this path only through its C++ class API; each entry
+ * point below names the reference call it replaces (paths are relative to the
+ * Simbody source tree).
+ *
+ * Conventions
+ *   - Every function returns an int status: 0 (SBG_OK) on success, an
+ *     sbg_status code otherwise; sbg_last_error() then holds a message for the
+ *     calling thread. No C++ exception crosses this boundary.
+ *   - The caller owns every host buffer; the library owns all device memory.
+ *   - One CUDA stream per batch. Calls on one batch handle are not re-entrant;
+ *     different handles may be used from different threads.
+ *   - Host state layout is Simbody's State::getY() = [q, u] per instance,
+ *     instances packed back to back in batch order (sbg_batch_layout gives
+ *     the offsets). Derivatives use the same packing: [qdot, udot].
+ */
+#ifndef SIMBODY_GB300_H_
+#define SIMBODY_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SBG_ABI_VERSION 1
+
+typedef enum sbg_status {
+    SBG_OK = 0,
+    SBG_ERR_INVALID = 1,      /* bad argument or ill-formed system */
+    SBG_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    SBG_ERR_NOMEM = 3,        /* device allocation failed */
+    SBG_ERR_BUDGET = 4,       /* request exceeds the configured device budget */
+    SBG_ERR_STATE = 5,        /* call out of order (e.g. no state set yet) */
+    SBG_ERR_UNSUPPORTED = 6,  /* feature outside the supported subset */
+    SBG_ERR_NO_DEVICE = 7     /* no CUDA device / driver */
+} sbg_status;
+
+/* Mobilizer kinds. Coordinates follow Simbody's defaults:
+ *   PIN       nq=1 nu=1  rotation about Fz            (RigidBodyNodeSpec_Pin.h:103-131)
+ *   SLIDER    nq=1 nu=1  translation along Fx         (RigidBodyNodeSpec_Slider.h:100-119)
+ *   UNIVERSAL nq=2 nu=2  body-fixed X then Y          (RigidBodyNodeSpec_Universal.h:124-189)
+ *   BALL      nq=4 nu=3  quaternion, w_FM in F        (RigidBodyNodeSpec_Ball.h:113-214)
+ *   FREE      nq=7 nu=6  [quat, p_FM], [w_FM, v_FM]   (RigidBodyNodeSpec_Free.h:142-219) */
+typedef enum sbg_mobilizer {
+    SBG_PIN = 0,
+    SBG_SLIDER = 1,
+    SBG_UNIVERSAL = 2,
+    SBG_BALL = 3,
+    SBG_FREE = 4
+} sbg_mobilizer;
+
+typedef enum sbg_precision {
+    SBG_PRECISION_FP64 = 0,   /* every recursion in FP64 */
+    SBG_PRECISION_MIXED = 1   /* FP32 spatial recursions, FP64 state accumulation,
+                                 quaternion normalisation and loop-closure solve */
+} sbg_precision;
+
+/* Per-instance status bits written by the kernels (never a device trap). */
+#define SBG_INST_OK                 0
+#define SBG_INST_NONFINITE          1   /* NaN/Inf in a derivative or state */
+#define SBG_INST_SINGULAR_D         2   /* zero pivot in a D = H^T P H inverse */
+#define SBG_INST_PROJECTION_FAILED  4   /* quaternion/constraint projection refused */
+#define SBG_INST_CHOLESKY_FAIL      8   /* G M^-1 G^T not positive definite */
+#define SBG_INST_TIMEOUT           16   /* persistent kernel hit its iteration budget */
+
+/* One mobilized body, numbered 1..nbodies in MobilizedBodyIndex order (Ground
+ * is 0); parent < own index, as Simbody requires
+ * (SimbodyMatterSubsystemRep.cpp:256-330). Transforms are 3x3 row-major
+ * rotation followed by the translation: {R00,R01,R02,R10,...,R22,p0,p1,p2}.
+ * Mass properties are Simbody's MassProperties(mass, com, UnitInertia) about
+ * the body origin Bo, expressed in B (RigidBodyNode.h:1001-1018). */
+typedef struct sbg_body_desc {
+    int32_t parent;
+    int32_t mobilizer;          /* sbg_mobilizer */
+    double  mass;
+    double  com[3];
+    double  unit_inertia[6];    /* xx yy zz xy xz yz */
+    double  X_PF[12];           /* inboard frame F on parent P */
+    double  X_BM[12];           /* outboard frame M on body B */
+} sbg_body_desc;
+
+/* Mobility force elements, applied in array order (Force.cpp:339-351, 434-443).
+ *   kind 0: MobilityLinearSpring(body, MobilizerQIndex which, k=coef, q0)
+ *           f[u(which)] -= k*(q[q(which)] - q0)  -- Simbody reads q[which] but
+ *           writes u[which] (Force.cpp:347-350); reproduced as is.
+ *   kind 1: MobilityLinearDamper(body, MobilizerUIndex which, c=coef)
+ *           f[u(which)] -= c*u[which] */
+typedef struct sbg_mobility_force_desc {
+    int32_t kind;
+    int32_t body;
+    int32_t which;
+    int32_t reserved;
+    double  coef;
+    double  q0;
+} sbg_mobility_force_desc;
+
+/* Constraint::Ball(body1, station1, body2, station2): station points fixed on
+ * two bodies are held coincident (ConstraintImpl.h:1835-1993). */
+typedef struct sbg_ball_constraint_desc {
+    int32_t body1;
+    int32_t body2;
+    double  station1[3];
+    double  station2[3];
+} sbg_ball_constraint_desc;
+
+/* A whole System: matter + Force::Gravity (gravity = g * direction) +
+ * mobility forces + Ball constraints. */
+typedef struct sbg_system_desc {
+    int32_t nbodies;
+    int32_t nforces;
+    int32_t nconstraints;
+    int32_t reserved;
+    double  gravity[3];
+    const sbg_body_desc*            bodies;       /* nbodies entries, body 1 first */
+    const sbg_mobility_force_desc*  forces;       /* nforces entries */
+    const sbg_ball_constraint_desc* constraints;  /* nconstraints entries */
+} sbg_system_desc;
+
+/* Integrator options (SimTKmath Integrator.h:352-383). Zero/negative fields
+ * take Simbody's defaults: accuracy 1e-3, constraint tolerance accuracy/10
+ * (IntegratorRep.h:737-740). */
+typedef struct sbg_integ_opts {
+    double  accuracy;
+    double  constraint_tolerance;
+    int32_t project_every_step;   /* Integrator::setProjectEveryStep */
+    int32_t reserved;
+} sbg_integ_opts;
+
+typedef struct sbg_batch_config {
+    int32_t precision;            /* sbg_precision */
+    int32_t device;               /* CUDA device ordinal */
+    int64_t device_budget_bytes;  /* 0 = no limit */
+} sbg_batch_config;
+
+typedef struct sbg_topology_s* sbg_topology;
+typedef struct sbg_batch_s*    sbg_batch;
+
+/* ---------------------------------------------------------------- library */
+
+/* Thread-local message for the last failing call on this thread. */
+const char* sbg_last_error(void);
+int sbg_abi_version(void);
+/* Number of CUDA devices visible (0 without a driver); never fails. */
+int sbg_device_count(void);
+
+/* --------------------------------------------------------------- topology */
+
+/* Replaces System::realizeTopology() / SimbodyMatterSubsystemRep::endConstruction
+ * (SimbodyMatterSubsystemRep.cpp:256-330): validates the system and flattens
+ * it into level-ordered structure-of-arrays tables. Host only; no GPU needed. */
+int sbg_topology_create(const sbg_system_desc* system, sbg_topology* out);
+int sbg_topology_destroy(sbg_topology topology);
+/* State sizes, as State::getNQ/getNU (State.h:962-966); levels = tree depth. */
+int sbg_topology_info(sbg_topology topology, int32_t* nq, int32_t* nu,
+                      int32_t* nbodies, int32_t* nlevels, int32_t* nquaternions,
+                      int32_t* nconstraint_equations);
+/* Simbody's default state q (quaternions = identity), u = 0
+ * (RigidBodyNodeSpec_Ball.h:405-415). y gets nq+nu values. */
+int sbg_topology_default_state(sbg_topology topology, double* y);
+
+/* ------------------------------------------------------------------ batch */
+
+/* A batch of States: instance i uses topologies[instance_topology[i]]. Device
+ * memory for the whole batch is allocated here, bounded by the budget. */
+int sbg_batch_create(const sbg_topology* topologies, int32_t ntopologies,
+                     const int32_t* instance_topology, int32_t ninstances,
+                     const sbg_batch_config* config, sbg_batch* out);
+int sbg_batch_destroy(sbg_batch batch);
+/* y_offsets gets ninstances+1 entries: instance i occupies
+ * y[y_offsets[i] .. y_offsets[i+1]) = [q, u]; ny_total gets the total length. */
+int sbg_batch_layout(sbg_batch batch, int64_t* y_offsets, int64_t* ny_total);
+/* Device bytes held by the batch (state, tables and scratch). */
+int sbg_batch_device_bytes(sbg_batch batch, int64_t* bytes);
+
+/* State::setTime/updY for every instance (State.h:1027-1034). t may be NULL
+ * (all zero). Copies host -> device. */
+int sbg_batch_set_state(sbg_batch batch, const double* t, const double* y);
+/* State::getTime/getY (State.h:962-966). Copies device -> host. */
+int sbg_batch_get_state(sbg_batch batch, double* t, double* y);
+
+/* System::realize(state, Stage::Acceleration) for every instance
+ * (SimTKcommon/Simulation/include/SimTKcommon/internal/System.h:283), then
+ * State::getYDot (State.h:1043-1048). ydot gets [qdot, udot] per instance in
+ * the y packing; status (may be NULL) gets one SBG_INST_* word per instance.
+ * Synchronous. */
+int sbg_realize_acceleration(sbg_batch batch, double* ydot, int32_t* status);
+
+/* SimbodyMatterSubsystem::multiplyByMInv(state, f, MInvf)
+ * (Simbody/include/simbody/internal/SimbodyMatterSubsystem.h:1343):
+ * f and out are packed like the u parts of y (nu values per instance). */
+int sbg_multiply_by_minv(sbg_batch batch, const double* f, double* out);
+
+/* RungeKuttaMersonIntegrator with setFixedStepSize(h), initialize(state) and
+ * stepTo(t0 + nsteps*h) looped until reached (RungeKuttaMersonIntegrator.cpp:86-140,
+ * AbstractIntegratorRep.cpp:137-207, 341-577), for every instance, on the
+ * batch's current device state, which is advanced in place. status (may be
+ * NULL) gets the OR of SBG_INST_* words per instance. opts may be NULL. */
+int sbg_rk_merson_fixed(sbg_batch batch, double h, int32_t nsteps,
+                        const sbg_integ_opts* opts, int32_t* status);
+
+/* ------------------------------------------- device-resident (timing) path */
+
+/* The batch's CUDA stream, as a cudaStream_t cast to void*. */
+void* sbg_batch_stream(sbg_batch batch);
+/* realize(Acceleration) on the resident state; ydot stays on the device.
+ * Asynchronous on the batch stream. */
+int sbg_realize_acceleration_async(sbg_batch batch);
+/* RK Merson on the resident state, asynchronous on the batch stream. */
+int sbg_rk_merson_fixed_async(sbg_batch batch, double h, int32_t nsteps,
+                              const sbg_integ_opts* opts);
+/* Copy the resident ydot / status of the last realize to host (synchronous). */
+int sbg_batch_get_ydot(sbg_batch batch, double* ydot, int32_t* status);
+int sbg_batch_sync(sbg_batch batch);
+/* Number of kernel launches issued by this batch since creation. */
+int64_t sbg_batch_launch_count(sbg_batch batch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIMBODY_GB300_H_ */

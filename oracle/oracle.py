@@ -1,0 +1,136 @@
+"""ctypes wrapper of oracle/_build/liboracle.so, the CPU restatement of
+Simbody's articulated-body recursions and fixed-step RK-Merson driver
+(sbg_oracle*.{hpp,cpp}). Test infrastructure only."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from simbody_gb300 import _native as N
+
+_LIB = None
+_HERE = Path(__file__).resolve().parent
+
+
+def lib() -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        path = _HERE / "_build" / "liboracle.so"
+        if not path.exists():
+            raise RuntimeError(f"oracle library missing: {path} (run python -m simbody_gb300.build)")
+        L = C.CDLL(str(path))
+        P = C.POINTER
+        dp, ip, i64p = P(C.c_double), P(C.c_int32), P(C.c_int64)
+        sd = P(N.SystemDesc)
+        L.oracle_last_error.restype = C.c_char_p
+        L.oracle_system_sizes.argtypes = [sd, ip, ip, ip]
+        L.oracle_realize_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, dp, ip, C.c_int32]
+        L.oracle_minv_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, i64p, dp, dp, C.c_int32]
+        L.oracle_rk_merson_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, dp, C.c_double, C.c_int32,
+                                             C.c_double, C.c_double, C.c_int32, ip, i64p, C.c_int32]
+        L.oracle_count_realize.argtypes = [sd, dp, i64p]
+        L.oracle_time_realize.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, dp, C.c_int32, C.c_int32]
+        L.oracle_time_realize.restype = C.c_double
+        L.oracle_hardware_threads.restype = C.c_int
+        _LIB = L
+    return _LIB
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _i(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def _l(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+def _check(rc):
+    if rc:
+        raise RuntimeError(lib().oracle_last_error().decode())
+
+
+def _systems_array(systems):
+    if isinstance(systems, C.Array) or hasattr(systems, "contents"):
+        return systems
+    arr = (N.SystemDesc * len(systems))(*systems)
+    return arr
+
+
+def hardware_threads() -> int:
+    return int(lib().oracle_hardware_threads())
+
+
+def realize(systems, nsys, sys_of, y_off, y, nthreads=0):
+    sys_of = np.ascontiguousarray(sys_of, dtype=np.int32)
+    y_off = np.ascontiguousarray(y_off, dtype=np.int64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    ydot = np.empty_like(y)
+    st = np.empty(len(sys_of), dtype=np.int32)
+    _check(lib().oracle_realize_batch(systems, nsys, _i(sys_of), len(sys_of), _l(y_off), _d(y), _d(ydot), _i(st),
+                                      nthreads))
+    return ydot, st
+
+
+def multiply_by_minv(systems, nsys, sys_of, y_off, y, u_off, f, nthreads=0):
+    sys_of = np.ascontiguousarray(sys_of, dtype=np.int32)
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    out = np.empty_like(f)
+    _check(lib().oracle_minv_batch(systems, nsys, _i(sys_of), len(sys_of), _l(np.ascontiguousarray(y_off)),
+                                   _d(np.ascontiguousarray(y)), _l(np.ascontiguousarray(u_off)), _d(f), _d(out),
+                                   nthreads))
+    return out
+
+
+def rk_merson(systems, nsys, sys_of, y_off, y, h, nsteps, t=None, accuracy=0.0, cons_tol=0.0,
+              project_every_step=False, nthreads=0):
+    sys_of = np.ascontiguousarray(sys_of, dtype=np.int32)
+    y = np.array(y, dtype=np.float64, copy=True)
+    tt = np.zeros(len(sys_of)) if t is None else np.array(t, dtype=np.float64, copy=True)
+    st = np.empty(len(sys_of), dtype=np.int32)
+    npj = C.c_int64()
+    _check(lib().oracle_rk_merson_batch(systems, nsys, _i(sys_of), len(sys_of), _l(np.ascontiguousarray(y_off)),
+                                        _d(y), _d(tt), float(h), int(nsteps), accuracy, cons_tol,
+                                        int(project_every_step), _i(st), C.byref(npj), nthreads))
+    return y, tt, st, npj.value
+
+
+def count_realize(system_ptr, y):
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    counts = np.zeros(6, dtype=np.int64)
+    _check(lib().oracle_count_realize(system_ptr, _d(y), _l(counts)))
+    return dict(zip(["add", "mul", "div", "sqrt", "trig", "cmp"], counts.tolist()))
+
+
+def time_realize(systems, nsys, sys_of, y_off, y, nreps=1, nthreads=0) -> float:
+    sys_of = np.ascontiguousarray(sys_of, dtype=np.int32)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    ydot = np.empty_like(y)
+    return float(lib().oracle_time_realize(systems, nsys, _i(sys_of), len(sys_of),
+                                           _l(np.ascontiguousarray(y_off)), _d(y), _d(ydot), int(nreps),
+                                           int(nthreads)))
+
+
+# ------------------------------------------------------ workload helpers
+def realize_workload(w, instances=None, nthreads=0):
+    idx = np.arange(w.ninst) if instances is None else np.asarray(instances)
+    sys_of = w.instance_system[idx]
+    y = np.concatenate([w.y0[w.instance_slice(int(i))] for i in idx])
+    lens = np.array([w.y_offsets[i + 1] - w.y_offsets[i] for i in idx], dtype=np.int64)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    return realize(w.systems, w.nsys, sys_of, off, y, nthreads)
+
+
+def rk_workload(w, h, nsteps, instances=None, nthreads=0, **kw):
+    idx = np.arange(w.ninst) if instances is None else np.asarray(instances)
+    sys_of = w.instance_system[idx]
+    y = np.concatenate([w.y0[w.instance_slice(int(i))] for i in idx])
+    lens = np.array([w.y_offsets[i + 1] - w.y_offsets[i] for i in idx], dtype=np.int64)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    return rk_merson(w.systems, w.nsys, sys_of, off, y, h, nsteps, nthreads=nthreads, **kw)

@@ -1,0 +1,582 @@
+// sbg_oracle.cpp -- CPU oracle: topology, RK-Merson driver, loop closures and
+// a C API for the tests and the CPU-baseline legs of bench.py.
+// TEST INFRASTRUCTURE ONLY (see sbg_oracle.hpp).
+#include "sbg_oracle_impl.hpp"
+#include "sbg_oracle_api.h"
+#include "flopcount.hpp"
+
+#include <atomic>
+#include <chrono>
+#include <limits>
+#include <string>
+#include <thread>
+
+namespace sbgo {
+
+bool buildTopology(const sbg_system_desc& d, Topology& t, const char** err) {
+    static thread_local std::string msg;
+    auto fail = [&](const std::string& m) { msg = m; if (err) *err = msg.c_str(); return false; };
+    if (d.nbodies < 1 || !d.bodies) return fail("system has no bodies");
+    t = Topology();
+    t.nb = d.nbodies;
+    t.b.resize(t.nb + 1);
+    for (int k = 0; k < 3; ++k) t.gravity[k] = d.gravity[k];
+    int qn = 0, un = 0;
+    for (int i = 1; i <= t.nb; ++i) {
+        const sbg_body_desc& bd = d.bodies[i - 1];
+        Body& b = t.b[i];
+        if (bd.parent < 0 || bd.parent >= i) return fail("body parent must precede the body");
+        if (bd.mobilizer < 0 || bd.mobilizer > 4) return fail("unknown mobilizer");
+        b.parent = bd.parent;
+        b.type = bd.mobilizer;
+        b.nq = mobNQ(b.type);
+        b.nu = mobNU(b.type);
+        b.qoff = qn; b.uoff = un;
+        qn += b.nq; un += b.nu;
+        if (b.type == SBG_BALL || b.type == SBG_FREE) t.nquat++;
+        b.level = t.b[b.parent].level + 1;
+        t.b[b.parent].children.push_back(i);
+        b.mass = bd.mass;
+        for (int k = 0; k < 3; ++k) b.com[k] = bd.com[k];
+        for (int k = 0; k < 6; ++k) b.G[k] = bd.unit_inertia[k];
+        for (int k = 0; k < 9; ++k) b.RPF[k] = bd.X_PF[k];
+        for (int k = 0; k < 3; ++k) b.pPF[k] = bd.X_PF[9 + k];
+        // X_MB = ~X_BM: R_MB = ~R_BM, p_MB = -(~R_BM p_BM)
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) b.RMB[3 * r + c] = bd.X_BM[3 * c + r];
+        for (int r = 0; r < 3; ++r)
+            b.pMB[r] = -(b.RMB[3 * r + 0] * bd.X_BM[9] + b.RMB[3 * r + 1] * bd.X_BM[10] + b.RMB[3 * r + 2] * bd.X_BM[11]);
+    }
+    t.nq = qn; t.nu = un;
+    int maxLevel = 0;
+    for (int i = 1; i <= t.nb; ++i) maxLevel = std::max(maxLevel, t.b[i].level);
+    t.levels.assign(maxLevel, {});
+    for (int i = 1; i <= t.nb; ++i) t.levels[t.b[i].level - 1].push_back(i);
+    for (int i = 0; i < d.nforces; ++i) {
+        const sbg_mobility_force_desc& f = d.forces[i];
+        if (f.body < 1 || f.body > t.nb) return fail("force on a bad body");
+        if (f.kind != 0 && f.kind != 1) return fail("unknown mobility force kind");
+        if (f.which < 0 || f.which >= t.b[f.body].nu) return fail("mobility index out of range");
+        t.forces.push_back(f);
+    }
+    for (int i = 0; i < d.nconstraints; ++i) {
+        const sbg_ball_constraint_desc& c = d.constraints[i];
+        if (c.body1 < 0 || c.body1 > t.nb || c.body2 < 0 || c.body2 > t.nb || c.body1 == c.body2)
+            return fail("Ball constraint on bad bodies");
+        t.constraints.push_back(c);
+    }
+    return true;
+}
+
+// ======================================================== loop closures
+// Constraint::Ball (ConstraintImpl.h:1835-1993). Station S1 on body1 and S2
+// on body2 must coincide: perr = p_G(S2) - p_G(S1) (3 equations each).
+// The loop forward dynamics (SimbodyMatterSubsystemRep.cpp:5076-5152) solves
+// (G M^-1 G^T) lambda = aerr(udot_tree); the reference factors with
+// rank-revealing QTZ, this restatement (and the engine) with Cholesky, which
+// agree for a full-rank G.
+template <class R> struct LoopWork {
+    std::vector<R> G;  // m x nu constraint Jacobian (rows)
+};
+
+// Station location and its velocity / acceleration (all in G).
+template <class R> static void stationKin(const Work<R>& w, int body, const double* st, V3<R>& p, V3<R>& v,
+                                          V3<R>* a, const V3<R>* Aw, const V3<R>* Av) {
+    const BodyCache<R>& c = w.c[body];
+    const V3<R> s_G = c.R_GB * loadV<R>(st);
+    p = c.p_GB + s_G;
+    v = c.Vv + cross(c.Vw, s_G);
+    if (a) *a = Av[body] + cross(Aw[body], s_G) + cross(c.Vw, cross(c.Vw, s_G));
+}
+
+// Jacobian row block of one Ball constraint: d(p2 - p1)/du, assembled by
+// propagating unit velocities (equivalent to the reference's
+// calcConstraintForcesFromMultipliers transpose at :2227).
+template <class R> static void ballJacobian(const Topology& t, const Work<R>& w, int body, const double* st,
+                                            R sign, R* Grow /* 3 x nu */) {
+    if (body == 0) return;
+    const V3<R> s_G = w.c[body].R_GB * loadV<R>(st);
+    const V3<R> pS = w.c[body].p_GB + s_G;
+    // Each mobility j of an ancestor a contributes Hw x (pS - p_a) + Hv.
+    for (int a = body; a != 0; a = t.b[a].parent) {
+        const Body& ab = t.b[a];
+        const BodyCache<R>& ac = w.c[a];
+        const V3<R> r = pS - ac.p_GB;
+        for (int j = 0; j < ab.nu; ++j) {
+            const V3<R> col = ac.Hv[j] + cross(ac.Hw[j], r);
+            for (int k = 0; k < 3; ++k) Grow[k * t.nu + ab.uoff + j] = Grow[k * t.nu + ab.uoff + j] + sign * col[k];
+        }
+    }
+}
+
+template <class R> static void constraintJacobian(const Topology& t, const Work<R>& w, std::vector<R>& G) {
+    const int m = 3 * (int)t.constraints.size();
+    G.assign((size_t)m * t.nu, R(0));
+    for (size_t ci = 0; ci < t.constraints.size(); ++ci) {
+        const auto& c = t.constraints[ci];
+        R* rows = G.data() + 3 * ci * t.nu;
+        ballJacobian(t, w, c.body2, c.station2, R(1), rows);
+        ballJacobian(t, w, c.body1, c.station1, R(-1), rows);
+    }
+}
+
+template <class R> static void perrAll(const Topology& t, const Work<R>& w, R* perr) {
+    for (size_t ci = 0; ci < t.constraints.size(); ++ci) {
+        const auto& c = t.constraints[ci];
+        V3<R> p1, v1, p2, v2;
+        stationKin(w, c.body1, c.station1, p1, v1, (V3<R>*)nullptr, (const V3<R>*)nullptr, (const V3<R>*)nullptr);
+        stationKin(w, c.body2, c.station2, p2, v2, (V3<R>*)nullptr, (const V3<R>*)nullptr, (const V3<R>*)nullptr);
+        for (int k = 0; k < 3; ++k) perr[3 * ci + k] = p2[k] - p1[k];
+    }
+}
+
+// Cholesky of an m x m SPD matrix in place (lower), then solve.
+static bool cholSolve(int m, std::vector<double>& A, std::vector<double>& b) {
+    for (int j = 0; j < m; ++j) {
+        double s = A[j * m + j];
+        for (int k = 0; k < j; ++k) s -= A[j * m + k] * A[j * m + k];
+        if (!(s > 0)) return false;
+        const double d = std::sqrt(s);
+        A[j * m + j] = d;
+        for (int i = j + 1; i < m; ++i) {
+            double v = A[i * m + j];
+            for (int k = 0; k < j; ++k) v -= A[i * m + k] * A[j * m + k];
+            A[i * m + j] = v / d;
+        }
+    }
+    for (int i = 0; i < m; ++i) {
+        double v = b[i];
+        for (int k = 0; k < i; ++k) v -= A[i * m + k] * b[k];
+        b[i] = v / A[i * m + i];
+    }
+    for (int i = m - 1; i >= 0; --i) {
+        double v = b[i];
+        for (int k = i + 1; k < m; ++k) v -= A[k * m + i] * b[k];
+        b[i] = v / A[i * m + i];
+    }
+    return true;
+}
+
+// realize(Acceleration) with Ball loop closures (double only). Returns
+// SBG_INST_* bits.
+static int realizeAccelerationLoops(const Topology& t, const double* y, Work<double>& w, double* ydot) {
+    int st = 0;
+    if (!realizeAcceleration(t, y, w, ydot)) st |= SBG_INST_SINGULAR_D;
+    const int m = 3 * (int)t.constraints.size();
+    if (m == 0) return st;
+    const int nu = t.nu;
+    double* udot = ydot + t.nq;
+    // Acceleration errors of the tree solution: aerr = a_S2 - a_S1.
+    std::vector<V3<double>> Aw(t.nb + 1), Av(t.nb + 1);
+    for (int b = 0; b <= t.nb; ++b) { Aw[b] = w.c[b].Aw; Av[b] = w.c[b].Av; }
+    std::vector<double> aerr(m);
+    for (size_t ci = 0; ci < t.constraints.size(); ++ci) {
+        const auto& c = t.constraints[ci];
+        V3<double> p1, v1, a1, p2, v2, a2;
+        stationKin(w, c.body1, c.station1, p1, v1, &a1, Aw.data(), Av.data());
+        stationKin(w, c.body2, c.station2, p2, v2, &a2, Aw.data(), Av.data());
+        for (int k = 0; k < 3; ++k) aerr[3 * ci + k] = a2[k] - a1[k];
+    }
+    std::vector<double> G;
+    constraintJacobian(t, w, G);
+    // G M^-1 G^T column by column: m multiplyByMInv calls (:3512-3558).
+    std::vector<double> A((size_t)m * m), x(nu);
+    for (int j = 0; j < m; ++j) {
+        multiplyByMInv(t, w, &G[(size_t)j * nu], x.data());
+        for (int i = 0; i < m; ++i) {
+            double s = 0;
+            for (int k = 0; k < nu; ++k) s += G[(size_t)i * nu + k] * x[k];
+            A[(size_t)i * m + j] = s;
+        }
+    }
+    std::vector<double> lam = aerr;
+    if (!cholSolve(m, A, lam)) return st | SBG_INST_CHOLESKY_FAIL;
+    // udot -= M^-1 G^T lambda
+    std::vector<double> gtl(nu, 0.0);
+    for (int i = 0; i < m; ++i)
+        for (int k = 0; k < nu; ++k) gtl[k] += G[(size_t)i * nu + k] * lam[i];
+    multiplyByMInv(t, w, gtl.data(), x.data());
+    for (int k = 0; k < nu; ++k) udot[k] -= x[k];
+    return st;
+}
+
+// ================================================================ RK Merson
+struct IntegOpts {
+    double accuracy = 1e-3, consTol = 1e-4;
+    bool projectEveryStep = false;
+};
+
+static double normRMS(const double* v, int n) {
+    if (n == 0) return 0;
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += v[i] * v[i];
+    return std::sqrt(s / n);
+}
+
+// calcErrorNorm (IntegratorRep.h:454-488) with unit u weights
+// (SimbodyMatterSubsystemRep.cpp:1625-1634); the q part is N*Wu*NInv*dq
+// (IntegratorRep.h:500-523, Rotation.h:742-748).
+static double errorNorm(const Topology& t, const double* y1, const double* yerr, const double* uScale) {
+    std::vector<double> dqw(t.nq);
+    for (int bi = 1; bi <= t.nb; ++bi) {
+        const Body& b = t.b[bi];
+        const double* q = y1 + b.qoff;
+        const double* dq = yerr + b.qoff;
+        double* o = dqw.data() + b.qoff;
+        if (b.type == SBG_BALL || b.type == SBG_FREE) {
+            const double e0 = 2 * q[0], e1 = 2 * q[1], e2 = 2 * q[2], e3 = 2 * q[3];
+            const double ne1 = -e1, ne2 = -e2, ne3 = -e3;
+            const double du0 = ne1 * dq[0] + e0 * dq[1] + ne3 * dq[2] + e2 * dq[3];
+            const double du1 = ne2 * dq[0] + e3 * dq[1] + e0 * dq[2] + ne1 * dq[3];
+            const double du2 = ne3 * dq[0] + ne2 * dq[1] + e1 * dq[2] + e0 * dq[3];
+            const double h0 = q[0] / 2, h1 = q[1] / 2, h2 = q[2] / 2, h3 = q[3] / 2;
+            o[0] = -h1 * du0 + -h2 * du1 + -h3 * du2;
+            o[1] = h0 * du0 + h3 * du1 + -h2 * du2;
+            o[2] = -h3 * du0 + h0 * du1 + h1 * du2;
+            o[3] = h2 * du0 + -h1 * du1 + h0 * du2;
+            if (b.type == SBG_FREE) { o[4] = dq[4]; o[5] = dq[5]; o[6] = dq[6]; }
+        } else {
+            for (int j = 0; j < b.nq; ++j) o[j] = dq[j];
+        }
+    }
+    const double qn = normRMS(dqw.data(), t.nq);
+    std::vector<double> us(t.nu);
+    for (int i = 0; i < t.nu; ++i) us[i] = uScale[i] * yerr[t.nq + i];
+    const double un = normRMS(us.data(), t.nu);
+    return qn >= un ? qn : un;
+}
+
+// normalizeQuaternions (SimbodyMatterSubsystemRep.cpp:4448-4475,
+// RigidBodyNodeSpec_Ball.h:417-434): q /= |q|.
+static void normalizeQuaternions(const Topology& t, double* q) {
+    for (int bi = 1; bi <= t.nb; ++bi) {
+        const Body& b = t.b[bi];
+        if (b.type != SBG_BALL && b.type != SBG_FREE) continue;
+        double* qq = q + b.qoff;
+        const double n = std::sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);
+        for (int k = 0; k < 4; ++k) qq[k] = qq[k] / n;
+    }
+}
+
+// Ball-constraint position projection: Newton on perr with the minimum-norm
+// step dq = N G^T (G G^T)^-1 perr through the u-space Jacobian (projectQ,
+// SimbodyMatterSubsystemRep.cpp:4271-4300, unit weights). Returns false when
+// it does not converge to tol within 20 iterations.
+static bool projectBallQ(const Topology& t, double* q, Work<double>& w, double tol) {
+    const int m = 3 * (int)t.constraints.size();
+    std::vector<double> perr(m), G, A((size_t)m * m), lam(m), du(t.nu);
+    for (int it = 0; it < 20; ++it) {
+        realizePosition(t, q, w);
+        perrAll(t, w, perr.data());
+        if (normRMS(perr.data(), m) <= tol) return true;
+        constraintJacobian(t, w, G);
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < m; ++j) {
+                double s = 0;
+                for (int k = 0; k < t.nu; ++k) s += G[(size_t)i * t.nu + k] * G[(size_t)j * t.nu + k];
+                A[(size_t)i * m + j] = s;
+            }
+        lam = perr;
+        if (!cholSolve(m, A, lam)) return false;
+        for (int k = 0; k < t.nu; ++k) {
+            double s = 0;
+            for (int i = 0; i < m; ++i) s += G[(size_t)i * t.nu + k] * lam[i];
+            du[k] = s;
+        }
+        // q -= N(q) du
+        for (int bi = 1; bi <= t.nb; ++bi) {
+            const Body& b = t.b[bi];
+            double* qb = q + b.qoff;
+            const double* ub = du.data() + b.uoff;
+            if (b.type == SBG_BALL || b.type == SBG_FREE) {
+                const double e0 = qb[0] / 2, e1 = qb[1] / 2, e2 = qb[2] / 2, e3 = qb[3] / 2;
+                const double d0 = -e1 * ub[0] - e2 * ub[1] - e3 * ub[2];
+                const double d1 = e0 * ub[0] + e3 * ub[1] - e2 * ub[2];
+                const double d2 = -e3 * ub[0] + e0 * ub[1] + e1 * ub[2];
+                const double d3 = e2 * ub[0] - e1 * ub[1] + e0 * ub[2];
+                qb[0] -= d0; qb[1] -= d1; qb[2] -= d2; qb[3] -= d3;
+                if (b.type == SBG_FREE) { qb[4] -= ub[3]; qb[5] -= ub[4]; qb[6] -= ub[5]; }
+            } else {
+                for (int j = 0; j < b.nq; ++j) qb[j] -= ub[j];
+            }
+        }
+        normalizeQuaternions(t, q);
+    }
+    realizePosition(t, q, w);
+    perrAll(t, w, perr.data());
+    return normRMS(perr.data(), m) <= tol;
+}
+
+// Velocity projection for Ball loops: u -= G^T (G G^T)^-1 (G u).
+static bool projectBallU(const Topology& t, const double* q, double* u, Work<double>& w) {
+    const int m = 3 * (int)t.constraints.size();
+    realizePosition(t, q, w);
+    std::vector<double> G, A((size_t)m * m), v(m);
+    constraintJacobian(t, w, G);
+    for (int i = 0; i < m; ++i) {
+        double s = 0;
+        for (int k = 0; k < t.nu; ++k) s += G[(size_t)i * t.nu + k] * u[k];
+        v[i] = s;
+        for (int j = 0; j < m; ++j) {
+            double a = 0;
+            for (int k = 0; k < t.nu; ++k) a += G[(size_t)i * t.nu + k] * G[(size_t)j * t.nu + k];
+            A[(size_t)i * m + j] = a;
+        }
+    }
+    if (!cholSolve(m, A, v)) return false;
+    for (int k = 0; k < t.nu; ++k) {
+        double s = 0;
+        for (int i = 0; i < m; ++i) s += G[(size_t)i * t.nu + k] * v[i];
+        u[k] -= s;
+    }
+    return true;
+}
+
+// One instance: Integrator::initialize (Integrator.cpp:333-377, which forces a
+// projection: quaternions are normalized) then nsteps fixed RK-Merson steps
+// (RungeKuttaMersonIntegrator.cpp:86-140, AbstractIntegratorRep.cpp:137-207,
+// 341-577). Step k runs from t to t1 = t + h (FP64 sum, tMax = infinity as
+// with interpolation allowed) with stage step hs = t1 - t.
+int rkMerson(const Topology& t, double* y, double* time, double h, int nsteps, const IntegOpts& o, Work<double>& w,
+             int64_t* nProjections) {
+    const int ny = t.nq + t.nu;
+    const bool loops = !t.constraints.empty();
+    int status = 0;
+    std::vector<double> y0(ny), f0(ny), fa(ny), fb(ny), ysave(ny), ytmp(ny), yerr(ny), uScale(t.nu);
+    auto rhs = [&](const double* yy, double* f) {
+        int st = loops ? realizeAccelerationLoops(t, yy, w, f) : (realizeAcceleration(t, yy, w, f) ? 0 : SBG_INST_SINGULAR_D);
+        status |= st;
+    };
+    // initialize: ForceProjection
+    normalizeQuaternions(t, y);
+    if (loops) {
+        if (!projectBallQ(t, y, w, o.consTol)) status |= SBG_INST_PROJECTION_FAILED;
+        if (!projectBallU(t, y, y + t.nq, w)) status |= SBG_INST_PROJECTION_FAILED;
+    }
+    double tc = *time;
+    for (int step = 0; step < nsteps; ++step) {
+        const double t0 = tc;
+        for (int i = 0; i < ny; ++i) y0[i] = y[i];
+        for (int i = 0; i < t.nu; ++i) {  // calcRelativeScaling (IntegratorRep.h:644-655), w = 1
+            const double vi = std::abs(y0[t.nq + i]);
+            uScale[i] = vi > 1 ? 1 / vi : 1.0;
+        }
+        rhs(y0.data(), f0.data());
+        const double t1 = t0 + h;
+        const double hs = t1 - t0;
+        const double h3 = hs / 3, h6 = hs / 6, h8 = hs / 8, h2 = hs / 2;
+        for (int i = 0; i < ny; ++i) ytmp[i] = y0[i] + h3 * f0[i];
+        rhs(ytmp.data(), fa.data());  // f1
+        for (int i = 0; i < ny; ++i) ytmp[i] = y0[i] + h6 * (f0[i] + fa[i]);
+        rhs(ytmp.data(), fa.data());  // f2
+        for (int i = 0; i < ny; ++i) ytmp[i] = y0[i] + h8 * (f0[i] + 3 * fa[i]);
+        rhs(ytmp.data(), fb.data());  // f3
+        for (int i = 0; i < ny; ++i) ysave[i] = y0[i] + h2 * ((f0[i] - 3 * fa[i]) + 4 * fb[i]);
+        rhs(ysave.data(), fa.data());  // f4
+        for (int i = 0; i < ny; ++i) y[i] = y0[i] + h6 * ((f0[i] + 4 * fb[i]) + fa[i]);
+        for (int i = 0; i < ny; ++i) yerr[i] = 0.2 * std::abs(y[i] - ysave[i]);
+        for (int i = 0; i < ny; ++i)
+            if (!std::isfinite(y[i])) status |= SBG_INST_NONFINITE;
+        // attemptDAEStep gate (AbstractIntegratorRep.cpp:158-166)
+        const double errNorm = errorNorm(t, y, yerr.data(), uScale.data());
+        if (errNorm <= 16 * o.accuracy) {
+            const double projLimit = std::max(2 * o.consTol, std::sqrt(o.consTol));
+            // quaternion errors of y1 (realizePosition qErr)
+            double s = 0;
+            int nqt = 0;
+            for (int bi = 1; bi <= t.nb; ++bi) {
+                const Body& b = t.b[bi];
+                if (b.type != SBG_BALL && b.type != SBG_FREE) continue;
+                const double* qq = y + b.qoff;
+                const double e = std::sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]) - 1;
+                s += e * e;
+                ++nqt;
+            }
+            const double quatNorm = nqt ? std::sqrt(s / nqt) : 0.0;
+            double perrNorm = 0;
+            std::vector<double> perr;
+            if (loops) {
+                realizePosition(t, y, w);
+                perr.resize(3 * t.constraints.size());
+                perrAll(t, w, perr.data());
+                perrNorm = normRMS(perr.data(), (int)perr.size());
+            }
+            const double normOnEntry = std::max(perrNorm, quatNorm);
+            if (normOnEntry > projLimit) {
+                status |= SBG_INST_PROJECTION_FAILED;  // step still accepted (fixed step)
+            } else if (perrNorm == 0 || (perrNorm <= o.consTol && !o.projectEveryStep)) {
+                if (quatNorm > o.consTol || o.projectEveryStep) {
+                    normalizeQuaternions(t, y);
+                    if (nProjections) ++*nProjections;
+                }
+            } else {
+                if (!projectBallQ(t, y, w, o.consTol)) status |= SBG_INST_PROJECTION_FAILED;
+                if (nProjections) ++*nProjections;
+            }
+            if (loops && !projectBallU(t, y, y + t.nq, w)) status |= SBG_INST_PROJECTION_FAILED;
+        }
+        tc = t1;
+    }
+    *time = tc;
+    return status;
+}
+
+}  // namespace sbgo
+
+// ===================================================================== C API
+using namespace sbgo;
+
+namespace {
+thread_local std::string g_err;
+int setErr(const char* m) { g_err = m ? m : "error"; return SBG_ERR_INVALID; }
+
+struct Inst {
+    Topology topo;
+};
+
+// Parallel for over instances with nthreads workers (0 = hardware).
+template <class F> void parallelFor(int n, int nthreads, F&& fn) {
+    if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+    nthreads = std::min(nthreads, std::max(1, n));
+    if (nthreads == 1) { for (int i = 0; i < n; ++i) fn(i, 0); return; }
+    std::atomic<int> next(0);
+    std::vector<std::thread> th;
+    for (int w = 0; w < nthreads; ++w)
+        th.emplace_back([&, w] {
+            for (;;) {
+                const int i = next.fetch_add(1);
+                if (i >= n) break;
+                fn(i, w);
+            }
+        });
+    for (auto& x : th) x.join();
+}
+}  // namespace
+
+extern "C" {
+
+const char* oracle_last_error(void) { return g_err.c_str(); }
+
+int oracle_system_sizes(const sbg_system_desc* d, int32_t* nq, int32_t* nu, int32_t* nquat) {
+    Topology t;
+    const char* e = nullptr;
+    if (!buildTopology(*d, t, &e)) return setErr(e);
+    if (nq) *nq = t.nq;
+    if (nu) *nu = t.nu;
+    if (nquat) *nquat = t.nquat;
+    return 0;
+}
+
+// Batch realize(Acceleration): systems[sys_of[i]] for instance i; y and ydot
+// packed [q,u] per instance at y_off[i]. status may be NULL.
+int oracle_realize_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
+                         const int64_t* y_off, const double* y, double* ydot, int32_t* status, int32_t nthreads) {
+    std::vector<Topology> topo(nsys);
+    for (int s = 0; s < nsys; ++s) {
+        const char* e = nullptr;
+        if (!buildTopology(systems[s], topo[s], &e)) return setErr(e);
+    }
+    parallelFor(ninst, nthreads, [&](int i, int) {
+        const Topology& t = topo[sys_of[i]];
+        Work<double> w;
+        w.resize(t);
+        int st = t.constraints.empty()
+                     ? (realizeAcceleration(t, y + y_off[i], w, ydot + y_off[i]) ? 0 : SBG_INST_SINGULAR_D)
+                     : realizeAccelerationLoops(t, y + y_off[i], w, ydot + y_off[i]);
+        for (int k = 0; k < t.nq + t.nu; ++k)
+            if (!std::isfinite(ydot[y_off[i] + k])) st |= SBG_INST_NONFINITE;
+        if (status) status[i] = st;
+    });
+    return 0;
+}
+
+// multiplyByMInv for a batch: f/out packed per instance (nu values) at u_off[i].
+int oracle_minv_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
+                      const int64_t* y_off, const double* y, const int64_t* u_off, const double* f, double* out,
+                      int32_t nthreads) {
+    std::vector<Topology> topo(nsys);
+    for (int s = 0; s < nsys; ++s) {
+        const char* e = nullptr;
+        if (!buildTopology(systems[s], topo[s], &e)) return setErr(e);
+    }
+    parallelFor(ninst, nthreads, [&](int i, int) {
+        const Topology& t = topo[sys_of[i]];
+        Work<double> w;
+        w.resize(t);
+        realizePosition(t, y + y_off[i], w);
+        realizeABI(t, w);
+        multiplyByMInv(t, w, f + u_off[i], out + u_off[i]);
+    });
+    return 0;
+}
+
+int oracle_rk_merson_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
+                           const int64_t* y_off, double* y, double* t, double h, int32_t nsteps, double accuracy,
+                           double consTol, int32_t projectEveryStep, int32_t* status, int64_t* nproj,
+                           int32_t nthreads) {
+    std::vector<Topology> topo(nsys);
+    for (int s = 0; s < nsys; ++s) {
+        const char* e = nullptr;
+        if (!buildTopology(systems[s], topo[s], &e)) return setErr(e);
+    }
+    IntegOpts o;
+    if (accuracy > 0) o.accuracy = accuracy;
+    o.consTol = consTol > 0 ? consTol : o.accuracy / 10;
+    o.projectEveryStep = projectEveryStep != 0;
+    std::atomic<int64_t> np(0);
+    parallelFor(ninst, nthreads, [&](int i, int) {
+        const Topology& tp = topo[sys_of[i]];
+        Work<double> w;
+        w.resize(tp);
+        double tt = t ? t[i] : 0.0;
+        int64_t p = 0;
+        const int st = rkMerson(tp, y + y_off[i], &tt, h, nsteps, o, w, &p);
+        if (t) t[i] = tt;
+        if (status) status[i] = st;
+        np += p;
+    });
+    if (nproj) *nproj = np.load();
+    return 0;
+}
+
+// Exact operation counts of one realize(Acceleration) of one instance with
+// the counting scalar: counts[0]=add/sub, [1]=mul, [2]=div, [3]=sqrt,
+// [4]=sin/cos, [5]=abs/compare.
+int oracle_count_realize(const sbg_system_desc* d, const double* y, int64_t* counts) {
+    Topology t;
+    const char* e = nullptr;
+    if (!buildTopology(*d, t, &e)) return setErr(e);
+    const int ny = t.nq + t.nu;
+    std::vector<CReal> yy(ny), yd(ny);
+    for (int i = 0; i < ny; ++i) yy[i] = CReal(y[i]);
+    Work<CReal> w;
+    w.resize(t);
+    CReal::reset();
+    realizeAcceleration(t, yy.data(), w, yd.data());
+    CReal::get(counts);
+    return 0;
+}
+
+// Wall-clock seconds of nreps realize(Acceleration) passes over all instances
+// with nthreads workers (the reference's CPU path restated; used as the CPU
+// baseline when the reference itself cannot be built).
+double oracle_time_realize(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
+                           const int64_t* y_off, const double* y, double* ydot, int32_t nreps, int32_t nthreads) {
+    std::vector<Topology> topo(nsys);
+    for (int s = 0; s < nsys; ++s) {
+        const char* e = nullptr;
+        if (!buildTopology(systems[s], topo[s], &e)) { setErr(e); return -1; }
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    parallelFor(ninst, nthreads, [&](int i, int) {
+        const Topology& t = topo[sys_of[i]];
+        Work<double> w;
+        w.resize(t);
+        for (int r = 0; r < nreps; ++r) realizeAcceleration(t, y + y_off[i], w, ydot + y_off[i]);
+    });
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+int oracle_hardware_threads(void) { return (int)std::thread::hardware_concurrency(); }
+
+}  // extern "C"

@@ -1,0 +1,153 @@
+"""ctypes bindings of the C ABI (include/simbody_gb300.h) and of the workload
+generator. The CUDA engine is the only compute path: if its shared library is
+missing, importing the engine API raises instead of falling back to anything.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+BUILD = PKG / "_build"
+
+# ----------------------------------------------------------------- structs
+SBG_PIN, SBG_SLIDER, SBG_UNIVERSAL, SBG_BALL, SBG_FREE = range(5)
+NQ = {SBG_PIN: 1, SBG_SLIDER: 1, SBG_UNIVERSAL: 2, SBG_BALL: 4, SBG_FREE: 7}
+NU = {SBG_PIN: 1, SBG_SLIDER: 1, SBG_UNIVERSAL: 2, SBG_BALL: 3, SBG_FREE: 6}
+PRECISION_FP64, PRECISION_MIXED = 0, 1
+
+INST_OK = 0
+INST_NONFINITE = 1
+INST_SINGULAR_D = 2
+INST_PROJECTION_FAILED = 4
+INST_CHOLESKY_FAIL = 8
+INST_TIMEOUT = 16
+
+STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "BUDGET", 5: "STATE", 6: "UNSUPPORTED",
+                7: "NO_DEVICE"}
+
+
+class BodyDesc(C.Structure):
+    _fields_ = [("parent", C.c_int32), ("mobilizer", C.c_int32), ("mass", C.c_double),
+                ("com", C.c_double * 3), ("unit_inertia", C.c_double * 6),
+                ("X_PF", C.c_double * 12), ("X_BM", C.c_double * 12)]
+
+
+class MobilityForceDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("body", C.c_int32), ("which", C.c_int32), ("reserved", C.c_int32),
+                ("coef", C.c_double), ("q0", C.c_double)]
+
+
+class BallConstraintDesc(C.Structure):
+    _fields_ = [("body1", C.c_int32), ("body2", C.c_int32), ("station1", C.c_double * 3),
+                ("station2", C.c_double * 3)]
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [("nbodies", C.c_int32), ("nforces", C.c_int32), ("nconstraints", C.c_int32),
+                ("reserved", C.c_int32), ("gravity", C.c_double * 3),
+                ("bodies", C.POINTER(BodyDesc)), ("forces", C.POINTER(MobilityForceDesc)),
+                ("constraints", C.POINTER(BallConstraintDesc))]
+
+
+class IntegOpts(C.Structure):
+    _fields_ = [("accuracy", C.c_double), ("constraint_tolerance", C.c_double),
+                ("project_every_step", C.c_int32), ("reserved", C.c_int32)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("device", C.c_int32), ("device_budget_bytes", C.c_int64)]
+
+
+assert C.sizeof(BodyDesc) == 280 and C.sizeof(MobilityForceDesc) == 32
+assert C.sizeof(BallConstraintDesc) == 56 and C.sizeof(SystemDesc) == 64
+
+P = C.POINTER
+dp, ip, i64p, vp = P(C.c_double), P(C.c_int32), P(C.c_int64), C.c_void_p
+
+# name -> (restype, argtypes); every entry point of include/simbody_gb300.h
+ENGINE_API = {
+    "sbg_last_error": (C.c_char_p, []),
+    "sbg_abi_version": (C.c_int, []),
+    "sbg_device_count": (C.c_int, []),
+    "sbg_topology_create": (C.c_int, [P(SystemDesc), P(vp)]),
+    "sbg_topology_destroy": (C.c_int, [vp]),
+    "sbg_topology_info": (C.c_int, [vp, ip, ip, ip, ip, ip, ip]),
+    "sbg_topology_default_state": (C.c_int, [vp, dp]),
+    "sbg_batch_create": (C.c_int, [P(vp), C.c_int32, ip, C.c_int32, P(BatchConfig), P(vp)]),
+    "sbg_batch_destroy": (C.c_int, [vp]),
+    "sbg_batch_layout": (C.c_int, [vp, i64p, i64p]),
+    "sbg_batch_device_bytes": (C.c_int, [vp, i64p]),
+    "sbg_batch_set_state": (C.c_int, [vp, dp, dp]),
+    "sbg_batch_get_state": (C.c_int, [vp, dp, dp]),
+    "sbg_realize_acceleration": (C.c_int, [vp, dp, ip]),
+    "sbg_multiply_by_minv": (C.c_int, [vp, dp, dp]),
+    "sbg_rk_merson_fixed": (C.c_int, [vp, C.c_double, C.c_int32, P(IntegOpts), ip]),
+    "sbg_batch_stream": (vp, [vp]),
+    "sbg_realize_acceleration_async": (C.c_int, [vp]),
+    "sbg_rk_merson_fixed_async": (C.c_int, [vp, C.c_double, C.c_int32, P(IntegOpts)]),
+    "sbg_batch_get_ydot": (C.c_int, [vp, dp, ip]),
+    "sbg_batch_sync": (C.c_int, [vp]),
+    "sbg_batch_launch_count": (C.c_int64, [vp]),
+}
+
+WORKLOAD_API = {
+    "sbg_workload_last_error": (C.c_char_p, []),
+    "sbg_workload_create": (C.c_int, [C.c_int32, C.c_int32, P(vp)]),
+    "sbg_workload_destroy": (C.c_int, [vp]),
+    "sbg_workload_num_systems": (C.c_int32, [vp]),
+    "sbg_workload_num_instances": (C.c_int32, [vp]),
+    "sbg_workload_systems": (P(SystemDesc), [vp]),
+    "sbg_workload_instance_system": (ip, [vp]),
+    "sbg_workload_y_offsets": (i64p, [vp]),
+    "sbg_workload_y0": (dp, [vp]),
+    "sbg_workload_h": (C.c_double, [vp]),
+    "sbg_workload_nsteps": (C.c_int32, [vp]),
+    "sbg_workload_horizons": (ip, [vp]),
+    "sbg_workload_arrivals": (dp, [vp]),
+}
+
+
+def _bind(lib: C.CDLL, api: dict) -> C.CDLL:
+    for name, (res, args) in api.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+_engine = None
+_workloads = None
+
+
+def engine_lib() -> C.CDLL:
+    """The CUDA engine library. Raises if it has not been built."""
+    global _engine
+    if _engine is None:
+        path = BUILD / "libsimbody_gb300.so"
+        if not path.exists():
+            raise RuntimeError(f"CUDA engine library missing: {path} (run python -m simbody_gb300.build)")
+        _engine = _bind(C.CDLL(str(path)), ENGINE_API)
+    return _engine
+
+
+def workload_lib() -> C.CDLL:
+    global _workloads
+    if _workloads is None:
+        path = BUILD / "libsbg_workloads.so"
+        if not path.exists():
+            raise RuntimeError(f"workload library missing: {path} (run python -m simbody_gb300.build)")
+        _workloads = _bind(C.CDLL(str(path)), WORKLOAD_API)
+    return _workloads
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        msg = engine_lib().sbg_last_error()
+        raise EngineError(rc, msg.decode() if msg else "")

@@ -1,0 +1,570 @@
+// capi.cpp -- host runtime behind the C ABI of include/simbody_gb300.h:
+// topology flattening, batch memory management and kernel dispatch.
+#include "../../include/simbody_gb300.h"
+#include "engine.h"
+#include "kernels.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+using namespace sbg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+int cudaFail(cudaError_t e, const char* what) {
+    g_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return SBG_ERR_CUDA;
+}
+#define SBG_CUDA(call, what)                                   \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cudaFail(e_, what);      \
+    } while (0)
+
+const int kNQ[5] = {1, 1, 2, 4, 7};
+const int kNU[5] = {1, 1, 2, 3, 6};
+
+bool isIdentityR(const double* X) {
+    return X[0] == 1 && X[1] == 0 && X[2] == 0 && X[3] == 0 && X[4] == 1 && X[5] == 0 && X[6] == 0 && X[7] == 0 &&
+           X[8] == 1;
+}
+
+}  // namespace
+
+// A flattened topology: bodies in level order (the reference's rbNodeLevels).
+struct sbg_topology_s {
+    int nb = 0, nq = 0, nu = 0, nlevels = 0, nquat = 0, ncons = 0;
+    int maxNonFreeDof = 0;
+    int64_t recSize = 0;                 // scratch elements per instance
+    std::vector<int32_t> parent, info, qoff, uoff, srec, fbeg, fcnt;
+    std::vector<double> par;             // kParamStride per row
+    std::vector<int32_t> fkw;            // force elements, grouped by row
+    std::vector<double> fcoef, fq0;
+    double gravity[3] = {0, 0, 0};
+    std::vector<double> defaultY;
+    std::vector<sbg_ball_constraint_desc> cons;
+};
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct sbg_batch_s {
+    int precision = 0, device = 0;
+    int64_t budget = 0;
+    int ninst = 0;
+    int nm = 3;
+    cudaStream_t stream = nullptr;
+    std::vector<int32_t> instTopo;
+    std::vector<int64_t> hostYOff, hostUOff;  // packed host offsets (n+1)
+    int64_t nyTotal = 0, nuTotal = 0, colElems = 0;
+    std::vector<DevBuf> bufs;
+    int64_t devBytes = 0;
+    DevTables T{};
+    // device pointers
+    double* y = nullptr;       // state columns
+    double* ydot = nullptr;    // derivative columns
+    double* fcol = nullptr;    // M^-1 input columns
+    double* time = nullptr;
+    int32_t* status = nullptr;
+    int64_t* dHostYOff = nullptr;
+    int64_t* dHostUOff = nullptr;
+    double* staging = nullptr;  // packed device staging (nyTotal)
+    void* scratch = nullptr;
+    void* fbuf = nullptr;       // RK stage derivatives, 4 planes
+    int64_t scratchElems = 0;
+    double* hostPinned = nullptr;  // pinned host staging (nyTotal)
+    bool stateSet = false;
+    int64_t launches = 0;
+
+    ~sbg_batch_s() {
+        if (device >= 0) cudaSetDevice(device);
+        for (auto& b : bufs) cudaFree(b.p);
+        if (hostPinned) cudaFreeHost(hostPinned);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    int alloc(void** out, size_t bytes, const char* what) {
+        if (budget > 0 && devBytes + (int64_t)bytes > budget)
+            return fail(SBG_ERR_BUDGET, std::string("device budget exceeded allocating ") + what);
+        void* p = nullptr;
+        if (bytes) {
+            cudaError_t e = cudaMalloc(&p, bytes);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return fail(SBG_ERR_NOMEM, std::string("cudaMalloc failed for ") + what + ": " + cudaGetErrorString(e));
+            }
+        }
+        bufs.push_back({p, bytes});
+        devBytes += (int64_t)bytes;
+        *out = p;
+        return SBG_OK;
+    }
+    template <class T_> int upload(const T_** dst, const std::vector<T_>& v, const char* what) {
+        void* p = nullptr;
+        int rc = alloc(&p, v.size() * sizeof(T_), what);
+        if (rc) return rc;
+        if (!v.empty()) {
+            cudaError_t e = cudaMemcpy(p, v.data(), v.size() * sizeof(T_), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return cudaFail(e, what);
+        }
+        *dst = static_cast<const T_*>(p);
+        return SBG_OK;
+    }
+};
+
+extern "C" {
+
+const char* sbg_last_error(void) { return g_err.c_str(); }
+int sbg_abi_version(void) { return SBG_ABI_VERSION; }
+int sbg_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+// ------------------------------------------------------------------ topology
+int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
+    if (!d || !out) return fail(SBG_ERR_INVALID, "null argument");
+    if (d->nbodies < 1 || !d->bodies) return fail(SBG_ERR_INVALID, "system has no bodies");
+    if (d->nforces < 0 || (d->nforces > 0 && !d->forces)) return fail(SBG_ERR_INVALID, "bad force list");
+    if (d->nconstraints < 0 || (d->nconstraints > 0 && !d->constraints))
+        return fail(SBG_ERR_INVALID, "bad constraint list");
+    const int nb = d->nbodies;
+    std::vector<int> level(nb + 1, 0), qo(nb + 1, 0), uo(nb + 1, 0);
+    int nq = 0, nu = 0, nquat = 0, maxnf = 0;
+    for (int i = 1; i <= nb; ++i) {
+        const sbg_body_desc& b = d->bodies[i - 1];
+        if (b.parent < 0 || b.parent >= i)
+            return fail(SBG_ERR_INVALID, "body " + std::to_string(i) + ": parent must precede the body");
+        if (b.mobilizer < 0 || b.mobilizer > 4)
+            return fail(SBG_ERR_INVALID, "body " + std::to_string(i) + ": unknown mobilizer");
+        if (!(b.mass > 0) || !std::isfinite(b.mass))
+            return fail(SBG_ERR_INVALID, "body " + std::to_string(i) + ": mass must be positive and finite");
+        level[i] = level[b.parent] + 1;
+        qo[i] = nq;
+        uo[i] = nu;
+        nq += kNQ[b.mobilizer];
+        nu += kNU[b.mobilizer];
+        if (b.mobilizer >= SBG_BALL) ++nquat;
+        if (b.mobilizer != SBG_FREE) maxnf = std::max(maxnf, kNU[b.mobilizer]);
+    }
+    for (int i = 0; i < d->nforces; ++i) {
+        const auto& f = d->forces[i];
+        if (f.body < 1 || f.body > nb) return fail(SBG_ERR_INVALID, "mobility force on a bad body");
+        if (f.kind != 0 && f.kind != 1) return fail(SBG_ERR_INVALID, "unknown mobility force kind");
+        if (f.which < 0 || f.which >= kNU[d->bodies[f.body - 1].mobilizer])
+            return fail(SBG_ERR_INVALID, "mobility index out of range");
+    }
+    for (int i = 0; i < d->nconstraints; ++i) {
+        const auto& c = d->constraints[i];
+        if (c.body1 < 0 || c.body1 > nb || c.body2 < 0 || c.body2 > nb || c.body1 == c.body2)
+            return fail(SBG_ERR_INVALID, "Ball constraint on bad bodies");
+    }
+    auto* t = new (std::nothrow) sbg_topology_s();
+    if (!t) return fail(SBG_ERR_NOMEM, "out of host memory");
+    t->nb = nb;
+    t->nq = nq;
+    t->nu = nu;
+    t->nquat = nquat;
+    t->ncons = d->nconstraints;
+    t->maxNonFreeDof = maxnf;
+    for (int k = 0; k < 3; ++k) t->gravity[k] = d->gravity[k];
+    // level order: stable sort of bodies by level
+    std::vector<int> order(nb);
+    std::iota(order.begin(), order.end(), 1);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return level[a] < level[b]; });
+    std::vector<int> rowOf(nb + 1, -1);
+    for (int r = 0; r < nb; ++r) rowOf[order[r]] = r;
+    t->nlevels = level[order.back()];
+    // forces grouped by body, application order preserved
+    std::vector<std::vector<int>> fOf(nb + 1);
+    for (int i = 0; i < d->nforces; ++i) fOf[d->forces[i].body].push_back(i);
+    int64_t rec = 0;
+    for (int r = 0; r < nb; ++r) {
+        const int bi = order[r];
+        const sbg_body_desc& b = d->bodies[bi - 1];
+        const int n = kNU[b.mobilizer];
+        int info = b.mobilizer | (n << 4);
+        if (isIdentityR(b.X_PF)) info |= 1 << 8;
+        if (isIdentityR(b.X_BM)) info |= 1 << 9;
+        if (b.X_BM[9] == 0 && b.X_BM[10] == 0 && b.X_BM[11] == 0) info |= 1 << 10;
+        if (b.X_PF[9] == 0 && b.X_PF[10] == 0 && b.X_PF[11] == 0) info |= 1 << 11;
+        t->parent.push_back(b.parent == 0 ? -1 : rowOf[b.parent]);
+        t->info.push_back(info);
+        t->qoff.push_back(qo[bi]);
+        t->uoff.push_back(uo[bi]);
+        t->srec.push_back((int32_t)rec);
+        rec += scratchRecordSize(n);
+        t->fbeg.push_back((int32_t)t->fkw.size());
+        t->fcnt.push_back((int32_t)fOf[bi].size());
+        for (int fi : fOf[bi]) {
+            const auto& f = d->forces[fi];
+            t->fkw.push_back((f.kind << 8) | f.which);
+            t->fcoef.push_back(f.coef);
+            t->fq0.push_back(f.q0);
+        }
+        // params: mass, com, G, R_PF, p_PF, R_MB = ~R_BM, p_MB = -(~R_BM p_BM)
+        double p[kParamStride];
+        p[0] = b.mass;
+        for (int k = 0; k < 3; ++k) p[1 + k] = b.com[k];
+        for (int k = 0; k < 6; ++k) p[4 + k] = b.unit_inertia[k];
+        for (int k = 0; k < 9; ++k) p[10 + k] = b.X_PF[k];
+        for (int k = 0; k < 3; ++k) p[19 + k] = b.X_PF[9 + k];
+        for (int r2 = 0; r2 < 3; ++r2)
+            for (int c = 0; c < 3; ++c) p[22 + 3 * r2 + c] = b.X_BM[3 * c + r2];
+        for (int r2 = 0; r2 < 3; ++r2)
+            p[31 + r2] = -(p[22 + 3 * r2] * b.X_BM[9] + p[22 + 3 * r2 + 1] * b.X_BM[10] + p[22 + 3 * r2 + 2] * b.X_BM[11]);
+        t->par.insert(t->par.end(), p, p + kParamStride);
+    }
+    t->recSize = rec;
+    t->defaultY.assign(nq + nu, 0.0);
+    for (int i = 1; i <= nb; ++i)
+        if (d->bodies[i - 1].mobilizer >= SBG_BALL) t->defaultY[qo[i]] = 1.0;
+    for (int i = 0; i < d->nconstraints; ++i) t->cons.push_back(d->constraints[i]);
+    *out = t;
+    return SBG_OK;
+}
+
+int sbg_topology_destroy(sbg_topology t) {
+    delete t;
+    return SBG_OK;
+}
+
+int sbg_topology_info(sbg_topology t, int32_t* nq, int32_t* nu, int32_t* nbodies, int32_t* nlevels,
+                      int32_t* nquaternions, int32_t* ncons) {
+    if (!t) return fail(SBG_ERR_INVALID, "null topology");
+    if (nq) *nq = t->nq;
+    if (nu) *nu = t->nu;
+    if (nbodies) *nbodies = t->nb;
+    if (nlevels) *nlevels = t->nlevels;
+    if (nquaternions) *nquaternions = t->nquat;
+    if (ncons) *ncons = 3 * t->ncons;
+    return SBG_OK;
+}
+
+int sbg_topology_default_state(sbg_topology t, double* y) {
+    if (!t || !y) return fail(SBG_ERR_INVALID, "null argument");
+    std::copy(t->defaultY.begin(), t->defaultY.end(), y);
+    return SBG_OK;
+}
+
+// --------------------------------------------------------------------- batch
+int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* instTopo, int32_t ninst,
+                     const sbg_batch_config* cfg, sbg_batch* out) {
+    if (!topos || ntopo < 1 || !instTopo || ninst < 0 || !out) return fail(SBG_ERR_INVALID, "bad batch arguments");
+    const int precision = cfg ? cfg->precision : SBG_PRECISION_FP64;
+    if (precision != SBG_PRECISION_FP64 && precision != SBG_PRECISION_MIXED)
+        return fail(SBG_ERR_INVALID, "unknown precision");
+    for (int i = 0; i < ninst; ++i)
+        if (instTopo[i] < 0 || instTopo[i] >= ntopo || !topos[instTopo[i]])
+            return fail(SBG_ERR_INVALID, "instance " + std::to_string(i) + " names a bad topology");
+    for (int k = 0; k < ntopo; ++k)
+        if (topos[k] && topos[k]->ncons > 0)
+            return fail(SBG_ERR_UNSUPPORTED, "loop closures are handled by the serving engine (sbg_serve_*)");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SBG_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    const int device = cfg ? cfg->device : 0;
+    if (device < 0 || device >= ndev) return fail(SBG_ERR_INVALID, "bad device ordinal");
+    SBG_CUDA(cudaSetDevice(device), "cudaSetDevice");
+
+    auto* b = new (std::nothrow) sbg_batch_s();
+    if (!b) return fail(SBG_ERR_NOMEM, "out of host memory");
+    b->precision = precision;
+    b->device = device;
+    b->budget = cfg ? cfg->device_budget_bytes : 0;
+    b->ninst = ninst;
+    b->instTopo.assign(instTopo, instTopo + ninst);
+    auto bail = [&](int rc) { delete b; return rc; };
+    {
+        cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return bail(cudaFail(e, "cudaStreamCreate"));
+    }
+
+    // distinct topologies used, concatenated body tables
+    std::vector<int> used(ntopo, -1);
+    std::vector<int32_t> parent, info, qoff, uoff, srec, fbeg, fcnt, fkw;
+    std::vector<double> par, fcoef, fq0;
+    std::vector<int32_t> rowBase(ntopo, 0);
+    int nm = 1;
+    for (int i = 0; i < ninst; ++i) {
+        const int k = instTopo[i];
+        if (used[k] >= 0) continue;
+        used[k] = 1;
+        const sbg_topology_s* t = topos[k];
+        rowBase[k] = (int32_t)parent.size();
+        const int32_t fOff = (int32_t)fkw.size();
+        parent.insert(parent.end(), t->parent.begin(), t->parent.end());
+        info.insert(info.end(), t->info.begin(), t->info.end());
+        qoff.insert(qoff.end(), t->qoff.begin(), t->qoff.end());
+        uoff.insert(uoff.end(), t->uoff.begin(), t->uoff.end());
+        srec.insert(srec.end(), t->srec.begin(), t->srec.end());
+        for (int32_t fb : t->fbeg) fbeg.push_back(fb + fOff);
+        fcnt.insert(fcnt.end(), t->fcnt.begin(), t->fcnt.end());
+        fkw.insert(fkw.end(), t->fkw.begin(), t->fkw.end());
+        fcoef.insert(fcoef.end(), t->fcoef.begin(), t->fcoef.end());
+        fq0.insert(fq0.end(), t->fq0.begin(), t->fq0.end());
+        par.insert(par.end(), t->par.begin(), t->par.end());
+        if (t->maxNonFreeDof > 1) nm = 3;
+    }
+    b->nm = nm;
+    const bool uniform = ninst > 0 && std::all_of(instTopo, instTopo + ninst, [&](int32_t k) { return k == instTopo[0]; });
+
+    // instance table and column addressing
+    std::vector<int32_t> ibody(ninst), inb(ninst), inq(ninst), inu(ninst), order(ninst);
+    std::vector<int64_t> ybase(ninst), ystride(ninst), sbase(ninst), sstride(ninst);
+    std::vector<double> grav(3 * (size_t)ninst);
+    b->hostYOff.assign(ninst + 1, 0);
+    b->hostUOff.assign(ninst + 1, 0);
+    int64_t sOff = 0;
+    for (int i = 0; i < ninst; ++i) {
+        const sbg_topology_s* t = topos[instTopo[i]];
+        ibody[i] = rowBase[instTopo[i]];
+        inb[i] = t->nb;
+        inq[i] = t->nq;
+        inu[i] = t->nu;
+        for (int k = 0; k < 3; ++k) grav[3 * i + k] = t->gravity[k];
+        b->hostYOff[i + 1] = b->hostYOff[i] + t->nq + t->nu;
+        b->hostUOff[i + 1] = b->hostUOff[i] + t->nu;
+        if (uniform) {
+            ybase[i] = i; ystride[i] = ninst;
+            sbase[i] = i; sstride[i] = ninst;
+        } else {
+            ybase[i] = b->hostYOff[i]; ystride[i] = 1;
+            sbase[i] = sOff; sstride[i] = 1;
+            sOff += t->recSize;
+        }
+    }
+    b->nyTotal = b->hostYOff[ninst];
+    b->nuTotal = b->hostUOff[ninst];
+    b->colElems = b->nyTotal;
+    b->scratchElems = uniform ? (ninst ? topos[instTopo[0]]->recSize * (int64_t)ninst : 0) : sOff;
+    // threads take instances in decreasing body count so a warp's lanes walk
+    // trees of similar size
+    std::iota(order.begin(), order.end(), 0);
+    if (!uniform) std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return inb[a] > inb[c]; });
+
+    int rc = 0;
+    DevTables& T = b->T;
+    T.ninst = ninst;
+    std::vector<float> par32(par.begin(), par.end()), fcoef32(fcoef.begin(), fcoef.end()), fq032(fq0.begin(), fq0.end());
+    if ((rc = b->upload(&T.parent, parent, "body table"))) return bail(rc);
+    if ((rc = b->upload(&T.info, info, "body table"))) return bail(rc);
+    if ((rc = b->upload(&T.qoff, qoff, "body table"))) return bail(rc);
+    if ((rc = b->upload(&T.uoff, uoff, "body table"))) return bail(rc);
+    if ((rc = b->upload(&T.srec, srec, "body table"))) return bail(rc);
+    if ((rc = b->upload(&T.fbeg, fbeg, "body table"))) return bail(rc);
+    if ((rc = b->upload(&T.fcnt, fcnt, "body table"))) return bail(rc);
+    if ((rc = b->upload(&T.par64, par, "parameters"))) return bail(rc);
+    if ((rc = b->upload(&T.par32, par32, "parameters"))) return bail(rc);
+    if ((rc = b->upload(&T.fkind_which, fkw, "force table"))) return bail(rc);
+    if ((rc = b->upload(&T.fcoef64, fcoef, "force table"))) return bail(rc);
+    if ((rc = b->upload(&T.fq064, fq0, "force table"))) return bail(rc);
+    if ((rc = b->upload(&T.fcoef32, fcoef32, "force table"))) return bail(rc);
+    if ((rc = b->upload(&T.fq032, fq032, "force table"))) return bail(rc);
+    if ((rc = b->upload(&T.ibody, ibody, "instance table"))) return bail(rc);
+    if ((rc = b->upload(&T.inb, inb, "instance table"))) return bail(rc);
+    if ((rc = b->upload(&T.inq, inq, "instance table"))) return bail(rc);
+    if ((rc = b->upload(&T.inu, inu, "instance table"))) return bail(rc);
+    if ((rc = b->upload(&T.ybase, ybase, "instance table"))) return bail(rc);
+    if ((rc = b->upload(&T.ystride, ystride, "instance table"))) return bail(rc);
+    if ((rc = b->upload(&T.sbase, sbase, "instance table"))) return bail(rc);
+    if ((rc = b->upload(&T.sstride, sstride, "instance table"))) return bail(rc);
+    if ((rc = b->upload(&T.grav, grav, "instance table"))) return bail(rc);
+    if ((rc = b->upload(&T.order, order, "instance table"))) return bail(rc);
+    const int64_t* dOff = nullptr;
+    if ((rc = b->upload(&dOff, b->hostYOff, "offsets"))) return bail(rc);
+    b->dHostYOff = const_cast<int64_t*>(dOff);
+    if ((rc = b->upload(&dOff, b->hostUOff, "offsets"))) return bail(rc);
+    b->dHostUOff = const_cast<int64_t*>(dOff);
+
+    const size_t rsz = precision == SBG_PRECISION_FP64 ? sizeof(double) : sizeof(float);
+    void* p = nullptr;
+    if ((rc = b->alloc(&p, b->colElems * sizeof(double), "state"))) return bail(rc);
+    b->y = static_cast<double*>(p);
+    if ((rc = b->alloc(&p, b->colElems * sizeof(double), "derivatives"))) return bail(rc);
+    b->ydot = static_cast<double*>(p);
+    if ((rc = b->alloc(&p, b->colElems * sizeof(double), "M^-1 input"))) return bail(rc);
+    b->fcol = static_cast<double*>(p);
+    if ((rc = b->alloc(&p, std::max<int64_t>(ninst, 1) * sizeof(double), "time"))) return bail(rc);
+    b->time = static_cast<double*>(p);
+    if ((rc = b->alloc(&p, std::max<int64_t>(ninst, 1) * sizeof(int32_t), "status"))) return bail(rc);
+    b->status = static_cast<int32_t*>(p);
+    if ((rc = b->alloc(&p, std::max<int64_t>(b->nyTotal, 1) * sizeof(double), "staging"))) return bail(rc);
+    b->staging = static_cast<double*>(p);
+    if ((rc = b->alloc(&b->scratch, std::max<int64_t>(b->scratchElems, 1) * rsz, "scratch"))) return bail(rc);
+    if ((rc = b->alloc(&b->fbuf, 4 * std::max<int64_t>(b->colElems, 1) * rsz, "stage derivatives"))) return bail(rc);
+    {
+        cudaError_t e = cudaMallocHost(&b->hostPinned, std::max<int64_t>(b->nyTotal, 1) * sizeof(double));
+        if (e != cudaSuccess) return bail(cudaFail(e, "cudaMallocHost"));
+    }
+    cudaError_t e = cudaMemsetAsync(b->time, 0, std::max<int64_t>(ninst, 1) * sizeof(double), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->status, 0, std::max<int64_t>(ninst, 1) * sizeof(int32_t), b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return bail(cudaFail(e, "batch initialisation"));
+    *out = b;
+    return SBG_OK;
+}
+
+int sbg_batch_destroy(sbg_batch b) {
+    delete b;
+    return SBG_OK;
+}
+
+int sbg_batch_layout(sbg_batch b, int64_t* yOff, int64_t* nyTotal) {
+    if (!b) return fail(SBG_ERR_INVALID, "null batch");
+    if (yOff) std::copy(b->hostYOff.begin(), b->hostYOff.end(), yOff);
+    if (nyTotal) *nyTotal = b->nyTotal;
+    return SBG_OK;
+}
+
+int sbg_batch_device_bytes(sbg_batch b, int64_t* bytes) {
+    if (!b || !bytes) return fail(SBG_ERR_INVALID, "null argument");
+    *bytes = b->devBytes;
+    return SBG_OK;
+}
+
+void* sbg_batch_stream(sbg_batch b) { return b ? (void*)b->stream : nullptr; }
+int64_t sbg_batch_launch_count(sbg_batch b) { return b ? b->launches : 0; }
+
+int sbg_batch_set_state(sbg_batch b, const double* t, const double* y) {
+    if (!b || !y) return fail(SBG_ERR_INVALID, "null argument");
+    SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    const size_t bytes = b->nyTotal * sizeof(double);
+    std::memcpy(b->hostPinned, y, bytes);
+    SBG_CUDA(cudaMemcpyAsync(b->staging, b->hostPinned, bytes, cudaMemcpyHostToDevice, b->stream), "state upload");
+    SBG_CUDA(launchScatter(b->T, b->dHostYOff, b->staging, b->y, 0, b->stream), "state scatter");
+    ++b->launches;
+    if (t) {
+        SBG_CUDA(cudaStreamSynchronize(b->stream), "state upload");
+        std::memcpy(b->hostPinned, t, b->ninst * sizeof(double));
+        SBG_CUDA(cudaMemcpyAsync(b->time, b->hostPinned, b->ninst * sizeof(double), cudaMemcpyHostToDevice, b->stream),
+                 "time upload");
+    } else {
+        SBG_CUDA(cudaMemsetAsync(b->time, 0, std::max(b->ninst, 1) * sizeof(double), b->stream), "time reset");
+    }
+    SBG_CUDA(cudaStreamSynchronize(b->stream), "state upload");
+    b->stateSet = true;
+    return SBG_OK;
+}
+
+int sbg_batch_get_state(sbg_batch b, double* t, double* y) {
+    if (!b || !y) return fail(SBG_ERR_INVALID, "null argument");
+    if (!b->stateSet) return fail(SBG_ERR_STATE, "no state has been set");
+    SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    SBG_CUDA(launchGather(b->T, b->dHostYOff, b->y, b->staging, 0, b->stream), "state gather");
+    ++b->launches;
+    SBG_CUDA(cudaMemcpyAsync(b->hostPinned, b->staging, b->nyTotal * sizeof(double), cudaMemcpyDeviceToHost, b->stream),
+             "state download");
+    SBG_CUDA(cudaStreamSynchronize(b->stream), "state download");
+    std::memcpy(y, b->hostPinned, b->nyTotal * sizeof(double));
+    if (t) SBG_CUDA(cudaMemcpy(t, b->time, b->ninst * sizeof(double), cudaMemcpyDeviceToHost), "time download");
+    return SBG_OK;
+}
+
+int sbg_realize_acceleration_async(sbg_batch b) {
+    if (!b) return fail(SBG_ERR_INVALID, "null batch");
+    if (!b->stateSet) return fail(SBG_ERR_STATE, "no state has been set");
+    SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    SBG_CUDA(launchRealize(b->T, b->precision, b->nm, b->y, b->ydot, b->scratch, b->status, b->stream),
+             "realize kernel launch");
+    ++b->launches;
+    return SBG_OK;
+}
+
+int sbg_batch_get_ydot(sbg_batch b, double* ydot, int32_t* status) {
+    if (!b) return fail(SBG_ERR_INVALID, "null batch");
+    SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    if (ydot) {
+        SBG_CUDA(launchGather(b->T, b->dHostYOff, b->ydot, b->staging, 0, b->stream), "derivative gather");
+        ++b->launches;
+        SBG_CUDA(cudaMemcpyAsync(b->hostPinned, b->staging, b->nyTotal * sizeof(double), cudaMemcpyDeviceToHost,
+                                 b->stream), "derivative download");
+    }
+    SBG_CUDA(cudaStreamSynchronize(b->stream), "derivative download");
+    if (ydot) std::memcpy(ydot, b->hostPinned, b->nyTotal * sizeof(double));
+    if (status) SBG_CUDA(cudaMemcpy(status, b->status, b->ninst * sizeof(int32_t), cudaMemcpyDeviceToHost), "status download");
+    return SBG_OK;
+}
+
+int sbg_realize_acceleration(sbg_batch b, double* ydot, int32_t* status) {
+    int rc = sbg_realize_acceleration_async(b);
+    if (rc) return rc;
+    return sbg_batch_get_ydot(b, ydot, status);
+}
+
+int sbg_multiply_by_minv(sbg_batch b, const double* f, double* outp) {
+    if (!b || !f || !outp) return fail(SBG_ERR_INVALID, "null argument");
+    if (!b->stateSet) return fail(SBG_ERR_STATE, "no state has been set");
+    SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    const size_t bytes = b->nuTotal * sizeof(double);
+    std::memcpy(b->hostPinned, f, bytes);
+    SBG_CUDA(cudaMemcpyAsync(b->staging, b->hostPinned, bytes, cudaMemcpyHostToDevice, b->stream), "force upload");
+    SBG_CUDA(launchScatter(b->T, b->dHostUOff, b->staging, b->fcol, 1, b->stream), "force scatter");
+    SBG_CUDA(launchMInv(b->T, b->precision, b->nm, b->y, b->fcol, b->ydot, b->scratch, b->status, b->stream),
+             "M^-1 kernel launch");
+    SBG_CUDA(launchGather(b->T, b->dHostUOff, b->ydot, b->staging, 1, b->stream), "result gather");
+    b->launches += 3;
+    SBG_CUDA(cudaMemcpyAsync(b->hostPinned, b->staging, bytes, cudaMemcpyDeviceToHost, b->stream), "result download");
+    SBG_CUDA(cudaStreamSynchronize(b->stream), "M^-1");
+    std::memcpy(outp, b->hostPinned, bytes);
+    return SBG_OK;
+}
+
+int sbg_rk_merson_fixed_async(sbg_batch b, double h, int32_t nsteps, const sbg_integ_opts* opts) {
+    if (!b) return fail(SBG_ERR_INVALID, "null batch");
+    if (!b->stateSet) return fail(SBG_ERR_STATE, "no state has been set");
+    if (!(h > 0) || !std::isfinite(h)) return fail(SBG_ERR_INVALID, "step size must be positive");
+    if (nsteps < 0) return fail(SBG_ERR_INVALID, "negative step count");
+    double acc = 1e-3, ctol = -1;
+    int pes = 0;
+    if (opts) {
+        if (opts->accuracy > 0) acc = opts->accuracy;
+        if (opts->constraint_tolerance > 0) ctol = opts->constraint_tolerance;
+        pes = opts->project_every_step;
+    }
+    if (ctol <= 0) ctol = acc / 10;
+    SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    SBG_CUDA(cudaMemsetAsync(b->status, 0, std::max(b->ninst, 1) * sizeof(int32_t), b->stream), "status reset");
+    SBG_CUDA(launchNormalizeQuat(b->T, b->y, b->stream), "initialize");
+    SBG_CUDA(launchRKMerson(b->T, b->precision, b->nm, b->y, b->time, b->fbuf, b->colElems, b->scratch, b->status, h,
+                            nsteps, acc, ctol, pes, b->stream),
+             "RK-Merson kernel launch");
+    b->launches += 2;
+    return SBG_OK;
+}
+
+int sbg_rk_merson_fixed(sbg_batch b, double h, int32_t nsteps, const sbg_integ_opts* opts, int32_t* status) {
+    int rc = sbg_rk_merson_fixed_async(b, h, nsteps, opts);
+    if (rc) return rc;
+    SBG_CUDA(cudaStreamSynchronize(b->stream), "RK-Merson");
+    if (status) SBG_CUDA(cudaMemcpy(status, b->status, b->ninst * sizeof(int32_t), cudaMemcpyDeviceToHost), "status download");
+    return SBG_OK;
+}
+
+int sbg_batch_sync(sbg_batch b) {
+    if (!b) return fail(SBG_ERR_INVALID, "null batch");
+    SBG_CUDA(cudaStreamSynchronize(b->stream), "synchronize");
+    return SBG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,74 @@
+// engine.h -- device-side table layout shared by the host runtime (capi.cpp)
+// and the CUDA kernels (abi_kernels.cu).
+//
+// HBM layout of a batch
+//   Body table (one row per mobilized body of every distinct topology, bodies
+//   of a topology stored in level order, i.e. the rbNodeLevels order of
+//   SimbodyMatterSubsystemRep.cpp:256-330):
+//     parent  local row of the parent body within its topology, -1 = Ground
+//     info    mobilizer | ndof << 4
+//     qoff/uoff  Simbody q/u slot of the body (body-index order)
+//     srec    offset of the body's scratch record within its instance record
+//     fbeg/fcnt  mobility-force elements of this body, in application order
+//     par     kParamStride parameters per body (AoS): mass, com[3],
+//             unit inertia[6] (xx yy zz xy xz yz), R_PF[9], p_PF[3],
+//             R_MB[9], p_MB[3]; stored in FP64 and, for the mixed form, FP32.
+//   Instance table: first body row, body count, q/u sizes, addressing of its
+//   state column and scratch record, gravity index.
+//   State y, derivatives and scratch are "columns": element k of instance i
+//   lives at base_i + k*stride_i. A group of instances that share one
+//   topology uses stride = ninstances (structure of arrays: a warp's loads of
+//   element k coalesce); instances with their own topology use stride 1
+//   (each thread walks its own contiguous record).
+#pragma once
+#include <cstdint>
+
+namespace sbg {
+
+constexpr int kParamStride = 34;
+constexpr int kMaxDof = 6;
+
+// Scratch record of one body (elements of the arithmetic type R), n = ndof:
+//   0  R_GB[9] p_GB[3] V_GB[6]   kinematics; reused for A_GB[6] in pass 3
+//  18  pc[3] Gi[6] l[3] a[6] bF[6]
+//  42  Pacc: M[6] J[6] F[9], zacc[6]
+//  69  H[6n] f[n] DI[n*n] G[6n] eps[n]
+#ifdef __CUDACC__
+#define SBG_HD __host__ __device__
+#else
+#define SBG_HD
+#endif
+SBG_HD constexpr int scratchRecordSize(int n) { return 69 + 14 * n + n * n; }
+constexpr int kRecKin = 0, kRecPc = 18, kRecGi = 21, kRecL = 27, kRecA = 30, kRecBF = 36, kRecPacc = 42,
+              kRecZacc = 63, kRecH = 69;
+
+struct DevTables {
+    const int32_t* parent;
+    const int32_t* info;
+    const int32_t* qoff;
+    const int32_t* uoff;
+    const int32_t* srec;
+    const int32_t* fbeg;
+    const int32_t* fcnt;
+    const double* par64;
+    const float* par32;
+    const int32_t* fkind_which;  // kind << 8 | which
+    const double* fcoef64;
+    const double* fq064;
+    const float* fcoef32;
+    const float* fq032;
+    // per instance
+    const int32_t* ibody;    // first body row
+    const int32_t* inb;      // number of bodies
+    const int32_t* inq;
+    const int32_t* inu;
+    const int64_t* ybase;    // state column base
+    const int64_t* ystride;
+    const int64_t* sbase;    // scratch column base
+    const int64_t* sstride;
+    const double* grav;      // per instance gravity (3)
+    const int32_t* order;    // thread -> instance (size-sorted)
+    int32_t ninst;
+};
+
+}  // namespace sbg

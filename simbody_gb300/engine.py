@@ -1,0 +1,162 @@
+"""Python face of the C ABI: topologies and device-resident batches of states.
+
+A ``Batch`` holds the states of many instances on one GPU. Its methods map to
+Simbody calls (paths relative to the Simbody source tree):
+
+  set_state / get_state      State::updY / getY       (State.h:962-1034)
+  realize_acceleration       System::realize(s, Stage::Acceleration) + getYDot
+  multiply_by_minv           SimbodyMatterSubsystem::multiplyByMInv (.h:1343)
+  rk_merson_fixed            RungeKuttaMersonIntegrator, setFixedStepSize(h),
+                             initialize, stepTo(t0 + n h)
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from . import _native as N
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class Topology:
+    """A realized topology (System::realizeTopology) owned by the engine."""
+
+    def __init__(self, desc: N.SystemDesc, keepalive=None):
+        lib = N.engine_lib()
+        h = C.c_void_p()
+        N.check(lib.sbg_topology_create(C.byref(desc), C.byref(h)))
+        self._h = h
+        self._keep = keepalive
+        nq, nu, nb, nl, nqt, nc = (C.c_int32() for _ in range(6))
+        N.check(lib.sbg_topology_info(h, C.byref(nq), C.byref(nu), C.byref(nb), C.byref(nl), C.byref(nqt),
+                                      C.byref(nc)))
+        self.nq, self.nu, self.nbodies = nq.value, nu.value, nb.value
+        self.nlevels, self.nquaternions, self.nconstraint_equations = nl.value, nqt.value, nc.value
+
+    @property
+    def handle(self):
+        return self._h
+
+    def default_state(self) -> np.ndarray:
+        y = np.zeros(self.nq + self.nu)
+        N.check(N.engine_lib().sbg_topology_default_state(self._h, _dptr(y)))
+        return y
+
+    def __del__(self):
+        if getattr(self, "_h", None) and N._engine is not None:
+            N._engine.sbg_topology_destroy(self._h)
+            self._h = None
+
+
+class Batch:
+    """A device-resident batch of instances; instance i uses
+    ``topologies[instance_topology[i]]``."""
+
+    def __init__(self, topologies: Sequence[Topology], instance_topology, precision: str = "fp64",
+                 device: int = 0, device_budget_bytes: int = 0):
+        lib = N.engine_lib()
+        self.topologies = list(topologies)
+        self.instance_topology = np.ascontiguousarray(instance_topology, dtype=np.int32)
+        self.ninst = len(self.instance_topology)
+        prec = {"fp64": N.PRECISION_FP64, "mixed": N.PRECISION_MIXED}[precision]
+        self.precision = precision
+        cfg = N.BatchConfig(prec, device, int(device_budget_bytes))
+        handles = (C.c_void_p * len(self.topologies))(*[t.handle for t in self.topologies])
+        h = C.c_void_p()
+        N.check(lib.sbg_batch_create(handles, len(self.topologies), _iptr(self.instance_topology), self.ninst,
+                                     C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.y_offsets = np.zeros(self.ninst + 1, dtype=np.int64)
+        nyt = C.c_int64()
+        N.check(lib.sbg_batch_layout(h, self.y_offsets.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(nyt)))
+        self.ny_total = nyt.value
+        nqs = np.array([self.topologies[k].nq for k in self.instance_topology], dtype=np.int64)
+        nus = np.array([self.topologies[k].nu for k in self.instance_topology], dtype=np.int64)
+        self.nq = nqs
+        self.nu = nus
+        self.u_offsets = np.concatenate([[0], np.cumsum(nus)]).astype(np.int64)
+
+    # -- state
+    def set_state(self, y: np.ndarray, t: np.ndarray | None = None) -> None:
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        assert y.size == self.ny_total
+        tt = None if t is None else np.ascontiguousarray(t, dtype=np.float64)
+        N.check(N.engine_lib().sbg_batch_set_state(self._h, None if tt is None else _dptr(tt), _dptr(y)))
+
+    def get_state(self):
+        y = np.empty(self.ny_total)
+        t = np.empty(self.ninst)
+        N.check(N.engine_lib().sbg_batch_get_state(self._h, _dptr(t), _dptr(y)))
+        return y, t
+
+    # -- operators
+    def realize_acceleration(self):
+        ydot = np.empty(self.ny_total)
+        st = np.empty(self.ninst, dtype=np.int32)
+        N.check(N.engine_lib().sbg_realize_acceleration(self._h, _dptr(ydot), _iptr(st)))
+        return ydot, st
+
+    def multiply_by_minv(self, f: np.ndarray) -> np.ndarray:
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        assert f.size == self.u_offsets[-1]
+        out = np.empty_like(f)
+        N.check(N.engine_lib().sbg_multiply_by_minv(self._h, _dptr(f), _dptr(out)))
+        return out
+
+    def rk_merson_fixed(self, h: float, nsteps: int, accuracy: float = 0.0, constraint_tolerance: float = 0.0,
+                        project_every_step: bool = False) -> np.ndarray:
+        opts = N.IntegOpts(accuracy, constraint_tolerance, int(project_every_step), 0)
+        st = np.empty(self.ninst, dtype=np.int32)
+        N.check(N.engine_lib().sbg_rk_merson_fixed(self._h, float(h), int(nsteps), C.byref(opts), _iptr(st)))
+        return st
+
+    # -- device-resident timing path
+    @property
+    def stream(self) -> int:
+        return N.engine_lib().sbg_batch_stream(self._h) or 0
+
+    def realize_acceleration_async(self) -> None:
+        N.check(N.engine_lib().sbg_realize_acceleration_async(self._h))
+
+    def rk_merson_fixed_async(self, h: float, nsteps: int) -> None:
+        N.check(N.engine_lib().sbg_rk_merson_fixed_async(self._h, float(h), int(nsteps), None))
+
+    def get_ydot(self):
+        ydot = np.empty(self.ny_total)
+        st = np.empty(self.ninst, dtype=np.int32)
+        N.check(N.engine_lib().sbg_batch_get_ydot(self._h, _dptr(ydot), _iptr(st)))
+        return ydot, st
+
+    def sync(self) -> None:
+        N.check(N.engine_lib().sbg_batch_sync(self._h))
+
+    @property
+    def launch_count(self) -> int:
+        return int(N.engine_lib().sbg_batch_launch_count(self._h))
+
+    @property
+    def device_bytes(self) -> int:
+        b = C.c_int64()
+        N.check(N.engine_lib().sbg_batch_device_bytes(self._h, C.byref(b)))
+        return b.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and N._engine is not None:
+            N._engine.sbg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def device_count() -> int:
+    return int(N.engine_lib().sbg_device_count())

@@ -1,0 +1,76 @@
+"""Parity of the CUDA engine (through the C ABI) with the CPU oracle.
+
+Tolerances: the plain FP64 form must reproduce realize(Acceleration) to
+<= 1e-12 relative (norm-wise per instance) and short trajectories to <= 1e-12;
+the mixed form must keep the relative udot error <= 1e-5 against FP64.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from simbody_gb300 import Workload, engine_batch
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_err_per_instance(a, b, offsets, part=None):
+    errs = []
+    for i in range(len(offsets) - 1):
+        s = slice(offsets[i], offsets[i + 1])
+        x, y = a[s], b[s]
+        errs.append(np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300))
+    return np.array(errs)
+
+
+@pytest.mark.parametrize("config,n", [(1, 256), (2, 512), (3, 128), (4, 64)])
+def test_realize_fp64_matches_oracle(engine, config, n):
+    w = Workload(config, n)
+    b, y0 = engine_batch(w, "fp64")
+    b.set_state(y0)
+    ydot, st = b.realize_acceleration()
+    ref, rst = O.realize_workload(w)
+    assert (st == 0).all() and (rst == 0).all()
+    err = rel_err_per_instance(ydot, ref, b.y_offsets)
+    assert err.max() <= 1e-12, err.max()
+
+
+@pytest.mark.parametrize("config,n", [(2, 512), (3, 128), (4, 64)])
+def test_realize_mixed_udot_error(engine, config, n):
+    w = Workload(config, n)
+    b64, y0 = engine_batch(w, "fp64")
+    b32, _ = engine_batch(w, "mixed")
+    b64.set_state(y0)
+    b32.set_state(y0)
+    d64, _ = b64.realize_acceleration()
+    d32, st = b32.realize_acceleration()
+    assert (st == 0).all()
+    udot64 = np.concatenate([d64[b64.y_offsets[i] + b64.nq[i]:b64.y_offsets[i + 1]] for i in range(b64.ninst)])
+    udot32 = np.concatenate([d32[b32.y_offsets[i] + b32.nq[i]:b32.y_offsets[i + 1]] for i in range(b32.ninst)])
+    err = rel_err_per_instance(udot32, udot64, b64.u_offsets)
+    assert err.max() <= 1e-5, err.max()
+
+
+@pytest.mark.parametrize("config,n,steps", [(1, 256, 50), (3, 64, 20), (4, 32, 20)])
+def test_rk_merson_fp64_short_horizon(engine, config, n, steps):
+    w = Workload(config, n)
+    b, y0 = engine_batch(w, "fp64")
+    b.set_state(y0)
+    st = b.rk_merson_fixed(w.h, steps)
+    y, t = b.get_state()
+    ref, rt, rst, _ = O.rk_workload(w, w.h, steps)
+    assert (st & ~4 == 0).all()
+    err = rel_err_per_instance(y, ref, b.y_offsets)
+    assert err.max() <= 1e-12, err.max()
+    np.testing.assert_array_equal(t, rt)
+
+
+def test_multiply_by_minv_fp64(engine):
+    w = Workload(3, 64)
+    b, y0 = engine_batch(w, "fp64")
+    b.set_state(y0)
+    rng = np.random.default_rng(7)
+    f = rng.normal(size=int(b.u_offsets[-1]))
+    out = b.multiply_by_minv(f)
+    ref = O.multiply_by_minv(w.systems, w.nsys, w.instance_system[:64], b.y_offsets, y0, b.u_offsets, f)
+    err = rel_err_per_instance(out, ref, b.u_offsets)
+    assert err.max() <= 1e-12, err.max()
