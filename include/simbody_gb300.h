@@ -223,6 +223,29 @@ int sbg_batch_sync(sbg_batch batch);
 /* Number of kernel launches issued by this batch since creation. */
 int64_t sbg_batch_launch_count(sbg_batch batch);
 
+/* ------------------------------------------------ allocation-free realize */
+
+/* No counterpart in the reference: an addition for callers that may not
+ * allocate device memory (a control loop that allocates only at start-up, a
+ * host framework that hands out device buffers from its own pool). It runs
+ * the plain FP64 realize(Stage::Acceleration) for ninstances states of ONE
+ * topology with no cudaMalloc/cudaFree: the caller passes device buffers
+ *   y      ninstances * (nq+nu) doubles, [q, u] per instance, back to back
+ *   ydot   same size, receives [qdot, udot]
+ *   status ninstances SBG_INST_* words
+ * and the per-body scratch lives in a 16 MiB file-scope device array (the
+ * topology tables in fixed device arrays: at most 256 bodies and 4096
+ * mobility-force elements); larger topologies are rejected with
+ * SBG_ERR_INVALID. Runs asynchronously on `stream` (a cudaStream_t, NULL =
+ * default stream) of the current device. The first call on a device looks up
+ * the arrays' device addresses, so make it before any stream capture. All
+ * calls share the arrays: calls that overlap on the GPU race. Message of the
+ * last failure: sbg_noalloc_last_error(). */
+int sbg_realize_acceleration_noalloc(sbg_topology topology, int32_t ninstances,
+                                     const double* y, double* ydot,
+                                     int32_t* status, void* stream);
+const char* sbg_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
