@@ -197,14 +197,19 @@ def run_ours(args):
 
     b64, y0 = engine_batch(w, "fp64")
     bmx, _ = engine_batch(w, "mixed")
-    b64.set_state(y0)
-    bmx.set_state(y0)
+    bft, _ = engine_batch(w, "mixed_fast")
+    for b in (b64, bmx, bft):
+        b.set_state(y0)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         ms_mx, launches = time_resident(bmx, args.steps, args.warmup)
         ms_64, _ = time_resident(b64, max(3, args.steps // 4), 1)
+        ms_ft, _ = time_resident(bft, max(3, args.steps // 4), 1)
     d64, st64 = b64.realize_acceleration()
     dmx, stmx = bmx.realize_acceleration()
+    dft, _ = bft.realize_acceleration()
     err = udot_rel_err(dmx, d64, bmx)
+    err_ft = udot_rel_err(dft, d64, bft)
+    bft.close()
     ms_e2e, e2e_launches, _ = time_e2e(bmx, y0, max(3, args.steps // 2), 1)
 
     if world > 1:
@@ -239,6 +244,8 @@ def run_ours(args):
                    "instances": w.ninst, "bodies_per_instance": 32, "dof_per_instance": 96,
                    "l2": "working set (state 117 MB + derivatives + per-body scratch) larger than L2; no flush"},
         "fp64": {"value": value64, "ms_per_step": ms_64, "speedup_mixed_over_fp64": value / value64},
+        "fp32_unrefined": {"value": nb_total / (ms_ft * 1e-3), "ms_per_step": ms_ft,
+                           "udot_rel_err_max": float(err_ft.max())},
         "udot_rel_err": {"max": float(err.max()), "p99": float(np.quantile(err, 0.99)), "mean": float(err.mean()),
                          "definition": "per instance ||udot_mixed - udot_fp64||_2 / ||udot_fp64||_2"},
         "status_nonzero": int((stmx != 0).sum() + (st64 != 0).sum()),

@@ -60,8 +60,11 @@ typedef enum sbg_mobilizer {
 
 typedef enum sbg_precision {
     SBG_PRECISION_FP64 = 0,   /* every recursion in FP64 */
-    SBG_PRECISION_MIXED = 1   /* FP32 spatial recursions, FP64 state accumulation,
-                                 quaternion normalisation and loop-closure solve */
+    SBG_PRECISION_MIXED = 1,  /* FP32 spatial recursions + one refinement step
+                                 with a double-float inverse-dynamics residual;
+                                 FP64 state accumulation, quaternion
+                                 normalisation and loop-closure solve */
+    SBG_PRECISION_MIXED_FAST = 2  /* FP32 spatial recursions without refinement */
 } sbg_precision;
 
 /* Per-instance status bits written by the kernels (never a device trap). */

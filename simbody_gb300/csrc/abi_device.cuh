@@ -1,8 +1,8 @@
 // abi_device.cuh -- articulated-body forward dynamics and fixed-step
 // Runge-Kutta-Merson integration for a batch of multibody instances.
 //
-// One thread owns one instance (a System state). The RHS is three sweeps over
-// the instance's level-ordered body table:
+// One thread owns one instance (a System state). The RHS is a set of sweeps
+// over the instance's level-ordered body table:
 //   pass 1 (base to tip)  position + velocity kinematics, gravity and mobility
 //                         forces (RigidBodyNodeSpec.h:229-333,
 //                         RigidBodyNode.cpp:54-174, Force_Gravity.cpp:531-556,
@@ -10,9 +10,19 @@
 //   pass 2 (tip to base)  articulated body inertias fused with the first udot
 //                         pass (RigidBodyNodeSpec.cpp:249-400)
 //   pass 3 (base to tip)  second udot pass (RigidBodyNodeSpec.cpp:408-446)
-// Per-body intermediates live in a scratch record addressed as a column
-// (see engine.h). The arithmetic type R is double for the plain form and
-// float for the mixed form, whose integrator state stays in FP64.
+// The mixed form (R = float) adds one step of iterative refinement: pass 3
+// also runs the outward half of inverse dynamics in double-float (hi+lo FP32
+// pairs with error-free transformations), pass 4 (tip to base) finishes the
+// residual r = f - tau(udot0) and runs the first M^-1 pass on it, pass 5 (base
+// to tip) applies udot = udot0 + M^-1 r with the FP32 factorization. This
+// takes the relative udot error of an FP32 recursion (up to ~1e-4 on random
+// trees) to the few-1e-6 level set by the FP32 kinematics.
+//
+// Per-body intermediates live in a scratch record (engine.h); its element e
+// is at p[e*SS]: SS = 32 for warp-tiled records of instances sharing one
+// topology (a warp's accesses coalesce), SS = 1 for per-instance contiguous
+// records. Along a chain (parent = previous row) the parent's values travel
+// in registers instead of through the record.
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -25,12 +35,10 @@
 namespace sbg {
 
 enum { T_PIN = 0, T_SLIDER = 1, T_UNIV = 2, T_BALL = 3, T_FREE = 4 };
-enum { F_RPF_I = 1 << 8, F_RMB_I = 1 << 9, F_PMB_0 = 1 << 10, F_PPF_0 = 1 << 11 };
 
-template <class R> struct Scr {
+template <class R, int SS> struct Scr {
     R* p;
-    int64_t base, stride;
-    __device__ __forceinline__ R& operator()(int64_t e) const { return p[base + e * stride]; }
+    __device__ __forceinline__ R& operator()(int e) const { return p[e * SS]; }
 };
 
 template <class R> __device__ __forceinline__ const R* paramTable(const DevTables& T) {
@@ -43,8 +51,12 @@ template <class R> __device__ __forceinline__ const R* q0Table(const DevTables& 
     if constexpr (std::is_same<R, double>::value) return T.fq064; else return T.fq032;
 }
 
-template <class R> __device__ __forceinline__ void st3(const Scr<R>& S, int64_t e, V3<R> v) { S(e) = v.x; S(e + 1) = v.y; S(e + 2) = v.z; }
-template <class R> __device__ __forceinline__ V3<R> ld3(const Scr<R>& S, int64_t e) { return V3<R>{S(e), S(e + 1), S(e + 2)}; }
+template <class R, int SS> __device__ __forceinline__ void st3(const Scr<R, SS>& S, int e, V3<R> v) {
+    S(e) = v.x; S(e + 1) = v.y; S(e + 2) = v.z;
+}
+template <class R, int SS> __device__ __forceinline__ V3<R> ld3(const Scr<R, SS>& S, int e) {
+    return V3<R>{S(e), S(e + 1), S(e + 2)};
+}
 
 template <class R> __device__ __forceinline__ void sincosR(R x, R* s, R* c) {
     if constexpr (std::is_same<R, double>::value) sincos(x, s, c); else sincosf(x, s, c);
@@ -53,21 +65,81 @@ template <class R> __device__ __forceinline__ R sqrtR(R x) {
     if constexpr (std::is_same<R, double>::value) return sqrt(x); else return sqrtf(x);
 }
 
+// ------------------------------------------------------------- double-float
+// hi + lo pairs of FP32 with error-free transformations (Dekker/Knuth two-sum,
+// FMA-based two-product); the intrinsics keep the compiler from contracting
+// or reassociating them.
+struct DF { float hi, lo; };
+__device__ __forceinline__ DF dfq(float a) { return DF{a, 0.f}; }
+__device__ __forceinline__ DF twoSum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return DF{s, e};
+}
+__device__ __forceinline__ DF quickTwoSum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF operator+(DF a, DF b) {
+    DF s = twoSum(a.hi, b.hi);
+    const DF t = twoSum(a.lo, b.lo);
+    s.lo = __fadd_rn(s.lo, t.hi);
+    s = quickTwoSum(s.hi, s.lo);
+    s.lo = __fadd_rn(s.lo, t.lo);
+    return quickTwoSum(s.hi, s.lo);
+}
+__device__ __forceinline__ DF operator+(DF a, float b) {
+    DF s = twoSum(a.hi, b);
+    s.lo = __fadd_rn(s.lo, a.lo);
+    return quickTwoSum(s.hi, s.lo);
+}
+__device__ __forceinline__ DF operator-(DF a) { return DF{-a.hi, -a.lo}; }
+__device__ __forceinline__ DF operator-(DF a, DF b) { return a + (-b); }
+__device__ __forceinline__ DF operator*(DF a, float b) {
+    const float p = __fmul_rn(a.hi, b);
+    const float e = __fmaf_rn(a.hi, b, -p);
+    return quickTwoSum(p, __fmaf_rn(a.lo, b, e));
+}
+struct DF3 { DF x, y, z; };
+__device__ __forceinline__ DF3 dfq3(V3<float> v) { return DF3{dfq(v.x), dfq(v.y), dfq(v.z)}; }
+__device__ __forceinline__ DF3 operator+(DF3 a, DF3 b) { return DF3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ DF3 operator+(DF3 a, V3<float> b) { return DF3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ DF3 operator-(DF3 a, DF3 b) { return DF3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ DF3 scale(DF3 a, float s) { return DF3{a.x * s, a.y * s, a.z * s}; }
+// a + s*v with s a df scalar's hi part times float vector (s exact float)
+__device__ __forceinline__ DF3 axpyDF(DF3 a, float s, V3<float> v) {
+    return DF3{a.x + DF{__fmul_rn(s, v.x), __fmaf_rn(s, v.x, -__fmul_rn(s, v.x))},
+               a.y + DF{__fmul_rn(s, v.y), __fmaf_rn(s, v.y, -__fmul_rn(s, v.y))},
+               a.z + DF{__fmul_rn(s, v.z), __fmaf_rn(s, v.z, -__fmul_rn(s, v.z))}};
+}
+// float vector x df vector (exact-float left operand)
+__device__ __forceinline__ DF3 crossFD(V3<float> a, DF3 b) {
+    return DF3{b.z * a.y - b.y * a.z, b.x * a.z - b.z * a.x, b.y * a.x - b.x * a.y};
+}
+__device__ __forceinline__ DF dotFD(V3<float> a, DF3 b) { return (b.x * a.x + b.y * a.y) + b.z * a.z; }
+__device__ __forceinline__ DF3 symMulDF(const S3<float>& S, DF3 v) {
+    return DF3{(v.x * S.xx + v.y * S.xy) + v.z * S.xz, (v.x * S.xy + v.y * S.yy) + v.z * S.yz,
+               (v.x * S.xz + v.y * S.yz) + v.z * S.zz};
+}
+
 // ------------------------------------------------------------------ pass 1
 // Src::q(k), Src::u(k) give the (double) state; Out::qdot(k, v) receives qdot.
-template <class R, class Src, class Out>
-__device__ void pass1(const DevTables& T, int body0, int nb, const Scr<R>& S, const Src& src, Out& out,
-                      V3<R> g) {
+template <class R, int SS, class Src, class Out>
+__device__ __forceinline__ void pass1(const DevTables& T, int body0, int nb, const Scr<R, SS>& S, const Src& src,
+                                      Out& out, V3<R> g) {
     const R* PT = paramTable<R>(T);
     const R* FC = coefTable<R>(T);
     const R* FQ = q0Table<R>(T);
+    M3<R> cR = ident3<R>();
+    V3<R> cp = z3<R>(), cw = z3<R>(), cv = z3<R>();  // previous row's kinematics
     for (int lb = 0; lb < nb; ++lb) {
         const int row = body0 + lb;
         const int info = T.info[row];
         const int type = info & 15, n = (info >> 4) & 15;
         const int parent = T.parent[row];
         const int qo = T.qoff[row], uo = T.uoff[row];
-        const int64_t rec = T.srec[row];
+        const int rec = T.srec[row];
         const R* pr = PT + (int64_t)row * kParamStride;
         const R m = pr[0];
         const V3<R> com = mk3(pr[1], pr[2], pr[3]);
@@ -78,8 +150,10 @@ __device__ void pass1(const DevTables& T, int body0, int nb, const Scr<R>& S, co
         V3<R> pGP, wGP, vGP;
         if (parent < 0) {
             RGP = ident3<R>(); pGP = z3<R>(); wGP = z3<R>(); vGP = z3<R>();
+        } else if (info & F_CARRY) {
+            RGP = cR; pGP = cp; wGP = cw; vGP = cv;
         } else {
-            const int64_t pe = T.srec[body0 + parent];
+            const int pe = T.srec[body0 + parent];
 #pragma unroll
             for (int i = 0; i < 9; ++i) RGP.a[i] = S(pe + i);
             pGP = ld3(S, pe + 9); wGP = ld3(S, pe + 12); vGP = ld3(S, pe + 15);
@@ -88,7 +162,9 @@ __device__ void pass1(const DevTables& T, int body0, int nb, const Scr<R>& S, co
         // state of this mobilizer
         R q[7], u[6];
         const int nq = type == T_BALL ? 4 : (type == T_FREE ? 7 : n);
+#pragma unroll
         for (int j = 0; j < 7; ++j) q[j] = j < nq ? R(src.q(qo + j)) : R(0);
+#pragma unroll
         for (int j = 0; j < 6; ++j) u[j] = j < n ? R(src.u(uo + j)) : R(0);
 
         // X_FM (mobilizer specific) and qdot = N(q) u
@@ -147,11 +223,10 @@ __device__ void pass1(const DevTables& T, int body0, int nb, const Scr<R>& S, co
 
         // body transforms (RigidBodyNodeSpec.h:554-569)
         M3<R> RPF, RMB;
-        V3<R> pPF, pMB;
 #pragma unroll
         for (int i = 0; i < 9; ++i) { RPF.a[i] = pr[10 + i]; RMB.a[i] = pr[22 + i]; }
-        pPF = mk3(pr[19], pr[20], pr[21]);
-        pMB = mk3(pr[31], pr[32], pr[33]);
+        const V3<R> pPF = mk3(pr[19], pr[20], pr[21]);
+        const V3<R> pMB = mk3(pr[31], pr[32], pr[33]);
         const M3<R> RFB = (info & F_RMB_I) ? RFM : mul(RFM, RMB);
         const V3<R> r = (info & F_PMB_0) ? z3<R>() : mul(RFM, pMB);  // r_MB_F
         const V3<R> pFB = r + pFM;
@@ -165,7 +240,7 @@ __device__ void pass1(const DevTables& T, int body0, int nb, const Scr<R>& S, co
         // H_PB_G columns (RigidBodyNodeSpec.cpp:44-74), stored; V_PB_G = H u
         V3<R> VPw = z3<R>(), VPv = z3<R>();
         V3<R> wFM = z3<R>();
-        const int64_t eH = rec + kRecH;
+        const int eH = rec + kRecH;
         auto putH = [&](int j, V3<R> hw, V3<R> hv) {
             st3(S, eH + 6 * j, hw);
             st3(S, eH + 6 * j + 3, hv);
@@ -235,16 +310,18 @@ __device__ void pass1(const DevTables& T, int body0, int nb, const Scr<R>& S, co
             R v;
             if ((kw >> 8) == 0) v = -coef * (R(src.q(qo + which)) - FQ[fb + k]);
             else v = -coef * u[which];
-            // which < n by construction
 #pragma unroll
             for (int j = 0; j < 6; ++j)
                 if (j == which) f[j] = f[j] + v;
         }
 
         // store
+        if (info & F_MEMCHILD) {
 #pragma unroll
-        for (int i = 0; i < 9; ++i) S(rec + i) = RGB.a[i];
-        st3(S, rec + 9, pGB); st3(S, rec + 12, wGB); st3(S, rec + 15, vGB);
+            for (int i = 0; i < 9; ++i) S(rec + i) = RGB.a[i];
+            st3(S, rec + 9, pGB); st3(S, rec + 12, wGB); st3(S, rec + 15, vGB);
+        }
+        cR = RGB; cp = pGB; cw = wGB; cv = vGB;
         st3(S, rec + kRecPc, pc);
         S(rec + kRecGi + 0) = Gi.xx; S(rec + kRecGi + 1) = Gi.yy; S(rec + kRecGi + 2) = Gi.zz;
         S(rec + kRecGi + 3) = Gi.xy; S(rec + kRecGi + 4) = Gi.xz; S(rec + kRecGi + 5) = Gi.yz;
@@ -252,8 +329,9 @@ __device__ void pass1(const DevTables& T, int body0, int nb, const Scr<R>& S, co
         st3(S, rec + kRecA, aw); st3(S, rec + kRecA + 3, av);
         if constexpr (Src::kMInv) { st3(S, rec + kRecBF, z3<R>()); st3(S, rec + kRecBF + 3, z3<R>()); }
         else { st3(S, rec + kRecBF, bw - Fw); st3(S, rec + kRecBF + 3, bv - Fv); }
-        for (int i = 0; i < 27; ++i) S(rec + kRecPacc + i) = R(0);
-        const int64_t ef = eH + 6 * n;
+        if (info & F_MEMACC)
+            for (int i = 0; i < 27; ++i) S(rec + kRecPacc + i) = R(0);
+        const int ef = eH + 6 * n;
         for (int j = 0; j < n; ++j) S(ef + j) = f[j];
     }
 }
@@ -262,8 +340,6 @@ __device__ void pass1(const DevTables& T, int body0, int nb, const Scr<R>& S, co
 // Articulated body inertia fused with the first udot pass for one body with
 // N columns (N = 6 for Free, else the batch width NM with unused columns
 // zero and an identity block in D). Returns false on a singular D.
-// Order chosen for short live ranges: P, c = P a, z, PH, eps, D, DI, then G
-// one column at a time folded into P+ and z+.
 template <class R, int N> __device__ __forceinline__ bool invertSmall(const R* D, R* DI) {
     bool ok = true;
     if constexpr (N == 1) {
@@ -357,32 +433,62 @@ template <class R, int N> __device__ __forceinline__ bool invertSmall(const R* D
     return ok;
 }
 
-template <class R, int N>
-__device__ __forceinline__ bool pass2BodyImpl(const DevTables& T, int body0, int row, int n, const Scr<R>& S, R m) {
-    const int64_t rec = T.srec[row];
-    const int64_t eH = rec + kRecH;
-    const int64_t ef = eH + 6 * n, eDI = ef + n, eG = eDI + n * n, eEps = eG + 6 * n;
-    // P = ArticulatedInertia(Mk) + accumulated children (RigidBodyNodeSpec.cpp:259-279)
+// Values a child hands to its parent in the inward sweeps.
+template <class R> struct Carry2 {
+    AB<R> P;        // shifted P+
+    V3<R> zw, zv;   // Phi z+
+};
+
+// Order chosen for short live ranges: P, c = P a, z, PH, eps, D, DI, then G
+// one column at a time folded into P+ and z+.
+template <class R, int N, int SS>
+__device__ __forceinline__ bool pass2BodyImpl(const DevTables& T, int body0, int row, int n, const Scr<R, SS>& S,
+                                              R m, bool haveCarry, Carry2<R>& cy) {
+    const int info = T.info[row];
+    const int rec = T.srec[row];
+    const int eH = rec + kRecH;
+    const int ef = eH + 6 * n, eDI = ef + n, eG = eDI + n * n, eEps = eG + 6 * n;
+    // P = ArticulatedInertia(Mk) + children (RigidBodyNodeSpec.cpp:259-279)
     AB<R> P;
+    V3<R> zaw = z3<R>(), zav = z3<R>();
     {
         const V3<R> pc = ld3(S, rec + kRecPc);
-        const int64_t ea = rec + kRecPacc;
-        P.M = S3<R>{m + S(ea + 0), m + S(ea + 1), m + S(ea + 2), S(ea + 3), S(ea + 4), S(ea + 5)};
-        P.J = S3<R>{m * S(rec + kRecGi) + S(ea + 6), m * S(rec + kRecGi + 1) + S(ea + 7),
-                    m * S(rec + kRecGi + 2) + S(ea + 8), m * S(rec + kRecGi + 3) + S(ea + 9),
-                    m * S(rec + kRecGi + 4) + S(ea + 10), m * S(rec + kRecGi + 5) + S(ea + 11)};
+        P.M = S3<R>{m, m, m, R(0), R(0), R(0)};
+        P.J = S3<R>{m * S(rec + kRecGi), m * S(rec + kRecGi + 1), m * S(rec + kRecGi + 2),
+                    m * S(rec + kRecGi + 3), m * S(rec + kRecGi + 4), m * S(rec + kRecGi + 5)};
         const V3<R> mp = m * pc;
-        P.F.a[0] = S(ea + 12);         P.F.a[1] = -mp.z + S(ea + 13); P.F.a[2] = mp.y + S(ea + 14);
-        P.F.a[3] = mp.z + S(ea + 15);  P.F.a[4] = S(ea + 16);         P.F.a[5] = -mp.x + S(ea + 17);
-        P.F.a[6] = -mp.y + S(ea + 18); P.F.a[7] = mp.x + S(ea + 19);  P.F.a[8] = S(ea + 20);
+        P.F.a[0] = R(0);  P.F.a[1] = -mp.z; P.F.a[2] = mp.y;
+        P.F.a[3] = mp.z;  P.F.a[4] = R(0);  P.F.a[5] = -mp.x;
+        P.F.a[6] = -mp.y; P.F.a[7] = mp.x;  P.F.a[8] = R(0);
+        if (info & F_MEMACC) {
+            const int ea = rec + kRecPacc;
+            P.M.xx += S(ea + 0); P.M.yy += S(ea + 1); P.M.zz += S(ea + 2);
+            P.M.xy += S(ea + 3); P.M.xz += S(ea + 4); P.M.yz += S(ea + 5);
+            P.J.xx += S(ea + 6); P.J.yy += S(ea + 7); P.J.zz += S(ea + 8);
+            P.J.xy += S(ea + 9); P.J.xz += S(ea + 10); P.J.yz += S(ea + 11);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) P.F.a[i] += S(ea + 12 + i);
+            zaw = ld3(S, rec + kRecZacc);
+            zav = ld3(S, rec + kRecZacc + 3);
+        }
+        if (haveCarry) {
+            P.M.xx += cy.P.M.xx; P.M.yy += cy.P.M.yy; P.M.zz += cy.P.M.zz;
+            P.M.xy += cy.P.M.xy; P.M.xz += cy.P.M.xz; P.M.yz += cy.P.M.yz;
+            P.J.xx += cy.P.J.xx; P.J.yy += cy.P.J.yy; P.J.zz += cy.P.J.zz;
+            P.J.xy += cy.P.J.xy; P.J.xz += cy.P.J.xz; P.J.yz += cy.P.J.yz;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) P.F.a[i] += cy.P.F.a[i];
+            zaw = zaw + cy.zw;
+            zav = zav + cy.zv;
+        }
     }
     // z = (P a + b) - F + sum_children Phi z+ (RigidBodyNodeSpec.cpp:380-392)
     V3<R> zw, zv;
     {
         V3<R> cw, cv;
         abmul(P, ld3(S, rec + kRecA), ld3(S, rec + kRecA + 3), cw, cv);
-        zw = (cw + ld3(S, rec + kRecBF)) + ld3(S, rec + kRecZacc);
-        zv = (cv + ld3(S, rec + kRecBF + 3)) + ld3(S, rec + kRecZacc + 3);
+        zw = (cw + ld3(S, rec + kRecBF)) + zaw;
+        zv = (cv + ld3(S, rec + kRecBF + 3)) + zav;
     }
     // PH = P H; D = ~H PH; eps = f - ~H z (:294-296, :394)
     V3<R> PHw[N], PHv[N];
@@ -446,52 +552,80 @@ __device__ __forceinline__ bool pass2BodyImpl(const DevTables& T, int body0, int
 #pragma unroll
     for (int i = 0; i < 9; ++i) PP.F.a[i] = P.F.a[i] - mm[i];
 
-    // push P+ (shifted by -l) and Phi z+ into the parent's accumulators
+    // hand P+ (shifted by -l) and Phi z+ to the parent
     const int parent = T.parent[row];
     if (parent >= 0) {
         const V3<R> l = ld3(S, rec + kRecL);
-        const AB<R> Q = abshift(PP, l);
-        const int64_t pa = T.srec[body0 + parent] + kRecPacc;
-        S(pa + 0) += Q.M.xx; S(pa + 1) += Q.M.yy; S(pa + 2) += Q.M.zz;
-        S(pa + 3) += Q.M.xy; S(pa + 4) += Q.M.xz; S(pa + 5) += Q.M.yz;
-        S(pa + 6) += Q.J.xx; S(pa + 7) += Q.J.yy; S(pa + 8) += Q.J.zz;
-        S(pa + 9) += Q.J.xy; S(pa + 10) += Q.J.xz; S(pa + 11) += Q.J.yz;
+        cy.P = abshift(PP, l);
+        cy.zw = zpw + cross(l, zpv);
+        cy.zv = zpv;
+        if (!(info & F_CARRY)) {
+            const int pa = T.srec[body0 + parent] + kRecPacc;
+            S(pa + 0) += cy.P.M.xx; S(pa + 1) += cy.P.M.yy; S(pa + 2) += cy.P.M.zz;
+            S(pa + 3) += cy.P.M.xy; S(pa + 4) += cy.P.M.xz; S(pa + 5) += cy.P.M.yz;
+            S(pa + 6) += cy.P.J.xx; S(pa + 7) += cy.P.J.yy; S(pa + 8) += cy.P.J.zz;
+            S(pa + 9) += cy.P.J.xy; S(pa + 10) += cy.P.J.xz; S(pa + 11) += cy.P.J.yz;
 #pragma unroll
-        for (int i = 0; i < 9; ++i) S(pa + 12 + i) += Q.F.a[i];
-        const V3<R> tw = zpw + cross(l, zpv);
-        S(pa + 21) += tw.x; S(pa + 22) += tw.y; S(pa + 23) += tw.z;
-        S(pa + 24) += zpv.x; S(pa + 25) += zpv.y; S(pa + 26) += zpv.z;
+            for (int i = 0; i < 9; ++i) S(pa + 12 + i) += cy.P.F.a[i];
+            S(pa + 21) += cy.zw.x; S(pa + 22) += cy.zw.y; S(pa + 23) += cy.zw.z;
+            S(pa + 24) += cy.zv.x; S(pa + 25) += cy.zv.y; S(pa + 26) += cy.zv.z;
+        }
     }
     return ok;
 }
 
 // Free (6 columns) runs once per tree; kept out of line so its register
 // demand does not spill the common path.
-template <class R>
-__device__ __noinline__ bool pass2Free(const DevTables& T, int body0, int row, const Scr<R>& S, R m) {
-    return pass2BodyImpl<R, 6>(T, body0, row, 6, S, m);
+template <class R, int SS>
+__device__ __noinline__ bool pass2Free(const DevTables& T, int body0, int row, const Scr<R, SS>& S, R m,
+                                       bool haveCarry, Carry2<R>& cy) {
+    return pass2BodyImpl<R, 6, SS>(T, body0, row, 6, S, m, haveCarry, cy);
 }
 
 // ------------------------------------------------------------------ pass 3
-template <class R, int N, class Out>
-__device__ __forceinline__ void pass3Body(const DevTables& T, int body0, int row, int n, const Scr<R>& S, Out& out) {
-    const int64_t rec = T.srec[row];
-    const int64_t eH = rec + kRecH;
-    const int64_t ef = eH + 6 * n, eDI = ef + n, eG = eDI + n * n, eEps = eG + 6 * n;
+// udot = DI eps - ~G A+, A = A+ + H udot + a (RigidBodyNodeSpec.cpp:408-446).
+// With REF (mixed form) udot0 goes to the record and the outward half of the
+// double-float inverse dynamics runs alongside: A_df, then the body's own
+// force term F_df = Mk A_df + b - F_gravity.
+struct Carry3 {
+    V3<float> Aw, Av;
+    DF3 Dw, Dv;
+};
+template <class R> struct Carry3T { V3<R> Aw, Av; };
+
+template <class R, int N, int SS, bool REF, class Out>
+__device__ __forceinline__ void pass3BodyImpl(const DevTables& T, int body0, int row, int n, const Scr<R, SS>& S,
+                                              Out& out, Carry3T<R>& cy, DF3& cDw, DF3& cDv) {
+    const int info = T.info[row];
+    const int rec = T.srec[row];
+    const int eH = rec + kRecH;
+    const int ef = eH + 6 * n, eDI = ef + n, eG = eDI + n * n, eEps = eG + 6 * n, eU0 = eEps + n;
     const int parent = T.parent[row];
-    V3<R> Apw = z3<R>(), Apv = z3<R>();
     const V3<R> l = ld3(S, rec + kRecL);
+    V3<R> Apw = z3<R>(), Apv = z3<R>();
+    DF3 Dpw{}, Dpv{};
+    if constexpr (REF) { Dpw = DF3{dfq(0.f), dfq(0.f), dfq(0.f)}; Dpv = Dpw; }
     if (parent >= 0) {
-        const int64_t pe = T.srec[body0 + parent];
-        const V3<R> w = ld3(S, pe), v = ld3(S, pe + 3);
+        V3<R> w, v;
+        if (info & F_CARRY) {
+            w = cy.Aw; v = cy.Av;
+            if constexpr (REF) { Dpw = cDw; Dpv = cDv; }
+        } else {
+            const int pe = T.srec[body0 + parent];
+            w = ld3(S, pe); v = ld3(S, pe + 3);
+            if constexpr (REF) {
+                Dpw = DF3{DF{S(pe + 6), S(pe + 7)}, DF{S(pe + 8), S(pe + 9)}, DF{S(pe + 10), S(pe + 11)}};
+                Dpv = DF3{DF{S(pe + 12), S(pe + 13)}, DF{S(pe + 14), S(pe + 15)}, DF{S(pe + 16), S(pe + 17)}};
+            }
+        }
         Apw = w;
         Apv = v + cross(w, l);
+        if constexpr (REF) Dpv = Dpv - crossFD(l, Dpw);  // A_v + A_w x l = A_v - l x A_w, in df
     }
     R eps[N];
 #pragma unroll
     for (int j = 0; j < N; ++j) eps[j] = j < n ? S(eEps + j) : R(0);
     V3<R> Aw = Apw, Av = Apv;
-    const int uo = T.uoff[row];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
         if (i < n) {
@@ -500,44 +634,239 @@ __device__ __forceinline__ void pass3Body(const DevTables& T, int body0, int row
             for (int k = 0; k < N; ++k)
                 if (k < n) s = s + S(eDI + i * n + k) * eps[k];
             const R ud = s - (dot(ld3(S, eG + 6 * i), Apw) + dot(ld3(S, eG + 6 * i + 3), Apv));
-            out.udot(uo + i, ud);
-            Aw = axpy(Aw, ud, ld3(S, eH + 6 * i));
-            Av = axpy(Av, ud, ld3(S, eH + 6 * i + 3));
+            const V3<R> hw = ld3(S, eH + 6 * i), hv = ld3(S, eH + 6 * i + 3);
+            if constexpr (REF) {
+                S(eU0 + i) = ud;
+                Dpw = axpyDF(Dpw, ud, hw);
+                Dpv = axpyDF(Dpv, ud, hv);
+            } else {
+                out.udot(T.uoff[row] + i, ud);
+            }
+            Aw = axpy(Aw, ud, hw);
+            Av = axpy(Av, ud, hv);
         }
     }
-    Aw = Aw + ld3(S, rec + kRecA);
-    Av = Av + ld3(S, rec + kRecA + 3);
-    st3(S, rec, Aw);
-    st3(S, rec + 3, Av);
+    const V3<R> aw = ld3(S, rec + kRecA), av = ld3(S, rec + kRecA + 3);
+    Aw = Aw + aw;
+    Av = Av + av;
+    cy.Aw = Aw;
+    cy.Av = Av;
+    if (info & F_MEMCHILD) { st3(S, rec, Aw); st3(S, rec + 3, Av); }
+    if constexpr (REF) {
+        Dpw = Dpw + aw;
+        Dpv = Dpv + av;
+        cDw = Dpw;
+        cDv = Dpv;
+        if (info & F_MEMCHILD) {
+            S(rec + 6) = Dpw.x.hi; S(rec + 7) = Dpw.x.lo; S(rec + 8) = Dpw.y.hi; S(rec + 9) = Dpw.y.lo;
+            S(rec + 10) = Dpw.z.hi; S(rec + 11) = Dpw.z.lo;
+            S(rec + 12) = Dpv.x.hi; S(rec + 13) = Dpv.x.lo; S(rec + 14) = Dpv.y.hi; S(rec + 15) = Dpv.y.lo;
+            S(rec + 16) = Dpv.z.hi; S(rec + 17) = Dpv.z.lo;
+        }
+        // own inverse-dynamics force: Mk A + b - F (SpatialInertia*SpatialVec,
+        // MassProperties.h:1071-1072)
+        const R m = paramTable<R>(T)[(int64_t)row * kParamStride];
+        const V3<R> pc = ld3(S, rec + kRecPc);
+        const S3<R> Gi{S(rec + kRecGi), S(rec + kRecGi + 1), S(rec + kRecGi + 2), S(rec + kRecGi + 3),
+                       S(rec + kRecGi + 4), S(rec + kRecGi + 5)};
+        const DF3 Fw = scale(symMulDF(Gi, Dpw) + crossFD(pc, Dpv), m) + ld3(S, rec + kRecBF);
+        const DF3 Fv = scale(Dpv - crossFD(pc, Dpw), m) + ld3(S, rec + kRecBF + 3);
+        const int eF = rec + kRecFdf;
+        S(eF + 0) = Fw.x.hi; S(eF + 1) = Fw.x.lo; S(eF + 2) = Fw.y.hi; S(eF + 3) = Fw.y.lo;
+        S(eF + 4) = Fw.z.hi; S(eF + 5) = Fw.z.lo;
+        S(eF + 6) = Fv.x.hi; S(eF + 7) = Fv.x.lo; S(eF + 8) = Fv.y.hi; S(eF + 9) = Fv.y.lo;
+        S(eF + 10) = Fv.z.hi; S(eF + 11) = Fv.z.lo;
+        if (info & F_MEMACC)
+            for (int i = 0; i < 6; ++i) S(rec + kRecZ2acc + i) = R(0);
+    }
 }
 
-template <class R, class Out>
-__device__ __noinline__ void pass3Free(const DevTables& T, int body0, int row, const Scr<R>& S, Out& out) {
-    pass3Body<R, 6>(T, body0, row, 6, S, out);
+template <class R, int SS, bool REF, class Out>
+__device__ __noinline__ void pass3Free(const DevTables& T, int body0, int row, const Scr<R, SS>& S, Out& out,
+                                       Carry3T<R>& cy, DF3& cDw, DF3& cDv) {
+    pass3BodyImpl<R, 6, SS, REF>(T, body0, row, 6, S, out, cy, cDw, cDv);
 }
 
-// One RHS evaluation of one instance. Returns SBG_INST_* bits.
-template <class R, int NM, class Src, class Out>
-__device__ __noinline__ int rhsInstance(const DevTables& T, int inst, const Scr<R>& S, const Src& src, Out& out) {
+// ------------------------------------------------------- passes 4 and 5 (REF)
+// Pass 4 (tip to base): F_df = own + children (Phi F), r = f - ~H F_df, then
+// the first M^-1 pass on r: z2 = children Phi z2+, eps2 = r - ~H z2,
+// z2+ = z2 + G eps2 (RigidBodyNodeSpec.cpp:483-515).
+struct Carry4 { DF3 Fw, Fv; V3<float> zw, zv; };
+
+template <int N, int SS>
+__device__ __forceinline__ void pass4BodyImpl(const DevTables& T, int body0, int row, int n,
+                                              const Scr<float, SS>& S, bool haveCarry, Carry4& cy) {
+    const int info = T.info[row];
+    const int rec = T.srec[row];
+    const int eH = rec + kRecH;
+    const int ef = eH + 6 * n, eDI = ef + n, eG = eDI + n * n, eEps = eG + 6 * n;
+    const int eF = rec + kRecFdf;
+    DF3 Fw{DF{S(eF + 0), S(eF + 1)}, DF{S(eF + 2), S(eF + 3)}, DF{S(eF + 4), S(eF + 5)}};
+    DF3 Fv{DF{S(eF + 6), S(eF + 7)}, DF{S(eF + 8), S(eF + 9)}, DF{S(eF + 10), S(eF + 11)}};
+    V3<float> zw = z3<float>(), zv = z3<float>();
+    if (info & F_MEMACC) { zw = ld3(S, rec + kRecZ2acc); zv = ld3(S, rec + kRecZ2acc + 3); }
+    if (haveCarry) {
+        Fw = Fw + cy.Fw; Fv = Fv + cy.Fv;
+        zw = zw + cy.zw; zv = zv + cy.zv;
+    }
+    V3<float> zpw = zw, zpv = zv;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        if (j < n) {
+            const V3<float> hw = ld3(S, eH + 6 * j), hv = ld3(S, eH + 6 * j + 3);
+            const DF tau = dotFD(hw, Fw) + dotFD(hv, Fv);
+            const DF rr = dfq(S(ef + j)) - tau;
+            const float r = __fadd_rn(rr.hi, rr.lo);
+            const float e2 = r - (dot(hw, zw) + dot(hv, zv));
+            S(eEps + j) = e2;
+            zpw = axpy(zpw, e2, ld3(S, eG + 6 * j));
+            zpv = axpy(zpv, e2, ld3(S, eG + 6 * j + 3));
+        }
+    }
+    const int parent = T.parent[row];
+    if (parent >= 0) {
+        const V3<float> l = ld3(S, rec + kRecL);
+        cy.Fw = Fw + crossFD(l, Fv);
+        cy.Fv = Fv;
+        cy.zw = zpw + cross(l, zpv);
+        cy.zv = zpv;
+        if (!(info & F_CARRY)) {
+            const int pr = T.srec[body0 + parent];
+            const int pF = pr + kRecFdf;
+            DF3 a{DF{S(pF + 0), S(pF + 1)}, DF{S(pF + 2), S(pF + 3)}, DF{S(pF + 4), S(pF + 5)}};
+            DF3 b{DF{S(pF + 6), S(pF + 7)}, DF{S(pF + 8), S(pF + 9)}, DF{S(pF + 10), S(pF + 11)}};
+            a = a + cy.Fw;
+            b = b + cy.Fv;
+            S(pF + 0) = a.x.hi; S(pF + 1) = a.x.lo; S(pF + 2) = a.y.hi; S(pF + 3) = a.y.lo;
+            S(pF + 4) = a.z.hi; S(pF + 5) = a.z.lo;
+            S(pF + 6) = b.x.hi; S(pF + 7) = b.x.lo; S(pF + 8) = b.y.hi; S(pF + 9) = b.y.lo;
+            S(pF + 10) = b.z.hi; S(pF + 11) = b.z.lo;
+            const int pz = pr + kRecZ2acc;
+            S(pz + 0) += cy.zw.x; S(pz + 1) += cy.zw.y; S(pz + 2) += cy.zw.z;
+            S(pz + 3) += cy.zv.x; S(pz + 4) += cy.zv.y; S(pz + 5) += cy.zv.z;
+        }
+    }
+}
+
+template <int SS>
+__device__ __noinline__ void pass4Free(const DevTables& T, int body0, int row, const Scr<float, SS>& S,
+                                       bool haveCarry, Carry4& cy) {
+    pass4BodyImpl<6, SS>(T, body0, row, 6, S, haveCarry, cy);
+}
+
+// Pass 5 (base to tip): delta = DI eps2 - ~G A+, A = A+ + H delta; the result
+// udot = udot0 + delta (RigidBodyNodeSpec.cpp:521-552).
+template <int N, int SS, class Out>
+__device__ __forceinline__ void pass5BodyImpl(const DevTables& T, int body0, int row, int n,
+                                              const Scr<float, SS>& S, Out& out, Carry3T<float>& cy) {
+    const int info = T.info[row];
+    const int rec = T.srec[row];
+    const int eH = rec + kRecH;
+    const int ef = eH + 6 * n, eDI = ef + n, eG = eDI + n * n, eEps = eG + 6 * n, eU0 = eEps + n;
+    const int parent = T.parent[row];
+    V3<float> Apw = z3<float>(), Apv = z3<float>();
+    if (parent >= 0) {
+        V3<float> w, v;
+        if (info & F_CARRY) { w = cy.Aw; v = cy.Av; }
+        else {
+            const int pe = T.srec[body0 + parent];
+            w = ld3(S, pe); v = ld3(S, pe + 3);
+        }
+        const V3<float> l = ld3(S, rec + kRecL);
+        Apw = w;
+        Apv = v + cross(w, l);
+    }
+    float eps[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) eps[j] = j < n ? S(eEps + j) : 0.f;
+    V3<float> Aw = Apw, Av = Apv;
+    const int uo = T.uoff[row];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        if (i < n) {
+            float s = 0.f;
+#pragma unroll
+            for (int k = 0; k < N; ++k)
+                if (k < n) s = s + S(eDI + i * n + k) * eps[k];
+            const float d = s - (dot(ld3(S, eG + 6 * i), Apw) + dot(ld3(S, eG + 6 * i + 3), Apv));
+            out.udot(uo + i, S(eU0 + i) + d);
+            Aw = axpy(Aw, d, ld3(S, eH + 6 * i));
+            Av = axpy(Av, d, ld3(S, eH + 6 * i + 3));
+        }
+    }
+    cy.Aw = Aw;
+    cy.Av = Av;
+    if (info & F_MEMCHILD) { st3(S, rec, Aw); st3(S, rec + 3, Av); }
+}
+
+template <int SS, class Out>
+__device__ __noinline__ void pass5Free(const DevTables& T, int body0, int row, const Scr<float, SS>& S, Out& out,
+                                       Carry3T<float>& cy) {
+    pass5BodyImpl<6, SS>(T, body0, row, 6, S, out, cy);
+}
+
+// One RHS evaluation of one instance. Returns SBG_INST_* bits. REF turns on
+// the refinement step of the mixed form (R = float only).
+template <class R, int NM, int SS, bool REF, class Src, class Out>
+__device__ __noinline__ int rhsInstance(const DevTables& T, int inst, const Scr<R, SS>& S, const Src& src,
+                                        Out& out) {
+    static_assert(!REF || std::is_same<R, float>::value, "refinement is for the FP32 recursion");
     const int body0 = T.ibody[inst], nb = T.inb[inst];
     const V3<R> g = mk3(R(T.grav[3 * inst]), R(T.grav[3 * inst + 1]), R(T.grav[3 * inst + 2]));
     const R* PT = paramTable<R>(T);
-    pass1<R>(T, body0, nb, S, src, out, g);
+    pass1<R, SS>(T, body0, nb, S, src, out, g);
     bool ok = true;
-    for (int lb = nb - 1; lb >= 0; --lb) {
-        const int row = body0 + lb;
-        const int n = (T.info[row] >> 4) & 15;
-        const R m = PT[(int64_t)row * kParamStride];
-        if (n == 6) ok &= pass2Free<R>(T, body0, row, S, m);
-        else ok &= pass2BodyImpl<R, NM>(T, body0, row, n, S, m);
+    {
+        Carry2<R> cy;
+        bool have = false;
+        for (int lb = nb - 1; lb >= 0; --lb) {
+            const int row = body0 + lb;
+            const int info = T.info[row];
+            const int n = (info >> 4) & 15;
+            const R m = PT[(int64_t)row * kParamStride];
+            if (n == 6) ok &= pass2Free<R, SS>(T, body0, row, S, m, have, cy);
+            else ok &= pass2BodyImpl<R, NM, SS>(T, body0, row, n, S, m, have, cy);
+            have = (info & F_CARRY) != 0;
+        }
     }
-    for (int lb = 0; lb < nb; ++lb) {
-        const int row = body0 + lb;
-        const int n = (T.info[row] >> 4) & 15;
-        if (n == 6) pass3Free<R>(T, body0, row, S, out);
-        else pass3Body<R, NM>(T, body0, row, n, S, out);
+    {
+        Carry3T<R> cy{z3<R>(), z3<R>()};
+        DF3 cDw{}, cDv{};
+        for (int lb = 0; lb < nb; ++lb) {
+            const int row = body0 + lb;
+            const int n = (T.info[row] >> 4) & 15;
+            if (n == 6) pass3Free<R, SS, REF>(T, body0, row, S, out, cy, cDw, cDv);
+            else pass3BodyImpl<R, NM, SS, REF>(T, body0, row, n, S, out, cy, cDw, cDv);
+        }
+    }
+    if constexpr (REF) {
+        {
+            Carry4 cy;
+            bool have = false;
+            for (int lb = nb - 1; lb >= 0; --lb) {
+                const int row = body0 + lb;
+                const int info = T.info[row];
+                const int n = (info >> 4) & 15;
+                if (n == 6) pass4Free<SS>(T, body0, row, S, have, cy);
+                else pass4BodyImpl<NM, SS>(T, body0, row, n, S, have, cy);
+                have = (info & F_CARRY) != 0;
+            }
+        }
+        {
+            Carry3T<float> cy{z3<float>(), z3<float>()};
+            for (int lb = 0; lb < nb; ++lb) {
+                const int row = body0 + lb;
+                const int n = (T.info[row] >> 4) & 15;
+                if (n == 6) pass5Free<SS>(T, body0, row, S, out, cy);
+                else pass5BodyImpl<NM, SS>(T, body0, row, n, S, out, cy);
+            }
+        }
     }
     return ok ? 0 : SBG_INST_SINGULAR_D;
+}
+
+template <class R, int SS> __device__ __forceinline__ Scr<R, SS> scratchOf(const DevTables& T, R* scratch, int inst) {
+    return Scr<R, SS>{scratch + T.sbase[inst]};
 }
 
 // ------------------------------------------------------------ realize kernel
@@ -564,17 +893,17 @@ struct YdOut {
     }
 };
 
-template <class R, int NM>
+template <class R, int NM, int SS, bool REF>
 __global__ void __launch_bounds__(128) realizeKernel(DevTables T, const double* __restrict__ y,
                                                      double* __restrict__ ydot, R* __restrict__ scratch,
                                                      int32_t* __restrict__ status) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T.ninst) return;
     const int inst = T.order[t];
-    const Scr<R> S{scratch, T.sbase[inst], T.sstride[inst]};
+    const Scr<R, SS> S = scratchOf<R, SS>(T, scratch, inst);
     YSrc src{y, T.ybase[inst], T.ystride[inst], T.inq[inst]};
     YdOut out{ydot, T.ybase[inst], T.ystride[inst], T.inq[inst]};
-    int st = rhsInstance<R, NM>(T, inst, S, src, out);
+    int st = rhsInstance<R, NM, SS, REF>(T, inst, S, src, out);
     if (!out.finite) st |= SBG_INST_NONFINITE;
     status[inst] = st;
 }
@@ -603,17 +932,17 @@ struct MInvOut {
     }
 };
 
-template <class R, int NM>
+template <class R, int NM, int SS>
 __global__ void __launch_bounds__(128) minvKernel(DevTables T, const double* __restrict__ y,
                                                   const double* __restrict__ f, double* __restrict__ out,
                                                   R* __restrict__ scratch, int32_t* __restrict__ status) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T.ninst) return;
     const int inst = T.order[t];
-    const Scr<R> S{scratch, T.sbase[inst], T.sstride[inst]};
+    const Scr<R, SS> S = scratchOf<R, SS>(T, scratch, inst);
     MInvSrc src{y, f, T.ybase[inst], T.ystride[inst], T.inq[inst]};
     MInvOut o{out, T.ybase[inst], T.ystride[inst], T.inq[inst]};
-    int st = rhsInstance<R, NM>(T, inst, S, src, o);
+    int st = rhsInstance<R, NM, SS, false>(T, inst, S, src, o);
     if (!o.finite) st |= SBG_INST_NONFINITE;
     status[inst] = st;
 }
@@ -650,7 +979,7 @@ template <class F> struct FOut {
     template <class R> __device__ __forceinline__ void udot(int k, R v) { f[base + (int64_t)(nq + k) * stride] = F(v); finite &= isfinite(v); }
 };
 
-template <class R, int NM>
+template <class R, int NM, int SS, bool REF>
 __global__ void __launch_bounds__(128) rkMersonKernel(DevTables T, double* __restrict__ y, double* __restrict__ time,
                                                       R* __restrict__ fbuf, int64_t fplane, R* __restrict__ scratch,
                                                       int32_t* __restrict__ status, double h, int nsteps,
@@ -658,9 +987,9 @@ __global__ void __launch_bounds__(128) rkMersonKernel(DevTables T, double* __res
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T.ninst) return;
     const int inst = T.order[t];
-    const Scr<R> S{scratch, T.sbase[inst], T.sstride[inst]};
+    const Scr<R, SS> S = scratchOf<R, SS>(T, scratch, inst);
     const int64_t base = T.ybase[inst], stride = T.ystride[inst];
-    const int nq = T.inq[inst], nu = T.inu[inst], ny = nq + nu;
+    const int nq = T.inq[inst], nu = T.inu[inst];
     const int body0 = T.ibody[inst], nb = T.inb[inst];
     R* f0 = fbuf;
     R* fA = fbuf + fplane;
@@ -676,28 +1005,28 @@ __global__ void __launch_bounds__(128) rkMersonKernel(DevTables T, double* __res
         {
             StageSrc<R> src{y, f0, fA, fB, base, stride, nq, 0, 0.0};
             FOut<R> o{f0, base, stride, nq};
-            st |= rhsInstance<R, NM>(T, inst, S, src, o);
+            st |= rhsInstance<R, NM, SS, REF>(T, inst, S, src, o);
             if (!o.finite) st |= SBG_INST_NONFINITE;
         }
         {   // f1 -> fA
             StageSrc<R> src{y, f0, fA, fB, base, stride, nq, 1, hs / 3};
             FOut<R> o{fA, base, stride, nq};
-            st |= rhsInstance<R, NM>(T, inst, S, src, o);
+            st |= rhsInstance<R, NM, SS, REF>(T, inst, S, src, o);
         }
         {   // f2 -> fB   (input uses f1 in fA)
             StageSrc<R> src{y, f0, fA, fB, base, stride, nq, 2, hs / 6};
             FOut<R> o{fB, base, stride, nq};
-            st |= rhsInstance<R, NM>(T, inst, S, src, o);
+            st |= rhsInstance<R, NM, SS, REF>(T, inst, S, src, o);
         }
         {   // f3 -> fC   (input uses f2 in fB)
             StageSrc<R> src{y, f0, fB, fB, base, stride, nq, 3, hs / 8};
             FOut<R> o{fC, base, stride, nq};
-            st |= rhsInstance<R, NM>(T, inst, S, src, o);
+            st |= rhsInstance<R, NM, SS, REF>(T, inst, S, src, o);
         }
         {   // f4 -> fA   (ysave input uses f2 in fB, f3 in fC)
             StageSrc<R> src{y, f0, fB, fC, base, stride, nq, 4, hs / 2};
             FOut<R> o{fA, base, stride, nq};
-            st |= rhsInstance<R, NM>(T, inst, S, src, o);
+            st |= rhsInstance<R, NM, SS, REF>(T, inst, S, src, o);
         }
         // y1 = y0 + h/6 (f0 + 4 f3 + f4); yerr = 0.2 |y1 - ysave|; error norm
         // (RungeKuttaMersonIntegrator.cpp:124-139, IntegratorRep.h:454-523).

@@ -56,6 +56,7 @@ struct sbg_batch_s {
     int64_t budget = 0;
     int ninst = 0;
     int nm = 3;
+    bool tiled = false;
     cudaStream_t stream = nullptr;
     std::vector<int32_t> instTopo;
     std::vector<int64_t> hostYOff, hostUOff;  // packed host offsets (n+1)
@@ -194,6 +195,9 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
         if (isIdentityR(b.X_BM)) info |= 1 << 9;
         if (b.X_BM[9] == 0 && b.X_BM[10] == 0 && b.X_BM[11] == 0) info |= 1 << 10;
         if (b.X_PF[9] == 0 && b.X_PF[10] == 0 && b.X_PF[11] == 0) info |= 1 << 11;
+        if (b.parent != 0 && rowOf[b.parent] == r - 1) info |= F_CARRY;
+        for (int c = bi + 1; c <= nb; ++c)
+            if (d->bodies[c - 1].parent == bi && rowOf[c] != r + 1) info |= F_MEMCHILD;
         t->parent.push_back(b.parent == 0 ? -1 : rowOf[b.parent]);
         t->info.push_back(info);
         t->qoff.push_back(qo[bi]);
@@ -258,7 +262,7 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
                      const sbg_batch_config* cfg, sbg_batch* out) {
     if (!topos || ntopo < 1 || !instTopo || ninst < 0 || !out) return fail(SBG_ERR_INVALID, "bad batch arguments");
     const int precision = cfg ? cfg->precision : SBG_PRECISION_FP64;
-    if (precision != SBG_PRECISION_FP64 && precision != SBG_PRECISION_MIXED)
+    if (precision != SBG_PRECISION_FP64 && precision != SBG_PRECISION_MIXED && precision != SBG_PRECISION_MIXED_FAST)
         return fail(SBG_ERR_INVALID, "unknown precision");
     for (int i = 0; i < ninst; ++i)
         if (instTopo[i] < 0 || instTopo[i] >= ntopo || !topos[instTopo[i]])
@@ -334,8 +338,10 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
         b->hostYOff[i + 1] = b->hostYOff[i] + t->nq + t->nu;
         b->hostUOff[i + 1] = b->hostUOff[i] + t->nu;
         if (uniform) {
+            // warp-tiled scratch: element e of instance i at
+            // (i / 32) * 32 * recSize + e * 32 + i % 32
             ybase[i] = i; ystride[i] = ninst;
-            sbase[i] = i; sstride[i] = ninst;
+            sbase[i] = (int64_t)(i / kTile) * kTile * t->recSize + (i % kTile); sstride[i] = kTile;
         } else {
             ybase[i] = b->hostYOff[i]; ystride[i] = 1;
             sbase[i] = sOff; sstride[i] = 1;
@@ -345,7 +351,9 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     b->nyTotal = b->hostYOff[ninst];
     b->nuTotal = b->hostUOff[ninst];
     b->colElems = b->nyTotal;
-    b->scratchElems = uniform ? (ninst ? topos[instTopo[0]]->recSize * (int64_t)ninst : 0) : sOff;
+    b->tiled = uniform;
+    b->scratchElems = uniform ? (ninst ? topos[instTopo[0]]->recSize * (int64_t)((ninst + kTile - 1) / kTile) * kTile : 0)
+                              : sOff;
     // threads take instances in decreasing body count so a warp's lanes walk
     // trees of similar size
     std::iota(order.begin(), order.end(), 0);
@@ -473,7 +481,7 @@ int sbg_realize_acceleration_async(sbg_batch b) {
     if (!b) return fail(SBG_ERR_INVALID, "null batch");
     if (!b->stateSet) return fail(SBG_ERR_STATE, "no state has been set");
     SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
-    SBG_CUDA(launchRealize(b->T, b->precision, b->nm, b->y, b->ydot, b->scratch, b->status, b->stream),
+    SBG_CUDA(launchRealize(b->T, b->precision, b->nm, b->tiled, b->y, b->ydot, b->scratch, b->status, b->stream),
              "realize kernel launch");
     ++b->launches;
     return SBG_OK;
@@ -508,7 +516,7 @@ int sbg_multiply_by_minv(sbg_batch b, const double* f, double* outp) {
     std::memcpy(b->hostPinned, f, bytes);
     SBG_CUDA(cudaMemcpyAsync(b->staging, b->hostPinned, bytes, cudaMemcpyHostToDevice, b->stream), "force upload");
     SBG_CUDA(launchScatter(b->T, b->dHostUOff, b->staging, b->fcol, 1, b->stream), "force scatter");
-    SBG_CUDA(launchMInv(b->T, b->precision, b->nm, b->y, b->fcol, b->ydot, b->scratch, b->status, b->stream),
+    SBG_CUDA(launchMInv(b->T, b->precision, b->nm, b->tiled, b->y, b->fcol, b->ydot, b->scratch, b->status, b->stream),
              "M^-1 kernel launch");
     SBG_CUDA(launchGather(b->T, b->dHostUOff, b->ydot, b->staging, 1, b->stream), "result gather");
     b->launches += 3;
@@ -534,7 +542,7 @@ int sbg_rk_merson_fixed_async(sbg_batch b, double h, int32_t nsteps, const sbg_i
     SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
     SBG_CUDA(cudaMemsetAsync(b->status, 0, std::max(b->ninst, 1) * sizeof(int32_t), b->stream), "status reset");
     SBG_CUDA(launchNormalizeQuat(b->T, b->y, b->stream), "initialize");
-    SBG_CUDA(launchRKMerson(b->T, b->precision, b->nm, b->y, b->time, b->fbuf, b->colElems, b->scratch, b->status, h,
+    SBG_CUDA(launchRKMerson(b->T, b->precision, b->nm, b->tiled, b->y, b->time, b->fbuf, b->colElems, b->scratch, b->status, h,
                             nsteps, acc, ctol, pes, b->stream),
              "RK-Merson kernel launch");
     b->launches += 2;

@@ -29,18 +29,36 @@ constexpr int kParamStride = 34;
 constexpr int kMaxDof = 6;
 
 // Scratch record of one body (elements of the arithmetic type R), n = ndof:
-//   0  R_GB[9] p_GB[3] V_GB[6]   kinematics; reused for A_GB[6] in pass 3
+//   0  R_GB[9] p_GB[3] V_GB[6]  kinematics (only for children that are not the
+//                               next row); pass 3 reuses [0,6) for A_GB and,
+//                               in the mixed form, [6,18) for A in double-float
 //  18  pc[3] Gi[6] l[3] a[6] bF[6]
-//  42  Pacc: M[6] J[6] F[9], zacc[6]
-//  69  H[6n] f[n] DI[n*n] G[6n] eps[n]
+//  42  Pacc: M[6] J[6] F[9], zacc[6]      (pass 2 accumulators)
+//      reused after pass 2: [42,54) F_df (double-float inverse-dynamics force),
+//      [54,60) z2acc (refinement M^-1 accumulator)
+//  69  H[6n] f[n] DI[n*n] G[6n] eps[n] udot0[n]
 #ifdef __CUDACC__
 #define SBG_HD __host__ __device__
 #else
 #define SBG_HD
 #endif
-SBG_HD constexpr int scratchRecordSize(int n) { return 69 + 14 * n + n * n; }
+SBG_HD constexpr int scratchRecordSize(int n) { return 69 + 15 * n + n * n; }
 constexpr int kRecKin = 0, kRecPc = 18, kRecGi = 21, kRecL = 27, kRecA = 30, kRecBF = 36, kRecPacc = 42,
-              kRecZacc = 63, kRecH = 69;
+              kRecZacc = 63, kRecH = 69, kRecFdf = 42, kRecZ2acc = 54;
+
+// Body-table info word: mobilizer | ndof << 4 | flags.
+enum : int {
+    F_RPF_I = 1 << 8,      // R_PF is the identity
+    F_RMB_I = 1 << 9,      // R_BM is the identity
+    F_PMB_0 = 1 << 10,     // p_BM is zero
+    F_PPF_0 = 1 << 11,     // p_PF is zero
+    F_CARRY = 1 << 12,     // the parent is the previous row: values travel in registers
+    F_MEMCHILD = 1 << 13,  // some child is not the next row: it reads/accumulates through the record
+};
+constexpr int F_MEMACC = F_MEMCHILD;
+
+// Warp tile of the shared-topology scratch layout.
+constexpr int kTile = 32;
 
 struct DevTables {
     const int32_t* parent;

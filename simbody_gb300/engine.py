@@ -67,7 +67,7 @@ class Batch:
         self.topologies = list(topologies)
         self.instance_topology = np.ascontiguousarray(instance_topology, dtype=np.int32)
         self.ninst = len(self.instance_topology)
-        prec = {"fp64": N.PRECISION_FP64, "mixed": N.PRECISION_MIXED}[precision]
+        prec = {"fp64": N.PRECISION_FP64, "mixed": N.PRECISION_MIXED, "mixed_fast": N.PRECISION_MIXED_FAST}[precision]
         self.precision = precision
         cfg = N.BatchConfig(prec, device, int(device_budget_bytes))
         handles = (C.c_void_p * len(self.topologies))(*[t.handle for t in self.topologies])

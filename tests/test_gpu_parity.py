@@ -34,8 +34,14 @@ def test_realize_fp64_matches_oracle(engine, config, n):
     assert err.max() <= 1e-12, err.max()
 
 
-@pytest.mark.parametrize("config,n", [(2, 512), (3, 128), (4, 64)])
+def _udot(d, b):
+    return np.concatenate([d[b.y_offsets[i] + b.nq[i]:b.y_offsets[i + 1]] for i in range(b.ninst)])
+
+
+@pytest.mark.parametrize("config,n", [(1, 512), (2, 2048), (3, 512), (4, 256)])
 def test_realize_mixed_udot_error(engine, config, n):
+    """Mixed form (FP32 recursions + double-float residual refinement):
+    relative udot error per instance <= 1e-5 against FP64."""
     w = Workload(config, n)
     b64, y0 = engine_batch(w, "fp64")
     b32, _ = engine_batch(w, "mixed")
@@ -44,10 +50,43 @@ def test_realize_mixed_udot_error(engine, config, n):
     d64, _ = b64.realize_acceleration()
     d32, st = b32.realize_acceleration()
     assert (st == 0).all()
-    udot64 = np.concatenate([d64[b64.y_offsets[i] + b64.nq[i]:b64.y_offsets[i + 1]] for i in range(b64.ninst)])
-    udot32 = np.concatenate([d32[b32.y_offsets[i] + b32.nq[i]:b32.y_offsets[i + 1]] for i in range(b32.ninst)])
-    err = rel_err_per_instance(udot32, udot64, b64.u_offsets)
+    err = rel_err_per_instance(_udot(d32, b32), _udot(d64, b64), b64.u_offsets)
     assert err.max() <= 1e-5, err.max()
+    # qdot = N(q) u is part of the same RHS
+    assert rel_err_per_instance(d32, d64, b64.y_offsets).max() <= 1e-5
+
+
+@pytest.mark.parametrize("config,n", [(2, 512), (3, 256)])
+def test_realize_mixed_fast_is_plain_fp32(engine, config, n):
+    """Without refinement the FP32 recursion alone is within FP32 reach."""
+    w = Workload(config, n)
+    b64, y0 = engine_batch(w, "fp64")
+    bf, _ = engine_batch(w, "mixed_fast")
+    b64.set_state(y0)
+    bf.set_state(y0)
+    d64, _ = b64.realize_acceleration()
+    df, st = bf.realize_acceleration()
+    assert (st == 0).all()
+    err = rel_err_per_instance(_udot(df, bf), _udot(d64, b64), b64.u_offsets)
+    assert err.max() <= 1e-3, err.max()
+
+
+@pytest.mark.parametrize("config,n,steps,tol", [(1, 256, 50, 1e-6), (3, 64, 20, 1e-6), (4, 32, 20, 1e-6)])
+def test_rk_merson_mixed_short_horizon(engine, config, n, steps, tol):
+    """FP32 recursions with FP64 state accumulation stay close to the FP64
+    trajectory over a short horizon."""
+    w = Workload(config, n)
+    b64, y0 = engine_batch(w, "fp64")
+    bm, _ = engine_batch(w, "mixed")
+    b64.set_state(y0)
+    bm.set_state(y0)
+    b64.rk_merson_fixed(w.h, steps)
+    st = bm.rk_merson_fixed(w.h, steps)
+    assert (st & ~4 == 0).all()
+    y64, _ = b64.get_state()
+    ym, _ = bm.get_state()
+    err = rel_err_per_instance(ym, y64, b64.y_offsets)
+    assert err.max() <= tol, err.max()
 
 
 @pytest.mark.parametrize("config,n,steps", [(1, 256, 50), (3, 64, 20), (4, 32, 20)])
