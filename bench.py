@@ -257,6 +257,7 @@ def run_ours(args):
         "fp_work": {"flops_per_instance_fp64_algorithm": flops_inst,
                     "achieved_tflops": flops_inst * w.ninst / (ms_mx * 1e-3) / 1e12},
         "gpu_launches": launches,
+        "kernel_variant": bmx.kernel_variant,
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

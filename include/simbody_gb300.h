@@ -225,6 +225,10 @@ int sbg_batch_get_ydot(sbg_batch batch, double* ydot, int32_t* status);
 int sbg_batch_sync(sbg_batch batch);
 /* Number of kernel launches issued by this batch since creation. */
 int64_t sbg_batch_launch_count(sbg_batch batch);
+/* Occupancy variant the batch's tuner picked for its FP32 kernels (1 = two
+ * 128-thread blocks per SM, 4 = four), 0 before the first realize or
+ * integration, -1 for a null batch. No counterpart in the reference. */
+int sbg_batch_kernel_variant(sbg_batch batch);
 
 /* ------------------------------------------------ allocation-free realize */
 

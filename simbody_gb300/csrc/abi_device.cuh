@@ -125,7 +125,7 @@ __device__ __forceinline__ DF3 symMulDF(const S3<float>& S, DF3 v) {
 
 // ------------------------------------------------------------------ pass 1
 // Src::q(k), Src::u(k) give the (double) state; Out::qdot(k, v) receives qdot.
-template <class R, int SS, class Src, class Out>
+template <class R, int NM, int SS, class Src, class Out>
 __device__ __forceinline__ void pass1(const DevTables& T, int body0, int nb, const Scr<R, SS>& S, const Src& src,
                                       Out& out, V3<R> g) {
     const R* PT = paramTable<R>(T);
@@ -137,6 +137,7 @@ __device__ __forceinline__ void pass1(const DevTables& T, int body0, int nb, con
         const int row = body0 + lb;
         const int info = T.info[row];
         const int type = info & 15, n = (info >> 4) & 15;
+        const int nw = n == 6 ? 6 : NM;  // padded record width of this row
         const int parent = T.parent[row];
         const int qo = T.qoff[row], uo = T.uoff[row];
         const int rec = T.srec[row];
@@ -331,7 +332,7 @@ __device__ __forceinline__ void pass1(const DevTables& T, int body0, int nb, con
         else { st3(S, rec + kRecBF, bw - Fw); st3(S, rec + kRecBF + 3, bv - Fv); }
         if (info & F_MEMACC)
             for (int i = 0; i < 27; ++i) S(rec + kRecPacc + i) = R(0);
-        const int ef = eH + 6 * n;
+        const int ef = eH + 6 * nw;
         for (int j = 0; j < n; ++j) S(ef + j) = f[j];
     }
 }
@@ -447,7 +448,7 @@ __device__ __forceinline__ bool pass2BodyImpl(const DevTables& T, int body0, int
     const int info = T.info[row];
     const int rec = T.srec[row];
     const int eH = rec + kRecH;
-    const int ef = eH + 6 * n, eDI = ef + n, eG = eDI + n * n, eEps = eG + 6 * n;
+    const int ef = eH + 6 * N, eDI = ef + N, eG = eDI + N * N, eEps = eG + 6 * N;
     // P = ArticulatedInertia(Mk) + children (RigidBodyNodeSpec.cpp:259-279)
     AB<R> P;
     V3<R> zaw = z3<R>(), zav = z3<R>();
@@ -543,7 +544,7 @@ __device__ __forceinline__ bool pass2BodyImpl(const DevTables& T, int body0, int
     for (int i = 0; i < N; ++i)
 #pragma unroll
         for (int j = 0; j < N; ++j)
-            if (i < n && j < n) S(eDI + i * n + j) = DI[i * N + j];
+            if (i < n && j < n) S(eDI + i * N + j) = DI[i * N + j];
     AB<R> PP;
     PP.M = S3<R>{P.M.xx - ms[0], P.M.yy - ms[4], P.M.zz - ms[8], P.M.xy - (ms[3] + ms[1]) / R(2),
                  P.M.xz - (ms[6] + ms[2]) / R(2), P.M.yz - (ms[7] + ms[5]) / R(2)};
@@ -599,7 +600,7 @@ __device__ __forceinline__ void pass3BodyImpl(const DevTables& T, int body0, int
     const int info = T.info[row];
     const int rec = T.srec[row];
     const int eH = rec + kRecH;
-    const int ef = eH + 6 * n, eDI = ef + n, eG = eDI + n * n, eEps = eG + 6 * n, eU0 = eEps + n;
+    const int ef = eH + 6 * N, eDI = ef + N, eG = eDI + N * N, eEps = eG + 6 * N, eU0 = eEps + N;
     const int parent = T.parent[row];
     const V3<R> l = ld3(S, rec + kRecL);
     V3<R> Apw = z3<R>(), Apv = z3<R>();
@@ -632,7 +633,7 @@ __device__ __forceinline__ void pass3BodyImpl(const DevTables& T, int body0, int
             R s = R(0);
 #pragma unroll
             for (int k = 0; k < N; ++k)
-                if (k < n) s = s + S(eDI + i * n + k) * eps[k];
+                if (k < n) s = s + S(eDI + i * N + k) * eps[k];
             const R ud = s - (dot(ld3(S, eG + 6 * i), Apw) + dot(ld3(S, eG + 6 * i + 3), Apv));
             const V3<R> hw = ld3(S, eH + 6 * i), hv = ld3(S, eH + 6 * i + 3);
             if constexpr (REF) {
@@ -699,7 +700,7 @@ __device__ __forceinline__ void pass4BodyImpl(const DevTables& T, int body0, int
     const int info = T.info[row];
     const int rec = T.srec[row];
     const int eH = rec + kRecH;
-    const int ef = eH + 6 * n, eDI = ef + n, eG = eDI + n * n, eEps = eG + 6 * n;
+    const int ef = eH + 6 * N, eDI = ef + N, eG = eDI + N * N, eEps = eG + 6 * N;
     const int eF = rec + kRecFdf;
     DF3 Fw{DF{S(eF + 0), S(eF + 1)}, DF{S(eF + 2), S(eF + 3)}, DF{S(eF + 4), S(eF + 5)}};
     DF3 Fv{DF{S(eF + 6), S(eF + 7)}, DF{S(eF + 8), S(eF + 9)}, DF{S(eF + 10), S(eF + 11)}};
@@ -762,7 +763,7 @@ __device__ __forceinline__ void pass5BodyImpl(const DevTables& T, int body0, int
     const int info = T.info[row];
     const int rec = T.srec[row];
     const int eH = rec + kRecH;
-    const int ef = eH + 6 * n, eDI = ef + n, eG = eDI + n * n, eEps = eG + 6 * n, eU0 = eEps + n;
+    const int ef = eH + 6 * N, eDI = ef + N, eG = eDI + N * N, eEps = eG + 6 * N, eU0 = eEps + N;
     const int parent = T.parent[row];
     V3<float> Apw = z3<float>(), Apv = z3<float>();
     if (parent >= 0) {
@@ -787,7 +788,7 @@ __device__ __forceinline__ void pass5BodyImpl(const DevTables& T, int body0, int
             float s = 0.f;
 #pragma unroll
             for (int k = 0; k < N; ++k)
-                if (k < n) s = s + S(eDI + i * n + k) * eps[k];
+                if (k < n) s = s + S(eDI + i * N + k) * eps[k];
             const float d = s - (dot(ld3(S, eG + 6 * i), Apw) + dot(ld3(S, eG + 6 * i + 3), Apv));
             out.udot(uo + i, S(eU0 + i) + d);
             Aw = axpy(Aw, d, ld3(S, eH + 6 * i));
@@ -814,7 +815,7 @@ __device__ __noinline__ int rhsInstance(const DevTables& T, int inst, const Scr<
     const int body0 = T.ibody[inst], nb = T.inb[inst];
     const V3<R> g = mk3(R(T.grav[3 * inst]), R(T.grav[3 * inst + 1]), R(T.grav[3 * inst + 2]));
     const R* PT = paramTable<R>(T);
-    pass1<R, SS>(T, body0, nb, S, src, out, g);
+    pass1<R, NM, SS>(T, body0, nb, S, src, out, g);
     bool ok = true;
     {
         Carry2<R> cy;
@@ -893,8 +894,8 @@ struct YdOut {
     }
 };
 
-template <class R, int NM, int SS, bool REF>
-__global__ void __launch_bounds__(128) realizeKernel(DevTables T, const double* __restrict__ y,
+template <class R, int NM, int SS, bool REF, int MINB = 1>
+__global__ void __launch_bounds__(128, MINB) realizeKernel(DevTables T, const double* __restrict__ y,
                                                      double* __restrict__ ydot, R* __restrict__ scratch,
                                                      int32_t* __restrict__ status) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -979,8 +980,8 @@ template <class F> struct FOut {
     template <class R> __device__ __forceinline__ void udot(int k, R v) { f[base + (int64_t)(nq + k) * stride] = F(v); finite &= isfinite(v); }
 };
 
-template <class R, int NM, int SS, bool REF>
-__global__ void __launch_bounds__(128) rkMersonKernel(DevTables T, double* __restrict__ y, double* __restrict__ time,
+template <class R, int NM, int SS, bool REF, int MINB = 1>
+__global__ void __launch_bounds__(128, MINB) rkMersonKernel(DevTables T, double* __restrict__ y, double* __restrict__ time,
                                                       R* __restrict__ fbuf, int64_t fplane, R* __restrict__ scratch,
                                                       int32_t* __restrict__ status, double h, int nsteps,
                                                       double accuracy, double consTol, int projectEveryStep) {

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <numeric>
@@ -57,6 +58,7 @@ struct sbg_batch_s {
     int ninst = 0;
     int nm = 3;
     bool tiled = false;
+    int variant = 0;  // kernel occupancy variant: 0 = not tuned yet, 1 or 4
     cudaStream_t stream = nullptr;
     std::vector<int32_t> instTopo;
     std::vector<int64_t> hostYOff, hostUOff;  // packed host offsets (n+1)
@@ -292,12 +294,16 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
         if (e != cudaSuccess) return bail(cudaFail(e, "cudaStreamCreate"));
     }
 
+    // batch width: 1 when every non-Free body has one mobility, else 3
+    int nm = 1;
+    for (int i = 0; i < ninst; ++i)
+        if (topos[instTopo[i]]->maxNonFreeDof > 1) nm = 3;
     // distinct topologies used, concatenated body tables
     std::vector<int> used(ntopo, -1);
+    std::vector<int64_t> recTotal(ntopo, 0);
     std::vector<int32_t> parent, info, qoff, uoff, srec, fbeg, fcnt, fkw;
     std::vector<double> par, fcoef, fq0;
     std::vector<int32_t> rowBase(ntopo, 0);
-    int nm = 1;
     for (int i = 0; i < ninst; ++i) {
         const int k = instTopo[i];
         if (used[k] >= 0) continue;
@@ -309,25 +315,28 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
         info.insert(info.end(), t->info.begin(), t->info.end());
         qoff.insert(qoff.end(), t->qoff.begin(), t->qoff.end());
         uoff.insert(uoff.end(), t->uoff.begin(), t->uoff.end());
-        srec.insert(srec.end(), t->srec.begin(), t->srec.end());
+        const std::vector<int32_t> pr = paddedRecords(*t, nm, &recTotal[k]);
+        srec.insert(srec.end(), pr.begin(), pr.end());
         for (int32_t fb : t->fbeg) fbeg.push_back(fb + fOff);
         fcnt.insert(fcnt.end(), t->fcnt.begin(), t->fcnt.end());
         fkw.insert(fkw.end(), t->fkw.begin(), t->fkw.end());
         fcoef.insert(fcoef.end(), t->fcoef.begin(), t->fcoef.end());
         fq0.insert(fq0.end(), t->fq0.begin(), t->fq0.end());
         par.insert(par.end(), t->par.begin(), t->par.end());
-        if (t->maxNonFreeDof > 1) nm = 3;
     }
     b->nm = nm;
     const bool uniform = ninst > 0 && std::all_of(instTopo, instTopo + ninst, [&](int32_t k) { return k == instTopo[0]; });
 
-    // instance table and column addressing
+    // instance table and column addressing. Threads take instances in
+    // decreasing body count so a warp's lanes walk trees of similar size;
+    // every 32 consecutive threads form a tile whose state columns and
+    // scratch records interleave lane by lane (element e of the lane-l
+    // instance at tileBase + e*32 + l), padded to the tile's largest instance.
     std::vector<int32_t> ibody(ninst), inb(ninst), inq(ninst), inu(ninst), order(ninst);
     std::vector<int64_t> ybase(ninst), ystride(ninst), sbase(ninst), sstride(ninst);
     std::vector<double> grav(3 * (size_t)ninst);
     b->hostYOff.assign(ninst + 1, 0);
     b->hostUOff.assign(ninst + 1, 0);
-    int64_t sOff = 0;
     for (int i = 0; i < ninst; ++i) {
         const sbg_topology_s* t = topos[instTopo[i]];
         ibody[i] = rowBase[instTopo[i]];
@@ -337,27 +346,33 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
         for (int k = 0; k < 3; ++k) grav[3 * i + k] = t->gravity[k];
         b->hostYOff[i + 1] = b->hostYOff[i] + t->nq + t->nu;
         b->hostUOff[i + 1] = b->hostUOff[i] + t->nu;
-        if (uniform) {
-            // warp-tiled scratch: element e of instance i at
-            // (i / 32) * 32 * recSize + e * 32 + i % 32
-            ybase[i] = i; ystride[i] = ninst;
-            sbase[i] = (int64_t)(i / kTile) * kTile * t->recSize + (i % kTile); sstride[i] = kTile;
-        } else {
-            ybase[i] = b->hostYOff[i]; ystride[i] = 1;
-            sbase[i] = sOff; sstride[i] = 1;
-            sOff += t->recSize;
+    }
+    std::iota(order.begin(), order.end(), 0);
+    if (!uniform) std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return inb[a] > inb[c]; });
+    int64_t yOff = 0, sOff = 0;
+    for (int t0 = 0; t0 < ninst; t0 += kTile) {
+        const int t1 = std::min(ninst, t0 + kTile);
+        int64_t yw = 0, sw = 0;
+        for (int p = t0; p < t1; ++p) {
+            const int i = order[p];
+            yw = std::max<int64_t>(yw, inq[i] + inu[i]);
+            sw = std::max<int64_t>(sw, recTotal[instTopo[i]]);
         }
+        for (int p = t0; p < t1; ++p) {
+            const int i = order[p];
+            ybase[i] = yOff + (p - t0); ystride[i] = kTile;
+            sbase[i] = sOff + (p - t0); sstride[i] = kTile;
+        }
+        yOff += yw * kTile;
+        sOff += sw * kTile;
     }
     b->nyTotal = b->hostYOff[ninst];
     b->nuTotal = b->hostUOff[ninst];
-    b->colElems = b->nyTotal;
-    b->tiled = uniform;
-    b->scratchElems = uniform ? (ninst ? topos[instTopo[0]]->recSize * (int64_t)((ninst + kTile - 1) / kTile) * kTile : 0)
-                              : sOff;
-    // threads take instances in decreasing body count so a warp's lanes walk
-    // trees of similar size
-    std::iota(order.begin(), order.end(), 0);
-    if (!uniform) std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return inb[a] > inb[c]; });
+    b->colElems = yOff;
+    b->scratchElems = sOff;
+    b->tiled = true;
+    if (precision == SBG_PRECISION_FP64) b->variant = 1;  // FP64 needs every register
+    if (const char* v = std::getenv("SBG_VARIANT")) b->variant = std::atoi(v) == 4 ? 4 : 1;
 
     int rc = 0;
     DevTables& T = b->T;
@@ -477,11 +492,46 @@ int sbg_batch_get_state(sbg_batch b, double* t, double* y) {
     return SBG_OK;
 }
 
+// Occupancy tuner: the FP32 kernels come in two register budgets (all the
+// registers they want, 2 blocks of 128 threads per SM; or at most 128, 4
+// blocks per SM with a few spills). The first realize or integration of a
+// batch times both on the batch's own state and keeps the faster.
+static int tuneVariant(sbg_batch b) {
+    if (b->variant != 0) return SBG_OK;
+    cudaEvent_t e0, e1;
+    SBG_CUDA(cudaEventCreate(&e0), "tuner");
+    SBG_CUDA(cudaEventCreate(&e1), "tuner");
+    float best = 1e30f;
+    int bestV = 1;
+    for (int v : {1, 4}) {
+        for (int rep = 0; rep < 2; ++rep)
+            SBG_CUDA(launchRealize(b->T, b->precision, b->nm, v, b->y, b->ydot, b->scratch, b->status, b->stream),
+                     "tuner launch");
+        SBG_CUDA(cudaEventRecord(e0, b->stream), "tuner");
+        for (int rep = 0; rep < 3; ++rep)
+            SBG_CUDA(launchRealize(b->T, b->precision, b->nm, v, b->y, b->ydot, b->scratch, b->status, b->stream),
+                     "tuner launch");
+        SBG_CUDA(cudaEventRecord(e1, b->stream), "tuner");
+        SBG_CUDA(cudaEventSynchronize(e1), "tuner");
+        float ms = 0;
+        SBG_CUDA(cudaEventElapsedTime(&ms, e0, e1), "tuner");
+        b->launches += 5;
+        if (ms < best) { best = ms; bestV = v; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->variant = bestV;
+    return SBG_OK;
+}
+
+int sbg_batch_kernel_variant(sbg_batch b) { return b ? b->variant : -1; }
+
 int sbg_realize_acceleration_async(sbg_batch b) {
     if (!b) return fail(SBG_ERR_INVALID, "null batch");
     if (!b->stateSet) return fail(SBG_ERR_STATE, "no state has been set");
     SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
-    SBG_CUDA(launchRealize(b->T, b->precision, b->nm, b->tiled, b->y, b->ydot, b->scratch, b->status, b->stream),
+    if (int rc = tuneVariant(b)) return rc;
+    SBG_CUDA(launchRealize(b->T, b->precision, b->nm, b->variant, b->y, b->ydot, b->scratch, b->status, b->stream),
              "realize kernel launch");
     ++b->launches;
     return SBG_OK;
@@ -516,7 +566,7 @@ int sbg_multiply_by_minv(sbg_batch b, const double* f, double* outp) {
     std::memcpy(b->hostPinned, f, bytes);
     SBG_CUDA(cudaMemcpyAsync(b->staging, b->hostPinned, bytes, cudaMemcpyHostToDevice, b->stream), "force upload");
     SBG_CUDA(launchScatter(b->T, b->dHostUOff, b->staging, b->fcol, 1, b->stream), "force scatter");
-    SBG_CUDA(launchMInv(b->T, b->precision, b->nm, b->tiled, b->y, b->fcol, b->ydot, b->scratch, b->status, b->stream),
+    SBG_CUDA(launchMInv(b->T, b->precision, b->nm, b->y, b->fcol, b->ydot, b->scratch, b->status, b->stream),
              "M^-1 kernel launch");
     SBG_CUDA(launchGather(b->T, b->dHostUOff, b->ydot, b->staging, 1, b->stream), "result gather");
     b->launches += 3;
@@ -540,9 +590,10 @@ int sbg_rk_merson_fixed_async(sbg_batch b, double h, int32_t nsteps, const sbg_i
     }
     if (ctol <= 0) ctol = acc / 10;
     SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    if (int rc = tuneVariant(b)) return rc;  // realize leaves the state untouched
     SBG_CUDA(cudaMemsetAsync(b->status, 0, std::max(b->ninst, 1) * sizeof(int32_t), b->stream), "status reset");
     SBG_CUDA(launchNormalizeQuat(b->T, b->y, b->stream), "initialize");
-    SBG_CUDA(launchRKMerson(b->T, b->precision, b->nm, b->tiled, b->y, b->time, b->fbuf, b->colElems, b->scratch, b->status, h,
+    SBG_CUDA(launchRKMerson(b->T, b->precision, b->nm, b->variant, b->y, b->time, b->fbuf, b->colElems, b->scratch, b->status, h,
                             nsteps, acc, ctol, pes, b->stream),
              "RK-Merson kernel launch");
     b->launches += 2;

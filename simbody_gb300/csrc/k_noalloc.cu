@@ -138,7 +138,9 @@ int sbg_realize_acceleration_noalloc(sbg_topology topo, int32_t ninst, const dou
         return naFail(SBG_ERR_INVALID, "topology has " + std::to_string(topo->fkw.size()) +
                                            " mobility forces; the no-alloc path takes at most " +
                                            std::to_string(kNoAllocMaxForces));
-    const int64_t recBytes = topo->recSize * (int64_t)sizeof(double);
+    int64_t padRec = 0;
+    paddedRecords(*topo, topo->maxNonFreeDof <= 1 ? 1 : 3, &padRec);
+    const int64_t recBytes = padRec * (int64_t)sizeof(double);
     if (recBytes > (int64_t)kNoAllocScratchBytes)
         return naFail(SBG_ERR_INVALID, "one instance needs " + std::to_string(recBytes) +
                                            " bytes of scratch, above the no-alloc capacity of " +
@@ -160,7 +162,10 @@ int sbg_realize_acceleration_noalloc(sbg_topology topo, int32_t ninst, const dou
     SBG_UP(g_naInfo, topo->info.data(), nb * sizeof(int32_t))
     SBG_UP(g_naQoff, topo->qoff.data(), nb * sizeof(int32_t))
     SBG_UP(g_naUoff, topo->uoff.data(), nb * sizeof(int32_t))
-    SBG_UP(g_naSrec, topo->srec.data(), nb * sizeof(int32_t))
+    const int nmw = topo->maxNonFreeDof <= 1 ? 1 : 3;
+    int64_t recSize = 0;
+    const std::vector<int32_t> srecPad = paddedRecords(*topo, nmw, &recSize);
+    SBG_UP(g_naSrec, srecPad.data(), nb * sizeof(int32_t))
     SBG_UP(g_naFbeg, topo->fbeg.data(), nb * sizeof(int32_t))
     SBG_UP(g_naFcnt, topo->fcnt.data(), nb * sizeof(int32_t))
     SBG_UP(g_naPar, topo->par.data(), topo->par.size() * sizeof(double))
@@ -178,12 +183,12 @@ int sbg_realize_acceleration_noalloc(sbg_topology topo, int32_t ninst, const dou
     const int block = (int)std::min<int64_t>(threads, nthreads);
     const int grid = (int)(nthreads / block);
     const DevTables& T = g_naTables[dev];
-    if (topo->maxNonFreeDof <= 1)
+    if (nmw == 1)
         realizeNoAllocKernel<1><<<grid, block, 0, s>>>(T, y, ydot, status, g_naScratchPtr[dev], ninst, topo->nq,
-                                                       topo->nq + topo->nu, topo->recSize);
+                                                       topo->nq + topo->nu, recSize);
     else
         realizeNoAllocKernel<3><<<grid, block, 0, s>>>(T, y, ydot, status, g_naScratchPtr[dev], ninst, topo->nq,
-                                                       topo->nq + topo->nu, topo->recSize);
+                                                       topo->nq + topo->nu, recSize);
     if ((e = cudaGetLastError()) != cudaSuccess)
         return naFail(SBG_ERR_CUDA, std::string("no-alloc kernel launch: ") + cudaGetErrorString(e));
     return SBG_OK;

@@ -45,40 +45,40 @@ __global__ void gatherKernel(DevTables T, const int64_t* __restrict__ hostOff, c
     for (int k = threadIdx.x; k < cnt; k += blockDim.x) packed[off + k] = cols[base + (int64_t)(c0 + k) * stride];
 }
 
-cudaError_t launchRealize64(const DevTables& T, int nm, bool tiled, const double* y, double* ydot, void* scratch,
+cudaError_t launchRealize64(const DevTables& T, int nm, const double* y, double* ydot, void* scratch,
                             int32_t* status, cudaStream_t s);
-cudaError_t launchRealize32(const DevTables& T, int nm, bool tiled, bool refine, const double* y, double* ydot,
-                            void* scratch, int32_t* status, cudaStream_t s);
-cudaError_t launchMInv64(const DevTables& T, int nm, bool tiled, const double* y, const double* f, double* out,
+cudaError_t launchRealize32(const DevTables& T, int nm, bool refine, int variant, const double* y,
+                            double* ydot, void* scratch, int32_t* status, cudaStream_t s);
+cudaError_t launchMInv64(const DevTables& T, int nm, const double* y, const double* f, double* out,
                          void* scratch, int32_t* status, cudaStream_t s);
-cudaError_t launchMInv32(const DevTables& T, int nm, bool tiled, const double* y, const double* f, double* out,
+cudaError_t launchMInv32(const DevTables& T, int nm, const double* y, const double* f, double* out,
                          void* scratch, int32_t* status, cudaStream_t s);
-cudaError_t launchRK64(const DevTables& T, int nm, bool tiled, double* y, double* time, void* fbuf, int64_t fplane,
+cudaError_t launchRK64(const DevTables& T, int nm, double* y, double* time, void* fbuf, int64_t fplane,
                        void* scratch, int32_t* status, double h, int nsteps, double acc, double ctol, int pes,
                        cudaStream_t s);
-cudaError_t launchRK32(const DevTables& T, int nm, bool tiled, bool refine, double* y, double* time, void* fbuf,
+cudaError_t launchRK32(const DevTables& T, int nm, bool refine, int variant, double* y, double* time, void* fbuf,
                        int64_t fplane, void* scratch, int32_t* status, double h, int nsteps, double acc, double ctol,
                        int pes, cudaStream_t s);
 
-cudaError_t launchRealize(const DevTables& T, int precision, int nm, bool tiled, const double* y, double* ydot,
-                          void* scratch, int32_t* status, cudaStream_t s) {
-    if (precision == SBG_PRECISION_FP64) return launchRealize64(T, nm, tiled, y, ydot, scratch, status, s);
-    return launchRealize32(T, nm, tiled, precision == SBG_PRECISION_MIXED, y, ydot, scratch, status, s);
+cudaError_t launchRealize(const DevTables& T, int precision, int nm, int variant, const double* y,
+                          double* ydot, void* scratch, int32_t* status, cudaStream_t s) {
+    if (precision == SBG_PRECISION_FP64) return launchRealize64(T, nm, y, ydot, scratch, status, s);
+    return launchRealize32(T, nm, precision == SBG_PRECISION_MIXED, variant, y, ydot, scratch, status, s);
 }
 
-cudaError_t launchMInv(const DevTables& T, int precision, int nm, bool tiled, const double* y, const double* f,
+cudaError_t launchMInv(const DevTables& T, int precision, int nm, const double* y, const double* f,
                        double* out, void* scratch, int32_t* status, cudaStream_t s) {
-    return precision == SBG_PRECISION_FP64 ? launchMInv64(T, nm, tiled, y, f, out, scratch, status, s)
-                                           : launchMInv32(T, nm, tiled, y, f, out, scratch, status, s);
+    return precision == SBG_PRECISION_FP64 ? launchMInv64(T, nm, y, f, out, scratch, status, s)
+                                           : launchMInv32(T, nm, y, f, out, scratch, status, s);
 }
 
-cudaError_t launchRKMerson(const DevTables& T, int precision, int nm, bool tiled, double* y, double* time,
+cudaError_t launchRKMerson(const DevTables& T, int precision, int nm, int variant, double* y, double* time,
                            void* fbuf, int64_t fplane, void* scratch, int32_t* status, double h, int nsteps,
                            double accuracy, double consTol, int projectEveryStep, cudaStream_t s) {
     if (precision == SBG_PRECISION_FP64)
-        return launchRK64(T, nm, tiled, y, time, fbuf, fplane, scratch, status, h, nsteps, accuracy, consTol,
+        return launchRK64(T, nm, y, time, fbuf, fplane, scratch, status, h, nsteps, accuracy, consTol,
                           projectEveryStep, s);
-    return launchRK32(T, nm, tiled, precision == SBG_PRECISION_MIXED, y, time, fbuf, fplane, scratch, status, h,
+    return launchRK32(T, nm, precision == SBG_PRECISION_MIXED, variant, y, time, fbuf, fplane, scratch, status, h,
                       nsteps, accuracy, consTol, projectEveryStep, s);
 }
 

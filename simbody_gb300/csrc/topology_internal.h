@@ -21,3 +21,19 @@ struct sbg_topology_s {
     std::vector<sbg_ball_constraint_desc> cons;
 };
 
+// Scratch-record offsets of the rows of `t` when every non-Free row is given
+// the record of an nm-mobility body (Free rows keep 6): lanes of a warp that
+// process the same row of different topologies then address the same record
+// elements. *total gets the record length of one instance.
+inline std::vector<int32_t> paddedRecords(const sbg_topology_s& t, int nm, int64_t* total) {
+    std::vector<int32_t> off(t.nb);
+    int64_t rec = 0;
+    for (int r = 0; r < t.nb; ++r) {
+        const int n = (t.info[r] >> 4) & 15;
+        off[r] = (int32_t)rec;
+        rec += sbg::scratchRecordSize(n == 6 ? 6 : nm);
+    }
+    if (total) *total = rec;
+    return off;
+}
+

@@ -144,6 +144,10 @@ class Batch:
         return int(N.engine_lib().sbg_batch_launch_count(self._h))
 
     @property
+    def kernel_variant(self) -> int:
+        return int(N.engine_lib().sbg_batch_kernel_variant(self._h))
+
+    @property
     def device_bytes(self) -> int:
         b = C.c_int64()
         N.check(N.engine_lib().sbg_batch_device_bytes(self._h, C.byref(b)))
