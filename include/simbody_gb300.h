@@ -229,6 +229,10 @@ int64_t sbg_batch_launch_count(sbg_batch batch);
  * 128-thread blocks per SM, 4 = four), 0 before the first realize or
  * integration, -1 for a null batch. No counterpart in the reference. */
 int sbg_batch_kernel_variant(sbg_batch batch);
+/* Lanes-per-tree setting the tuner picked for the batch's level-parallel
+ * segment (lanes = next power of two of the widest level, shifted right by
+ * this), -1 for a null batch. No counterpart in the reference. */
+int sbg_batch_group_lanes_shift(sbg_batch batch);
 
 /* ------------------------------------------------ allocation-free realize */
 

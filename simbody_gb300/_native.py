@@ -90,6 +90,7 @@ ENGINE_API = {
     "sbg_batch_sync": (C.c_int, [vp]),
     "sbg_batch_launch_count": (C.c_int64, [vp]),
     "sbg_batch_kernel_variant": (C.c_int, [vp]),
+    "sbg_batch_group_lanes_shift": (C.c_int, [vp]),
     "sbg_realize_acceleration_noalloc": (C.c_int, [vp, C.c_int32, vp, vp, vp, vp]),
     "sbg_noalloc_last_error": (C.c_char_p, []),
 }

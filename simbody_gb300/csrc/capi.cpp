@@ -81,11 +81,61 @@ struct sbg_batch_s {
     double* hostPinned = nullptr;  // pinned host staging (nyTotal)
     bool stateSet = false;
     int64_t launches = 0;
+    // mapping
+    int nChain = 0;                       // order positions of the chain segment
+    std::vector<int32_t> groupWidthKey;   // widest level of each group-segment instance
+    int groupShift = -1;                  // G = pow2ceil(width) >> shift, clamped to [2, 32]
+    int nGroupBlocks = 0;
+    int32_t* dBlkFirst = nullptr;
+    int32_t* dBlkG = nullptr;
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
+    cudaEvent_t evT0 = nullptr, evT1 = nullptr;
+    bool tuned = false;
+    cudaGraphExec_t realizeGraph = nullptr;  // captured after tuning
+
+    Streams streams() const { return Streams{stream, stream2, evFork, evJoin}; }
+    LaunchPlan plan() const { return LaunchPlan{nChain, nGroupBlocks, nm, variant == 0 ? 1 : variant}; }
+
+    // Lanes per instance of the group segment: blocks of 128 threads hold
+    // 128/G instances of equal G (the order is sorted by widest level, so G is
+    // non-increasing along it).
+    int setGroupShift(int shift) {
+        if (shift == groupShift) return SBG_OK;
+        std::vector<int32_t> first, gs;
+        const int ng = (int)groupWidthKey.size();
+        int p = 0;
+        while (p < ng) {
+            int w = 1;
+            while (w < groupWidthKey[p]) w <<= 1;
+            const int G = std::max(2, std::min(32, w >> shift));
+            int q = p;
+            auto gOf = [&](int k) { int ww = 1; while (ww < groupWidthKey[k]) ww <<= 1; return std::max(2, std::min(32, ww >> shift)); };
+            while (q < ng && q - p < 128 / G && gOf(q) == G) ++q;
+            first.push_back(nChain + p);
+            gs.push_back(G);
+            p = q;
+        }
+        first.push_back(nChain + ng);
+        gs.push_back(0);
+        nGroupBlocks = (int)gs.size() - 1;
+        cudaError_t e = cudaMemcpy(dBlkFirst, first.data(), first.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(dBlkG, gs.data(), gs.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cudaFail(e, "group block table");
+        groupShift = shift;
+        return SBG_OK;
+    }
 
     ~sbg_batch_s() {
         if (device >= 0) cudaSetDevice(device);
         for (auto& b : bufs) cudaFree(b.p);
         if (hostPinned) cudaFreeHost(hostPinned);
+        if (realizeGraph) cudaGraphExecDestroy(realizeGraph);
+        if (evFork) cudaEventDestroy(evFork);
+        if (evT0) cudaEventDestroy(evT0);
+        if (evT1) cudaEventDestroy(evT1);
+        if (evJoin) cudaEventDestroy(evJoin);
+        if (stream2) cudaStreamDestroy(stream2);
         if (stream) cudaStreamDestroy(stream);
     }
     int alloc(void** out, size_t bytes, const char* what) {
@@ -187,6 +237,8 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
     // forces grouped by body, application order preserved
     std::vector<std::vector<int>> fOf(nb + 1);
     for (int i = 0; i < d->nforces; ++i) fOf[d->forces[i].body].push_back(i);
+    std::vector<std::vector<int>> kids(nb + 1);
+    for (int i = 1; i <= nb; ++i) kids[d->bodies[i - 1].parent].push_back(i);
     int64_t rec = 0;
     for (int r = 0; r < nb; ++r) {
         const int bi = order[r];
@@ -198,8 +250,8 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
         if (b.X_BM[9] == 0 && b.X_BM[10] == 0 && b.X_BM[11] == 0) info |= 1 << 10;
         if (b.X_PF[9] == 0 && b.X_PF[10] == 0 && b.X_PF[11] == 0) info |= 1 << 11;
         if (b.parent != 0 && rowOf[b.parent] == r - 1) info |= F_CARRY;
-        for (int c = bi + 1; c <= nb; ++c)
-            if (d->bodies[c - 1].parent == bi && rowOf[c] != r + 1) info |= F_MEMCHILD;
+        for (int c : kids[bi])
+            if (rowOf[c] != r + 1) info |= F_MEMCHILD;
         t->parent.push_back(b.parent == 0 ? -1 : rowOf[b.parent]);
         t->info.push_back(info);
         t->qoff.push_back(qo[bi]);
@@ -228,6 +280,25 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
         t->par.insert(t->par.end(), p, p + kParamStride);
     }
     t->recSize = rec;
+    // level table, children lists and shape of the tree (local rows)
+    t->levStart.assign(t->nlevels + 1, nb);
+    for (int r = nb - 1; r >= 0; --r) t->levStart[level[order[r]] - 1] = r;
+    t->levStart[t->nlevels] = nb;
+    for (int L = 0; L < t->nlevels; ++L) t->maxLevelWidth = std::max(t->maxLevelWidth, t->levStart[L + 1] - t->levStart[L]);
+    t->cbeg.assign(nb, 0);
+    t->ccnt.assign(nb, 0);
+    for (int r = 0; r < nb; ++r)
+        if (t->parent[r] >= 0) ++t->ccnt[t->parent[r]];
+    for (int r = 1; r < nb; ++r) t->cbeg[r] = t->cbeg[r - 1] + t->ccnt[r - 1];
+    t->clist.assign(nb > 0 ? t->cbeg[nb - 1] + t->ccnt[nb - 1] : 0, 0);
+    {
+        std::vector<int32_t> fill(t->cbeg);
+        for (int r = 0; r < nb; ++r)
+            if (t->parent[r] >= 0) t->clist[fill[t->parent[r]]++] = r;
+    }
+    t->chain = true;
+    for (int r = 0; r < nb; ++r)
+        if (t->parent[r] != r - 1) t->chain = false;
     t->defaultY.assign(nq + nu, 0.0);
     for (int i = 1; i <= nb; ++i)
         if (d->bodies[i - 1].mobilizer >= SBG_BALL) t->defaultY[qo[i]] = 1.0;
@@ -291,7 +362,10 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     auto bail = [&](int rc) { delete b; return rc; };
     {
         cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
-        if (e != cudaSuccess) return bail(cudaFail(e, "cudaStreamCreate"));
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->evFork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->evJoin, cudaEventDisableTiming);
+        if (e != cudaSuccess) return bail(cudaFail(e, "stream/event creation"));
     }
 
     // batch width: 1 when every non-Free body has one mobility, else 3
@@ -327,31 +401,65 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     b->nm = nm;
     const bool uniform = ninst > 0 && std::all_of(instTopo, instTopo + ninst, [&](int32_t k) { return k == instTopo[0]; });
 
-    // instance table and column addressing. Threads take instances in
-    // decreasing body count so a warp's lanes walk trees of similar size;
-    // every 32 consecutive threads form a tile whose state columns and
-    // scratch records interleave lane by lane (element e of the lane-l
-    // instance at tileBase + e*32 + l), padded to the tile's largest instance.
-    std::vector<int32_t> ibody(ninst), inb(ninst), inq(ninst), inu(ninst), order(ninst);
+    // Instance table and column addressing.
+    //  - chain segment (order positions [0, nChain)): chains and near-chains,
+    //    one thread per instance, largest first; 32 consecutive positions form
+    //    a tile whose state columns and scratch records interleave lane by
+    //    lane (element e of the lane-l instance at tileBase + e*32 + l),
+    //    padded to the tile's largest instance;
+    //  - group segment (the rest): trees with wide levels, G lanes per
+    //    instance; each instance's state is contiguous and its scratch is
+    //    field-major (element f of row r at base + r + f*nbodies).
+    std::vector<int32_t> ibody(ninst), inb(ninst), inq(ninst), inu(ninst), order(ninst), ilev(ninst), inlev(ninst);
     std::vector<int64_t> ybase(ninst), ystride(ninst), sbase(ninst), sstride(ninst);
     std::vector<double> grav(3 * (size_t)ninst);
+    std::vector<int32_t> levBase(ntopo, 0);
+    std::vector<int32_t> levStart, cbeg, ccnt, clist;
+    for (int k = 0; k < ntopo; ++k) {
+        if (used[k] < 0) continue;
+        const sbg_topology_s* t = topos[k];
+        levBase[k] = (int32_t)levStart.size();
+        levStart.insert(levStart.end(), t->levStart.begin(), t->levStart.end());
+        const int32_t cOff = (int32_t)clist.size();
+        for (int32_t v : t->cbeg) cbeg.push_back(v + cOff);
+        ccnt.insert(ccnt.end(), t->ccnt.begin(), t->ccnt.end());
+        clist.insert(clist.end(), t->clist.begin(), t->clist.end());
+    }
     b->hostYOff.assign(ninst + 1, 0);
     b->hostUOff.assign(ninst + 1, 0);
+    // Trees with fewer bodies run one per thread (their lanes would mostly
+    // idle or diverge in a group); larger trees with wide levels get a group.
+    int groupMinBodies = 48;
+    if (const char* v = std::getenv("SBG_GROUP_MIN_BODIES")) groupMinBodies = std::atoi(v);  // tuning override
+    std::vector<int> chainPos, groupPos;
     for (int i = 0; i < ninst; ++i) {
         const sbg_topology_s* t = topos[instTopo[i]];
         ibody[i] = rowBase[instTopo[i]];
         inb[i] = t->nb;
         inq[i] = t->nq;
         inu[i] = t->nu;
+        ilev[i] = levBase[instTopo[i]];
+        inlev[i] = t->nlevels;
         for (int k = 0; k < 3; ++k) grav[3 * i + k] = t->gravity[k];
         b->hostYOff[i + 1] = b->hostYOff[i] + t->nq + t->nu;
         b->hostUOff[i + 1] = b->hostUOff[i] + t->nu;
+        if (t->chain || t->maxLevelWidth <= 2 || t->nb < groupMinBodies) chainPos.push_back(i);
+        else groupPos.push_back(i);
     }
-    std::iota(order.begin(), order.end(), 0);
-    if (!uniform) std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return inb[a] > inb[c]; });
+    if (!uniform) {
+        std::stable_sort(chainPos.begin(), chainPos.end(), [&](int a, int c) { return inb[a] > inb[c]; });
+        auto wkey = [&](int i) { int w = 1; while (w < topos[instTopo[i]]->maxLevelWidth) w <<= 1; return w; };
+        std::stable_sort(groupPos.begin(), groupPos.end(), [&](int a, int c) {
+            const int wa = wkey(a), wc = wkey(c);
+            return wa != wc ? wa > wc : inb[a] > inb[c];
+        });
+    }
+    b->nChain = (int)chainPos.size();
+    std::copy(chainPos.begin(), chainPos.end(), order.begin());
+    std::copy(groupPos.begin(), groupPos.end(), order.begin() + b->nChain);
     int64_t yOff = 0, sOff = 0;
-    for (int t0 = 0; t0 < ninst; t0 += kTile) {
-        const int t1 = std::min(ninst, t0 + kTile);
+    for (int t0 = 0; t0 < b->nChain; t0 += kTile) {
+        const int t1 = std::min(b->nChain, t0 + kTile);
         int64_t yw = 0, sw = 0;
         for (int p = t0; p < t1; ++p) {
             const int i = order[p];
@@ -366,13 +474,23 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
         yOff += yw * kTile;
         sOff += sw * kTile;
     }
+    b->groupWidthKey.clear();
+    for (int p = b->nChain; p < ninst; ++p) {
+        const int i = order[p];
+        const sbg_topology_s* t = topos[instTopo[i]];
+        ybase[i] = yOff; ystride[i] = 1;
+        yOff += t->nq + t->nu;
+        sbase[i] = sOff; sstride[i] = 1;
+        sOff += (int64_t)t->nb * rowsRecordWidth(*t, 3);
+        b->groupWidthKey.push_back(t->maxLevelWidth);
+    }
     b->nyTotal = b->hostYOff[ninst];
     b->nuTotal = b->hostUOff[ninst];
     b->colElems = yOff;
     b->scratchElems = sOff;
     b->tiled = true;
     if (precision == SBG_PRECISION_FP64) b->variant = 1;  // FP64 needs every register
-    if (const char* v = std::getenv("SBG_VARIANT")) b->variant = std::atoi(v) == 4 ? 4 : 1;
+    if (const char* v = std::getenv("SBG_VARIANT")) b->variant = std::atoi(v) == 4 ? 4 : 1;  // tuning override
 
     int rc = 0;
     DevTables& T = b->T;
@@ -402,6 +520,23 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     if ((rc = b->upload(&T.sstride, sstride, "instance table"))) return bail(rc);
     if ((rc = b->upload(&T.grav, grav, "instance table"))) return bail(rc);
     if ((rc = b->upload(&T.order, order, "instance table"))) return bail(rc);
+    if ((rc = b->upload(&T.ilev, ilev, "instance table"))) return bail(rc);
+    if ((rc = b->upload(&T.inlev, inlev, "instance table"))) return bail(rc);
+    if ((rc = b->upload(&T.levStart, levStart, "level table"))) return bail(rc);
+    if ((rc = b->upload(&T.cbeg, cbeg, "children table"))) return bail(rc);
+    if ((rc = b->upload(&T.ccnt, ccnt, "children table"))) return bail(rc);
+    if ((rc = b->upload(&T.clist, clist, "children table"))) return bail(rc);
+    {   // group block table (capacity: one block per group instance + end)
+        void* q = nullptr;
+        const size_t cap = (size_t)(ninst - b->nChain) + 2;
+        if ((rc = b->alloc(&q, cap * sizeof(int32_t), "group block table"))) return bail(rc);
+        b->dBlkFirst = static_cast<int32_t*>(q);
+        if ((rc = b->alloc(&q, cap * sizeof(int32_t), "group block table"))) return bail(rc);
+        b->dBlkG = static_cast<int32_t*>(q);
+        T.blkFirst = b->dBlkFirst;
+        T.blkG = b->dBlkG;
+        if ((rc = b->setGroupShift(1))) return bail(rc);
+    }
     const int64_t* dOff = nullptr;
     if ((rc = b->upload(&dOff, b->hostYOff, "offsets"))) return bail(rc);
     b->dHostYOff = const_cast<int64_t*>(dOff);
@@ -492,48 +627,80 @@ int sbg_batch_get_state(sbg_batch b, double* t, double* y) {
     return SBG_OK;
 }
 
-// Occupancy tuner: the FP32 kernels come in two register budgets (all the
-// registers they want, 2 blocks of 128 threads per SM; or at most 128, 4
-// blocks per SM with a few spills). The first realize or integration of a
-// batch times both on the batch's own state and keeps the faster.
-static int tuneVariant(sbg_batch b) {
-    if (b->variant != 0) return SBG_OK;
-    cudaEvent_t e0, e1;
-    SBG_CUDA(cudaEventCreate(&e0), "tuner");
-    SBG_CUDA(cudaEventCreate(&e1), "tuner");
-    float best = 1e30f;
-    int bestV = 1;
-    for (int v : {1, 4}) {
-        for (int rep = 0; rep < 2; ++rep)
-            SBG_CUDA(launchRealize(b->T, b->precision, b->nm, v, b->y, b->ydot, b->scratch, b->status, b->stream),
-                     "tuner launch");
-        SBG_CUDA(cudaEventRecord(e0, b->stream), "tuner");
-        for (int rep = 0; rep < 3; ++rep)
-            SBG_CUDA(launchRealize(b->T, b->precision, b->nm, v, b->y, b->ydot, b->scratch, b->status, b->stream),
-                     "tuner launch");
-        SBG_CUDA(cudaEventRecord(e1, b->stream), "tuner");
-        SBG_CUDA(cudaEventSynchronize(e1), "tuner");
-        float ms = 0;
-        SBG_CUDA(cudaEventElapsedTime(&ms, e0, e1), "tuner");
-        b->launches += 5;
-        if (ms < best) { best = ms; bestV = v; }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    b->variant = bestV;
+// Tuner: the FP32 kernels come in two register budgets (all the registers
+// they want, 2 blocks of 128 threads per SM; or at most 128, 4 blocks per SM
+// with a few spills), and the level-parallel segment can give each tree more
+// or fewer lanes (G = pow2ceil(widest level) >> shift). The first realize or
+// integration of a batch times the candidates on the batch's own state and
+// keeps the fastest (the realize leaves the state untouched).
+static int timePlan(sbg_batch b, float* ms) {
+    for (int rep = 0; rep < 2; ++rep)
+        SBG_CUDA(launchRealize(b->T, b->plan(), b->precision, b->y, b->ydot, b->scratch, b->status, b->streams()),
+                 "tuner launch");
+    SBG_CUDA(cudaEventRecord(b->evT0, b->stream), "tuner");
+    for (int rep = 0; rep < 3; ++rep)
+        SBG_CUDA(launchRealize(b->T, b->plan(), b->precision, b->y, b->ydot, b->scratch, b->status, b->streams()),
+                 "tuner launch");
+    SBG_CUDA(cudaEventRecord(b->evT1, b->stream), "tuner");
+    SBG_CUDA(cudaEventSynchronize(b->evT1), "tuner");
+    SBG_CUDA(cudaEventElapsedTime(ms, b->evT0, b->evT1), "tuner");
+    b->launches += 5 * ((b->nChain > 0) + (b->nGroupBlocks > 0));
     return SBG_OK;
 }
 
-int sbg_batch_kernel_variant(sbg_batch b) { return b ? b->variant : -1; }
+static int tuneVariant(sbg_batch b) {
+    if (b->tuned) return SBG_OK;
+    if (!b->evT0) {
+        SBG_CUDA(cudaEventCreate(&b->evT0), "tuner");
+        SBG_CUDA(cudaEventCreate(&b->evT1), "tuner");
+    }
+    const bool fixedVariant = b->variant != 0;
+    if (!fixedVariant) b->variant = 1;
+    float best = 1e30f, ms = 0;
+    int bestShift = b->groupShift;
+    if (!b->groupWidthKey.empty()) {
+        for (int shift : {0, 1, 2}) {
+            if (int rc = b->setGroupShift(shift)) return rc;
+            if (int rc = timePlan(b, &ms)) return rc;
+            if (ms < best) { best = ms; bestShift = shift; }
+        }
+        if (int rc = b->setGroupShift(bestShift)) return rc;
+    } else if (int rc = timePlan(b, &best)) {
+        return rc;
+    }
+    if (!fixedVariant && b->precision != SBG_PRECISION_FP64) {
+        b->variant = 4;
+        if (int rc = timePlan(b, &ms)) return rc;
+        if (!(ms < best)) b->variant = 1;
+    }
+    b->tuned = true;
+    return SBG_OK;
+}
+
+int sbg_batch_kernel_variant(sbg_batch b) { return b ? (b->tuned ? b->variant : 0) : -1; }
+int sbg_batch_group_lanes_shift(sbg_batch b) { return b ? b->groupShift : -1; }
 
 int sbg_realize_acceleration_async(sbg_batch b) {
     if (!b) return fail(SBG_ERR_INVALID, "null batch");
     if (!b->stateSet) return fail(SBG_ERR_STATE, "no state has been set");
     SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
     if (int rc = tuneVariant(b)) return rc;
-    SBG_CUDA(launchRealize(b->T, b->precision, b->nm, b->variant, b->y, b->ydot, b->scratch, b->status, b->stream),
-             "realize kernel launch");
-    ++b->launches;
+    // The tuned launch sequence (chain segment on the main stream, tree
+    // segment forked onto the side stream) is captured once as a CUDA graph
+    // and replayed.
+    if (!b->realizeGraph) {
+        cudaGraph_t g = nullptr;
+        SBG_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+        cudaError_t e = launchRealize(b->T, b->plan(), b->precision, b->y, b->ydot, b->scratch, b->status, b->streams());
+        cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+        if (e != cudaSuccess) return cudaFail(e, "realize capture");
+        if (e2 != cudaSuccess) return cudaFail(e2, "graph capture");
+        e = cudaGraphInstantiate(&b->realizeGraph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cudaFail(e, "graph instantiate");
+    }
+    SBG_CUDA(cudaGraphLaunch(b->realizeGraph, b->stream), "realize graph launch");
+    b->launches += (b->nChain > 0) + (b->nGroupBlocks > 0);
     return SBG_OK;
 }
 
@@ -566,7 +733,7 @@ int sbg_multiply_by_minv(sbg_batch b, const double* f, double* outp) {
     std::memcpy(b->hostPinned, f, bytes);
     SBG_CUDA(cudaMemcpyAsync(b->staging, b->hostPinned, bytes, cudaMemcpyHostToDevice, b->stream), "force upload");
     SBG_CUDA(launchScatter(b->T, b->dHostUOff, b->staging, b->fcol, 1, b->stream), "force scatter");
-    SBG_CUDA(launchMInv(b->T, b->precision, b->nm, b->y, b->fcol, b->ydot, b->scratch, b->status, b->stream),
+    SBG_CUDA(launchMInv(b->T, b->plan(), b->precision, b->y, b->fcol, b->ydot, b->scratch, b->status, b->streams()),
              "M^-1 kernel launch");
     SBG_CUDA(launchGather(b->T, b->dHostUOff, b->ydot, b->staging, 1, b->stream), "result gather");
     b->launches += 3;
@@ -593,10 +760,10 @@ int sbg_rk_merson_fixed_async(sbg_batch b, double h, int32_t nsteps, const sbg_i
     if (int rc = tuneVariant(b)) return rc;  // realize leaves the state untouched
     SBG_CUDA(cudaMemsetAsync(b->status, 0, std::max(b->ninst, 1) * sizeof(int32_t), b->stream), "status reset");
     SBG_CUDA(launchNormalizeQuat(b->T, b->y, b->stream), "initialize");
-    SBG_CUDA(launchRKMerson(b->T, b->precision, b->nm, b->variant, b->y, b->time, b->fbuf, b->colElems, b->scratch, b->status, h,
-                            nsteps, acc, ctol, pes, b->stream),
+    SBG_CUDA(launchRKMerson(b->T, b->plan(), b->precision, b->y, b->time, b->fbuf, b->colElems, b->scratch, b->status, h,
+                            nsteps, acc, ctol, pes, b->streams()),
              "RK-Merson kernel launch");
-    b->launches += 2;
+    b->launches += 1 + (b->nChain > 0) + (b->nGroupBlocks > 0);
     return SBG_OK;
 }
 

@@ -85,8 +85,27 @@ struct DevTables {
     const int64_t* sbase;    // scratch column base
     const int64_t* sstride;
     const double* grav;      // per instance gravity (3)
-    const int32_t* order;    // thread -> instance (size-sorted)
+    const int32_t* order;    // position -> instance (chain segment first, then group segment)
     int32_t ninst;
+    // level-parallel (group) driver
+    const int32_t* ilev;     // per instance: first entry of its level table in levStart
+    const int32_t* inlev;    // per instance: number of levels
+    const int32_t* levStart; // per topology: local row where each level starts (+ end)
+    const int32_t* cbeg;     // per body row: first child in clist
+    const int32_t* ccnt;     // per body row: number of children
+    const int32_t* clist;    // children as local rows
+    const int32_t* blkFirst; // per group block: first order position (+ end)
+    const int32_t* blkG;     // per group block: lanes per instance
+};
+
+// How one batch operation is launched: order positions [0, nChain) run the
+// chain driver (one thread per instance, width nm), then nGroupBlocks blocks
+// of the level-parallel driver cover the rest.
+struct LaunchPlan {
+    int nChain;
+    int nGroupBlocks;
+    int nm;
+    int variant;  // 1: registers as needed; 4: at most 128 registers (FP32 only)
 };
 
 }  // namespace sbg

@@ -52,12 +52,12 @@ __global__ void __launch_bounds__(128) realizeNoAllocKernel(DevTables T, const d
                                                             int64_t recSize) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     const int nthreads = gridDim.x * blockDim.x;
-    const Scr<double, 1> S{scratch + (int64_t)slot * recSize};
+    const ScrRows<double> S{scratch + (int64_t)slot * recSize, 1};  // contiguous record per slot
     for (int inst = slot; inst < ninst; inst += nthreads) {
         const int64_t base = (int64_t)inst * ny;
         YSrc src{y, base, 1, nq};
         YdOut out{ydot, base, 1, nq};
-        int st = rhsInstance<double, NM, 1, false>(T, 0, S, src, out);
+        int st = rhsChain<double, NM, false>(T, 0, S, src, out);
         if (!out.finite) st |= SBG_INST_NONFINITE;
         status[inst] = st;
     }

@@ -1,0 +1,29 @@
+// k_r64.cu -- realize(Acceleration) and M^-1 f kernel instantiations, FP64.
+#include "abi_device.cuh"
+
+namespace sbg {
+
+static inline int chainBlocks(const LaunchPlan& P) { return (P.nChain + 127) / 128; }
+
+void realize64Chain(const KArgs& a, cudaStream_t s) {
+    const int nb = chainBlocks(*a.P);
+    double* sc = static_cast<double*>(a.scratch);
+    if (a.P->nm == 1) realizeKernel<double, 1, false, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.ydot, sc, a.status);
+    else realizeKernel<double, 3, false, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.ydot, sc, a.status);
+}
+void realize64Group(const KArgs& a, cudaStream_t s) {
+    realizeKernel<double, 3, false, true><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, 0, 0, a.y, a.ydot,
+                                                                              static_cast<double*>(a.scratch), a.status);
+}
+void minv64Chain(const KArgs& a, cudaStream_t s) {
+    const int nb = chainBlocks(*a.P);
+    double* sc = static_cast<double*>(a.scratch);
+    if (a.P->nm == 1) minvKernel<double, 1, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.f, a.ydot, sc, a.status);
+    else minvKernel<double, 3, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.f, a.ydot, sc, a.status);
+}
+void minv64Group(const KArgs& a, cudaStream_t s) {
+    minvKernel<double, 3, true><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, 0, 0, a.y, a.f, a.ydot,
+                                                                    static_cast<double*>(a.scratch), a.status);
+}
+
+}  // namespace sbg

@@ -1,20 +1,23 @@
-// k_rk64.cu -- fixed-step RK-Merson persistent kernel instantiations, FP64 recursions.
+// k_rk64.cu -- fixed-step RK-Merson persistent kernel instantiations, FP64.
 #include "abi_device.cuh"
 
 namespace sbg {
 
-cudaError_t launchRK64(const DevTables& T, int nm, double* y, double* time, void* fbuf, int64_t fplane,
-                       void* scratch, int32_t* status, double h, int nsteps, double acc, double ctol, int pes,
-                       cudaStream_t s) {
-    const int threads = 128, blocks = (T.ninst + threads - 1) / threads;
-    if (blocks == 0) return cudaSuccess;
-    double* fb = static_cast<double*>(fbuf);
-    double* sc = static_cast<double*>(scratch);
-    if (nm == 1)
-        rkMersonKernel<double, 1, kTile, false><<<blocks, threads, 0, s>>>(T, y, time, fb, fplane, sc, status, h, nsteps, acc, ctol, pes);
+void rk64Chain(const KArgs& a, cudaStream_t s) {
+    const int nb = (a.P->nChain + 127) / 128;
+    double* fb = static_cast<double*>(a.fbuf);
+    double* sc = static_cast<double*>(a.scratch);
+    if (a.P->nm == 1)
+        rkMersonKernel<double, 1, false, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.ystate, a.time, fb, a.fplane, sc,
+                                                                   a.status, a.h, a.nsteps, a.accuracy, a.consTol, a.projectEveryStep);
     else
-        rkMersonKernel<double, 3, kTile, false><<<blocks, threads, 0, s>>>(T, y, time, fb, fplane, sc, status, h, nsteps, acc, ctol, pes);
-    return cudaGetLastError();
+        rkMersonKernel<double, 3, false, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.ystate, a.time, fb, a.fplane, sc,
+                                                                   a.status, a.h, a.nsteps, a.accuracy, a.consTol, a.projectEveryStep);
+}
+void rk64Group(const KArgs& a, cudaStream_t s) {
+    rkMersonKernel<double, 3, false, true><<<a.P->nGroupBlocks, 128, 0, s>>>(
+        *a.T, 0, 0, a.ystate, a.time, static_cast<double*>(a.fbuf), a.fplane, static_cast<double*>(a.scratch), a.status,
+        a.h, a.nsteps, a.accuracy, a.consTol, a.projectEveryStep);
 }
 
 }  // namespace sbg

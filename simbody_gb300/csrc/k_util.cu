@@ -45,41 +45,59 @@ __global__ void gatherKernel(DevTables T, const int64_t* __restrict__ hostOff, c
     for (int k = threadIdx.x; k < cnt; k += blockDim.x) packed[off + k] = cols[base + (int64_t)(c0 + k) * stride];
 }
 
-cudaError_t launchRealize64(const DevTables& T, int nm, const double* y, double* ydot, void* scratch,
-                            int32_t* status, cudaStream_t s);
-cudaError_t launchRealize32(const DevTables& T, int nm, bool refine, int variant, const double* y,
-                            double* ydot, void* scratch, int32_t* status, cudaStream_t s);
-cudaError_t launchMInv64(const DevTables& T, int nm, const double* y, const double* f, double* out,
-                         void* scratch, int32_t* status, cudaStream_t s);
-cudaError_t launchMInv32(const DevTables& T, int nm, const double* y, const double* f, double* out,
-                         void* scratch, int32_t* status, cudaStream_t s);
-cudaError_t launchRK64(const DevTables& T, int nm, double* y, double* time, void* fbuf, int64_t fplane,
-                       void* scratch, int32_t* status, double h, int nsteps, double acc, double ctol, int pes,
-                       cudaStream_t s);
-cudaError_t launchRK32(const DevTables& T, int nm, bool refine, int variant, double* y, double* time, void* fbuf,
-                       int64_t fplane, void* scratch, int32_t* status, double h, int nsteps, double acc, double ctol,
-                       int pes, cudaStream_t s);
-
-cudaError_t launchRealize(const DevTables& T, int precision, int nm, int variant, const double* y,
-                          double* ydot, void* scratch, int32_t* status, cudaStream_t s) {
-    if (precision == SBG_PRECISION_FP64) return launchRealize64(T, nm, y, ydot, scratch, status, s);
-    return launchRealize32(T, nm, precision == SBG_PRECISION_MIXED, variant, y, ydot, scratch, status, s);
+// Run the chain segment on the main stream and the level-parallel segment on
+// the side stream, forked from and joined back into the main stream.
+template <class FC, class FG>
+static cudaError_t forkJoin(const LaunchPlan& P, const Streams& s, FC chain, FG group) {
+    const bool c = P.nChain > 0, g = P.nGroupBlocks > 0;
+    if (c && g) {
+        cudaError_t e = cudaEventRecord(s.fork, s.main);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s.side, s.fork, 0);
+        if (e != cudaSuccess) return e;
+        group(s.side);
+        chain(s.main);
+        e = cudaEventRecord(s.join, s.side);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s.main, s.join, 0);
+        if (e != cudaSuccess) return e;
+    } else if (c) {
+        chain(s.main);
+    } else if (g) {
+        group(s.main);
+    }
+    return cudaGetLastError();
 }
 
-cudaError_t launchMInv(const DevTables& T, int precision, int nm, const double* y, const double* f,
-                       double* out, void* scratch, int32_t* status, cudaStream_t s) {
-    return precision == SBG_PRECISION_FP64 ? launchMInv64(T, nm, y, f, out, scratch, status, s)
-                                           : launchMInv32(T, nm, y, f, out, scratch, status, s);
-}
-
-cudaError_t launchRKMerson(const DevTables& T, int precision, int nm, int variant, double* y, double* time,
-                           void* fbuf, int64_t fplane, void* scratch, int32_t* status, double h, int nsteps,
-                           double accuracy, double consTol, int projectEveryStep, cudaStream_t s) {
+cudaError_t launchRealize(const DevTables& T, const LaunchPlan& P, int precision, const double* y, double* ydot,
+                          void* scratch, int32_t* status, const Streams& s) {
+    KArgs a{};
+    a.T = &T; a.P = &P; a.y = y; a.ydot = ydot; a.scratch = scratch; a.status = status;
     if (precision == SBG_PRECISION_FP64)
-        return launchRK64(T, nm, y, time, fbuf, fplane, scratch, status, h, nsteps, accuracy, consTol,
-                          projectEveryStep, s);
-    return launchRK32(T, nm, precision == SBG_PRECISION_MIXED, variant, y, time, fbuf, fplane, scratch, status, h,
-                      nsteps, accuracy, consTol, projectEveryStep, s);
+        return forkJoin(P, s, [&](cudaStream_t st) { realize64Chain(a, st); }, [&](cudaStream_t st) { realize64Group(a, st); });
+    const bool ref = precision == SBG_PRECISION_MIXED;
+    return forkJoin(P, s, [&](cudaStream_t st) { realize32Chain(a, ref, st); },
+                    [&](cudaStream_t st) { realize32Group(a, ref, st); });
+}
+
+cudaError_t launchMInv(const DevTables& T, const LaunchPlan& P, int precision, const double* y, const double* f,
+                       double* out, void* scratch, int32_t* status, const Streams& s) {
+    KArgs a{};
+    a.T = &T; a.P = &P; a.y = y; a.f = f; a.ydot = out; a.scratch = scratch; a.status = status;
+    if (precision == SBG_PRECISION_FP64)
+        return forkJoin(P, s, [&](cudaStream_t st) { minv64Chain(a, st); }, [&](cudaStream_t st) { minv64Group(a, st); });
+    return forkJoin(P, s, [&](cudaStream_t st) { minv32Chain(a, st); }, [&](cudaStream_t st) { minv32Group(a, st); });
+}
+
+cudaError_t launchRKMerson(const DevTables& T, const LaunchPlan& P, int precision, double* y, double* time,
+                           void* fbuf, int64_t fplane, void* scratch, int32_t* status, double h, int nsteps,
+                           double accuracy, double consTol, int projectEveryStep, const Streams& s) {
+    KArgs a{};
+    a.T = &T; a.P = &P; a.ystate = y; a.time = time; a.fbuf = fbuf; a.fplane = fplane; a.scratch = scratch;
+    a.status = status; a.h = h; a.nsteps = nsteps; a.accuracy = accuracy; a.consTol = consTol;
+    a.projectEveryStep = projectEveryStep;
+    if (precision == SBG_PRECISION_FP64)
+        return forkJoin(P, s, [&](cudaStream_t st) { rk64Chain(a, st); }, [&](cudaStream_t st) { rk64Group(a, st); });
+    const bool ref = precision == SBG_PRECISION_MIXED;
+    return forkJoin(P, s, [&](cudaStream_t st) { rk32Chain(a, ref, st); }, [&](cudaStream_t st) { rk32Group(a, ref, st); });
 }
 
 cudaError_t launchNormalizeQuat(const DevTables& T, double* y, cudaStream_t s) {

@@ -7,23 +7,58 @@
 
 namespace sbg {
 
+// Streams of a batch: the chain segment runs on `main`, the level-parallel
+// segment on `side` (forked from and joined back into `main` with events),
+// so the two overlap on the GPU.
+struct Streams {
+    cudaStream_t main, side;
+    cudaEvent_t fork, join;
+};
+
 // precision: SBG_PRECISION_FP64, _MIXED (FP32 recursions + double-float
-// residual refinement) or _MIXED_FAST (FP32 recursions only). nm = largest
-// non-Free mobility count (1 or 3), a compile-time width. Every batch uses
-// warp-tiled state columns and scratch records.
-// variant: kernel occupancy variant (1 or 4), chosen by the batch's tuner.
-cudaError_t launchRealize(const DevTables& T, int precision, int nm, int variant, const double* y,
-                          double* ydot, void* scratch, int32_t* status, cudaStream_t s);
-cudaError_t launchRKMerson(const DevTables& T, int precision, int nm, int variant, double* y, double* time,
+// residual refinement) or _MIXED_FAST (FP32 recursions only).
+cudaError_t launchRealize(const DevTables& T, const LaunchPlan& P, int precision, const double* y, double* ydot,
+                          void* scratch, int32_t* status, const Streams& s);
+cudaError_t launchMInv(const DevTables& T, const LaunchPlan& P, int precision, const double* y, const double* f,
+                       double* out, void* scratch, int32_t* status, const Streams& s);
+cudaError_t launchRKMerson(const DevTables& T, const LaunchPlan& P, int precision, double* y, double* time,
                            void* fbuf, int64_t fplane, void* scratch, int32_t* status, double h, int nsteps,
-                           double accuracy, double consTol, int projectEveryStep, cudaStream_t s);
+                           double accuracy, double consTol, int projectEveryStep, const Streams& s);
 cudaError_t launchNormalizeQuat(const DevTables& T, double* y, cudaStream_t s);
 // part 0 moves whole [q,u] records, part 1 only the u slots.
 cudaError_t launchScatter(const DevTables& T, const int64_t* hostOff, const double* packed, double* cols, int part,
                           cudaStream_t s);
 cudaError_t launchGather(const DevTables& T, const int64_t* hostOff, const double* cols, double* packed, int part,
                          cudaStream_t s);
-cudaError_t launchMInv(const DevTables& T, int precision, int nm, const double* y, const double* f,
-                       double* out, void* scratch, int32_t* status, cudaStream_t s);
+
+// Per-segment launchers (k_r64.cu, k_r32c.cu, k_r32g.cu, k_rk64.cu,
+// k_rk32c.cu, k_rk32g.cu).
+struct KArgs {
+    const DevTables* T;
+    const LaunchPlan* P;
+    const double* y;     // realize / M^-1 input state
+    double* ydot;        // realize / M^-1 output
+    const double* f;     // M^-1 input forces
+    double* ystate;      // RK state (in place)
+    double* time;
+    void* fbuf;
+    int64_t fplane;
+    void* scratch;
+    int32_t* status;
+    double h, accuracy, consTol;
+    int nsteps, projectEveryStep;
+};
+void realize64Chain(const KArgs& a, cudaStream_t s);
+void realize64Group(const KArgs& a, cudaStream_t s);
+void minv64Chain(const KArgs& a, cudaStream_t s);
+void minv64Group(const KArgs& a, cudaStream_t s);
+void realize32Chain(const KArgs& a, bool refine, cudaStream_t s);
+void realize32Group(const KArgs& a, bool refine, cudaStream_t s);
+void minv32Chain(const KArgs& a, cudaStream_t s);
+void minv32Group(const KArgs& a, cudaStream_t s);
+void rk64Chain(const KArgs& a, cudaStream_t s);
+void rk64Group(const KArgs& a, cudaStream_t s);
+void rk32Chain(const KArgs& a, bool refine, cudaStream_t s);
+void rk32Group(const KArgs& a, bool refine, cudaStream_t s);
 
 }  // namespace sbg

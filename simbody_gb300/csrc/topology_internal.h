@@ -13,6 +13,10 @@ struct sbg_topology_s {
     int maxNonFreeDof = 0;
     int64_t recSize = 0;                 // scratch elements per instance
     std::vector<int32_t> parent, info, qoff, uoff, srec, fbeg, fcnt;
+    std::vector<int32_t> levStart;              // nlevels + 1 local rows
+    std::vector<int32_t> cbeg, ccnt, clist;     // children (local rows) per row
+    int maxLevelWidth = 0;
+    bool chain = false;                         // every row's parent is the previous row
     std::vector<double> par;             // kParamStride per row
     std::vector<int32_t> fkw;            // force elements, grouped by row
     std::vector<double> fcoef, fq0;
@@ -35,5 +39,14 @@ inline std::vector<int32_t> paddedRecords(const sbg_topology_s& t, int nm, int64
     }
     if (total) *total = rec;
     return off;
+}
+
+// Field-major record length of the level-parallel layout: every row gets the
+// widest record of the instance (6 columns if any row is Free, else nm).
+inline int64_t rowsRecordWidth(const sbg_topology_s& t, int nm) {
+    int w = nm;
+    for (int r = 0; r < t.nb; ++r)
+        if (((t.info[r] >> 4) & 15) == 6) w = 6;
+    return sbg::scratchRecordSize(w);
 }
 

@@ -148,6 +148,10 @@ class Batch:
         return int(N.engine_lib().sbg_batch_kernel_variant(self._h))
 
     @property
+    def group_lanes_shift(self) -> int:
+        return int(N.engine_lib().sbg_batch_group_lanes_shift(self._h))
+
+    @property
     def device_bytes(self) -> int:
         b = C.c_int64()
         N.check(N.engine_lib().sbg_batch_device_bytes(self._h, C.byref(b)))
