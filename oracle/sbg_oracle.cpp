@@ -89,15 +89,21 @@ template <class R> static void stationKin(const Work<R>& w, int body, const doub
     if (a) *a = Av[body] + cross(Aw[body], s_G) + cross(c.Vw, cross(c.Vw, s_G));
 }
 
-// Jacobian row block of one Ball constraint: d(p2 - p1)/du, assembled by
-// propagating unit velocities (equivalent to the reference's
-// calcConstraintForcesFromMultipliers transpose at :2227).
-template <class R> static void ballJacobian(const Topology& t, const Work<R>& w, int body, const double* st,
-                                            R sign, R* Grow /* 3 x nu */) {
-    if (body == 0) return;
-    const V3<R> s_G = w.c[body].R_GB * loadV<R>(st);
-    const V3<R> pS = w.c[body].p_GB + s_G;
-    // Each mobility j of an ancestor a contributes Hw x (pS - p_a) + Hv.
+// Kinematics of the material point of `body` now at Ground location pG.
+template <class R> static void pointKin(const Work<R>& w, int body, const V3<R>& pG, V3<R>& v, V3<R>* a,
+                                        const V3<R>* Aw, const V3<R>* Av) {
+    const BodyCache<R>& c = w.c[body];
+    const V3<R> r = pG - c.p_GB;
+    v = c.Vv + cross(c.Vw, r);
+    if (a) *a = Av[body] + cross(Aw[body], r) + cross(c.Vw, cross(c.Vw, r));
+}
+
+// Jacobian row block d(v)/du of the material point of `body` at Ground
+// location pS, added with `sign`: each mobility j of an ancestor a
+// contributes Hv + Hw x (pS - p_a) (the transpose of applying a station
+// force, SimbodyMatterSubsystemRep.cpp:2227).
+template <class R> static void pointJacobian(const Topology& t, const Work<R>& w, int body, const V3<R>& pS, R sign,
+                                             R* Grow /* 3 x nu */) {
     for (int a = body; a != 0; a = t.b[a].parent) {
         const Body& ab = t.b[a];
         const BodyCache<R>& ac = w.c[a];
@@ -109,14 +115,25 @@ template <class R> static void ballJacobian(const Topology& t, const Work<R>& w,
     }
 }
 
+// Ground location of station S (station2 on body2).
+template <class R> static V3<R> pointS(const Work<R>& w, const sbg_ball_constraint_desc& c) {
+    return w.c[c.body2].p_GB + w.c[c.body2].R_GB * loadV<R>(c.station2);
+}
+
+// The Ball constraint (ConstraintImpl.h:1835-1993) keeps station P
+// (station1 on body1) and S (station2 on body2) together. perr = p_S - p_P;
+// the velocity and acceleration errors and the constraint forces use the
+// material point C of body1 coincident with S, not P (:1915-1991):
+// verr = v_S - v_C, aerr = a_S - a_C, +lambda at S on body2, -lambda at C.
 template <class R> static void constraintJacobian(const Topology& t, const Work<R>& w, std::vector<R>& G) {
     const int m = 3 * (int)t.constraints.size();
     G.assign((size_t)m * t.nu, R(0));
     for (size_t ci = 0; ci < t.constraints.size(); ++ci) {
         const auto& c = t.constraints[ci];
         R* rows = G.data() + 3 * ci * t.nu;
-        ballJacobian(t, w, c.body2, c.station2, R(1), rows);
-        ballJacobian(t, w, c.body1, c.station1, R(-1), rows);
+        const V3<R> pS = pointS(w, c);
+        pointJacobian(t, w, c.body2, pS, R(1), rows);
+        pointJacobian(t, w, c.body1, pS, R(-1), rows);
     }
 }
 
@@ -172,9 +189,10 @@ static int realizeAccelerationLoops(const Topology& t, const double* y, Work<dou
     std::vector<double> aerr(m);
     for (size_t ci = 0; ci < t.constraints.size(); ++ci) {
         const auto& c = t.constraints[ci];
-        V3<double> p1, v1, a1, p2, v2, a2;
-        stationKin(w, c.body1, c.station1, p1, v1, &a1, Aw.data(), Av.data());
-        stationKin(w, c.body2, c.station2, p2, v2, &a2, Aw.data(), Av.data());
+        const V3<double> pS = pointS(w, c);
+        V3<double> v1, a1, v2, a2;
+        pointKin(w, c.body1, pS, v1, &a1, Aw.data(), Av.data());
+        pointKin(w, c.body2, pS, v2, &a2, Aw.data(), Av.data());
         for (int k = 0; k < 3; ++k) aerr[3 * ci + k] = a2[k] - a1[k];
     }
     std::vector<double> G;
@@ -258,76 +276,183 @@ static void normalizeQuaternions(const Topology& t, double* q) {
     }
 }
 
-// Ball-constraint position projection: Newton on perr with the minimum-norm
-// step dq = N G^T (G G^T)^-1 perr through the u-space Jacobian (projectQ,
-// SimbodyMatterSubsystemRep.cpp:4271-4300, unit weights). Returns false when
-// it does not converge to tol within 20 iterations.
-static bool projectBallQ(const Topology& t, double* q, Work<double>& w, double tol) {
-    const int m = 3 * (int)t.constraints.size();
-    std::vector<double> perr(m), G, A((size_t)m * m), lam(m), du(t.nu);
-    for (int it = 0; it < 20; ++it) {
-        realizePosition(t, q, w);
-        perrAll(t, w, perr.data());
-        if (normRMS(perr.data(), m) <= tol) return true;
-        constraintJacobian(t, w, G);
-        for (int i = 0; i < m; ++i)
-            for (int j = 0; j < m; ++j) {
-                double s = 0;
-                for (int k = 0; k < t.nu; ++k) s += G[(size_t)i * t.nu + k] * G[(size_t)j * t.nu + k];
-                A[(size_t)i * m + j] = s;
-            }
-        lam = perr;
-        if (!cholSolve(m, A, lam)) return false;
-        for (int k = 0; k < t.nu; ++k) {
-            double s = 0;
-            for (int i = 0; i < m; ++i) s += G[(size_t)i * t.nu + k] * lam[i];
-            du[k] = s;
-        }
-        // q -= N(q) du
-        for (int bi = 1; bi <= t.nb; ++bi) {
-            const Body& b = t.b[bi];
-            double* qb = q + b.qoff;
-            const double* ub = du.data() + b.uoff;
-            if (b.type == SBG_BALL || b.type == SBG_FREE) {
-                const double e0 = qb[0] / 2, e1 = qb[1] / 2, e2 = qb[2] / 2, e3 = qb[3] / 2;
-                const double d0 = -e1 * ub[0] - e2 * ub[1] - e3 * ub[2];
-                const double d1 = e0 * ub[0] + e3 * ub[1] - e2 * ub[2];
-                const double d2 = -e3 * ub[0] + e0 * ub[1] + e1 * ub[2];
-                const double d3 = e2 * ub[0] - e1 * ub[1] + e0 * ub[2];
-                qb[0] -= d0; qb[1] -= d1; qb[2] -= d2; qb[3] -= d3;
-                if (b.type == SBG_FREE) { qb[4] -= ub[3]; qb[5] -= ub[4]; qb[6] -= ub[5]; }
-            } else {
-                for (int j = 0; j < b.nq; ++j) qb[j] -= ub[j];
-            }
-        }
-        normalizeQuaternions(t, q);
+// ---------------------------------------------------------- projection
+// Both projections solve a weighted minimum-norm correction through the
+// normal equations, factored by Cholesky (the reference factors the
+// weighted Jacobian with rank-revealing QTZ; the two agree for full-rank G).
+//
+// Position (projectQ, SimbodyMatterSubsystemRep.cpp:4096-4442): the reference
+// solves (P NInv) x = perr for the minimum-norm x and steps q -= N NInv x
+// (Wu = 1, Tp = 1; :4271-4300). With D = NInv NInv^T, which is 4|q|^2 I on
+// the rotational mobilities of a quaternion joint (Rotation.h:742-748) and 1
+// elsewhere, that is du = D G^T (G D G^T)^-1 perr, q -= N(q) du. Full Newton
+// until RMS(perr) <= 0.1 tol, at most 20 iterations; with localOnly the
+// iteration stops when the norm grows (:4310-4321); the entry q is restored
+// if the result is worse than on entry (:4336-4341); then quaternions are
+// normalized (:4411-4413).
+//
+// Velocity (projectU, :4664-4943): weights uRelScale_i = max(|u_i|, 1)
+// taken at entry (:4760-4765), du = E^2 G^T (G E^2 G^T)^-1 verr with the
+// factorization made once (:4806-4808), at most 7 iterations.
+
+static double normRMSv(const std::vector<double>& v) { return normRMS(v.data(), (int)v.size()); }
+
+// D = diag(NInv NInv^T) per mobility for the current (unnormalized) q.
+static void projectionWeightsQ(const Topology& t, const double* q, std::vector<double>& D) {
+    D.assign(t.nu, 1.0);
+    for (int bi = 1; bi <= t.nb; ++bi) {
+        const Body& b = t.b[bi];
+        if (b.type != SBG_BALL && b.type != SBG_FREE) continue;
+        const double* qq = q + b.qoff;
+        const double n2 = qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3];
+        for (int k = 0; k < 3; ++k) D[b.uoff + k] = 4 * n2;
     }
-    realizePosition(t, q, w);
-    perrAll(t, w, perr.data());
-    return normRMS(perr.data(), m) <= tol;
 }
 
-// Velocity projection for Ball loops: u -= G^T (G G^T)^-1 (G u).
-static bool projectBallU(const Topology& t, const double* q, double* u, Work<double>& w) {
-    const int m = 3 * (int)t.constraints.size();
-    realizePosition(t, q, w);
-    std::vector<double> G, A((size_t)m * m), v(m);
-    constraintJacobian(t, w, G);
-    for (int i = 0; i < m; ++i) {
-        double s = 0;
-        for (int k = 0; k < t.nu; ++k) s += G[(size_t)i * t.nu + k] * u[k];
-        v[i] = s;
+// A = G diag(Wt) G^T (m x m).
+static void weightedGram(int m, int nu, const std::vector<double>& G, const std::vector<double>& Wt,
+                         std::vector<double>& A) {
+    A.assign((size_t)m * m, 0.0);
+    for (int i = 0; i < m; ++i)
         for (int j = 0; j < m; ++j) {
-            double a = 0;
-            for (int k = 0; k < t.nu; ++k) a += G[(size_t)i * t.nu + k] * G[(size_t)j * t.nu + k];
-            A[(size_t)i * m + j] = a;
+            double s = 0;
+            for (int k = 0; k < nu; ++k) s += G[(size_t)i * nu + k] * Wt[k] * G[(size_t)j * nu + k];
+            A[(size_t)i * m + j] = s;
+        }
+}
+
+// du = diag(Wt) G^T lambda.
+static void weightedGT(int m, int nu, const std::vector<double>& G, const std::vector<double>& Wt,
+                       const std::vector<double>& lam, std::vector<double>& du) {
+    du.assign(nu, 0.0);
+    for (int k = 0; k < nu; ++k) {
+        double s = 0;
+        for (int i = 0; i < m; ++i) s += G[(size_t)i * nu + k] * lam[i];
+        du[k] = Wt[k] * s;
+    }
+}
+
+// dq = N(q) du with the unnormalized N of Rotation.h:712-719.
+static void multiplyByN(const Topology& t, const double* q, const double* du, double* dq) {
+    for (int bi = 1; bi <= t.nb; ++bi) {
+        const Body& b = t.b[bi];
+        const double* qb = q + b.qoff;
+        const double* ub = du + b.uoff;
+        double* d = dq + b.qoff;
+        if (b.type == SBG_BALL || b.type == SBG_FREE) {
+            const double e0 = qb[0] / 2, e1 = qb[1] / 2, e2 = qb[2] / 2, e3 = qb[3] / 2;
+            d[0] = -e1 * ub[0] - e2 * ub[1] - e3 * ub[2];
+            d[1] = e0 * ub[0] + e3 * ub[1] - e2 * ub[2];
+            d[2] = -e3 * ub[0] + e0 * ub[1] + e1 * ub[2];
+            d[3] = e2 * ub[0] - e1 * ub[1] + e0 * ub[2];
+            if (b.type == SBG_FREE) { d[4] = ub[3]; d[5] = ub[4]; d[6] = ub[5]; }
+        } else {
+            for (int j = 0; j < b.nq; ++j) d[j] = ub[j];
         }
     }
-    if (!cholSolve(m, A, v)) return false;
+}
+
+static void perrAt(const Topology& t, const double* q, Work<double>& w, std::vector<double>& perr) {
+    realizePosition(t, q, w);
+    perr.resize(3 * t.constraints.size());
+    perrAll(t, w, perr.data());
+}
+
+// Velocity errors v_G(S2) - v_G(S1) at (q, u); realizePosition must be current.
+static void verrAt(const Topology& t, const double* q, const double* u, Work<double>& w, std::vector<double>& verr) {
+    std::vector<double> qdot(t.nq);
+    realizeVelocity(t, q, u, w, qdot.data());
+    verr.resize(3 * t.constraints.size());
+    for (size_t ci = 0; ci < t.constraints.size(); ++ci) {
+        const auto& c = t.constraints[ci];
+        const V3<double> pS = pointS(w, c);
+        V3<double> v1, v2;
+        pointKin(w, c.body1, pS, v1, (V3<double>*)nullptr, (const V3<double>*)nullptr, (const V3<double>*)nullptr);
+        pointKin(w, c.body2, pS, v2, (V3<double>*)nullptr, (const V3<double>*)nullptr, (const V3<double>*)nullptr);
+        for (int k = 0; k < 3; ++k) verr[3 * ci + k] = v2[k] - v1[k];
+    }
+}
+
+// Newton iteration of projectQ (loops present, perr not yet acceptable).
+static bool projectQNewton(const Topology& t, double* q, Work<double>& w, double tol, bool localOnly) {
+    const int m = 3 * (int)t.constraints.size();
+    std::vector<double> perr, G, D, A, lam, du, dq(t.nq);
+    perrAt(t, q, w, perr);
+    const double normOnEntry = normRMSv(perr);
+    const std::vector<double> saveQ(q, q + t.nq);
+    const double tryFor = std::max(0.1 * tol, std::pow(std::numeric_limits<double>::epsilon(), 0.875));
+    double achieved = normOnEntry, prev = normOnEntry;
+    int its = 0;
+    do {
+        constraintJacobian(t, w, G);
+        projectionWeightsQ(t, q, D);
+        weightedGram(m, t.nu, G, D, A);
+        lam = perr;
+        if (!cholSolve(m, A, lam)) return false;
+        weightedGT(m, t.nu, G, D, lam, du);
+        multiplyByN(t, q, du.data(), dq.data());
+        for (int k = 0; k < t.nq; ++k) q[k] -= dq[k];
+        perrAt(t, q, w, perr);
+        achieved = normRMSv(perr);
+        ++its;
+        if (localOnly && its >= 2 && achieved > prev) {
+            for (int k = 0; k < t.nq; ++k) q[k] += dq[k];
+            perrAt(t, q, w, perr);
+            achieved = normRMSv(perr);
+            break;
+        }
+        prev = achieved;
+    } while (achieved > tryFor && its < 20);
+    if (achieved > tol) {
+        if (achieved >= normOnEntry) std::copy(saveQ.begin(), saveQ.end(), q);
+        return false;
+    }
+    normalizeQuaternions(t, q);
+    return true;
+}
+
+// projectU with loops present; force = ProjectOptions::ForceProjection.
+static bool projectULoops(const Topology& t, const double* q, double* u, Work<double>& w, double tol, bool force,
+                          double limit, bool localOnly) {
+    const int m = 3 * (int)t.constraints.size();
+    std::vector<double> verr, G, E2(t.nu), A, lam, du;
+    realizePosition(t, q, w);
+    verrAt(t, q, u, w, verr);
+    const double normOnEntry = normRMSv(verr);
+    if (normOnEntry > limit) return false;
+    if (normOnEntry == 0 || (normOnEntry <= tol && !force)) return true;
     for (int k = 0; k < t.nu; ++k) {
-        double s = 0;
-        for (int i = 0; i < m; ++i) s += G[(size_t)i * t.nu + k] * v[i];
-        u[k] -= s;
+        const double e = std::abs(u[k]) > 1 ? std::abs(u[k]) : 1.0;
+        E2[k] = e * e;
+    }
+    constraintJacobian(t, w, G);
+    weightedGram(m, t.nu, G, E2, A);
+    // factor once: cholSolve factors in place, so keep the factor for reuse
+    const std::vector<double> A0 = A;
+    const std::vector<double> saveU(u, u + t.nu);
+    const double tryFor = std::max(0.1 * tol, std::pow(std::numeric_limits<double>::epsilon(), 0.875));
+    double achieved = normOnEntry, prev = normOnEntry;
+    int its = 0;
+    do {
+        A = A0;
+        lam = verr;
+        if (!cholSolve(m, A, lam)) return false;
+        weightedGT(m, t.nu, G, E2, lam, du);
+        for (int k = 0; k < t.nu; ++k) u[k] -= du[k];
+        verrAt(t, q, u, w, verr);
+        achieved = normRMSv(verr);
+        ++its;
+        if (localOnly && its >= 2 && achieved > prev) {
+            for (int k = 0; k < t.nu; ++k) u[k] += du[k];
+            verrAt(t, q, u, w, verr);
+            achieved = normRMSv(verr);
+            break;
+        }
+        prev = achieved;
+    } while (achieved > tryFor && its < 7);
+    if (achieved > tol) {
+        if (achieved >= normOnEntry) std::copy(saveU.begin(), saveU.end(), u);
+        return false;
     }
     return true;
 }
@@ -348,10 +473,15 @@ int rkMerson(const Topology& t, double* y, double* time, double h, int nsteps, c
         status |= st;
     };
     // initialize: ForceProjection
-    normalizeQuaternions(t, y);
+    // ForceProjection, not LocalOnly, no projection limit (IntegratorRep.h:856-895):
+    // with loops at least one Newton iteration runs unless perr is exactly 0.
+    std::vector<double> perr0;
+    if (loops) perrAt(t, y, w, perr0);
+    if (!loops || normRMSv(perr0) == 0) normalizeQuaternions(t, y);
+    else if (!projectQNewton(t, y, w, o.consTol, false)) status |= SBG_INST_PROJECTION_FAILED;
     if (loops) {
-        if (!projectBallQ(t, y, w, o.consTol)) status |= SBG_INST_PROJECTION_FAILED;
-        if (!projectBallU(t, y, y + t.nq, w)) status |= SBG_INST_PROJECTION_FAILED;
+        if (!projectULoops(t, y, y + t.nq, w, o.consTol, true, HUGE_VAL, false))
+            status |= SBG_INST_PROJECTION_FAILED;
     }
     double tc = *time;
     for (int step = 0; step < nsteps; ++step) {
@@ -402,18 +532,23 @@ int rkMerson(const Topology& t, double* y, double* time, double h, int nsteps, c
                 perrNorm = normRMS(perr.data(), (int)perr.size());
             }
             const double normOnEntry = std::max(perrNorm, quatNorm);
+            // A failed projection fails attemptDAEStep (:185-187, :197-199);
+            // a fixed step cannot shrink, so the step stands and the status
+            // records the failure.
+            bool qok = true;
             if (normOnEntry > projLimit) {
-                status |= SBG_INST_PROJECTION_FAILED;  // step still accepted (fixed step)
+                qok = false;
             } else if (perrNorm == 0 || (perrNorm <= o.consTol && !o.projectEveryStep)) {
                 if (quatNorm > o.consTol || o.projectEveryStep) {
                     normalizeQuaternions(t, y);
                     if (nProjections) ++*nProjections;
                 }
             } else {
-                if (!projectBallQ(t, y, w, o.consTol)) status |= SBG_INST_PROJECTION_FAILED;
+                qok = projectQNewton(t, y, w, o.consTol, true);
                 if (nProjections) ++*nProjections;
             }
-            if (loops && !projectBallU(t, y, y + t.nq, w)) status |= SBG_INST_PROJECTION_FAILED;
+            if (qok && loops) qok = projectULoops(t, y, y + t.nq, w, o.consTol, o.projectEveryStep, projLimit, true);
+            if (!qok) status |= SBG_INST_PROJECTION_FAILED;
         }
         tc = t1;
     }

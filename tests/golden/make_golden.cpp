@@ -1,0 +1,186 @@
+// make_golden.cpp -- writes golden input/output vectors for the hot path by
+// running a built Simbody (the reference) on the seeded synthetic workloads.
+//
+// Built and run by make_golden.py next to this file; it is not part of the
+// library and nothing at test time compiles or runs it. For each selected
+// instance of workload configs 1-5 it records:
+//   y0                      the seeded state (from libsbg_workloads)
+//   ydot                    System::realize(s, Stage::Acceleration); s.getYDot()
+//   f, minv_f               SimbodyMatterSubsystem::multiplyByMInv(s, f, out)
+//   y_rk, t_rk              RungeKuttaMersonIntegrator with setFixedStepSize(h),
+//                           default accuracy, the default constraint tolerance
+//                           or cons_tol when it is nonzero (tight tolerances
+//                           make the in-step projections run), stepped for
+//                           exactly nsteps steps
+// Reference calls used (paths relative to the Simbody source tree):
+//   MobilizedBody::{Pin,Slider,Universal,Ball,Free} (Simbody/include/simbody/internal/MobilizedBody_*.h)
+//   Force::Gravity, Force::MobilityLinearSpring/Damper (Simbody/include/simbody/internal/Force*.h)
+//   Constraint::Ball (Simbody/include/simbody/internal/Constraint_Ball.h)
+//   RungeKuttaMersonIntegrator (SimTKmath/Integrators/include/simmath/RungeKuttaMersonIntegrator.h)
+//
+// Output: one binary file of records
+//   int64 cfg, inst, ny, nu, nsteps, status   double h, t_rk, cons_tol
+//   double y0[ny], ydot[ny], f[nu], minv_f[nu], y_rk[ny]
+#include "Simbody.h"
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "sbg_workloads.h"
+
+using namespace SimTK;
+
+namespace {
+
+Transform toTransform(const double* x) {
+    // x = row-major 3x3 rotation followed by the translation
+    const Mat33 R(x[0], x[1], x[2], x[3], x[4], x[5], x[6], x[7], x[8]);
+    return Transform(Rotation(R, true), Vec3(x[9], x[10], x[11]));
+}
+
+// One MultibodySystem per described system; body index 0 is Ground and body
+// k >= 1 is desc.bodies[k-1].
+struct Model {
+    MultibodySystem sys;
+    SimbodyMatterSubsystem matter;
+    GeneralForceSubsystem forces;
+    std::vector<MobilizedBody> mobods;
+
+    explicit Model(const sbg_system_desc& d) : matter(sys), forces(sys) {
+        const Vec3 g(d.gravity[0], d.gravity[1], d.gravity[2]);
+        Force::Gravity(forces, matter, UnitVec3(g), g.norm());
+        mobods.push_back(matter.Ground());
+        for (int i = 0; i < d.nbodies; ++i) {
+            const sbg_body_desc& b = d.bodies[i];
+            const UnitInertia G(b.unit_inertia[0], b.unit_inertia[1], b.unit_inertia[2], b.unit_inertia[3],
+                                b.unit_inertia[4], b.unit_inertia[5]);
+            Body::Rigid body(MassProperties(b.mass, Vec3(b.com[0], b.com[1], b.com[2]), G));
+            MobilizedBody& P = mobods[b.parent];
+            const Transform X_PF = toTransform(b.X_PF), X_BM = toTransform(b.X_BM);
+            switch (b.mobilizer) {
+            case SBG_PIN: mobods.push_back(MobilizedBody::Pin(P, X_PF, body, X_BM)); break;
+            case SBG_SLIDER: mobods.push_back(MobilizedBody::Slider(P, X_PF, body, X_BM)); break;
+            case SBG_UNIVERSAL: mobods.push_back(MobilizedBody::Universal(P, X_PF, body, X_BM)); break;
+            case SBG_BALL: mobods.push_back(MobilizedBody::Ball(P, X_PF, body, X_BM)); break;
+            default: mobods.push_back(MobilizedBody::Free(P, X_PF, body, X_BM)); break;
+            }
+        }
+        for (int i = 0; i < d.nforces; ++i) {
+            const sbg_mobility_force_desc& f = d.forces[i];
+            if (f.kind == 0)
+                Force::MobilityLinearSpring(forces, mobods[f.body], MobilizerQIndex(f.which), f.coef, f.q0);
+            else
+                Force::MobilityLinearDamper(forces, mobods[f.body], MobilizerUIndex(f.which), f.coef);
+        }
+        for (int i = 0; i < d.nconstraints; ++i) {
+            const sbg_ball_constraint_desc& c = d.constraints[i];
+            Constraint::Ball(mobods[c.body1], Vec3(c.station1[0], c.station1[1], c.station1[2]), mobods[c.body2],
+                             Vec3(c.station2[0], c.station2[1], c.station2[2]));
+        }
+        sys.realizeTopology();
+    }
+};
+
+void put(FILE* fp, const void* p, size_t bytes) {
+    if (fwrite(p, 1, bytes, fp) != bytes) {
+        fprintf(stderr, "write failed\n");
+        std::exit(1);
+    }
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 2) {
+        fprintf(stderr, "usage: make_golden OUT.bin\n");
+        return 2;
+    }
+    FILE* fp = fopen(argv[1], "wb");
+    if (!fp) return 1;
+    struct Sel { int cfg, ninst, nsteps; double h; std::vector<int> pick; double consTol; };
+    // cfg 5 draws 1-4 Ball loops for about one request in five; the
+    // instances listed are ones that carry loops and ones that do not.
+    const Sel sels[] = {
+        {1, 8, 1000, 1e-3, {0, 1, 2, 3}, 0},
+        {1, 8, 20, 1e-3, {4, 5, 6, 7}, 0},
+        {2, 4, 20, 5e-4, {0, 1, 2, 3}, 0},
+        {3, 6, 20, 5e-4, {0, 1, 2, 3, 4, 5}, 0},
+        {4, 8, 20, 5e-4, {0, 1, 2, 3, 4, 5, 6, 7}, 0},
+        {5, 64, 20, 5e-4, {}, 0},
+        {5, 64, 200, 5e-4, {}, 1e-9},
+    };
+    int written = 0;
+    for (const Sel& s : sels) {
+        sbg_workload w;
+        if (sbg_workload_create(s.cfg, s.ninst, &w)) {
+            fprintf(stderr, "workload %d: %s\n", s.cfg, sbg_workload_last_error());
+            return 1;
+        }
+        const sbg_system_desc* systems = sbg_workload_systems(w);
+        const int32_t* isys = sbg_workload_instance_system(w);
+        const int64_t* yo = sbg_workload_y_offsets(w);
+        const double* y0 = sbg_workload_y0(w);
+        std::vector<int> pick = s.pick;
+        if (pick.empty()) {  // config 5: four constrained requests and two free ones
+            int withLoops = 0, without = 0;
+            for (int i = 0; i < s.ninst; ++i) {
+                const bool loops = systems[isys[i]].nconstraints > 0;
+                if (loops && withLoops < 4) { pick.push_back(i); ++withLoops; }
+                if (!loops && without < 2) { pick.push_back(i); ++without; }
+            }
+        }
+        for (int i : pick) {
+            const sbg_system_desc& d = systems[isys[i]];
+            Model m(d);
+            const int64_t ny = yo[i + 1] - yo[i];
+            int64_t status = 0;
+            State st = m.sys.getDefaultState();
+            if (st.getNY() != ny) {
+                fprintf(stderr, "cfg %d inst %d: ny %d != %lld\n", s.cfg, i, st.getNY(), (long long)ny);
+                return 1;
+            }
+            const int64_t nu = st.getNU();
+            for (int k = 0; k < ny; ++k) st.updY()[k] = y0[yo[i] + k];
+            std::vector<double> ydot(ny), f(nu), minv(nu), yrk(ny);
+            m.sys.realize(st, Stage::Acceleration);
+            for (int k = 0; k < ny; ++k) ydot[k] = st.getYDot()[k];
+            Vector fv((int)nu), out;
+            for (int k = 0; k < nu; ++k) fv[k] = f[k] = std::cos(0.7 * k + 0.3 * i + s.cfg);
+            m.matter.multiplyByMInv(st, fv, out);
+            for (int k = 0; k < nu; ++k) minv[k] = out[k];
+            double trk = 0;
+            try {
+                State s2 = m.sys.getDefaultState();
+                for (int k = 0; k < ny; ++k) s2.updY()[k] = y0[yo[i] + k];
+                RungeKuttaMersonIntegrator integ(m.sys);
+                integ.setFixedStepSize(s.h);
+                integ.setReturnEveryInternalStep(true);
+                if (s.consTol > 0) integ.setConstraintTolerance(s.consTol);
+                integ.initialize(s2);
+                while (integ.getNumStepsTaken() < s.nsteps) integ.stepTo(1e9);
+                for (int k = 0; k < ny; ++k) yrk[k] = integ.getState().getY()[k];
+                trk = integ.getTime();
+            } catch (const std::exception& e) {
+                fprintf(stderr, "cfg %d inst %d: integrator failed: %s\n", s.cfg, i, e.what());
+                status = 1;
+            }
+            const int64_t hdr[6] = {s.cfg, i, ny, nu, s.nsteps, status};
+            const double hd[3] = {s.h, trk, s.consTol};
+            put(fp, hdr, sizeof hdr);
+            put(fp, hd, sizeof hd);
+            put(fp, &y0[yo[i]], ny * 8);
+            put(fp, ydot.data(), ny * 8);
+            put(fp, f.data(), nu * 8);
+            put(fp, minv.data(), nu * 8);
+            put(fp, yrk.data(), ny * 8);
+            ++written;
+        }
+        sbg_workload_destroy(w);
+    }
+    fclose(fp);
+    printf("%d records\n", written);
+    return 0;
+}

@@ -1,0 +1,93 @@
+"""Regenerates tests/golden/reference_vectors.npz from a built Simbody.
+
+  python tests/golden/make_golden.py --simbody-src SRC --simbody-lib LIBDIR
+
+SRC is a Simbody source tree (its public headers are used) and LIBDIR holds
+libSimTKcommon/libSimTKmath/libSimTKsimbody from a Release build of it. The
+driver make_golden.cpp is compiled against them, run on the seeded workloads
+(libsbg_workloads), and its records are packed into one .npz:
+
+  cfg, inst, ny, nu, nsteps, status, h, t_rk,    one entry per record
+  cons_tol (0 = the integrator's default)
+  y_off, u_off                                   offsets into the flat arrays
+  y0, ydot, y_rk (by y_off); f, minv_f (by u_off)
+
+The vectors are committed; the tests only read the .npz.
+"""
+from __future__ import annotations
+
+import argparse
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+
+
+def include_dirs(src: Path) -> list[str]:
+    dirs = []
+    for p in sorted(src.rglob("include")):
+        rel = p.relative_to(src).parts
+        if p.is_dir() and not any(x in ("tests", "examples", "doc", "src") for x in rel):
+            dirs.append(str(p))
+    return dirs
+
+
+def read_records(path: Path) -> dict:
+    raw = path.read_bytes()
+    pos = 0
+    recs = []
+    while pos < len(raw):
+        hdr = np.frombuffer(raw, dtype=np.int64, count=6, offset=pos)
+        pos += 48
+        h, t, ctol = np.frombuffer(raw, dtype=np.float64, count=3, offset=pos)
+        pos += 24
+        cfg, inst, ny, nu, nsteps, status = (int(v) for v in hdr)
+        arrs = {}
+        for name, n in (("y0", ny), ("ydot", ny), ("f", nu), ("minv_f", nu), ("y_rk", ny)):
+            arrs[name] = np.frombuffer(raw, dtype=np.float64, count=n, offset=pos).copy()
+            pos += 8 * n
+        recs.append(dict(cfg=cfg, inst=inst, ny=ny, nu=nu, nsteps=nsteps, status=status, h=h, t_rk=t, cons_tol=ctol, **arrs))
+    out = {k: np.array([r[k] for r in recs]) for k in ("cfg", "inst", "ny", "nu", "nsteps", "status", "h", "t_rk",
+                                                 "cons_tol")}
+    out["y_off"] = np.concatenate([[0], np.cumsum(out["ny"])]).astype(np.int64)
+    out["u_off"] = np.concatenate([[0], np.cumsum(out["nu"])]).astype(np.int64)
+    for k in ("y0", "ydot", "y_rk"):
+        out[k] = np.concatenate([r[k] for r in recs])
+    for k in ("f", "minv_f"):
+        out[k] = np.concatenate([r[k] for r in recs])
+    return out
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--simbody-src", required=True, type=Path)
+    ap.add_argument("--simbody-lib", required=True, type=Path)
+    ap.add_argument("--out", type=Path, default=HERE / "reference_vectors.npz")
+    a = ap.parse_args()
+    sys.path.insert(0, str(ROOT))
+    from simbody_gb300.build import OUT, build_workloads
+
+    wl = build_workloads()
+    with tempfile.TemporaryDirectory() as td:
+        exe = Path(td) / "make_golden"
+        cmd = ["g++", "-O2", "-std=c++17", str(HERE / "make_golden.cpp"), "-o", str(exe),
+               f"-I{ROOT / 'simbody_gb300' / 'csrc'}", f"-I{ROOT / 'include'}"]
+        cmd += [f"-I{d}" for d in include_dirs(a.simbody_src)]
+        cmd += [f"-L{a.simbody_lib}", "-lSimTKsimbody", "-lSimTKmath", "-lSimTKcommon",
+                f"-Wl,-rpath,{a.simbody_lib}", str(wl), f"-Wl,-rpath,{OUT}"]
+        subprocess.run(cmd, check=True)
+        binf = Path(td) / "records.bin"
+        subprocess.run([str(exe), str(binf)], check=True, env={"OPENBLAS_NUM_THREADS": "1"})
+        data = read_records(binf)
+    np.savez_compressed(a.out, **data)
+    print(f"wrote {a.out}: {len(data['cfg'])} records")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,112 @@
+"""The CPU oracle against golden vectors recorded from the reference.
+
+tests/golden/reference_vectors.npz holds, for seeded instances of workload
+configs 1-5, the outputs of a built Simbody (make_golden.py / .cpp beside it):
+realize(Stage::Acceleration) y-derivatives, multiplyByMInv(f), and the state
+after a fixed number of RungeKuttaMersonIntegrator steps (fixed step size,
+default accuracy; some config-5 records with loop closures use a 1e-9
+constraint tolerance so that the in-step position and velocity projections
+run). These pin the oracle, which in turn is the reference the CUDA engine
+is checked against.
+
+Tolerances (relative 2-norm per record): 1e-12 for realize and M^-1 f;
+1e-11 for trajectories (20-1000 steps; roundoff grows along a trajectory).
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from simbody_gb300 import Workload
+
+GOLD = Path(__file__).resolve().parent / "golden" / "reference_vectors.npz"
+WORKLOAD_SIZES = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64}
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return dict(np.load(GOLD))
+
+
+@pytest.fixture(scope="module")
+def workloads():
+    return {c: Workload(c, n) for c, n in WORKLOAD_SIZES.items()}
+
+
+def _records(g):
+    for r in range(len(g["cfg"])):
+        ys = slice(int(g["y_off"][r]), int(g["y_off"][r + 1]))
+        us = slice(int(g["u_off"][r]), int(g["u_off"][r + 1]))
+        yield r, int(g["cfg"][r]), int(g["inst"][r]), ys, us
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def test_fixture_inputs_match_generator(gold, workloads):
+    """The seeded generator still produces the recorded inputs bit for bit."""
+    for r, cfg, inst, ys, _ in _records(gold):
+        w = workloads[cfg]
+        assert np.array_equal(w.y0[w.instance_slice(inst)], gold["y0"][ys]), (cfg, inst)
+
+
+def test_fixture_covers_every_mobilizer_and_loops(gold, workloads):
+    kinds, loops = set(), 0
+    for r, cfg, inst, ys, _ in _records(gold):
+        d = workloads[cfg].systems[int(workloads[cfg].instance_system[inst])]
+        kinds |= {d.bodies[k].mobilizer for k in range(d.nbodies)}
+        loops += d.nconstraints > 0
+    assert kinds == {0, 1, 2, 3, 4} and loops >= 4
+
+
+def test_realize_matches_reference(gold, workloads):
+    for r, cfg, inst, ys, _ in _records(gold):
+        ydot, st = O.realize_workload(workloads[cfg], [inst])
+        assert st[0] == 0
+        assert _rel(ydot, gold["ydot"][ys]) <= 1e-12, (cfg, inst)
+
+
+def test_multiply_by_minv_matches_reference(gold, workloads):
+    for r, cfg, inst, ys, us in _records(gold):
+        w = workloads[cfg]
+        y0 = gold["y0"][ys]
+        out = O.multiply_by_minv(w.systems, w.nsys, w.instance_system[[inst]], np.array([0, len(y0)]), y0,
+                                 np.array([0, us.stop - us.start]), gold["f"][us])
+        assert _rel(out, gold["minv_f"][us]) <= 1e-12, (cfg, inst)
+
+
+def test_rk_merson_matches_reference(gold, workloads):
+    for r, cfg, inst, ys, _ in _records(gold):
+        ctol = float(gold["cons_tol"][r])
+        kw = {"cons_tol": ctol} if ctol > 0 else {}
+        y, t, st, _ = O.rk_workload(workloads[cfg], float(gold["h"][r]), int(gold["nsteps"][r]), [inst], **kw)
+        assert st[0] == 0
+        assert t[0] == gold["t_rk"][r]
+        assert _rel(y, gold["y_rk"][ys]) <= 1e-11, (cfg, inst, _rel(y, gold["y_rk"][ys]))
+
+
+def test_double_pendulum_one_second_recorded_value(gold):
+    """Config 1, instance 0, 1000 steps of h = 1e-3: the reference gives
+    q0(1 s) = 0.47628747478039263 and u0(1 s) = 4.3677176498038577."""
+    w = Workload(1, 1)
+    y, t, st, _ = O.rk_workload(w, 1e-3, 1000)
+    assert abs(y[0] - 0.47628747478039263) <= 1e-13
+    assert abs(y[2] - 4.3677176498038577) <= 1e-12
+
+
+def test_tight_tolerance_records_project_in_steps(gold, workloads):
+    """With a 1e-9 constraint tolerance the oracle projects during the steps
+    (the reference does too), so the fixture exercises projectQ/projectU."""
+    done = 0
+    for r, cfg, inst, ys, _ in _records(gold):
+        if gold["cons_tol"][r] == 0:
+            continue
+        w = workloads[cfg]
+        if w.systems[int(w.instance_system[inst])].nconstraints == 0:
+            continue
+        _, _, _, nproj = O.rk_workload(w, float(gold["h"][r]), int(gold["nsteps"][r]), [inst],
+                                       cons_tol=float(gold["cons_tol"][r]))
+        done += nproj > 0
+    assert done >= 3
