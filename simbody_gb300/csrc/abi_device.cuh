@@ -784,7 +784,7 @@ __device__ __noinline__ void body5Free(const DevTables& T, int row, int rec, con
 // ---------------------------------------------------------------- drivers
 // Chain driver: one thread, rows in order; carries along chains, pushes into
 // the parent's record otherwise. Returns SBG_INST_* bits.
-template <class R, int NM, bool REF, class SC, class Src, class Out>
+template <class R, int NM, bool REF, bool LOOPS = false, class SC, class Src, class Out>
 __device__ __noinline__ int rhsChain(const DevTables& T, int inst, const SC& S, const Src& src, Out& out) {
     static_assert(!REF || std::is_same<R, float>::value, "refinement is for the FP32 recursion");
     const int body0 = T.ibody[inst], nb = T.inb[inst];
@@ -804,6 +804,8 @@ __device__ __noinline__ int rhsChain(const DevTables& T, int inst, const SC& S, 
                 storeKin(S, rec, carry);
                 storeC2(S, rec, zeroC2<R>());
             }
+            if constexpr (LOOPS)
+                if (info & F_LOOPBODY) storeKin(S, T.lrec[row], carry);
         }
     }
     bool ok = true;
@@ -838,6 +840,11 @@ __device__ __noinline__ int rhsChain(const DevTables& T, int inst, const SC& S, 
             const A3<R> Ap = parent < 0 ? A3<R>{} : (info & F_CARRY) ? carry : loadA3<R>(S, T.srec[body0 + parent], REF);
             if (n == 6) body3Free<R, REF>(T, row, rec, S, out, Ap, parent >= 0, carry);
             else carry = body3<R, NM, REF>(T, row, rec, n, S, out, Ap, parent >= 0);
+            if constexpr (LOOPS)
+                if (info & F_LOOPBODY) {
+                    st3<R>(S, T.lrec[row], kSlotA, carry.w);
+                    st3<R>(S, T.lrec[row], kSlotA + 3, carry.v);
+                }
             if (info & F_MEMCHILD) {
                 storeA3(S, rec, carry, REF);
                 if constexpr (REF)
@@ -996,6 +1003,7 @@ struct YdOut {
         yd[base + (int64_t)(nq + k) * stride] = double(v);
         finite &= isfinite(v);
     }
+    __device__ __forceinline__ double udotGet(int k) const { return yd[base + (int64_t)(nq + k) * stride]; }
 };
 // M^-1 f: q from the state columns, u = 0, f from fcol (u slots); the result
 // goes to the u slots of out (SimbodyMatterSubsystemRep.cpp:5357-5400).
@@ -1050,6 +1058,7 @@ template <class F> struct FOut {
     bool finite = true;
     template <class R> __device__ __forceinline__ void qdot(int k, R v) { f[base + (int64_t)k * stride] = F(v); finite &= isfinite(v); }
     template <class R> __device__ __forceinline__ void udot(int k, R v) { f[base + (int64_t)(nq + k) * stride] = F(v); finite &= isfinite(v); }
+    __device__ __forceinline__ double udotGet(int k) const { return double(f[base + (int64_t)(nq + k) * stride]); }
 };
 
 // Thread/group -> instance mapping. Chain kernels: thread t of the launch
@@ -1073,10 +1082,19 @@ __device__ __forceinline__ Slot groupSlot(const DevTables& T, int blk0) {
     return Slot{pos < T.blkFirst[b + 1] ? T.order[pos] : -1, (int)threadIdx.x % G, G, mask};
 }
 
-// One RHS of the instance owned by slot s, through either driver.
-template <class R, int NM, bool REF, bool GROUP, class Src, class Out>
+#include "loops_device.cuh"
+
+// One RHS of the instance owned by slot s, through either driver; LOOPS adds
+// the Ball loop-closure multipliers (FP64 chain driver).
+template <class R, int NM, bool REF, bool GROUP, bool LOOPS = false, class Src, class Out>
 __device__ __forceinline__ int rhs(const DevTables& T, const Slot& s, R* scratch, const Src& src, Out& out) {
-    if constexpr (GROUP) {
+    if constexpr (LOOPS) {
+        static_assert(std::is_same<R, double>::value && !GROUP && !REF, "loop closures run the FP64 chain driver");
+        const ScrTiled<double> S{scratch + T.sbase[s.inst]};
+        int st = rhsChain<double, NM, false, true>(T, s.inst, S, src, out);
+        if (T.incons[s.inst] > 0) st |= loopForwardDynamics<NM>(T, s.inst, S, out);
+        return st;
+    } else if constexpr (GROUP) {
         const ScrRows<R> S{scratch + T.sbase[s.inst], T.inb[s.inst]};
         return rhsGroup<R, NM, REF>(T, s.inst, S, src, out, s.gl, s.G, s.mask);
     } else {
@@ -1090,7 +1108,7 @@ template <bool GROUP> __device__ __forceinline__ bool groupAll(bool v, const Slo
 }
 
 // ------------------------------------------------------------ realize kernel
-template <class R, int NM, bool REF, bool GROUP, int MINB = 1>
+template <class R, int NM, bool REF, bool GROUP, int MINB = 1, bool LOOPS = false>
 __global__ void __launch_bounds__(128, MINB) realizeKernel(DevTables T, int first, int count, const double* __restrict__ y,
                                                            double* __restrict__ ydot, R* __restrict__ scratch,
                                                            int32_t* __restrict__ status) {
@@ -1098,7 +1116,7 @@ __global__ void __launch_bounds__(128, MINB) realizeKernel(DevTables T, int firs
     if (s.inst < 0) return;
     YSrc src{y, T.ybase[s.inst], T.ystride[s.inst], T.inq[s.inst]};
     YdOut out{ydot, T.ybase[s.inst], T.ystride[s.inst], T.inq[s.inst]};
-    int st = rhs<R, NM, REF, GROUP>(T, s, scratch, src, out);
+    int st = rhs<R, NM, REF, GROUP, LOOPS>(T, s, scratch, src, out);
     if (!groupAll<GROUP>(out.finite, s)) st |= SBG_INST_NONFINITE;
     if (s.gl == 0) status[s.inst] = st;
 }
@@ -1123,7 +1141,7 @@ __device__ __forceinline__ double groupSum(double v, const Slot& s) {
     return v;
 }
 
-template <class R, int NM, bool REF, bool GROUP, int MINB = 1>
+template <class R, int NM, bool REF, bool GROUP, int MINB = 1, bool LOOPS = false>
 __global__ void __launch_bounds__(128, MINB) rkMersonKernel(DevTables T, int first, int count, double* __restrict__ y,
                                                             double* __restrict__ time, R* __restrict__ fbuf,
                                                             int64_t fplane, R* __restrict__ scratch,
@@ -1145,10 +1163,18 @@ __global__ void __launch_bounds__(128, MINB) rkMersonKernel(DevTables T, int fir
     auto stage = [&](int stg, double c, const R* a, const R* b, R* dst) {
         StageSrc<R> src{y, f0, a, b, base, stride, nq, stg, c};
         FOut<R> o{dst, base, stride, nq};
-        st |= rhs<R, NM, REF, GROUP>(T, s, scratch, src, o);
+        st |= rhs<R, NM, REF, GROUP, LOOPS>(T, s, scratch, src, o);
         if (!groupAll<GROUP>(o.finite, s)) st |= SBG_INST_NONFINITE;
         if constexpr (GROUP) __syncwarp(s.mask);  // the next stage reads what other lanes wrote
     };
+    // Integrator::initialize with loop closures: forced position and
+    // velocity projection (IntegratorRep.h:856-895); the buffers fB/fC are
+    // free outside a step.
+    if constexpr (LOOPS)
+        if (T.incons[inst] > 0) {
+            const LoopState L{T, inst, ScrTiled<double>{scratch + T.sbase[inst]}, y, fB, fC, base, stride};
+            st |= loopInitialize<NM>(L, consTol);
+        }
     for (int step = 0; step < nsteps; ++step) {
         const double t1 = tc + h;
         const double hs = t1 - tc;
@@ -1226,7 +1252,17 @@ __global__ void __launch_bounds__(128, MINB) rkMersonKernel(DevTables T, int fir
         const double errNorm = qn >= un ? qn : un;
         // projection gate and quaternion normalization
         // (AbstractIntegratorRep.cpp:158-190, SimbodyMatterSubsystemRep.cpp:4096-4183)
-        if (errNorm <= 16 * accuracy && nquat > 0) {
+        bool loopsDone = false;
+        if constexpr (LOOPS)
+            if (T.incons[inst] > 0) {
+                loopsDone = true;
+                if (errNorm <= 16 * accuracy) {
+                    const LoopState L{T, inst, ScrTiled<double>{scratch + T.sbase[inst]}, y, fB, fC, base, stride};
+                    const double quatNorm = nquat > 0 ? sqrt(squat / nquat) : 0.0;
+                    st |= loopProjectStep<NM>(L, quatNorm, consTol, projLimit, projectEveryStep != 0);
+                }
+            }
+        if (!loopsDone && errNorm <= 16 * accuracy && nquat > 0) {
             const double quatNorm = sqrt(squat / nquat);
             if (quatNorm > projLimit) st |= SBG_INST_PROJECTION_FAILED;
             else if (quatNorm > consTol || projectEveryStep) {

@@ -77,6 +77,9 @@ struct sbg_batch_s {
     double* staging = nullptr;  // packed device staging (nyTotal)
     void* scratch = nullptr;
     void* fbuf = nullptr;       // RK stage derivatives, 4 planes
+    void* scratchLoop = nullptr;  // FP64 scratch of the loop-closure segment
+    void* fbufLoop = nullptr;     // FP64 stage derivatives of that segment (fbuf itself in FP64 batches)
+    int nLoop = 0;                // order positions [nChain, nChain + nLoop)
     int64_t scratchElems = 0;
     double* hostPinned = nullptr;  // pinned host staging (nyTotal)
     bool stateSet = false;
@@ -95,7 +98,9 @@ struct sbg_batch_s {
     cudaGraphExec_t realizeGraph = nullptr;  // captured after tuning
 
     Streams streams() const { return Streams{stream, stream2, evFork, evJoin}; }
-    LaunchPlan plan() const { return LaunchPlan{nChain, nGroupBlocks, nm, variant == 0 ? 1 : variant}; }
+    LaunchPlan plan() const { return LaunchPlan{nChain, nGroupBlocks, nm, variant == 0 ? 1 : variant, nLoop}; }
+    BatchBufs bufsArg() const { return BatchBufs{scratch, scratchLoop, fbuf, fbufLoop, colElems}; }
+    int segments() const { return (nChain > 0) + (nLoop > 0) + (nGroupBlocks > 0); }
 
     // Lanes per instance of the group segment: blocks of 128 threads hold
     // 128/G instances of equal G (the order is sorted by widest level, so G is
@@ -112,11 +117,11 @@ struct sbg_batch_s {
             int q = p;
             auto gOf = [&](int k) { int ww = 1; while (ww < groupWidthKey[k]) ww <<= 1; return std::max(2, std::min(32, ww >> shift)); };
             while (q < ng && q - p < 128 / G && gOf(q) == G) ++q;
-            first.push_back(nChain + p);
+            first.push_back(nChain + nLoop + p);
             gs.push_back(G);
             p = q;
         }
-        first.push_back(nChain + ng);
+        first.push_back(nChain + nLoop + ng);
         gs.push_back(0);
         nGroupBlocks = (int)gs.size() - 1;
         cudaError_t e = cudaMemcpy(dBlkFirst, first.data(), first.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
@@ -252,6 +257,8 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
         if (b.parent != 0 && rowOf[b.parent] == r - 1) info |= F_CARRY;
         for (int c : kids[bi])
             if (rowOf[c] != r + 1) info |= F_MEMCHILD;
+        for (int i = 0; i < d->nconstraints; ++i)
+            if (d->constraints[i].body1 == bi || d->constraints[i].body2 == bi) info |= F_LOOPBODY;
         t->parent.push_back(b.parent == 0 ? -1 : rowOf[b.parent]);
         t->info.push_back(info);
         t->qoff.push_back(qo[bi]);
@@ -303,6 +310,15 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
     for (int i = 1; i <= nb; ++i)
         if (d->bodies[i - 1].mobilizer >= SBG_BALL) t->defaultY[qo[i]] = 1.0;
     for (int i = 0; i < d->nconstraints; ++i) t->cons.push_back(d->constraints[i]);
+    t->lslot.assign(nb, -1);
+    for (int r = 0; r < nb; ++r)
+        if (t->info[r] & F_LOOPBODY) t->lslot[r] = t->nslots++;
+    for (const auto& c : t->cons) {
+        t->lcons.push_back(c.body1 == 0 ? -1 : rowOf[c.body1]);
+        t->lcons.push_back(c.body2 == 0 ? -1 : rowOf[c.body2]);
+        t->lst.insert(t->lst.end(), c.station1, c.station1 + 3);
+        t->lst.insert(t->lst.end(), c.station2, c.station2 + 3);
+    }
     *out = t;
     return SBG_OK;
 }
@@ -341,8 +357,9 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
         if (instTopo[i] < 0 || instTopo[i] >= ntopo || !topos[instTopo[i]])
             return fail(SBG_ERR_INVALID, "instance " + std::to_string(i) + " names a bad topology");
     for (int k = 0; k < ntopo; ++k)
-        if (topos[k] && topos[k]->ncons > 0)
-            return fail(SBG_ERR_UNSUPPORTED, "loop closures are handled by the serving engine (sbg_serve_*)");
+        if (topos[k] && topos[k]->ncons > kMaxLoopCons)
+            return fail(SBG_ERR_UNSUPPORTED, "at most " + std::to_string(kMaxLoopCons) +
+                                                 " Ball loop closures per system are supported");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -431,7 +448,7 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     // idle or diverge in a group); larger trees with wide levels get a group.
     int groupMinBodies = 48;
     if (const char* v = std::getenv("SBG_GROUP_MIN_BODIES")) groupMinBodies = std::atoi(v);  // tuning override
-    std::vector<int> chainPos, groupPos;
+    std::vector<int> chainPos, loopPos, groupPos;
     for (int i = 0; i < ninst; ++i) {
         const sbg_topology_s* t = topos[instTopo[i]];
         ibody[i] = rowBase[instTopo[i]];
@@ -443,11 +460,13 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
         for (int k = 0; k < 3; ++k) grav[3 * i + k] = t->gravity[k];
         b->hostYOff[i + 1] = b->hostYOff[i] + t->nq + t->nu;
         b->hostUOff[i + 1] = b->hostUOff[i] + t->nu;
-        if (t->chain || t->maxLevelWidth <= 2 || t->nb < groupMinBodies) chainPos.push_back(i);
+        if (t->ncons > 0) loopPos.push_back(i);
+        else if (t->chain || t->maxLevelWidth <= 2 || t->nb < groupMinBodies) chainPos.push_back(i);
         else groupPos.push_back(i);
     }
     if (!uniform) {
         std::stable_sort(chainPos.begin(), chainPos.end(), [&](int a, int c) { return inb[a] > inb[c]; });
+        std::stable_sort(loopPos.begin(), loopPos.end(), [&](int a, int c) { return inb[a] > inb[c]; });
         auto wkey = [&](int i) { int w = 1; while (w < topos[instTopo[i]]->maxLevelWidth) w <<= 1; return w; };
         std::stable_sort(groupPos.begin(), groupPos.end(), [&](int a, int c) {
             const int wa = wkey(a), wc = wkey(c);
@@ -455,27 +474,57 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
         });
     }
     b->nChain = (int)chainPos.size();
+    b->nLoop = (int)loopPos.size();
     std::copy(chainPos.begin(), chainPos.end(), order.begin());
-    std::copy(groupPos.begin(), groupPos.end(), order.begin() + b->nChain);
-    int64_t yOff = 0, sOff = 0;
-    for (int t0 = 0; t0 < b->nChain; t0 += kTile) {
-        const int t1 = std::min(b->nChain, t0 + kTile);
-        int64_t yw = 0, sw = 0;
-        for (int p = t0; p < t1; ++p) {
-            const int i = order[p];
-            yw = std::max<int64_t>(yw, inq[i] + inu[i]);
-            sw = std::max<int64_t>(sw, recTotal[instTopo[i]]);
+    std::copy(loopPos.begin(), loopPos.end(), order.begin() + b->nChain);
+    std::copy(groupPos.begin(), groupPos.end(), order.begin() + b->nChain + b->nLoop);
+    // slot records of the loop-closure topologies follow their body records
+    std::vector<int32_t> lrec(parent.size(), -1);
+    for (int k = 0; k < ntopo; ++k) {
+        if (used[k] < 0) continue;
+        const sbg_topology_s* t = topos[k];
+        for (int r = 0; r < t->nb; ++r)
+            if (t->lslot[r] >= 0) lrec[rowBase[k] + r] = (int32_t)(recTotal[k] + (int64_t)t->lslot[r] * kSlotSize);
+    }
+    int64_t yOff = 0, sOff = 0, sOffLoop = 0;
+    // tiles of 32 chain-driver instances (the chain segment, then the
+    // loop-closure segment with its own FP64 scratch)
+    auto tile = [&](int p0, int p1, int64_t& sOffSeg, bool loops) {
+        for (int t0 = p0; t0 < p1; t0 += kTile) {
+            const int t1 = std::min(p1, t0 + kTile);
+            int64_t yw = 0, sw = 0;
+            for (int p = t0; p < t1; ++p) {
+                const int i = order[p];
+                const sbg_topology_s* t = topos[instTopo[i]];
+                yw = std::max<int64_t>(yw, inq[i] + inu[i]);
+                sw = std::max<int64_t>(sw, recTotal[instTopo[i]] + (loops ? (int64_t)t->nslots * kSlotSize : 0));
+            }
+            for (int p = t0; p < t1; ++p) {
+                const int i = order[p];
+                ybase[i] = yOff + (p - t0); ystride[i] = kTile;
+                sbase[i] = sOffSeg + (p - t0); sstride[i] = kTile;
+            }
+            yOff += yw * kTile;
+            sOffSeg += sw * kTile;
         }
-        for (int p = t0; p < t1; ++p) {
-            const int i = order[p];
-            ybase[i] = yOff + (p - t0); ystride[i] = kTile;
-            sbase[i] = sOff + (p - t0); sstride[i] = kTile;
-        }
-        yOff += yw * kTile;
-        sOff += sw * kTile;
+    };
+    tile(0, b->nChain, sOff, false);
+    tile(b->nChain, b->nChain + b->nLoop, sOffLoop, true);
+    // constraint tables
+    std::vector<int32_t> lcons, icons(ninst, 0), incons(ninst, 0), consBase(ntopo, 0);
+    std::vector<double> lst;
+    for (int k = 0; k < ntopo; ++k) {
+        if (used[k] < 0) continue;
+        consBase[k] = (int32_t)(lcons.size() / 2);
+        lcons.insert(lcons.end(), topos[k]->lcons.begin(), topos[k]->lcons.end());
+        lst.insert(lst.end(), topos[k]->lst.begin(), topos[k]->lst.end());
+    }
+    for (int i = 0; i < ninst; ++i) {
+        icons[i] = consBase[instTopo[i]];
+        incons[i] = topos[instTopo[i]]->ncons;
     }
     b->groupWidthKey.clear();
-    for (int p = b->nChain; p < ninst; ++p) {
+    for (int p = b->nChain + b->nLoop; p < ninst; ++p) {
         const int i = order[p];
         const sbg_topology_s* t = topos[instTopo[i]];
         ybase[i] = yOff; ystride[i] = 1;
@@ -488,6 +537,7 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     b->nuTotal = b->hostUOff[ninst];
     b->colElems = yOff;
     b->scratchElems = sOff;
+    const int64_t scratchLoopElems = sOffLoop;
     b->tiled = true;
     if (precision == SBG_PRECISION_FP64) b->variant = 1;  // FP64 needs every register
     if (const char* v = std::getenv("SBG_VARIANT")) b->variant = std::atoi(v) == 4 ? 4 : 1;  // tuning override
@@ -526,9 +576,14 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     if ((rc = b->upload(&T.cbeg, cbeg, "children table"))) return bail(rc);
     if ((rc = b->upload(&T.ccnt, ccnt, "children table"))) return bail(rc);
     if ((rc = b->upload(&T.clist, clist, "children table"))) return bail(rc);
+    if ((rc = b->upload(&T.lrec, lrec, "loop table"))) return bail(rc);
+    if ((rc = b->upload(&T.lcons, lcons, "loop table"))) return bail(rc);
+    if ((rc = b->upload(&T.lst, lst, "loop table"))) return bail(rc);
+    if ((rc = b->upload(&T.icons, icons, "instance table"))) return bail(rc);
+    if ((rc = b->upload(&T.incons, incons, "instance table"))) return bail(rc);
     {   // group block table (capacity: one block per group instance + end)
         void* q = nullptr;
-        const size_t cap = (size_t)(ninst - b->nChain) + 2;
+        const size_t cap = (size_t)(ninst - b->nChain - b->nLoop) + 2;
         if ((rc = b->alloc(&q, cap * sizeof(int32_t), "group block table"))) return bail(rc);
         b->dBlkFirst = static_cast<int32_t*>(q);
         if ((rc = b->alloc(&q, cap * sizeof(int32_t), "group block table"))) return bail(rc);
@@ -559,6 +614,12 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     b->staging = static_cast<double*>(p);
     if ((rc = b->alloc(&b->scratch, std::max<int64_t>(b->scratchElems, 1) * rsz, "scratch"))) return bail(rc);
     if ((rc = b->alloc(&b->fbuf, 4 * std::max<int64_t>(b->colElems, 1) * rsz, "stage derivatives"))) return bail(rc);
+    if (b->nLoop > 0) {
+        if ((rc = b->alloc(&b->scratchLoop, scratchLoopElems * sizeof(double), "loop scratch"))) return bail(rc);
+        if (precision == SBG_PRECISION_FP64) b->fbufLoop = b->fbuf;
+        else if ((rc = b->alloc(&b->fbufLoop, 4 * b->colElems * sizeof(double), "loop stage derivatives")))
+            return bail(rc);
+    }
     {
         cudaError_t e = cudaMallocHost(&b->hostPinned, std::max<int64_t>(b->nyTotal, 1) * sizeof(double));
         if (e != cudaSuccess) return bail(cudaFail(e, "cudaMallocHost"));
@@ -635,16 +696,16 @@ int sbg_batch_get_state(sbg_batch b, double* t, double* y) {
 // keeps the fastest (the realize leaves the state untouched).
 static int timePlan(sbg_batch b, float* ms) {
     for (int rep = 0; rep < 2; ++rep)
-        SBG_CUDA(launchRealize(b->T, b->plan(), b->precision, b->y, b->ydot, b->scratch, b->status, b->streams()),
+        SBG_CUDA(launchRealize(b->T, b->plan(), b->precision, b->y, b->ydot, b->bufsArg(), b->status, b->streams()),
                  "tuner launch");
     SBG_CUDA(cudaEventRecord(b->evT0, b->stream), "tuner");
     for (int rep = 0; rep < 3; ++rep)
-        SBG_CUDA(launchRealize(b->T, b->plan(), b->precision, b->y, b->ydot, b->scratch, b->status, b->streams()),
+        SBG_CUDA(launchRealize(b->T, b->plan(), b->precision, b->y, b->ydot, b->bufsArg(), b->status, b->streams()),
                  "tuner launch");
     SBG_CUDA(cudaEventRecord(b->evT1, b->stream), "tuner");
     SBG_CUDA(cudaEventSynchronize(b->evT1), "tuner");
     SBG_CUDA(cudaEventElapsedTime(ms, b->evT0, b->evT1), "tuner");
-    b->launches += 5 * ((b->nChain > 0) + (b->nGroupBlocks > 0));
+    b->launches += 5 * b->segments();
     return SBG_OK;
 }
 
@@ -691,7 +752,7 @@ int sbg_realize_acceleration_async(sbg_batch b) {
     if (!b->realizeGraph) {
         cudaGraph_t g = nullptr;
         SBG_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
-        cudaError_t e = launchRealize(b->T, b->plan(), b->precision, b->y, b->ydot, b->scratch, b->status, b->streams());
+        cudaError_t e = launchRealize(b->T, b->plan(), b->precision, b->y, b->ydot, b->bufsArg(), b->status, b->streams());
         cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
         if (e != cudaSuccess) return cudaFail(e, "realize capture");
         if (e2 != cudaSuccess) return cudaFail(e2, "graph capture");
@@ -700,7 +761,7 @@ int sbg_realize_acceleration_async(sbg_batch b) {
         if (e != cudaSuccess) return cudaFail(e, "graph instantiate");
     }
     SBG_CUDA(cudaGraphLaunch(b->realizeGraph, b->stream), "realize graph launch");
-    b->launches += (b->nChain > 0) + (b->nGroupBlocks > 0);
+    b->launches += b->segments();
     return SBG_OK;
 }
 
@@ -733,10 +794,10 @@ int sbg_multiply_by_minv(sbg_batch b, const double* f, double* outp) {
     std::memcpy(b->hostPinned, f, bytes);
     SBG_CUDA(cudaMemcpyAsync(b->staging, b->hostPinned, bytes, cudaMemcpyHostToDevice, b->stream), "force upload");
     SBG_CUDA(launchScatter(b->T, b->dHostUOff, b->staging, b->fcol, 1, b->stream), "force scatter");
-    SBG_CUDA(launchMInv(b->T, b->plan(), b->precision, b->y, b->fcol, b->ydot, b->scratch, b->status, b->streams()),
+    SBG_CUDA(launchMInv(b->T, b->plan(), b->precision, b->y, b->fcol, b->ydot, b->bufsArg(), b->status, b->streams()),
              "M^-1 kernel launch");
     SBG_CUDA(launchGather(b->T, b->dHostUOff, b->ydot, b->staging, 1, b->stream), "result gather");
-    b->launches += 3;
+    b->launches += 2 + b->segments();
     SBG_CUDA(cudaMemcpyAsync(b->hostPinned, b->staging, bytes, cudaMemcpyDeviceToHost, b->stream), "result download");
     SBG_CUDA(cudaStreamSynchronize(b->stream), "M^-1");
     std::memcpy(outp, b->hostPinned, bytes);
@@ -760,10 +821,10 @@ int sbg_rk_merson_fixed_async(sbg_batch b, double h, int32_t nsteps, const sbg_i
     if (int rc = tuneVariant(b)) return rc;  // realize leaves the state untouched
     SBG_CUDA(cudaMemsetAsync(b->status, 0, std::max(b->ninst, 1) * sizeof(int32_t), b->stream), "status reset");
     SBG_CUDA(launchNormalizeQuat(b->T, b->y, b->stream), "initialize");
-    SBG_CUDA(launchRKMerson(b->T, b->plan(), b->precision, b->y, b->time, b->fbuf, b->colElems, b->scratch, b->status, h,
-                            nsteps, acc, ctol, pes, b->streams()),
+    SBG_CUDA(launchRKMerson(b->T, b->plan(), b->precision, b->y, b->time, b->bufsArg(), b->status, h, nsteps, acc, ctol,
+                            pes, b->streams()),
              "RK-Merson kernel launch");
-    b->launches += 1 + (b->nChain > 0) + (b->nGroupBlocks > 0);
+    b->launches += 1 + b->segments();
     return SBG_OK;
 }
 

@@ -54,7 +54,19 @@ enum : int {
     F_PPF_0 = 1 << 11,     // p_PF is zero
     F_CARRY = 1 << 12,     // the parent is the previous row: values travel in registers
     F_MEMCHILD = 1 << 13,  // some child is not the next row: it reads/accumulates through the record
+    F_LOOPBODY = 1 << 14,  // body 1 or 2 of a Ball loop closure: keeps a slot record
 };
+
+// Loop closures (Constraint::Ball), FP64 chain driver only. Each body named
+// by a constraint has a slot record after the body records of its instance:
+//   0  R_GB[9] p_GB[3] V_GB[6]   from the position/velocity pass
+//  18  A_GB[6]                   tree acceleration (pass 3)
+//  24  B[6]                      result of a unit-force sweep (acceleration
+//                                or velocity of the body origin)
+//  30  F[6]                      applied spatial force (torque, force) at Bo
+constexpr int kSlotA = 18, kSlotB = 24, kSlotF = 30, kSlotSize = 36;
+constexpr int kMaxLoopCons = 4;             // Ball constraints per instance
+constexpr int kMaxLoopEq = 3 * kMaxLoopCons;
 constexpr int F_MEMACC = F_MEMCHILD;
 
 // Warp tile of the shared-topology scratch layout.
@@ -96,16 +108,24 @@ struct DevTables {
     const int32_t* clist;    // children as local rows
     const int32_t* blkFirst; // per group block: first order position (+ end)
     const int32_t* blkG;     // per group block: lanes per instance
+    // loop closures
+    const int32_t* lrec;     // per body row: slot record offset, -1 if none
+    const int32_t* lcons;    // per constraint: local row of body 1, of body 2 (-1 = Ground)
+    const double* lst;       // per constraint: station 1 (in body 1), station 2 (in body 2)
+    const int32_t* icons;    // per instance: first constraint
+    const int32_t* incons;   // per instance: number of constraints
 };
 
 // How one batch operation is launched: order positions [0, nChain) run the
-// chain driver (one thread per instance, width nm), then nGroupBlocks blocks
-// of the level-parallel driver cover the rest.
+// chain driver (one thread per instance, width nm), the next nLoop positions
+// the FP64 chain driver with loop closures, and nGroupBlocks blocks of the
+// level-parallel driver cover the rest.
 struct LaunchPlan {
     int nChain;
     int nGroupBlocks;
     int nm;
     int variant;  // 1: registers as needed; 4: at most 128 registers (FP32 only)
+    int nLoop;    // order positions [nChain, nChain + nLoop): instances with loop closures (FP64 chain driver)
 };
 
 }  // namespace sbg

@@ -1,0 +1,42 @@
+// k_loops.cu -- kernels of the loop-closure segment: FP64 chain driver with
+// Constraint::Ball multipliers (realize, RK-Merson with projections) and the
+// tree M^-1 of those instances.
+#include "abi_device.cuh"
+
+namespace sbg {
+
+static inline int loopBlocks(const LaunchPlan& P) { return (P.nLoop + 127) / 128; }
+
+void realizeLoop(const KArgs& a, cudaStream_t s) {
+    double* sc = static_cast<double*>(a.scratchLoop);
+    const int first = a.P->nChain, nb = loopBlocks(*a.P);
+    if (a.P->nm == 1)
+        realizeKernel<double, 1, false, false, 1, true><<<nb, 128, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.ydot, sc, a.status);
+    else
+        realizeKernel<double, 3, false, false, 1, true><<<nb, 128, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.ydot, sc, a.status);
+}
+
+void minvLoop(const KArgs& a, cudaStream_t s) {
+    double* sc = static_cast<double*>(a.scratchLoop);
+    const int first = a.P->nChain, nb = loopBlocks(*a.P);
+    if (a.P->nm == 1)
+        minvKernel<double, 1, false><<<nb, 128, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.f, a.ydot, sc, a.status);
+    else
+        minvKernel<double, 3, false><<<nb, 128, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.f, a.ydot, sc, a.status);
+}
+
+void rkLoop(const KArgs& a, cudaStream_t s) {
+    double* sc = static_cast<double*>(a.scratchLoop);
+    double* fb = static_cast<double*>(a.fbufLoop);
+    const int first = a.P->nChain, nb = loopBlocks(*a.P);
+    if (a.P->nm == 1)
+        rkMersonKernel<double, 1, false, false, 1, true><<<nb, 128, 0, s>>>(
+            *a.T, first, a.P->nLoop, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.nsteps, a.accuracy, a.consTol,
+            a.projectEveryStep);
+    else
+        rkMersonKernel<double, 3, false, false, 1, true><<<nb, 128, 0, s>>>(
+            *a.T, first, a.P->nLoop, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.nsteps, a.accuracy, a.consTol,
+            a.projectEveryStep);
+}
+
+}  // namespace sbg

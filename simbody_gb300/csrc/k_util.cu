@@ -10,6 +10,7 @@ __global__ void normalizeQuatKernel(DevTables T, double* __restrict__ y) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T.ninst) return;
     const int inst = T.order[t];
+    if (T.incons[inst] > 0) return;  // loop closures: the RK kernel's initialization projects and normalizes
     const int64_t base = T.ybase[inst], stride = T.ystride[inst];
     const int body0 = T.ibody[inst], nb = T.inb[inst];
     for (int lb = 0; lb < nb; ++lb) {
@@ -45,59 +46,78 @@ __global__ void gatherKernel(DevTables T, const int64_t* __restrict__ hostOff, c
     for (int k = threadIdx.x; k < cnt; k += blockDim.x) packed[off + k] = cols[base + (int64_t)(c0 + k) * stride];
 }
 
-// Run the chain segment on the main stream and the level-parallel segment on
-// the side stream, forked from and joined back into the main stream.
-template <class FC, class FG>
-static cudaError_t forkJoin(const LaunchPlan& P, const Streams& s, FC chain, FG group) {
-    const bool c = P.nChain > 0, g = P.nGroupBlocks > 0;
+// Run the chain segment, then the loop-closure segment, on the main stream
+// and the level-parallel segment on the side stream, forked from and joined
+// back into the main stream.
+template <class FC, class FL, class FG>
+static cudaError_t forkJoin(const LaunchPlan& P, const Streams& s, FC chain, FL loops, FG group) {
+    const bool c = P.nChain > 0 || P.nLoop > 0, g = P.nGroupBlocks > 0;
+    auto mainWork = [&](cudaStream_t st) {
+        if (P.nChain > 0) chain(st);
+        if (P.nLoop > 0) loops(st);
+    };
     if (c && g) {
         cudaError_t e = cudaEventRecord(s.fork, s.main);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s.side, s.fork, 0);
         if (e != cudaSuccess) return e;
         group(s.side);
-        chain(s.main);
+        mainWork(s.main);
         e = cudaEventRecord(s.join, s.side);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s.main, s.join, 0);
         if (e != cudaSuccess) return e;
     } else if (c) {
-        chain(s.main);
+        mainWork(s.main);
     } else if (g) {
         group(s.main);
     }
     return cudaGetLastError();
 }
 
-cudaError_t launchRealize(const DevTables& T, const LaunchPlan& P, int precision, const double* y, double* ydot,
-                          void* scratch, int32_t* status, const Streams& s) {
+static KArgs baseArgs(const DevTables& T, const LaunchPlan& P, const BatchBufs& B, int32_t* status) {
     KArgs a{};
-    a.T = &T; a.P = &P; a.y = y; a.ydot = ydot; a.scratch = scratch; a.status = status;
+    a.T = &T; a.P = &P; a.scratch = B.scratch; a.scratchLoop = B.scratchLoop; a.fbuf = B.fbuf;
+    a.fbufLoop = B.fbufLoop; a.fplane = B.fplane; a.status = status;
+    return a;
+}
+
+cudaError_t launchRealize(const DevTables& T, const LaunchPlan& P, int precision, const double* y, double* ydot,
+                          const BatchBufs& B, int32_t* status, const Streams& s) {
+    KArgs a = baseArgs(T, P, B, status);
+    a.y = y; a.ydot = ydot;
+    auto loops = [&](cudaStream_t st) { realizeLoop(a, st); };
     if (precision == SBG_PRECISION_FP64)
-        return forkJoin(P, s, [&](cudaStream_t st) { realize64Chain(a, st); }, [&](cudaStream_t st) { realize64Group(a, st); });
+        return forkJoin(P, s, [&](cudaStream_t st) { realize64Chain(a, st); }, loops,
+                        [&](cudaStream_t st) { realize64Group(a, st); });
     const bool ref = precision == SBG_PRECISION_MIXED;
-    return forkJoin(P, s, [&](cudaStream_t st) { realize32Chain(a, ref, st); },
+    return forkJoin(P, s, [&](cudaStream_t st) { realize32Chain(a, ref, st); }, loops,
                     [&](cudaStream_t st) { realize32Group(a, ref, st); });
 }
 
 cudaError_t launchMInv(const DevTables& T, const LaunchPlan& P, int precision, const double* y, const double* f,
-                       double* out, void* scratch, int32_t* status, const Streams& s) {
-    KArgs a{};
-    a.T = &T; a.P = &P; a.y = y; a.f = f; a.ydot = out; a.scratch = scratch; a.status = status;
+                       double* out, const BatchBufs& B, int32_t* status, const Streams& s) {
+    KArgs a = baseArgs(T, P, B, status);
+    a.y = y; a.f = f; a.ydot = out;
+    auto loops = [&](cudaStream_t st) { minvLoop(a, st); };
     if (precision == SBG_PRECISION_FP64)
-        return forkJoin(P, s, [&](cudaStream_t st) { minv64Chain(a, st); }, [&](cudaStream_t st) { minv64Group(a, st); });
-    return forkJoin(P, s, [&](cudaStream_t st) { minv32Chain(a, st); }, [&](cudaStream_t st) { minv32Group(a, st); });
+        return forkJoin(P, s, [&](cudaStream_t st) { minv64Chain(a, st); }, loops,
+                        [&](cudaStream_t st) { minv64Group(a, st); });
+    return forkJoin(P, s, [&](cudaStream_t st) { minv32Chain(a, st); }, loops,
+                    [&](cudaStream_t st) { minv32Group(a, st); });
 }
 
 cudaError_t launchRKMerson(const DevTables& T, const LaunchPlan& P, int precision, double* y, double* time,
-                           void* fbuf, int64_t fplane, void* scratch, int32_t* status, double h, int nsteps,
-                           double accuracy, double consTol, int projectEveryStep, const Streams& s) {
-    KArgs a{};
-    a.T = &T; a.P = &P; a.ystate = y; a.time = time; a.fbuf = fbuf; a.fplane = fplane; a.scratch = scratch;
-    a.status = status; a.h = h; a.nsteps = nsteps; a.accuracy = accuracy; a.consTol = consTol;
+                           const BatchBufs& B, int32_t* status, double h, int nsteps, double accuracy,
+                           double consTol, int projectEveryStep, const Streams& s) {
+    KArgs a = baseArgs(T, P, B, status);
+    a.ystate = y; a.time = time; a.h = h; a.nsteps = nsteps; a.accuracy = accuracy; a.consTol = consTol;
     a.projectEveryStep = projectEveryStep;
+    auto loops = [&](cudaStream_t st) { rkLoop(a, st); };
     if (precision == SBG_PRECISION_FP64)
-        return forkJoin(P, s, [&](cudaStream_t st) { rk64Chain(a, st); }, [&](cudaStream_t st) { rk64Group(a, st); });
+        return forkJoin(P, s, [&](cudaStream_t st) { rk64Chain(a, st); }, loops,
+                        [&](cudaStream_t st) { rk64Group(a, st); });
     const bool ref = precision == SBG_PRECISION_MIXED;
-    return forkJoin(P, s, [&](cudaStream_t st) { rk32Chain(a, ref, st); }, [&](cudaStream_t st) { rk32Group(a, ref, st); });
+    return forkJoin(P, s, [&](cudaStream_t st) { rk32Chain(a, ref, st); }, loops,
+                    [&](cudaStream_t st) { rk32Group(a, ref, st); });
 }
 
 cudaError_t launchNormalizeQuat(const DevTables& T, double* y, cudaStream_t s) {

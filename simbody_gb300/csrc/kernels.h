@@ -17,13 +17,21 @@ struct Streams {
 
 // precision: SBG_PRECISION_FP64, _MIXED (FP32 recursions + double-float
 // residual refinement) or _MIXED_FAST (FP32 recursions only).
+// Buffers of a batch the launchers need besides the tables.
+struct BatchBufs {
+    void* scratch;       // scratch of the chain and group segments (R)
+    void* scratchLoop;   // FP64 scratch of the loop-closure segment
+    void* fbuf;          // RK stage derivatives (R), 4 planes of fplane elements
+    void* fbufLoop;      // FP64 stage derivatives of the loop-closure segment, 4 planes
+    int64_t fplane;
+};
 cudaError_t launchRealize(const DevTables& T, const LaunchPlan& P, int precision, const double* y, double* ydot,
-                          void* scratch, int32_t* status, const Streams& s);
+                          const BatchBufs& B, int32_t* status, const Streams& s);
 cudaError_t launchMInv(const DevTables& T, const LaunchPlan& P, int precision, const double* y, const double* f,
-                       double* out, void* scratch, int32_t* status, const Streams& s);
+                       double* out, const BatchBufs& B, int32_t* status, const Streams& s);
 cudaError_t launchRKMerson(const DevTables& T, const LaunchPlan& P, int precision, double* y, double* time,
-                           void* fbuf, int64_t fplane, void* scratch, int32_t* status, double h, int nsteps,
-                           double accuracy, double consTol, int projectEveryStep, const Streams& s);
+                           const BatchBufs& B, int32_t* status, double h, int nsteps, double accuracy,
+                           double consTol, int projectEveryStep, const Streams& s);
 cudaError_t launchNormalizeQuat(const DevTables& T, double* y, cudaStream_t s);
 // part 0 moves whole [q,u] records, part 1 only the u slots.
 cudaError_t launchScatter(const DevTables& T, const int64_t* hostOff, const double* packed, double* cols, int part,
@@ -44,6 +52,8 @@ struct KArgs {
     void* fbuf;
     int64_t fplane;
     void* scratch;
+    void* scratchLoop;   // FP64 scratch of the loop-closure segment
+    void* fbufLoop;      // FP64 stage derivatives of the loop-closure segment
     int32_t* status;
     double h, accuracy, consTol;
     int nsteps, projectEveryStep;
@@ -60,5 +70,8 @@ void rk64Chain(const KArgs& a, cudaStream_t s);
 void rk64Group(const KArgs& a, cudaStream_t s);
 void rk32Chain(const KArgs& a, bool refine, cudaStream_t s);
 void rk32Group(const KArgs& a, bool refine, cudaStream_t s);
+void realizeLoop(const KArgs& a, cudaStream_t s);  // k_loops.cu
+void minvLoop(const KArgs& a, cudaStream_t s);
+void rkLoop(const KArgs& a, cudaStream_t s);
 
 }  // namespace sbg

@@ -1,0 +1,612 @@
+// loops_device.cuh -- Constraint::Ball loop closures on the FP64 chain
+// driver: the multipliers of the loop forward dynamics and the integrator's
+// position and velocity projections. Textually included by abi_device.cuh
+// inside namespace sbg (it uses that file's records, kinematics and sweeps).
+//
+// Constraint::Ball (ConstraintImpl.h:1835-1993) keeps station P (station 1
+// on body 1) and S (station 2 on body 2) together: perr = p_S - p_P. The
+// velocity and acceleration errors and the constraint forces use C, the
+// material point of body 1 coincident with S:
+//   verr = v_S - v_C,  aerr = a_S - a_C,  +lambda at S on body 2, -lambda at C.
+// G = d verr / du is never formed: G^T x is the mobility force of point
+// forces x at S and -x at C (an inward sweep), G v the point-velocity
+// difference after an outward sweep.
+//
+// Loop forward dynamics (SimbodyMatterSubsystemRep.cpp:5076-5152, 3512-3558):
+// with the tree solution udot_t,  (G M^-1 G^T) lambda = aerr(udot_t),
+// udot = udot_t - M^-1 G^T lambda. Column j of G M^-1 G^T is the point
+// acceleration difference of an M^-1 sweep driven by unit forces of
+// equation j. The m x m system (m <= 12) is factored by Cholesky in FP64;
+// the reference uses rank-revealing QTZ, which agrees for a full-rank G.
+//
+// Projections (SimbodyMatterSubsystemRep.cpp:4096-4442 and 4664-4943):
+//   position  du = D G^T (G D G^T)^-1 perr, q -= N(q) du, full Newton until
+//             RMS(perr) <= 0.1 tol (at most 20 iterations), D = 4|q|^2 on the
+//             rotational mobilities of quaternion joints and 1 elsewhere
+//             (the weighting of the reference's (P N^+) minimum-norm solve,
+//             Rotation.h:742-748), then quaternions are normalized;
+//   velocity  du = E^2 G^T (G E^2 G^T)^-1 verr, E = max(|u|, 1) at entry,
+//             one factorization, at most 7 iterations.
+// With localOnly a growing norm stops the iteration and undoes the last
+// step; a result worse than the entry state is restored.
+
+using SC64 = ScrTiled<double>;
+using V3d = V3<double>;
+
+// One instance with loop closures inside a kernel. save/delta are column
+// planes that are free between integrator steps (entry q/u of a projection,
+// the last correction).
+struct LoopState {
+    const DevTables& T;
+    int inst;
+    SC64 S;
+    double* y;
+    double* save;
+    double* delta;
+    int64_t base, stride;
+};
+
+struct NullOut {
+    template <class R> __device__ __forceinline__ void qdot(int, R) {}
+    template <class R> __device__ __forceinline__ void udot(int, R) {}
+};
+
+enum : int { kMInvSweep = 0, kJacSweep = 1 };
+
+__device__ __forceinline__ int recN(int n, int NM) { return n == 6 ? 6 : NM; }
+__device__ __forceinline__ int recEps(int N) { return kRecH + 6 * N + N + N * N + 6 * N; }
+
+// Position and velocity kinematics of the state in y (pass 1 only): body
+// records (H, l, ...) and the slot records of the constrained bodies.
+template <int NM>
+__device__ __noinline__ void loopKinematics(const LoopState& L) {
+    const DevTables& T = L.T;
+    const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
+    const YSrc src{L.y, L.base, L.stride, T.inq[L.inst]};
+    NullOut out;
+    const V3d g = mk3(T.grav[3 * L.inst], T.grav[3 * L.inst + 1], T.grav[3 * L.inst + 2]);
+    Kin<double> carry = groundKin<double>();
+    for (int lb = 0; lb < nb; ++lb) {
+        const int row = body0 + lb;
+        const int info = T.info[row];
+        const int parent = T.parent[row];
+        const int rec = T.srec[row];
+        const Kin<double> P = parent < 0 ? groundKin<double>()
+                              : (info & F_CARRY) ? carry : loadKin<double>(L.S, T.srec[body0 + parent]);
+        carry = body1<double, NM>(T, row, rec, L.S, src, out, g, P);
+        if (info & F_MEMCHILD) storeKin(L.S, rec, carry);
+        if (info & F_LOOPBODY) storeKin(L.S, T.lrec[row], carry);
+    }
+}
+
+struct LoopGeom {
+    V3d pS, pP, r1, r2;  // S and P in Ground; S relative to the origins of body 1 and body 2
+    int s1, s2;          // slot records (-1 = Ground)
+};
+
+__device__ __forceinline__ void loopSlots(const LoopState& L, int c, int& s1, int& s2) {
+    const DevTables& T = L.T;
+    const int gc = T.icons[L.inst] + c, body0 = T.ibody[L.inst];
+    const int r1 = T.lcons[2 * gc], r2 = T.lcons[2 * gc + 1];
+    s1 = r1 >= 0 ? T.lrec[body0 + r1] : -1;
+    s2 = r2 >= 0 ? T.lrec[body0 + r2] : -1;
+}
+
+__device__ __forceinline__ LoopGeom loopGeom(const LoopState& L, int c) {
+    LoopGeom G;
+    loopSlots(L, c, G.s1, G.s2);
+    const double* st = L.T.lst + 6 * (int64_t)(L.T.icons[L.inst] + c);
+    const V3d st1 = mk3(st[0], st[1], st[2]), st2 = mk3(st[3], st[4], st[5]);
+    if (G.s2 >= 0) {
+        const Kin<double> K = loadKin<double>(L.S, G.s2);
+        G.r2 = mul(K.R_, st2);
+        G.pS = K.p + G.r2;
+    } else {
+        G.r2 = z3<double>();
+        G.pS = st2;
+    }
+    if (G.s1 >= 0) {
+        const Kin<double> K = loadKin<double>(L.S, G.s1);
+        G.pP = K.p + mul(K.R_, st1);
+        G.r1 = G.pS - K.p;
+    } else {
+        G.pP = st1;
+        G.r1 = z3<double>();
+    }
+    return G;
+}
+
+// Linear part of a spatial vector (angular at f, linear at f+3) moved to
+// the material point at offset r: x_v + x_w x r.
+__device__ __forceinline__ V3d slotPoint(const SC64& S, int slot, int f, V3d r) {
+    if (slot < 0) return z3<double>();
+    return ld3<double>(S, slot, f + 3) + cross(ld3<double>(S, slot, f), r);
+}
+__device__ __forceinline__ V3d slotCentripetal(const SC64& S, int slot, V3d r) {
+    if (slot < 0) return z3<double>();
+    const V3d w = ld3<double>(S, slot, 12);
+    return cross(w, cross(w, r));
+}
+
+__device__ __forceinline__ void loopClearForces(const LoopState& L) {
+    const int nc = L.T.incons[L.inst];
+    for (int c = 0; c < nc; ++c) {
+        int s1, s2;
+        loopSlots(L, c, s1, s2);
+        if (s1 >= 0) { st3<double>(L.S, s1, kSlotF, z3<double>()); st3<double>(L.S, s1, kSlotF + 3, z3<double>()); }
+        if (s2 >= 0) { st3<double>(L.S, s2, kSlotF, z3<double>()); st3<double>(L.S, s2, kSlotF + 3, z3<double>()); }
+    }
+}
+// Point force F at offset r from the body origin, as (r x F, F) at the origin.
+__device__ __forceinline__ void loopAddForce(const SC64& S, int slot, V3d r, V3d F) {
+    if (slot < 0) return;
+    st3<double>(S, slot, kSlotF, ld3<double>(S, slot, kSlotF) + cross(r, F));
+    st3<double>(S, slot, kSlotF + 3, ld3<double>(S, slot, kSlotF + 3) + F);
+}
+// +x at S on body 2, -x at C on body 1 (the forces of G^T x for constraint c).
+__device__ __forceinline__ void loopAddConstraintForce(const LoopState& L, const LoopGeom& G, V3d x) {
+    loopAddForce(L.S, G.s2, G.r2, x);
+    loopAddForce(L.S, G.s1, G.r1, -x);
+}
+
+// Inward half for one body; (zw, zv): in, the children's sum at the body
+// origin; out, the contribution to the parent.
+//   kMInvSweep: z = children - F, eps = -~H z (stored), z+ = z + G eps
+//               (RigidBodyNodeSpec.cpp:483-515 with f = 0)
+//   kJacSweep:  F = children + F_applied, g = ~H F (stored), F passed on
+template <int N, int KIND>
+__device__ __forceinline__ void loopIn(const LoopState& L, int row, int rec, int n, int info, V3d& zw, V3d& zv) {
+    const SC64& S = L.S;
+    const int eDI = kRecH + 7 * N, eG = eDI + N * N, eEps = eG + 6 * N;
+    if (info & F_LOOPBODY) {
+        const int sl = L.T.lrec[row];
+        const V3d tw = ld3<double>(S, sl, kSlotF), tv = ld3<double>(S, sl, kSlotF + 3);
+        if (KIND == kMInvSweep) { zw = zw - tw; zv = zv - tv; }
+        else { zw = zw + tw; zv = zv + tv; }
+    }
+    V3d pw = zw, pv = zv;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        if (j < n) {
+            const double d = dot(ld3<double>(S, rec, kRecH + 6 * j), zw) + dot(ld3<double>(S, rec, kRecH + 6 * j + 3), zv);
+            if (KIND == kMInvSweep) {
+                const double eps = -d;
+                S(rec, eEps + j) = eps;
+                pw = axpy(pw, eps, ld3<double>(S, rec, eG + 6 * j));
+                pv = axpy(pv, eps, ld3<double>(S, rec, eG + 6 * j + 3));
+            } else {
+                S(rec, eEps + j) = d;
+            }
+        }
+    }
+    const V3d l = ld3<double>(S, rec, kRecL);
+    zw = pw + cross(l, pv);
+    zv = pv;
+}
+
+// Outward half for one body; (Aw, Av): in, the parent's value; out, this
+// body's. ud gets the body's mobility values.
+//   kMInvSweep: udot = DI eps - ~G A+, A = A+ + H udot (a = 0)
+//               (RigidBodyNodeSpec.cpp:517-552)
+//   kJacSweep:  du = the stored (weighted) values, V = V+ + H du
+template <int N, int KIND>
+__device__ __forceinline__ void loopOut(const LoopState& L, int rec, int n, bool hasParent, V3d& Aw, V3d& Av,
+                                        double* ud) {
+    const SC64& S = L.S;
+    const int eDI = kRecH + 7 * N, eG = eDI + N * N, eEps = eG + 6 * N;
+    const V3d l = ld3<double>(S, rec, kRecL);
+    const V3d Apw = hasParent ? Aw : z3<double>();
+    const V3d Apv = hasParent ? Av + cross(Aw, l) : z3<double>();
+    double eps[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) eps[j] = j < n ? S(rec, eEps + j) : 0.0;
+    Aw = Apw;
+    Av = Apv;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        if (i < n) {
+            double s;
+            if (KIND == kMInvSweep) {
+                s = 0.0;
+#pragma unroll
+                for (int k = 0; k < N; ++k)
+                    if (k < n) s = s + S(rec, eDI + i * N + k) * eps[k];
+                s = s - (dot(ld3<double>(S, rec, eG + 6 * i), Apw) + dot(ld3<double>(S, rec, eG + 6 * i + 3), Apv));
+            } else {
+                s = eps[i];
+            }
+            ud[i] = s;
+            Aw = axpy(Aw, s, ld3<double>(S, rec, kRecH + 6 * i));
+            Av = axpy(Av, s, ld3<double>(S, rec, kRecH + 6 * i + 3));
+        }
+    }
+}
+
+template <int KIND>
+__device__ __noinline__ void loopIn6(const LoopState& L, int row, int rec, int info, V3d& zw, V3d& zv) {
+    loopIn<6, KIND>(L, row, rec, 6, info, zw, zv);
+}
+template <int KIND>
+__device__ __noinline__ void loopOut6(const LoopState& L, int rec, bool hasParent, V3d& Aw, V3d& Av, double* ud) {
+    loopOut<6, KIND>(L, rec, 6, hasParent, Aw, Av, ud);
+}
+
+// Children's sums of the inward sweeps live in the z accumulator of the
+// parent's record; it is read and cleared by the parent. Tree passes (and
+// fresh memory) leave other values there, so every entry point that starts
+// a series of sweeps clears them first.
+__device__ __forceinline__ void loopZeroAcc(const LoopState& L) {
+    const DevTables& T = L.T;
+    const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
+    for (int lb = 0; lb < nb; ++lb) {
+        const int row = body0 + lb;
+        if (T.info[row] & F_MEMCHILD) {
+            st3<double>(L.S, T.srec[row], kRecZacc, z3<double>());
+            st3<double>(L.S, T.srec[row], kRecZacc + 3, z3<double>());
+        }
+    }
+}
+
+// One inward and one outward sweep over the instance driven by the applied
+// forces in the slot records. The outward result of each constrained body
+// goes to its slot (kSlotB); onBody(row, n, ud) sees every body's mobility
+// values. kJacSweep multiplies g by wt(row, j) between the halves.
+template <int NM, int KIND, class Wt, class OnBody>
+__device__ __forceinline__ void loopSweep(const LoopState& L, const Wt& wt, const OnBody& onBody) {
+    const DevTables& T = L.T;
+    const SC64& S = L.S;
+    const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
+    {
+        V3d cw = z3<double>(), cv = z3<double>();
+        bool have = false;
+        for (int lb = nb - 1; lb >= 0; --lb) {
+            const int row = body0 + lb;
+            const int info = T.info[row];
+            const int n = (info >> 4) & 15;
+            const int rec = T.srec[row];
+            V3d zw = z3<double>(), zv = z3<double>();
+            if (info & F_MEMCHILD) {
+                zw = ld3<double>(S, rec, kRecZacc);
+                zv = ld3<double>(S, rec, kRecZacc + 3);
+                st3<double>(S, rec, kRecZacc, z3<double>());
+                st3<double>(S, rec, kRecZacc + 3, z3<double>());
+            }
+            if (have) { zw = zw + cw; zv = zv + cv; }
+            if (n == 6) loopIn6<KIND>(L, row, rec, info, zw, zv);
+            else loopIn<NM, KIND>(L, row, rec, n, info, zw, zv);
+            if (KIND == kJacSweep) {
+                const int eEps = recEps(recN(n, NM));
+                for (int j = 0; j < n; ++j) S(rec, eEps + j) = S(rec, eEps + j) * wt(row, j);
+            }
+            const int parent = T.parent[row];
+            have = (info & F_CARRY) != 0;
+            if (have) {
+                cw = zw;
+                cv = zv;
+            } else if (parent >= 0) {
+                const int pr = T.srec[body0 + parent];
+                st3<double>(S, pr, kRecZacc, ld3<double>(S, pr, kRecZacc) + zw);
+                st3<double>(S, pr, kRecZacc + 3, ld3<double>(S, pr, kRecZacc + 3) + zv);
+            }
+        }
+    }
+    {
+        V3d aw = z3<double>(), av = z3<double>();
+        for (int lb = 0; lb < nb; ++lb) {
+            const int row = body0 + lb;
+            const int info = T.info[row];
+            const int n = (info >> 4) & 15;
+            const int rec = T.srec[row];
+            const int parent = T.parent[row];
+            const bool hp = parent >= 0;
+            V3d pw = aw, pv = av;
+            if (hp && !(info & F_CARRY)) {
+                const int pr = T.srec[body0 + parent];
+                pw = ld3<double>(S, pr, 0);
+                pv = ld3<double>(S, pr, 3);
+            }
+            double ud[6];
+            if (n == 6) loopOut6<KIND>(L, rec, hp, pw, pv, ud);
+            else loopOut<NM, KIND>(L, rec, n, hp, pw, pv, ud);
+            onBody(row, n, ud);
+            if (info & F_LOOPBODY) {
+                st3<double>(S, T.lrec[row], kSlotB, pw);
+                st3<double>(S, T.lrec[row], kSlotB + 3, pv);
+            }
+            if (info & F_MEMCHILD) {
+                st3<double>(S, rec, 0, pw);
+                st3<double>(S, rec, 3, pv);
+            }
+            aw = pw;
+            av = pv;
+        }
+    }
+}
+
+// Cholesky of the leading m x m block (row stride kMaxLoopEq), lower factor
+// in place; then the two triangular solves.
+__device__ __forceinline__ bool loopCholFactor(int m, double* A) {
+    for (int j = 0; j < m; ++j) {
+        double s = A[j * kMaxLoopEq + j];
+        for (int k = 0; k < j; ++k) s -= A[j * kMaxLoopEq + k] * A[j * kMaxLoopEq + k];
+        if (!(s > 0)) return false;
+        const double d = sqrt(s);
+        A[j * kMaxLoopEq + j] = d;
+        for (int i = j + 1; i < m; ++i) {
+            double v = A[i * kMaxLoopEq + j];
+            for (int k = 0; k < j; ++k) v -= A[i * kMaxLoopEq + k] * A[j * kMaxLoopEq + k];
+            A[i * kMaxLoopEq + j] = v / d;
+        }
+    }
+    return true;
+}
+__device__ __forceinline__ void loopCholSolve(int m, const double* A, double* b) {
+    for (int i = 0; i < m; ++i) {
+        double v = b[i];
+        for (int k = 0; k < i; ++k) v -= A[i * kMaxLoopEq + k] * b[k];
+        b[i] = v / A[i * kMaxLoopEq + i];
+    }
+    for (int i = m - 1; i >= 0; --i) {
+        double v = b[i];
+        for (int k = i + 1; k < m; ++k) v -= A[k * kMaxLoopEq + i] * b[k];
+        b[i] = v / A[i * kMaxLoopEq + i];
+    }
+}
+
+// Column j of G W G^T (kJacSweep) or G M^-1 G^T (kMInvSweep) for every j.
+template <int NM, int KIND, class Wt>
+__device__ __forceinline__ void loopGram(const LoopState& L, const Wt& wt, double* A) {
+    const int nc = L.T.incons[L.inst], m = 3 * nc;
+    auto none = [](int, int, const double*) {};
+    for (int j = 0; j < m; ++j) {
+        loopClearForces(L);
+        V3d e = z3<double>();
+        if (j % 3 == 0) e.x = 1.0; else if (j % 3 == 1) e.y = 1.0; else e.z = 1.0;
+        loopAddConstraintForce(L, loopGeom(L, j / 3), e);
+        loopSweep<NM, KIND>(L, wt, none);
+        for (int i = 0; i < nc; ++i) {
+            const LoopGeom G = loopGeom(L, i);
+            const V3d d = slotPoint(L.S, G.s2, kSlotB, G.r2) - slotPoint(L.S, G.s1, kSlotB, G.r1);
+            A[(3 * i + 0) * kMaxLoopEq + j] = d.x;
+            A[(3 * i + 1) * kMaxLoopEq + j] = d.y;
+            A[(3 * i + 2) * kMaxLoopEq + j] = d.z;
+        }
+    }
+}
+
+// Loop forward dynamics after the tree RHS (which left the tree udot in out
+// and A_GB in the slots). Returns SBG_INST_* bits.
+template <int NM, class Out>
+__device__ __noinline__ int loopForwardDynamics(const DevTables& T, int inst, const SC64& S, Out& out) {
+    const LoopState L{T, inst, S, nullptr, nullptr, nullptr, 0, 0};
+    const int nc = T.incons[inst], m = 3 * nc;
+    loopZeroAcc(L);
+    double lam[kMaxLoopEq];
+    for (int c = 0; c < nc; ++c) {
+        const LoopGeom G = loopGeom(L, c);
+        const V3d aS = slotPoint(S, G.s2, kSlotA, G.r2) + slotCentripetal(S, G.s2, G.r2);
+        const V3d aC = slotPoint(S, G.s1, kSlotA, G.r1) + slotCentripetal(S, G.s1, G.r1);
+        const V3d d = aS - aC;
+        lam[3 * c] = d.x; lam[3 * c + 1] = d.y; lam[3 * c + 2] = d.z;
+    }
+    double A[kMaxLoopEq * kMaxLoopEq];
+    auto one = [](int, int) { return 1.0; };
+    loopGram<NM, kMInvSweep>(L, one, A);
+    if (!loopCholFactor(m, A)) return SBG_INST_CHOLESKY_FAIL;
+    loopCholSolve(m, A, lam);
+    loopClearForces(L);
+    for (int c = 0; c < nc; ++c) loopAddConstraintForce(L, loopGeom(L, c), mk3(lam[3 * c], lam[3 * c + 1], lam[3 * c + 2]));
+    loopSweep<NM, kMInvSweep>(L, one, [&](int row, int n, const double* ud) {
+        const int uo = T.uoff[row];
+        for (int i = 0; i < n; ++i) out.udot(uo + i, out.udotGet(uo + i) - ud[i]);
+    });
+    return 0;
+}
+
+// ----------------------------------------------------------- projections
+__device__ __forceinline__ double loopRMS(const double* v, int m) {
+    double s = 0;
+    for (int i = 0; i < m; ++i) s += v[i] * v[i];
+    return m ? sqrt(s / m) : 0.0;
+}
+__device__ __forceinline__ double loopPerr(const LoopState& L, double* perr) {
+    const int nc = L.T.incons[L.inst];
+    for (int c = 0; c < nc; ++c) {
+        const LoopGeom G = loopGeom(L, c);
+        const V3d d = G.pS - G.pP;
+        perr[3 * c] = d.x; perr[3 * c + 1] = d.y; perr[3 * c + 2] = d.z;
+    }
+    return loopRMS(perr, 3 * nc);
+}
+__device__ __forceinline__ double loopVerr(const LoopState& L, double* verr) {
+    const int nc = L.T.incons[L.inst];
+    for (int c = 0; c < nc; ++c) {
+        const LoopGeom G = loopGeom(L, c);
+        const V3d d = slotPoint(L.S, G.s2, 12, G.r2) - slotPoint(L.S, G.s1, 12, G.r1);
+        verr[3 * c] = d.x; verr[3 * c + 1] = d.y; verr[3 * c + 2] = d.z;
+    }
+    return loopRMS(verr, 3 * nc);
+}
+__device__ __forceinline__ double& yAt(const LoopState& L, int k) { return L.y[L.base + (int64_t)k * L.stride]; }
+__device__ __forceinline__ double& saveAt(const LoopState& L, int k) { return L.save[L.base + (int64_t)k * L.stride]; }
+__device__ __forceinline__ double& deltaAt(const LoopState& L, int k) { return L.delta[L.base + (int64_t)k * L.stride]; }
+
+__device__ __forceinline__ void loopNormalizeQuats(const LoopState& L) {
+    const DevTables& T = L.T;
+    const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
+    for (int lb = 0; lb < nb; ++lb) {
+        const int row = body0 + lb;
+        const int type = T.info[row] & 15;
+        if (type != T_BALL && type != T_FREE) continue;
+        const int qo = T.qoff[row];
+        const double q0 = yAt(L, qo), q1 = yAt(L, qo + 1), q2 = yAt(L, qo + 2), q3 = yAt(L, qo + 3);
+        const double len = sqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
+        yAt(L, qo) = q0 / len; yAt(L, qo + 1) = q1 / len; yAt(L, qo + 2) = q2 / len; yAt(L, qo + 3) = q3 / len;
+    }
+}
+
+__device__ __forceinline__ double loopTryFor(double tol) { return fmax(0.1 * tol, pow(2.220446049250313e-16, 0.875)); }
+
+// Position projection (Newton); kinematics must be current for y. Leaves
+// them current for the resulting y.
+template <int NM>
+__device__ __noinline__ bool loopProjectQ(const LoopState& L, double tol, bool localOnly) {
+    const DevTables& T = L.T;
+    const int nq = T.inq[L.inst], m = 3 * T.incons[L.inst];
+    const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
+    double perr[kMaxLoopEq], A[kMaxLoopEq * kMaxLoopEq];
+    const double normOnEntry = loopPerr(L, perr);
+    for (int k = 0; k < nq; ++k) saveAt(L, k) = yAt(L, k);
+    const double tryFor = loopTryFor(tol);
+    double achieved = normOnEntry, prev = normOnEntry;
+    int its = 0;
+    // D = diag(NInv NInv^T) of the current q
+    auto wq = [&](int row, int j) -> double {
+        const int type = T.info[row] & 15;
+        if ((type == T_BALL || type == T_FREE) && j < 3) {
+            const int qo = T.qoff[row];
+            const double q0 = yAt(L, qo), q1 = yAt(L, qo + 1), q2 = yAt(L, qo + 2), q3 = yAt(L, qo + 3);
+            return 4 * (q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
+        }
+        return 1.0;
+    };
+    do {
+        loopGram<NM, kJacSweep>(L, wq, A);
+        if (!loopCholFactor(m, A)) return false;
+        loopCholSolve(m, A, perr);
+        loopClearForces(L);
+        for (int c = 0; c < m / 3; ++c)
+            loopAddConstraintForce(L, loopGeom(L, c), mk3(perr[3 * c], perr[3 * c + 1], perr[3 * c + 2]));
+        // q -= N(q) du with the unnormalized N (Rotation.h:712-719)
+        loopSweep<NM, kJacSweep>(L, wq, [&](int row, int n, const double* du) {
+            const int type = T.info[row] & 15, qo = T.qoff[row];
+            double dq[7];
+            int nqb = n;
+            if (type == T_BALL || type == T_FREE) {
+                const double e0 = yAt(L, qo) / 2, e1 = yAt(L, qo + 1) / 2, e2 = yAt(L, qo + 2) / 2, e3 = yAt(L, qo + 3) / 2;
+                dq[0] = -e1 * du[0] - e2 * du[1] - e3 * du[2];
+                dq[1] = e0 * du[0] + e3 * du[1] - e2 * du[2];
+                dq[2] = -e3 * du[0] + e0 * du[1] + e1 * du[2];
+                dq[3] = e2 * du[0] - e1 * du[1] + e0 * du[2];
+                nqb = 4;
+                if (type == T_FREE) { dq[4] = du[3]; dq[5] = du[4]; dq[6] = du[5]; nqb = 7; }
+            } else {
+                for (int j = 0; j < n; ++j) dq[j] = du[j];
+            }
+            for (int j = 0; j < nqb; ++j) {
+                deltaAt(L, qo + j) = dq[j];
+                yAt(L, qo + j) -= dq[j];
+            }
+        });
+        loopKinematics<NM>(L);
+        achieved = loopPerr(L, perr);
+        ++its;
+        if (localOnly && its >= 2 && achieved > prev) {
+            for (int k = 0; k < nq; ++k) yAt(L, k) += deltaAt(L, k);
+            loopKinematics<NM>(L);
+            achieved = loopPerr(L, perr);
+            break;
+        }
+        prev = achieved;
+    } while (achieved > tryFor && its < 20);
+    (void)body0; (void)nb;
+    if (achieved > tol) {
+        if (achieved >= normOnEntry) {
+            for (int k = 0; k < nq; ++k) yAt(L, k) = saveAt(L, k);
+            loopKinematics<NM>(L);
+        }
+        return false;
+    }
+    loopNormalizeQuats(L);
+    loopKinematics<NM>(L);
+    return true;
+}
+
+// Velocity projection at the current (q, u); recomputes the kinematics first.
+template <int NM>
+__device__ __noinline__ bool loopProjectU(const LoopState& L, double tol, bool force, double limit, bool localOnly) {
+    const DevTables& T = L.T;
+    const int nq = T.inq[L.inst], nu = T.inu[L.inst], m = 3 * T.incons[L.inst];
+    loopKinematics<NM>(L);
+    double verr[kMaxLoopEq], A[kMaxLoopEq * kMaxLoopEq];
+    const double normOnEntry = loopVerr(L, verr);
+    if (normOnEntry > limit) return false;
+    if (normOnEntry == 0 || (normOnEntry <= tol && !force)) return true;
+    for (int k = 0; k < nu; ++k) saveAt(L, nq + k) = yAt(L, nq + k);
+    // E^2 with E = max(|u|, 1) frozen at entry
+    auto wu = [&](int row, int j) -> double {
+        const double a = fabs(saveAt(L, nq + T.uoff[row] + j));
+        const double e = a > 1 ? a : 1.0;
+        return e * e;
+    };
+    loopGram<NM, kJacSweep>(L, wu, A);
+    if (!loopCholFactor(m, A)) return false;
+    const double tryFor = loopTryFor(tol);
+    double achieved = normOnEntry, prev = normOnEntry;
+    int its = 0;
+    do {
+        loopCholSolve(m, A, verr);
+        loopClearForces(L);
+        for (int c = 0; c < m / 3; ++c)
+            loopAddConstraintForce(L, loopGeom(L, c), mk3(verr[3 * c], verr[3 * c + 1], verr[3 * c + 2]));
+        loopSweep<NM, kJacSweep>(L, wu, [&](int row, int n, const double* du) {
+            const int uo = nq + T.uoff[row];
+            for (int j = 0; j < n; ++j) {
+                deltaAt(L, uo + j) = du[j];
+                yAt(L, uo + j) -= du[j];
+            }
+        });
+        loopKinematics<NM>(L);
+        achieved = loopVerr(L, verr);
+        ++its;
+        if (localOnly && its >= 2 && achieved > prev) {
+            for (int k = 0; k < nu; ++k) yAt(L, nq + k) += deltaAt(L, nq + k);
+            loopKinematics<NM>(L);
+            achieved = loopVerr(L, verr);
+            break;
+        }
+        prev = achieved;
+    } while (achieved > tryFor && its < 7);
+    if (achieved > tol) {
+        if (achieved >= normOnEntry)
+            for (int k = 0; k < nu; ++k) yAt(L, nq + k) = saveAt(L, nq + k);
+        return false;
+    }
+    return true;
+}
+
+// Integrator::initialize: ProjectOptions::ForceProjection, no projection
+// limit, not LocalOnly (IntegratorRep.h:856-895). Returns SBG_INST_* bits.
+template <int NM>
+__device__ __noinline__ int loopInitialize(const LoopState& L, double tol) {
+    double perr[kMaxLoopEq];
+    loopZeroAcc(L);
+    loopKinematics<NM>(L);
+    bool ok = true;
+    if (loopPerr(L, perr) == 0) loopNormalizeQuats(L);
+    else ok = loopProjectQ<NM>(L, tol, false);
+    if (!loopProjectU<NM>(L, tol, true, INFINITY, false)) ok = false;
+    return ok ? 0 : SBG_INST_PROJECTION_FAILED;
+}
+
+// After an accepted step whose error passed the gate of
+// AbstractIntegratorRep.cpp:158-166: projectQ then projectU (:168-205),
+// both LocalOnly, with the projection limit. Returns SBG_INST_* bits.
+template <int NM>
+__device__ __noinline__ int loopProjectStep(const LoopState& L, double quatNorm, double tol, double limit, bool force) {
+    double perr[kMaxLoopEq];
+    loopZeroAcc(L);
+    loopKinematics<NM>(L);
+    const double perrNorm = loopPerr(L, perr);
+    const double normOnEntry = fmax(perrNorm, quatNorm);
+    bool ok = true;
+    if (normOnEntry > limit) {
+        ok = false;
+    } else if (perrNorm == 0 || (perrNorm <= tol && !force)) {
+        if (quatNorm > tol || force) loopNormalizeQuats(L);
+    } else {
+        ok = loopProjectQ<NM>(L, tol, true);
+    }
+    if (ok) ok = loopProjectU<NM>(L, tol, force, limit, true);
+    return ok ? 0 : SBG_INST_PROJECTION_FAILED;
+}

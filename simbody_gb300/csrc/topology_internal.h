@@ -23,6 +23,11 @@ struct sbg_topology_s {
     double gravity[3] = {0, 0, 0};
     std::vector<double> defaultY;
     std::vector<sbg_ball_constraint_desc> cons;
+    // loop closures in local rows: body 1, body 2 (-1 = Ground) and the
+    // stations (station 1, station 2); slot index per row (-1 = none)
+    std::vector<int32_t> lcons, lslot;
+    std::vector<double> lst;
+    int nslots = 0;
 };
 
 // Scratch-record offsets of the rows of `t` when every non-Free row is given

@@ -1,0 +1,115 @@
+"""Constraint::Ball loop closures on the GPU (through the C ABI) against the
+CPU oracle and the reference's golden vectors.
+
+Instances with loop closures run the FP64 chain driver in every precision
+(the multiplier solve and the projections are FP64), so they are held to the
+FP64 tolerances: realize <= 1e-12 relative, trajectories <= 1e-10 relative
+(projections are Newton solves stopped at a tolerance; roundoff differences
+between the Cholesky paths shift the iterates slightly).
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from simbody_gb300 import Workload, engine_batch
+
+pytestmark = pytest.mark.gpu
+
+GOLD = Path(__file__).resolve().parent / "golden" / "reference_vectors.npz"
+
+
+def rel(a, b, offsets):
+    return np.array([np.linalg.norm(a[offsets[i]:offsets[i + 1]] - b[offsets[i]:offsets[i + 1]]) /
+                     max(np.linalg.norm(b[offsets[i]:offsets[i + 1]]), 1e-300) for i in range(len(offsets) - 1)])
+
+
+def loop_instances(w, n):
+    return [i for i in range(w.ninst) if w.systems[int(w.instance_system[i])].nconstraints > 0][:n]
+
+
+@pytest.fixture(scope="module")
+def w5():
+    return Workload(5, 160)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_realize_with_loops_matches_oracle(engine, w5, precision):
+    idx = np.arange(64)
+    assert any(w5.systems[int(w5.instance_system[i])].nconstraints for i in idx)
+    b, y0 = engine_batch(w5, precision, instances=idx)
+    b.set_state(y0)
+    ydot, st = b.realize_acceleration()
+    ref, rst = O.realize_workload(w5, idx)
+    assert (st == 0).all() and (rst == 0).all()
+    err = rel(ydot, ref, b.y_offsets)
+    loops = np.array([w5.systems[int(w5.instance_system[i])].nconstraints > 0 for i in idx])
+    assert err[loops].max() <= 1e-12, err[loops].max()
+    assert err[~loops].max() <= (1e-12 if precision == "fp64" else 1e-5), err[~loops].max()
+
+
+def test_rk_merson_with_loops_default_tolerance(engine, w5):
+    idx = np.array(loop_instances(w5, 24))
+    b, y0 = engine_batch(w5, "fp64", instances=idx)
+    b.set_state(y0)
+    st = b.rk_merson_fixed(5e-4, 40)
+    y, t = b.get_state()
+    ref, rt, rst, _ = O.rk_workload(w5, 5e-4, 40, idx)
+    assert (st == 0).all() and (rst == 0).all()
+    assert rel(y, ref, b.y_offsets).max() <= 1e-10
+    np.testing.assert_array_equal(t, rt)
+
+
+def test_rk_merson_with_loops_projecting_every_few_steps(engine, w5):
+    """A 1e-9 constraint tolerance makes the position and velocity
+    projections run inside the steps."""
+    idx = np.array(loop_instances(w5, 16))
+    b, y0 = engine_batch(w5, "fp64", instances=idx)
+    b.set_state(y0)
+    st = b.rk_merson_fixed(5e-4, 100, constraint_tolerance=1e-9)
+    y, _ = b.get_state()
+    ref, _, rst, nproj = O.rk_workload(w5, 5e-4, 100, idx, cons_tol=1e-9)
+    assert nproj > 0
+    assert (st == rst).all()
+    assert rel(y, ref, b.y_offsets).max() <= 1e-10
+
+
+def test_mixed_batch_keeps_loops_in_fp64(engine, w5):
+    idx = np.arange(48)
+    bm, y0 = engine_batch(w5, "mixed", instances=idx)
+    b64, _ = engine_batch(w5, "fp64", instances=idx)
+    bm.set_state(y0)
+    b64.set_state(y0)
+    bm.rk_merson_fixed(5e-4, 20)
+    b64.rk_merson_fixed(5e-4, 20)
+    ym, _ = bm.get_state()
+    y64, _ = b64.get_state()
+    err = rel(ym, y64, b64.y_offsets)
+    loops = np.array([w5.systems[int(w5.instance_system[i])].nconstraints > 0 for i in idx])
+    assert err[loops].max() <= 1e-13
+    assert err[~loops].max() <= 1e-6
+
+
+def test_engine_matches_reference_golden_vectors(engine):
+    """Every golden record (configs 1-5) through the engine in FP64."""
+    g = dict(np.load(GOLD))
+    sizes = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64}
+    ws = {c: Workload(c, n) for c, n in sizes.items()}
+    for r in range(len(g["cfg"])):
+        cfg, inst = int(g["cfg"][r]), int(g["inst"][r])
+        ys = slice(int(g["y_off"][r]), int(g["y_off"][r + 1]))
+        us = slice(int(g["u_off"][r]), int(g["u_off"][r + 1]))
+        b, y0 = engine_batch(ws[cfg], "fp64", instances=[inst])
+        b.set_state(y0)
+        ydot, st = b.realize_acceleration()
+        assert st[0] == 0
+        assert np.linalg.norm(ydot - g["ydot"][ys]) <= 1e-12 * np.linalg.norm(g["ydot"][ys]), (cfg, inst)
+        mf = b.multiply_by_minv(g["f"][us])
+        assert np.linalg.norm(mf - g["minv_f"][us]) <= 1e-12 * np.linalg.norm(g["minv_f"][us]), (cfg, inst)
+        ctol = float(g["cons_tol"][r])
+        st = b.rk_merson_fixed(float(g["h"][r]), int(g["nsteps"][r]), constraint_tolerance=ctol)
+        y, t = b.get_state()
+        assert st[0] == 0, (cfg, inst, int(st[0]))
+        assert t[0] == g["t_rk"][r]
+        assert np.linalg.norm(y - g["y_rk"][ys]) <= 1e-10 * np.linalg.norm(g["y_rk"][ys]), (cfg, inst)
