@@ -45,6 +45,12 @@ def _args():
     p.add_argument("--instances", type=int, default=65536)
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target CPU-baseline sample duration")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--arm", default="all", choices=["all", "mixed", "fp64"],
+                   help="profiling aid: time only this form's realize (no e2e, no CPU baseline)")
+    p.add_argument("--no-trajectories", action="store_true")
+    p.add_argument("--serve-seconds", type=float, default=3.0, help="arrival window of the serving stream (0 = skip)")
+    p.add_argument("--serve-chunk", type=int, default=64)
+    p.add_argument("--serve-budget-gb", type=float, default=40.0)
     return p.parse_args()
 
 
@@ -157,17 +163,138 @@ def time_resident(b, steps: int, warmup: int):
     return start.elapsed_time(end) / steps, b.launch_count - n0
 
 
+def pinned(shape, dtype):
+    """A numpy array in page-locked host memory (a pinned torch tensor's
+    storage), as a caller that streams states would hold them."""
+    import torch
+
+    tdt = {np.float64: torch.float64, np.int32: torch.int32}[dtype]
+    return torch.empty(shape, dtype=tdt, pin_memory=True).numpy()
+
+
 def time_e2e(b, y0, steps: int, warmup: int):
+    """The public API with host buffers: per step set_state (host -> device)
+    and realize_acceleration (device -> host of [qdot, udot] and status)."""
+    yh = pinned(y0.shape, np.float64)
+    yh[:] = y0
+    ydot = pinned((b.ny_total,), np.float64)
+    st = pinned((b.ninst,), np.int32)
     for _ in range(warmup):
-        b.set_state(y0)
-        b.realize_acceleration()
+        b.set_state(yh)
+        b.realize_acceleration(ydot, st)
     t0 = time.perf_counter()
     n0 = b.launch_count
     for _ in range(steps):
-        b.set_state(y0)
-        ydot, st = b.realize_acceleration()
+        b.set_state(yh)
+        b.realize_acceleration(ydot, st)
     dt = (time.perf_counter() - t0) / steps
     return dt * 1e3, b.launch_count - n0, ydot
+
+
+def time_rk(b, h, nsteps):
+    """One fixed-step RK-Merson integration of the batch's resident state,
+    timed with CUDA events on the batch's stream."""
+    import torch
+
+    stream = torch.cuda.ExternalStream(b.stream)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = b.launch_count
+    start.record(stream)
+    b.rk_merson_fixed_async(h, nsteps)
+    end.record(stream)
+    end.synchronize()
+    return start.elapsed_time(end), b.launch_count - n0
+
+
+def trajectories():
+    """Fixed-step RK-Merson throughput (body-steps/s) on the trajectory
+    workloads: the double pendulum (FP64), the random trees and the uneven
+    batch (mixed, FP64 state), with the mixed form's state error after all
+    steps against the FP64 engine on a subset of instances."""
+    from simbody_gb300 import Workload, engine_batch
+
+    out = {}
+    for cfg, prec, n_inst, n_ref in [(1, "fp64", 1024, 0), (3, "mixed", 16384, 512), (4, "mixed", 10000, 256)]:
+        w = Workload(cfg, n_inst)
+        b, y0 = engine_batch(w, prec)
+        b.set_state(y0)
+        time_rk(b, w.h, 2)  # warm-up (the first call tunes the launch)
+        b.set_state(y0)
+        ms, launches = time_rk(b, w.h, w.nsteps)
+        y, _ = b.get_state()
+        body_steps = int(w.nbodies().sum()) * w.nsteps
+        rec = {"precision": prec, "instances": w.ninst, "steps": w.nsteps, "h": w.h, "ms": ms,
+               "body_steps_per_s": body_steps / (ms * 1e-3), "gpu_launches": launches}
+        if n_ref:
+            idx = np.arange(n_ref)
+            r, yr0 = engine_batch(w, "fp64", instances=idx)
+            r.set_state(yr0)
+            r.rk_merson_fixed(w.h, w.nsteps)
+            yr, _ = r.get_state()
+            errs = np.array([np.linalg.norm(y[b.y_offsets[i]:b.y_offsets[i + 1]] - yr[r.y_offsets[i]:r.y_offsets[i + 1]])
+                             / np.linalg.norm(yr[r.y_offsets[i]:r.y_offsets[i + 1]]) for i in idx])
+            rec["state_rel_err_vs_fp64"] = {"instances": n_ref, "median": float(np.median(errs)),
+                                            "max": float(errs.max())}
+        out[{1: "double_pendulum", 3: "random_trees", 4: "uneven_batch"}[cfg]] = rec
+        b.close()
+    return out
+
+
+def serving(seconds: float, chunk: int, budget_gb: float, cpu_sample_body_steps: float):
+    """The serving stream: Poisson arrivals at 2,000 requests/s for
+    `seconds`, trees from the uneven-batch distribution, horizons
+    log-uniform in [100, 10000] steps, 20% with 1-4 Ball loop closures;
+    continuous batching with a device budget. Latency = time the result
+    reached the host - scheduled arrival."""
+    from oracle import oracle as O
+    from simbody_gb300 import Server, Topology, Workload
+
+    n = int(round(2000 * seconds))
+    w = Workload(5, n)
+    topos = [Topology(w.systems[int(w.instance_system[i])], keepalive=w) for i in range(n)]
+    srv = Server("mixed", device_budget_bytes=int(budget_gb * (1 << 30)), chunk_steps=chunk)
+    ids = np.zeros(n, dtype=np.int64)
+    t_start = srv.clock()
+    nxt, max_queue = 0, 0
+    while nxt < n:
+        now = srv.clock() - t_start
+        while nxt < n and w.arrivals[nxt] <= now:
+            i = nxt
+            ids[i] = srv.submit(topos[i], w.y0[w.instance_slice(i)], w.h, int(w.horizons[i]))
+            nxt += 1
+        srv.tick()
+        max_queue = max(max_queue, srv.stats()["queued"])
+    srv.drain()
+    t_end = srv.clock()
+    lat, body_steps = np.empty(n), 0
+    status_bad = 0
+    for i in range(n):
+        inf = srv.info(ids[i])
+        lat[i] = inf["done_s"] - (t_start + w.arrivals[i])
+        body_steps += inf["nbodies"] * inf["nsteps"]
+        status_bad += inf["status"] != 0
+    st = srv.stats()
+    wall = t_end - t_start
+    offered = body_steps / float(w.arrivals[-1])
+    # CPU: requests run alone, one after another, on one core (the oracle)
+    cpu_t, cpu_bs, k = 0.0, 0, 0
+    while k < n and cpu_bs < cpu_sample_body_steps:
+        t0 = time.perf_counter()
+        O.rk_workload(w, w.h, int(w.horizons[k]), instances=[k], nthreads=1)
+        cpu_t += time.perf_counter() - t0
+        cpu_bs += int(w.nbodies()[k]) * int(w.horizons[k])
+        k += 1
+    srv.close()
+    return {"requests": n, "arrival_rate_per_s": 2000, "arrival_window_s": float(w.arrivals[-1]),
+            "precision": "mixed", "chunk_steps": chunk, "device_budget_bytes": st["device_bytes"],
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "mean": float(lat.mean()), "max": float(lat.max())},
+            "throughput_body_steps_per_s": body_steps / wall, "offered_body_steps_per_s": offered,
+            "completed_requests_per_s": n / wall, "wall_s": wall, "max_queued": int(max_queue),
+            "peak_resident": st["peak_resident"], "ticks": st["ticks"], "gpu_launches": st["launches"],
+            "requests_with_status": int(status_bad),
+            "cpu_alone_sequential": {"requests": k, "body_steps_per_s": cpu_bs / max(cpu_t, 1e-9), "cores": 1,
+                                     "kind": "port"}}
 
 
 def udot_rel_err(d_mixed, d_64, b):
@@ -194,6 +321,13 @@ def run_ours(args):
     build_all()
     w = Workload(2, args.instances)
     nb_total = int(w.nbodies().sum())
+    if args.arm != "all":
+        b, y0 = engine_batch(w, args.arm)
+        b.set_state(y0)
+        ms, launches = time_resident(b, args.steps, args.warmup)
+        print(json.dumps({"arm": args.arm, "instances": w.ninst, "ms_per_step": ms,
+                          "body_rhs_per_s": nb_total / (ms * 1e-3), "gpu_launches": launches}))
+        return
 
     b64, y0 = engine_batch(w, "fp64")
     bmx, _ = engine_batch(w, "mixed")
@@ -262,6 +396,12 @@ def run_ours(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, min(args.instances, 65536))
+    b64.close()
+    bmx.close()
+    if not args.no_trajectories:
+        result["trajectories"] = trajectories()
+    if args.serve_seconds > 0:
+        result["serving"] = serving(args.serve_seconds, args.serve_chunk, args.serve_budget_gb, 2e6)
     if rank == 0:
         print(json.dumps(result))
     if world > 1:

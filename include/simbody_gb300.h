@@ -226,13 +226,89 @@ int sbg_batch_sync(sbg_batch batch);
 /* Number of kernel launches issued by this batch since creation. */
 int64_t sbg_batch_launch_count(sbg_batch batch);
 /* Occupancy variant the batch's tuner picked for its FP32 kernels (1 = two
- * 128-thread blocks per SM, 4 = four), 0 before the first realize or
+ * 128-thread blocks per SM, 4 = four, 7 = seven 64-thread blocks per SM for
+ * the one-thread-per-instance segment), 0 before the first realize or
  * integration, -1 for a null batch. No counterpart in the reference. */
 int sbg_batch_kernel_variant(sbg_batch batch);
 /* Lanes-per-tree setting the tuner picked for the batch's level-parallel
  * segment (lanes = next power of two of the widest level, shifted right by
  * this), -1 for a null batch. No counterpart in the reference. */
 int sbg_batch_group_lanes_shift(sbg_batch batch);
+
+/* ----------------------------------------------------------------- serving */
+
+/* No counterpart in the reference (Simbody runs one Integrator per State on
+ * the calling thread). A server admits rollout requests -- one State of any
+ * supported System, Integrator::initialize(state) and fixed-step RK-Merson
+ * stepTo(t0 + nsteps*h), as sbg_rk_merson_fixed does for one instance --
+ * and runs them with continuous batching on one GPU: every tick, each
+ * resident request advances by min(chunk_steps, remaining) steps in the same
+ * kernel launch as all other resident requests; finished requests leave
+ * after their tick and queued ones (strict arrival order) take their slots
+ * and memory. The server allocates its whole device budget once, at
+ * creation (device arena split into table, state and scratch pools); a
+ * request is admitted only while its share fits. A request's result does
+ * not depend on which other requests share its ticks. */
+typedef struct sbg_server_s* sbg_server;
+
+typedef struct sbg_server_config {
+    int32_t precision;            /* sbg_precision of the tree recursions; loop
+                                     closures always run in FP64 */
+    int32_t device;               /* CUDA device ordinal */
+    int64_t device_budget_bytes;  /* device memory the server holds (> 0) */
+    int32_t max_slots;            /* resident requests at most (0 = 65536) */
+    int32_t chunk_steps;          /* RK steps per tick and request (0 = 64) */
+} sbg_server_config;
+
+typedef struct sbg_request_info {
+    int32_t done;       /* 1 once the final state is on the host */
+    int32_t status;     /* OR of the SBG_INST_* words of its steps */
+    int32_t nbodies;
+    int32_t nsteps;
+    double  t;          /* final time */
+    double  submit_s;   /* server clock (sbg_server_clock) at submission, */
+    double  admit_s;    /* at admission (-1 while queued) and */
+    double  done_s;     /* when the result reached the host (-1 before) */
+} sbg_request_info;
+
+typedef struct sbg_server_stats {
+    int64_t submitted, completed, queued, resident, peak_resident;
+    int64_t ticks, launches;
+    int64_t body_steps;          /* sum of bodies x steps of completed requests */
+    int64_t device_bytes;        /* device memory held (the arena) */
+    int32_t max_slots, chunk_steps;
+    int64_t pool_capacity[5];    /* rows, forces, state, scratch, loop scratch */
+    int64_t pool_in_use[5];
+} sbg_server_stats;
+
+int sbg_server_create(const sbg_server_config* config, sbg_server* out);
+int sbg_server_destroy(sbg_server server);
+/* Queue a request (host only, never waits for the GPU; thread-safe). The
+ * topology is copied: it may be destroyed after the call. y0 has nq+nu
+ * values. SBG_ERR_BUDGET if the request could never fit the server. */
+int sbg_server_submit(sbg_server server, sbg_topology topology, const double* y0, double t0, double h,
+                      int32_t nsteps, const sbg_integ_opts* opts, int64_t* request_id);
+/* One scheduling round: collect finished ticks, admit, launch one chunk of
+ * every resident request. Returns without waiting when the previous tick is
+ * still running (at most two ticks are in flight). ncompleted (may be NULL)
+ * gets the number of requests whose results arrived during this call. */
+int sbg_server_tick(sbg_server server, int32_t* ncompleted);
+/* Tick until every submitted request has its result on the host. */
+int sbg_server_drain(sbg_server server);
+/* Result of a request: y (nq+nu values, may be NULL) once info->done; with
+ * info given, an unfinished request returns SBG_OK and done = 0. */
+int sbg_server_result(sbg_server server, int64_t request_id, double* y, sbg_request_info* info);
+int sbg_server_get_stats(sbg_server server, sbg_server_stats* stats);
+/* Seconds since the server was created: the clock of sbg_request_info. */
+double sbg_server_clock(sbg_server server);
+/* The admission and chunk policy run without a device (for checking it):
+ * request i has footprint units[5*i .. 5*i+5) in the pools of `capacity`
+ * (rows, forces, state, scratch, loop scratch), horizon horizons[i], and
+ * arrives at tick arrival_tick[i] (non-decreasing). admit_tick / done_tick
+ * get the tick of its admission and of its last chunk. */
+int sbg_serve_simulate(int32_t n, const int64_t* units, const int32_t* horizons, const int64_t* arrival_tick,
+                       const int64_t* capacity, int32_t max_slots, int32_t chunk_steps, int64_t* admit_tick,
+                       int64_t* done_tick, int64_t* peak_resident);
 
 /* ------------------------------------------------ allocation-free realize */
 

@@ -7,6 +7,7 @@ behind the C ABI in include/simbody_gb300.h; there is no CPU fallback.
 """
 from . import _native  # noqa: F401
 from .engine import Batch, Topology, device_count  # noqa: F401
+from .serve import Server  # noqa: F401
 from .workloads import Workload, engine_batch  # noqa: F401
 
-__all__ = ["Batch", "Topology", "Workload", "engine_batch", "device_count"]
+__all__ = ["Batch", "Server", "Topology", "Workload", "engine_batch", "device_count"]

@@ -59,6 +59,24 @@ class BatchConfig(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32), ("device_budget_bytes", C.c_int64)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("device", C.c_int32), ("device_budget_bytes", C.c_int64),
+                ("max_slots", C.c_int32), ("chunk_steps", C.c_int32)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("done", C.c_int32), ("status", C.c_int32), ("nbodies", C.c_int32), ("nsteps", C.c_int32),
+                ("t", C.c_double), ("submit_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("queued", C.c_int64),
+                ("resident", C.c_int64), ("peak_resident", C.c_int64), ("ticks", C.c_int64),
+                ("launches", C.c_int64), ("body_steps", C.c_int64), ("device_bytes", C.c_int64),
+                ("max_slots", C.c_int32), ("chunk_steps", C.c_int32),
+                ("pool_capacity", C.c_int64 * 5), ("pool_in_use", C.c_int64 * 5)]
+
+
 assert C.sizeof(BodyDesc) == 280 and C.sizeof(MobilityForceDesc) == 32
 assert C.sizeof(BallConstraintDesc) == 56 and C.sizeof(SystemDesc) == 64
 
@@ -91,6 +109,15 @@ ENGINE_API = {
     "sbg_batch_launch_count": (C.c_int64, [vp]),
     "sbg_batch_kernel_variant": (C.c_int, [vp]),
     "sbg_batch_group_lanes_shift": (C.c_int, [vp]),
+    "sbg_server_create": (C.c_int, [P(ServerConfig), P(vp)]),
+    "sbg_server_destroy": (C.c_int, [vp]),
+    "sbg_server_submit": (C.c_int, [vp, vp, dp, C.c_double, C.c_double, C.c_int32, P(IntegOpts), i64p]),
+    "sbg_server_tick": (C.c_int, [vp, ip]),
+    "sbg_server_drain": (C.c_int, [vp]),
+    "sbg_server_result": (C.c_int, [vp, C.c_int64, dp, P(RequestInfo)]),
+    "sbg_server_get_stats": (C.c_int, [vp, P(ServerStats)]),
+    "sbg_server_clock": (C.c_double, [vp]),
+    "sbg_serve_simulate": (C.c_int, [C.c_int32, i64p, ip, i64p, i64p, C.c_int32, C.c_int32, i64p, i64p, i64p]),
     "sbg_realize_acceleration_noalloc": (C.c_int, [vp, C.c_int32, vp, vp, vp, vp]),
     "sbg_noalloc_last_error": (C.c_char_p, []),
 }

@@ -46,6 +46,14 @@ template <class R> struct ScrTiled {
     R* p;
     __device__ __forceinline__ R& operator()(int rec, int f) const { return p[(rec + f) * kTile]; }
 };
+// Loop-closure records: element f of record rec at (rec + f) * s, with the
+// stride of the instance (32 inside a batch's interleaved tiles, 1 for an
+// instance whose record is its own).
+template <class R> struct ScrStrided {
+    R* p;
+    int s;
+    __device__ __forceinline__ R& operator()(int rec, int f) const { return p[(rec + f) * s]; }
+};
 template <class R> struct ScrRows {
     R* p;
     int P;  // rows of the instance
@@ -1090,7 +1098,7 @@ template <class R, int NM, bool REF, bool GROUP, bool LOOPS = false, class Src, 
 __device__ __forceinline__ int rhs(const DevTables& T, const Slot& s, R* scratch, const Src& src, Out& out) {
     if constexpr (LOOPS) {
         static_assert(std::is_same<R, double>::value && !GROUP && !REF, "loop closures run the FP64 chain driver");
-        const ScrTiled<double> S{scratch + T.sbase[s.inst]};
+        const ScrStrided<double> S{scratch + T.sbase[s.inst], (int)T.sstride[s.inst]};
         int st = rhsChain<double, NM, false, true>(T, s.inst, S, src, out);
         if (T.incons[s.inst] > 0) st |= loopForwardDynamics<NM>(T, s.inst, S, out);
         return st;
@@ -1108,8 +1116,8 @@ template <bool GROUP> __device__ __forceinline__ bool groupAll(bool v, const Slo
 }
 
 // ------------------------------------------------------------ realize kernel
-template <class R, int NM, bool REF, bool GROUP, int MINB = 1, bool LOOPS = false>
-__global__ void __launch_bounds__(128, MINB) realizeKernel(DevTables T, int first, int count, const double* __restrict__ y,
+template <class R, int NM, bool REF, bool GROUP, int MINB = 1, bool LOOPS = false, int BS = 128>
+__global__ void __launch_bounds__(BS, MINB) realizeKernel(DevTables T, int first, int count, const double* __restrict__ y,
                                                            double* __restrict__ ydot, R* __restrict__ scratch,
                                                            int32_t* __restrict__ status) {
     const Slot s = GROUP ? groupSlot(T, first) : chainSlot(T, first, count);
@@ -1134,6 +1142,14 @@ __global__ void __launch_bounds__(128) minvKernel(DevTables T, int first, int co
     if (s.gl == 0) status[s.inst] = st;
 }
 
+// q /= |q| for the quaternion at q slot qo (RigidBodyNodeSpec_Ball.h:417-434).
+__device__ __forceinline__ void normalizeQuatAt(double* y, int64_t base, int64_t stride, int qo) {
+    double qq[4];
+    for (int j = 0; j < 4; ++j) qq[j] = y[base + (int64_t)(qo + j) * stride];
+    const double len = sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);
+    for (int j = 0; j < 4; ++j) y[base + (int64_t)(qo + j) * stride] = qq[j] / len;
+}
+
 // ---------------------------------------------------- RK Merson persistent
 // Sum over the lanes of a group (butterfly within the group's lanes).
 __device__ __forceinline__ double groupSum(double v, const Slot& s) {
@@ -1141,8 +1157,8 @@ __device__ __forceinline__ double groupSum(double v, const Slot& s) {
     return v;
 }
 
-template <class R, int NM, bool REF, bool GROUP, int MINB = 1, bool LOOPS = false>
-__global__ void __launch_bounds__(128, MINB) rkMersonKernel(DevTables T, int first, int count, double* __restrict__ y,
+template <class R, int NM, bool REF, bool GROUP, int MINB = 1, bool LOOPS = false, int BS = 128>
+__global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int first, int count, double* __restrict__ y,
                                                             double* __restrict__ time, R* __restrict__ fbuf,
                                                             int64_t fplane, R* __restrict__ scratch,
                                                             int32_t* __restrict__ status, double h, int nsteps,
@@ -1159,6 +1175,28 @@ __global__ void __launch_bounds__(128, MINB) rkMersonKernel(DevTables T, int fir
     R* fC = fbuf + 3 * fplane;
     int st = status[inst];
     double tc = time[inst];
+    // Per-instance control (serving): this launch's steps, whether it starts
+    // the integration, the instance's own step size and tolerances.
+    int nst = nsteps;
+    bool init = true, pes = projectEveryStep != 0;
+    if (T.ictl) {
+        const int c = T.ictl[inst];
+        nst = c & kCtlSteps;
+        init = (c & kCtlInit) != 0;
+        pes = (c & kCtlProjectEveryStep) != 0;
+        h = T.iparam[3 * inst];
+        accuracy = T.iparam[3 * inst + 1];
+        consTol = T.iparam[3 * inst + 2];
+        // Integrator::initialize normalizes quaternions (Integrator.cpp:376-377);
+        // instances with loop closures project in loopInitialize instead.
+        if (init && !(LOOPS && T.incons[inst] > 0)) {
+            for (int lb = s.gl; lb < nb; lb += s.G) {
+                const int type = T.info[body0 + lb] & 15;
+                if (type == T_BALL || type == T_FREE) normalizeQuatAt(y, base, stride, T.qoff[body0 + lb]);
+            }
+            if constexpr (GROUP) __syncwarp(s.mask);
+        }
+    }
     const double projLimit = fmax(2 * consTol, sqrt(consTol));
     auto stage = [&](int stg, double c, const R* a, const R* b, R* dst) {
         StageSrc<R> src{y, f0, a, b, base, stride, nq, stg, c};
@@ -1171,11 +1209,11 @@ __global__ void __launch_bounds__(128, MINB) rkMersonKernel(DevTables T, int fir
     // velocity projection (IntegratorRep.h:856-895); the buffers fB/fC are
     // free outside a step.
     if constexpr (LOOPS)
-        if (T.incons[inst] > 0) {
-            const LoopState L{T, inst, ScrTiled<double>{scratch + T.sbase[inst]}, y, fB, fC, base, stride};
+        if (init && T.incons[inst] > 0) {
+            const LoopState L{T, inst, ScrStrided<double>{scratch + T.sbase[inst], (int)T.sstride[inst]}, y, fB, fC, base, stride};
             st |= loopInitialize<NM>(L, consTol);
         }
-    for (int step = 0; step < nsteps; ++step) {
+    for (int step = 0; step < nst; ++step) {
         const double t1 = tc + h;
         const double hs = t1 - tc;
         stage(0, 0.0, fA, fB, f0);      // f0 = f(y0)
@@ -1257,24 +1295,19 @@ __global__ void __launch_bounds__(128, MINB) rkMersonKernel(DevTables T, int fir
             if (T.incons[inst] > 0) {
                 loopsDone = true;
                 if (errNorm <= 16 * accuracy) {
-                    const LoopState L{T, inst, ScrTiled<double>{scratch + T.sbase[inst]}, y, fB, fC, base, stride};
+                    const LoopState L{T, inst, ScrStrided<double>{scratch + T.sbase[inst], (int)T.sstride[inst]}, y, fB, fC, base, stride};
                     const double quatNorm = nquat > 0 ? sqrt(squat / nquat) : 0.0;
-                    st |= loopProjectStep<NM>(L, quatNorm, consTol, projLimit, projectEveryStep != 0);
+                    st |= loopProjectStep<NM>(L, quatNorm, consTol, projLimit, pes);
                 }
             }
         if (!loopsDone && errNorm <= 16 * accuracy && nquat > 0) {
             const double quatNorm = sqrt(squat / nquat);
             if (quatNorm > projLimit) st |= SBG_INST_PROJECTION_FAILED;
-            else if (quatNorm > consTol || projectEveryStep) {
+            else if (quatNorm > consTol || pes) {
                 for (int lb = s.gl; lb < nb; lb += s.G) {
                     const int row = body0 + lb;
                     const int type = T.info[row] & 15;
-                    if (type != T_BALL && type != T_FREE) continue;
-                    const int qo = T.qoff[row];
-                    double qq[4];
-                    for (int j = 0; j < 4; ++j) qq[j] = y[base + (int64_t)(qo + j) * stride];
-                    const double len = sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);
-                    for (int j = 0; j < 4; ++j) y[base + (int64_t)(qo + j) * stride] = qq[j] / len;
+                    if (type == T_BALL || type == T_FREE) normalizeQuatAt(y, base, stride, T.qoff[row]);
                 }
             }
         }

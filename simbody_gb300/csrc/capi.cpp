@@ -38,6 +38,18 @@ int cudaFail(cudaError_t e, const char* what) {
 const int kNQ[5] = {1, 1, 2, 4, 7};
 const int kNU[5] = {1, 1, 2, 3, 6};
 
+// Host buffers the caller allocated page-locked (cudaMallocHost,
+// cudaHostRegister, a pinned torch tensor) are copied to and from directly;
+// pageable ones go through the batch's pinned staging buffer.
+bool isPinned(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 bool isIdentityR(const double* X) {
     return X[0] == 1 && X[1] == 0 && X[2] == 0 && X[3] == 0 && X[4] == 1 && X[5] == 0 && X[6] == 0 && X[7] == 0 &&
            X[8] == 1;
@@ -46,6 +58,13 @@ bool isIdentityR(const double* X) {
 }  // namespace
 
 #include "topology_internal.h"
+
+namespace sbg {
+int setError(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+}  // namespace sbg
 
 struct DevBuf {
     void* p = nullptr;
@@ -540,7 +559,10 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     const int64_t scratchLoopElems = sOffLoop;
     b->tiled = true;
     if (precision == SBG_PRECISION_FP64) b->variant = 1;  // FP64 needs every register
-    if (const char* v = std::getenv("SBG_VARIANT")) b->variant = std::atoi(v) == 4 ? 4 : 1;  // tuning override
+    if (const char* v = std::getenv("SBG_VARIANT")) {  // tuning override
+        const int want = std::atoi(v);
+        b->variant = want == 4 || want == 7 ? want : 1;
+    }
 
     int rc = 0;
     DevTables& T = b->T;
@@ -657,8 +679,12 @@ int sbg_batch_set_state(sbg_batch b, const double* t, const double* y) {
     if (!b || !y) return fail(SBG_ERR_INVALID, "null argument");
     SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
     const size_t bytes = b->nyTotal * sizeof(double);
-    std::memcpy(b->hostPinned, y, bytes);
-    SBG_CUDA(cudaMemcpyAsync(b->staging, b->hostPinned, bytes, cudaMemcpyHostToDevice, b->stream), "state upload");
+    const double* src = y;
+    if (!isPinned(y)) {
+        std::memcpy(b->hostPinned, y, bytes);
+        src = b->hostPinned;
+    }
+    SBG_CUDA(cudaMemcpyAsync(b->staging, src, bytes, cudaMemcpyHostToDevice, b->stream), "state upload");
     SBG_CUDA(launchScatter(b->T, b->dHostYOff, b->staging, b->y, 0, b->stream), "state scatter");
     ++b->launches;
     if (t) {
@@ -680,10 +706,11 @@ int sbg_batch_get_state(sbg_batch b, double* t, double* y) {
     SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
     SBG_CUDA(launchGather(b->T, b->dHostYOff, b->y, b->staging, 0, b->stream), "state gather");
     ++b->launches;
-    SBG_CUDA(cudaMemcpyAsync(b->hostPinned, b->staging, b->nyTotal * sizeof(double), cudaMemcpyDeviceToHost, b->stream),
+    double* dst = isPinned(y) ? y : b->hostPinned;
+    SBG_CUDA(cudaMemcpyAsync(dst, b->staging, b->nyTotal * sizeof(double), cudaMemcpyDeviceToHost, b->stream),
              "state download");
     SBG_CUDA(cudaStreamSynchronize(b->stream), "state download");
-    std::memcpy(y, b->hostPinned, b->nyTotal * sizeof(double));
+    if (dst != y) std::memcpy(y, b->hostPinned, b->nyTotal * sizeof(double));
     if (t) SBG_CUDA(cudaMemcpy(t, b->time, b->ninst * sizeof(double), cudaMemcpyDeviceToHost), "time download");
     return SBG_OK;
 }
@@ -730,9 +757,14 @@ static int tuneVariant(sbg_batch b) {
         return rc;
     }
     if (!fixedVariant && b->precision != SBG_PRECISION_FP64) {
-        b->variant = 4;
-        if (int rc = timePlan(b, &ms)) return rc;
-        if (!(ms < best)) b->variant = 1;
+        int bestVariant = 1;
+        for (int v : {4, 7}) {
+            if (v == 7 && b->nChain == 0) continue;  // 64-thread blocks exist for the chain driver only
+            b->variant = v;
+            if (int rc = timePlan(b, &ms)) return rc;
+            if (ms < best) { best = ms; bestVariant = v; }
+        }
+        b->variant = bestVariant;
     }
     b->tuned = true;
     return SBG_OK;
@@ -768,15 +800,18 @@ int sbg_realize_acceleration_async(sbg_batch b) {
 int sbg_batch_get_ydot(sbg_batch b, double* ydot, int32_t* status) {
     if (!b) return fail(SBG_ERR_INVALID, "null batch");
     SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    double* dst = ydot && isPinned(ydot) ? ydot : b->hostPinned;
     if (ydot) {
         SBG_CUDA(launchGather(b->T, b->dHostYOff, b->ydot, b->staging, 0, b->stream), "derivative gather");
         ++b->launches;
-        SBG_CUDA(cudaMemcpyAsync(b->hostPinned, b->staging, b->nyTotal * sizeof(double), cudaMemcpyDeviceToHost,
-                                 b->stream), "derivative download");
+        SBG_CUDA(cudaMemcpyAsync(dst, b->staging, b->nyTotal * sizeof(double), cudaMemcpyDeviceToHost, b->stream),
+                 "derivative download");
     }
+    if (status)
+        SBG_CUDA(cudaMemcpyAsync(status, b->status, b->ninst * sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream),
+                 "status download");
     SBG_CUDA(cudaStreamSynchronize(b->stream), "derivative download");
-    if (ydot) std::memcpy(ydot, b->hostPinned, b->nyTotal * sizeof(double));
-    if (status) SBG_CUDA(cudaMemcpy(status, b->status, b->ninst * sizeof(int32_t), cudaMemcpyDeviceToHost), "status download");
+    if (ydot && dst != ydot) std::memcpy(ydot, b->hostPinned, b->nyTotal * sizeof(double));
     return SBG_OK;
 }
 

@@ -114,7 +114,14 @@ struct DevTables {
     const double* lst;       // per constraint: station 1 (in body 1), station 2 (in body 2)
     const int32_t* icons;    // per instance: first constraint
     const int32_t* incons;   // per instance: number of constraints
+    // per-instance integration control (the serving loop; null in a batch,
+    // whose instances share the launch's step count, step size and options)
+    const int32_t* ictl;     // steps of this launch | kCtl* flags
+    const double* iparam;    // h, accuracy, constraint tolerance (3 per instance)
 };
+constexpr int kCtlSteps = (1 << 24) - 1;
+constexpr int kCtlInit = 1 << 30;                // first launch: Integrator::initialize projections
+constexpr int kCtlProjectEveryStep = 1 << 29;    // Integrator::setProjectEveryStep(true)
 
 // How one batch operation is launched: order positions [0, nChain) run the
 // chain driver (one thread per instance, width nm), the next nLoop positions

@@ -1,20 +1,31 @@
 // k_r32c.cu -- realize(Acceleration) kernel instantiations, FP32 recursions,
-// chain driver (refine = double-float residual refinement; variant 4 = at
-// most 128 registers).
+// chain driver (refine = double-float residual refinement). Occupancy
+// variants: 1 = 128-thread blocks with every register the code wants; 4 =
+// 128-thread blocks, at most 128 registers (4 blocks per SM); 7 = 64-thread
+// blocks, at most 144 registers (7 blocks per SM), which keeps a batch of
+// 65,536 one-thread instances in a single balanced wave over 152 SMs.
 #include "abi_device.cuh"
 
 namespace sbg {
 
-template <bool REF, int MINB> static void go(const KArgs& a, cudaStream_t s) {
-    const int nb = (a.P->nChain + 127) / 128;
+template <bool REF, int MINB, int BS> static void go(const KArgs& a, cudaStream_t s) {
+    const int nb = (a.P->nChain + BS - 1) / BS;
     float* sc = static_cast<float*>(a.scratch);
-    if (a.P->nm == 1) realizeKernel<float, 1, REF, false, MINB><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.ydot, sc, a.status);
-    else realizeKernel<float, 3, REF, false, MINB><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.ydot, sc, a.status);
+    if (a.P->nm == 1)
+        realizeKernel<float, 1, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.ydot, sc, a.status);
+    else
+        realizeKernel<float, 3, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.ydot, sc, a.status);
+}
+
+template <bool REF> static void pick(const KArgs& a, cudaStream_t s) {
+    if (a.P->variant == 4) go<REF, 4, 128>(a, s);
+    else if (a.P->variant == 7) go<REF, 7, 64>(a, s);
+    else go<REF, 1, 128>(a, s);
 }
 
 void realize32Chain(const KArgs& a, bool refine, cudaStream_t s) {
-    if (refine) { if (a.P->variant == 4) go<true, 4>(a, s); else go<true, 1>(a, s); }
-    else { if (a.P->variant == 4) go<false, 4>(a, s); else go<false, 1>(a, s); }
+    if (refine) pick<true>(a, s);
+    else pick<false>(a, s);
 }
 
 }  // namespace sbg

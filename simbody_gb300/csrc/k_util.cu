@@ -16,12 +16,7 @@ __global__ void normalizeQuatKernel(DevTables T, double* __restrict__ y) {
     for (int lb = 0; lb < nb; ++lb) {
         const int row = body0 + lb;
         const int type = T.info[row] & 15;
-        if (type != T_BALL && type != T_FREE) continue;
-        const int qo = T.qoff[row];
-        double qq[4];
-        for (int j = 0; j < 4; ++j) qq[j] = y[base + (int64_t)(qo + j) * stride];
-        const double len = sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);
-        for (int j = 0; j < 4; ++j) y[base + (int64_t)(qo + j) * stride] = qq[j] / len;
+        if (type == T_BALL || type == T_FREE) normalizeQuatAt(y, base, stride, T.qoff[row]);
     }
 }
 

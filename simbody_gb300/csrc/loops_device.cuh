@@ -30,7 +30,7 @@
 // With localOnly a growing norm stops the iteration and undoes the last
 // step; a result worse than the entry state is restored.
 
-using SC64 = ScrTiled<double>;
+using SC64 = ScrStrided<double>;
 using V3d = V3<double>;
 
 // One instance with loop closures inside a kernel. save/delta are column

@@ -2,6 +2,7 @@
 // sbg_topology handle (shared by capi.cpp and k_noalloc.cu).
 #pragma once
 #include <cstdint>
+#include <string>
 #include <vector>
 
 #include "../../include/simbody_gb300.h"
@@ -29,6 +30,11 @@ struct sbg_topology_s {
     std::vector<double> lst;
     int nslots = 0;
 };
+
+namespace sbg {
+// Records msg as the calling thread's sbg_last_error() message; returns code.
+int setError(int code, const std::string& msg);
+}  // namespace sbg
 
 // Scratch-record offsets of the rows of `t` when every non-Free row is given
 // the record of an nm-mobility body (Free rows keep 6): lanes of a warp that

@@ -99,11 +99,18 @@ class Batch:
         return y, t
 
     # -- operators
-    def realize_acceleration(self):
-        ydot = np.empty(self.ny_total)
-        st = np.empty(self.ninst, dtype=np.int32)
-        N.check(N.engine_lib().sbg_realize_acceleration(self._h, _dptr(ydot), _iptr(st)))
-        return ydot, st
+    def realize_acceleration(self, ydot: np.ndarray | None = None, status: np.ndarray | None = None):
+        """System::realize(Stage::Acceleration) + getYDot for every instance.
+        ``ydot`` / ``status`` may be caller-owned output arrays (float64,
+        int32, C-contiguous); page-locked ones are written directly."""
+        if ydot is None:
+            ydot = np.empty(self.ny_total)
+        if status is None:
+            status = np.empty(self.ninst, dtype=np.int32)
+        assert ydot.dtype == np.float64 and ydot.size == self.ny_total and ydot.flags.c_contiguous
+        assert status.dtype == np.int32 and status.size == self.ninst and status.flags.c_contiguous
+        N.check(N.engine_lib().sbg_realize_acceleration(self._h, _dptr(ydot), _iptr(status)))
+        return ydot, status
 
     def multiply_by_minv(self, f: np.ndarray) -> np.ndarray:
         f = np.ascontiguousarray(f, dtype=np.float64)
