@@ -173,20 +173,20 @@ def pinned(shape, dtype):
 
 
 def time_e2e(b, y0, steps: int, warmup: int):
-    """The public API with host buffers: per step set_state (host -> device)
-    and realize_acceleration (device -> host of [qdot, udot] and status)."""
+    """The public API with host buffers: per step one
+    sbg_realize_acceleration_host call (State::updY + realize + getYDot:
+    host -> device state, realize, device -> host [qdot, udot] and status,
+    pipelined in chunks)."""
     yh = pinned(y0.shape, np.float64)
     yh[:] = y0
     ydot = pinned((b.ny_total,), np.float64)
     st = pinned((b.ninst,), np.int32)
     for _ in range(warmup):
-        b.set_state(yh)
-        b.realize_acceleration(ydot, st)
+        b.realize_acceleration_from(yh, ydot, st)
     t0 = time.perf_counter()
     n0 = b.launch_count
     for _ in range(steps):
-        b.set_state(yh)
-        b.realize_acceleration(ydot, st)
+        b.realize_acceleration_from(yh, ydot, st)
     dt = (time.perf_counter() - t0) / steps
     return dt * 1e3, b.launch_count - n0, ydot
 
@@ -231,10 +231,23 @@ def trajectories():
             r.set_state(yr0)
             r.rk_merson_fixed(w.h, w.nsteps)
             yr, _ = r.get_state()
-            errs = np.array([np.linalg.norm(y[b.y_offsets[i]:b.y_offsets[i + 1]] - yr[r.y_offsets[i]:r.y_offsets[i + 1]])
-                             / np.linalg.norm(yr[r.y_offsets[i]:r.y_offsets[i + 1]]) for i in idx])
+
+            def rel(a, oa, c, oc):
+                return np.array([np.linalg.norm(a[oa[i]:oa[i + 1]] - c[oc[i]:oc[i + 1]]) /
+                                 np.linalg.norm(c[oc[i]:oc[i + 1]]) for i in idx])
+
+            errs = rel(y, b.y_offsets, yr, r.y_offsets)
+            # the same FP64 run from a start perturbed by 1e-12 (relative):
+            # how far rounding-sized differences grow over the horizon
+            rng = np.random.default_rng(0)
+            r.set_state(yr0 * (1 + 1e-12 * rng.standard_normal(yr0.size)))
+            r.rk_merson_fixed(w.h, w.nsteps)
+            yp, _ = r.get_state()
+            pert = rel(yp, r.y_offsets, yr, r.y_offsets)
             rec["state_rel_err_vs_fp64"] = {"instances": n_ref, "median": float(np.median(errs)),
-                                            "max": float(errs.max())}
+                                            "max": float(errs.max()),
+                                            "fp64_from_1e-12_perturbed_start": {"median": float(np.median(pert)),
+                                                                                "max": float(pert.max())}}
         out[{1: "double_pendulum", 3: "random_trees", 4: "uneven_batch"}[cfg]] = rec
         b.close()
     return out
@@ -292,6 +305,7 @@ def serving(seconds: float, chunk: int, budget_gb: float, cpu_sample_body_steps:
             "throughput_body_steps_per_s": body_steps / wall, "offered_body_steps_per_s": offered,
             "completed_requests_per_s": n / wall, "wall_s": wall, "max_queued": int(max_queue),
             "peak_resident": st["peak_resident"], "ticks": st["ticks"], "gpu_launches": st["launches"],
+            "gpu_busy_fraction": st["gpu_seconds"] / wall, "host_tick_seconds": st["host_seconds"],
             "requests_with_status": int(status_bad),
             "cpu_alone_sequential": {"requests": k, "body_steps_per_s": cpu_bs / max(cpu_t, 1e-9), "cores": 1,
                                      "kind": "port"}}

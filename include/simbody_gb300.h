@@ -197,6 +197,16 @@ int sbg_batch_get_state(sbg_batch batch, double* t, double* y);
  * Synchronous. */
 int sbg_realize_acceleration(sbg_batch batch, double* ydot, int32_t* status);
 
+/* State::updY + System::realize(state, Stage::Acceleration) +
+ * State::getYDot in one call, from and to host buffers (y and ydot in the
+ * batch packing; status may be NULL): the same results as
+ * sbg_batch_set_state(batch, NULL, y) + sbg_realize_acceleration. For a
+ * batch of one topology on the one-thread-per-instance driver, the upload,
+ * realize and download run in chunks of instances on several streams so
+ * that copies overlap compute (after the batch's first realize has tuned
+ * it); page-locked y/ydot/status are copied directly. Synchronous. */
+int sbg_realize_acceleration_host(sbg_batch batch, const double* y, double* ydot, int32_t* status);
+
 /* SimbodyMatterSubsystem::multiplyByMInv(state, f, MInvf)
  * (Simbody/include/simbody/internal/SimbodyMatterSubsystem.h:1343):
  * f and out are packed like the u parts of y (nu values per instance). */
@@ -242,7 +252,7 @@ int sbg_batch_group_lanes_shift(sbg_batch batch);
  * supported System, Integrator::initialize(state) and fixed-step RK-Merson
  * stepTo(t0 + nsteps*h), as sbg_rk_merson_fixed does for one instance --
  * and runs them with continuous batching on one GPU: every tick, each
- * resident request advances by min(chunk_steps, remaining) steps in the same
+ * resident request advances by min(its chunk, remaining) steps in the same
  * kernel launch as all other resident requests; finished requests leave
  * after their tick and queued ones (strict arrival order) take their slots
  * and memory. The server allocates its whole device budget once, at
@@ -257,7 +267,10 @@ typedef struct sbg_server_config {
     int32_t device;               /* CUDA device ordinal */
     int64_t device_budget_bytes;  /* device memory the server holds (> 0) */
     int32_t max_slots;            /* resident requests at most (0 = 65536) */
-    int32_t chunk_steps;          /* RK steps per tick and request (0 = 64) */
+    int32_t chunk_steps;          /* RK steps per tick of a request of median
+                                     cost (0 = 64); each request's own chunk
+                                     scales with the inverse of its estimated
+                                     GPU time per step (1 .. 16x) */
 } sbg_server_config;
 
 typedef struct sbg_request_info {
@@ -279,6 +292,8 @@ typedef struct sbg_server_stats {
     int32_t max_slots, chunk_steps;
     int64_t pool_capacity[5];    /* rows, forces, state, scratch, loop scratch */
     int64_t pool_in_use[5];
+    double  gpu_seconds;         /* GPU time of the completed ticks (copies + kernels) */
+    double  host_seconds;        /* host time in sbg_server_tick, not counting waits for the GPU */
 } sbg_server_stats;
 
 int sbg_server_create(const sbg_server_config* config, sbg_server* out);

@@ -74,7 +74,8 @@ class ServerStats(C.Structure):
                 ("resident", C.c_int64), ("peak_resident", C.c_int64), ("ticks", C.c_int64),
                 ("launches", C.c_int64), ("body_steps", C.c_int64), ("device_bytes", C.c_int64),
                 ("max_slots", C.c_int32), ("chunk_steps", C.c_int32),
-                ("pool_capacity", C.c_int64 * 5), ("pool_in_use", C.c_int64 * 5)]
+                ("pool_capacity", C.c_int64 * 5), ("pool_in_use", C.c_int64 * 5),
+                ("gpu_seconds", C.c_double), ("host_seconds", C.c_double)]
 
 
 assert C.sizeof(BodyDesc) == 280 and C.sizeof(MobilityForceDesc) == 32
@@ -99,6 +100,7 @@ ENGINE_API = {
     "sbg_batch_set_state": (C.c_int, [vp, dp, dp]),
     "sbg_batch_get_state": (C.c_int, [vp, dp, dp]),
     "sbg_realize_acceleration": (C.c_int, [vp, dp, ip]),
+    "sbg_realize_acceleration_host": (C.c_int, [vp, dp, dp, ip]),
     "sbg_multiply_by_minv": (C.c_int, [vp, dp, dp]),
     "sbg_rk_merson_fixed": (C.c_int, [vp, C.c_double, C.c_int32, P(IntegOpts), ip]),
     "sbg_batch_stream": (vp, [vp]),

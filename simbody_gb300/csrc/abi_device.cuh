@@ -599,10 +599,11 @@ __device__ __forceinline__ bool body2(const DevTables& T, int row, int rec, int 
     return ok;
 }
 
-// Free (6 columns) runs rarely; kept out of line so its register demand does
-// not spill the common path.
+// Free (6 columns): inlined like the other mobilizers. An out-of-line call
+// would take the addresses of its in/out structs and of the state source and
+// sink, which puts them in local memory on every path.
 template <class R, class SC>
-__device__ __noinline__ bool body2Free(const DevTables& T, int row, int rec, const SC& S, R m, const C2<R>& in,
+__device__ __forceinline__ bool body2Free(const DevTables& T, int row, int rec, const SC& S, R m, const C2<R>& in,
                                        C2<R>& outC) {
     return body2<R, 6, SC>(T, row, rec, 6, S, m, in, outC);
 }
@@ -676,7 +677,7 @@ __device__ __forceinline__ A3<R> body3(const DevTables& T, int row, int rec, int
 }
 
 template <class R, bool REF, class SC, class Out>
-__device__ __noinline__ void body3Free(const DevTables& T, int row, int rec, const SC& S, Out& out, const A3<R>& Ap,
+__device__ __forceinline__ void body3Free(const DevTables& T, int row, int rec, const SC& S, Out& out, const A3<R>& Ap,
                                        bool hasParent, A3<R>& A) {
     A = body3<R, 6, REF>(T, row, rec, 6, S, out, Ap, hasParent);
 }
@@ -743,7 +744,7 @@ __device__ __forceinline__ C4 body4(const DevTables& T, int row, int rec, int n,
 }
 
 template <class SC>
-__device__ __noinline__ void body4Free(const DevTables& T, int row, int rec, const SC& S, const C4& own,
+__device__ __forceinline__ void body4Free(const DevTables& T, int row, int rec, const SC& S, const C4& own,
                                        const C4& in, C4& outC) {
     outC = body4<6>(T, row, rec, 6, S, own, in);
 }
@@ -784,7 +785,7 @@ __device__ __forceinline__ A3<float> body5(const DevTables& T, int row, int rec,
 }
 
 template <class SC, class Out>
-__device__ __noinline__ void body5Free(const DevTables& T, int row, int rec, const SC& S, Out& out,
+__device__ __forceinline__ void body5Free(const DevTables& T, int row, int rec, const SC& S, Out& out,
                                        const A3<float>& Ap, bool hasParent, A3<float>& A) {
     A = body5<6>(T, row, rec, 6, S, out, Ap, hasParent);
 }
@@ -793,7 +794,7 @@ __device__ __noinline__ void body5Free(const DevTables& T, int row, int rec, con
 // Chain driver: one thread, rows in order; carries along chains, pushes into
 // the parent's record otherwise. Returns SBG_INST_* bits.
 template <class R, int NM, bool REF, bool LOOPS = false, class SC, class Src, class Out>
-__device__ __noinline__ int rhsChain(const DevTables& T, int inst, const SC& S, const Src& src, Out& out) {
+__device__ __forceinline__ int rhsChain(const DevTables& T, int inst, const SC& S, const Src& src, Out& out) {
     static_assert(!REF || std::is_same<R, float>::value, "refinement is for the FP32 recursion");
     const int body0 = T.ibody[inst], nb = T.inb[inst];
     const V3<R> g = mk3(R(T.grav[3 * inst]), R(T.grav[3 * inst + 1]), R(T.grav[3 * inst + 2]));

@@ -112,6 +112,9 @@ struct sbg_batch_s {
     int32_t* dBlkG = nullptr;
     cudaStream_t stream2 = nullptr;
     cudaEvent_t evFork = nullptr, evJoin = nullptr;
+    bool orderIdentity = false;         // launch order = instance order (a one-topology chain batch)
+    cudaStream_t pipe[4] = {};          // streams of the pipelined host realize (pipe[0] = stream)
+    cudaEvent_t pipeEv[4] = {};
     cudaEvent_t evT0 = nullptr, evT1 = nullptr;
     bool tuned = false;
     cudaGraphExec_t realizeGraph = nullptr;  // captured after tuning
@@ -160,6 +163,10 @@ struct sbg_batch_s {
         if (evT1) cudaEventDestroy(evT1);
         if (evJoin) cudaEventDestroy(evJoin);
         if (stream2) cudaStreamDestroy(stream2);
+        for (int k = 1; k < 4; ++k)
+            if (pipe[k]) cudaStreamDestroy(pipe[k]);
+        for (int k = 0; k < 4; ++k)
+            if (pipeEv[k]) cudaEventDestroy(pipeEv[k]);
         if (stream) cudaStreamDestroy(stream);
     }
     int alloc(void** out, size_t bytes, const char* what) {
@@ -263,6 +270,11 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
     for (int i = 0; i < d->nforces; ++i) fOf[d->forces[i].body].push_back(i);
     std::vector<std::vector<int>> kids(nb + 1);
     for (int i = 1; i <= nb; ++i) kids[d->bodies[i - 1].parent].push_back(i);
+    // bodies on the way from a loop body to Ground
+    std::vector<char> onLoopPath(nb + 1, 0);
+    for (int i = 0; i < d->nconstraints; ++i)
+        for (int b : {d->constraints[i].body1, d->constraints[i].body2})
+            for (int k = b; k > 0 && !onLoopPath[k]; k = d->bodies[k - 1].parent) onLoopPath[k] = 1;
     int64_t rec = 0;
     for (int r = 0; r < nb; ++r) {
         const int bi = order[r];
@@ -278,6 +290,7 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
             if (rowOf[c] != r + 1) info |= F_MEMCHILD;
         for (int i = 0; i < d->nconstraints; ++i)
             if (d->constraints[i].body1 == bi || d->constraints[i].body2 == bi) info |= F_LOOPBODY;
+        if (onLoopPath[bi]) info |= F_LOOPPATH;
         t->parent.push_back(b.parent == 0 ? -1 : rowOf[b.parent]);
         t->info.push_back(info);
         t->qoff.push_back(qo[bi]);
@@ -494,6 +507,8 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     }
     b->nChain = (int)chainPos.size();
     b->nLoop = (int)loopPos.size();
+    b->orderIdentity = b->nChain == ninst;
+    for (int i = 0; i < b->nChain && b->orderIdentity; ++i) b->orderIdentity = chainPos[i] == i;
     std::copy(chainPos.begin(), chainPos.end(), order.begin());
     std::copy(loopPos.begin(), loopPos.end(), order.begin() + b->nChain);
     std::copy(groupPos.begin(), groupPos.end(), order.begin() + b->nChain + b->nLoop);
@@ -819,6 +834,86 @@ int sbg_realize_acceleration(sbg_batch b, double* ydot, int32_t* status) {
     int rc = sbg_realize_acceleration_async(b);
     if (rc) return rc;
     return sbg_batch_get_ydot(b, ydot, status);
+}
+
+// State::updY + realize(Stage::Acceleration) + getYDot from and to host
+// buffers in one call. For a batch whose instances all run the one-thread
+// driver in instance order, the instances are cut into tile-aligned chunks
+// and each chunk's upload, scatter, realize, gather and download go on one
+// of up to four streams, so the copies of one chunk overlap the compute of
+// the others. Other batches take the plain sequence.
+int sbg_realize_acceleration_host(sbg_batch b, const double* y, double* ydot, int32_t* status) {
+    if (!b || !y || !ydot) return fail(SBG_ERR_INVALID, "null argument");
+    int nchunks = 4;
+    if (const char* v = std::getenv("SBG_PIPE_CHUNKS")) nchunks = std::max(1, std::atoi(v));  // tuning override
+    const bool pipelined = b->orderIdentity && b->nGroupBlocks == 0 && b->nLoop == 0 && b->tuned && nchunks > 1 &&
+                           b->ninst >= nchunks * kTile;
+    if (!pipelined) {
+        if (int rc = sbg_batch_set_state(b, nullptr, y)) return rc;
+        return sbg_realize_acceleration(b, ydot, status);
+    }
+    SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    const size_t bytes = b->nyTotal * sizeof(double);
+    const double* src = y;
+    if (!isPinned(y)) {
+        std::memcpy(b->hostPinned, y, bytes);
+        src = b->hostPinned;
+    }
+    const bool dstPinned = isPinned(ydot);
+    double* dst = dstPinned ? ydot : b->hostPinned;
+    const bool stPinned = status && isPinned(status);
+    const int nstreams = std::min(nchunks, 4);
+    b->pipe[0] = b->stream;
+    for (int k = 0; k < nstreams; ++k) {
+        if (k > 0 && !b->pipe[k]) SBG_CUDA(cudaStreamCreateWithFlags(&b->pipe[k], cudaStreamNonBlocking), "streams");
+        if (!b->pipeEv[k]) SBG_CUDA(cudaEventCreateWithFlags(&b->pipeEv[k], cudaEventDisableTiming), "events");
+    }
+    // every stream starts after the work already queued on the batch stream
+    SBG_CUDA(cudaEventRecord(b->pipeEv[0], b->stream), "pipeline");
+    for (int k = 1; k < nstreams; ++k) SBG_CUDA(cudaStreamWaitEvent(b->pipe[k], b->pipeEv[0], 0), "pipeline");
+    SBG_CUDA(cudaMemsetAsync(b->time, 0, std::max(b->ninst, 1) * sizeof(double), b->stream), "time reset");
+    const int tiles = (b->ninst + kTile - 1) / kTile;
+    KArgs a{};
+    a.T = &b->T;
+    a.y = b->y;
+    a.ydot = b->ydot;
+    a.scratch = b->scratch;
+    a.status = b->status;
+    for (int c = 0; c < nchunks; ++c) {
+        const int i0 = std::min(b->ninst, (int)((int64_t)tiles * c / nchunks) * kTile);
+        const int i1 = std::min(b->ninst, (int)((int64_t)tiles * (c + 1) / nchunks) * kTile);
+        if (i1 <= i0) continue;
+        cudaStream_t st = b->pipe[c % nstreams];
+        const int64_t o0 = b->hostYOff[i0], o1 = b->hostYOff[i1];
+        SBG_CUDA(cudaMemcpyAsync(b->staging + o0, src + o0, (o1 - o0) * sizeof(double), cudaMemcpyHostToDevice, st),
+                 "state upload");
+        SBG_CUDA(launchScatter(b->T, b->dHostYOff, b->staging, b->y, 0, st, i0, i1 - i0), "state scatter");
+        LaunchPlan P = b->plan();
+        P.chainFirst = i0;
+        P.nChain = i1 - i0;
+        a.P = &P;
+        if (b->precision == SBG_PRECISION_FP64) realize64Chain(a, st);
+        else realize32Chain(a, b->precision == SBG_PRECISION_MIXED, st);
+        SBG_CUDA(cudaGetLastError(), "realize launch");
+        SBG_CUDA(launchGather(b->T, b->dHostYOff, b->ydot, b->staging, 0, st, i0, i1 - i0), "derivative gather");
+        SBG_CUDA(cudaMemcpyAsync(dst + o0, b->staging + o0, (o1 - o0) * sizeof(double), cudaMemcpyDeviceToHost, st),
+                 "derivative download");
+        if (stPinned)
+            SBG_CUDA(cudaMemcpyAsync(status + i0, b->status + i0, (i1 - i0) * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                     st), "status download");
+        b->launches += 3;
+    }
+    for (int k = 1; k < nstreams; ++k) {
+        SBG_CUDA(cudaEventRecord(b->pipeEv[k], b->pipe[k]), "pipeline");
+        SBG_CUDA(cudaStreamWaitEvent(b->stream, b->pipeEv[k], 0), "pipeline");
+    }
+    if (status && !stPinned)
+        SBG_CUDA(cudaMemcpyAsync(status, b->status, b->ninst * sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream),
+                 "status download");
+    SBG_CUDA(cudaStreamSynchronize(b->stream), "pipelined realize");
+    if (!dstPinned) std::memcpy(ydot, b->hostPinned, bytes);
+    b->stateSet = true;
+    return SBG_OK;
 }
 
 int sbg_multiply_by_minv(sbg_batch b, const double* f, double* outp) {

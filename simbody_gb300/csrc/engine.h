@@ -55,6 +55,8 @@ enum : int {
     F_CARRY = 1 << 12,     // the parent is the previous row: values travel in registers
     F_MEMCHILD = 1 << 13,  // some child is not the next row: it reads/accumulates through the record
     F_LOOPBODY = 1 << 14,  // body 1 or 2 of a Ball loop closure: keeps a slot record
+    F_LOOPPATH = 1 << 15,  // a loop body or an ancestor of one: the only rows a unit
+                           // constraint force reaches on its way to the base
 };
 
 // Loop closures (Constraint::Ball), FP64 chain driver only. Each body named
@@ -133,6 +135,7 @@ struct LaunchPlan {
     int nm;
     int variant;  // 1: registers as needed; 4: at most 128 registers (FP32 only)
     int nLoop;    // order positions [nChain, nChain + nLoop): instances with loop closures (FP64 chain driver)
+    int chainFirst;  // first order position of the chain segment launch (a sub-range of it: pipelined realize)
 };
 
 }  // namespace sbg

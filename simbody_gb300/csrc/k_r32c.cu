@@ -12,9 +12,9 @@ template <bool REF, int MINB, int BS> static void go(const KArgs& a, cudaStream_
     const int nb = (a.P->nChain + BS - 1) / BS;
     float* sc = static_cast<float*>(a.scratch);
     if (a.P->nm == 1)
-        realizeKernel<float, 1, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.ydot, sc, a.status);
+        realizeKernel<float, 1, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
     else
-        realizeKernel<float, 3, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.ydot, sc, a.status);
+        realizeKernel<float, 3, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
 }
 
 template <bool REF> static void pick(const KArgs& a, cudaStream_t s) {

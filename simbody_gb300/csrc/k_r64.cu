@@ -8,8 +8,8 @@ static inline int chainBlocks(const LaunchPlan& P) { return (P.nChain + 127) / 1
 void realize64Chain(const KArgs& a, cudaStream_t s) {
     const int nb = chainBlocks(*a.P);
     double* sc = static_cast<double*>(a.scratch);
-    if (a.P->nm == 1) realizeKernel<double, 1, false, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.ydot, sc, a.status);
-    else realizeKernel<double, 3, false, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.ydot, sc, a.status);
+    if (a.P->nm == 1) realizeKernel<double, 1, false, false><<<nb, 128, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
+    else realizeKernel<double, 3, false, false><<<nb, 128, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
 }
 void realize64Group(const KArgs& a, cudaStream_t s) {
     realizeKernel<double, 3, false, true><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, 0, 0, a.y, a.ydot,

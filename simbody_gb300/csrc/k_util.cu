@@ -23,8 +23,8 @@ __global__ void normalizeQuatKernel(DevTables T, double* __restrict__ y) {
 // Pack/unpack between the host's per-instance packing and the columns.
 // part 0: all of [q,u]; part 1: the u slots only (nu values per instance).
 __global__ void scatterKernel(DevTables T, const int64_t* __restrict__ hostOff, const double* __restrict__ packed,
-                              double* __restrict__ cols, int part) {
-    const int inst = blockIdx.x;
+                              double* __restrict__ cols, int part, int inst0) {
+    const int inst = inst0 + blockIdx.x;
     const int nq = T.inq[inst];
     const int cnt = part == 0 ? nq + T.inu[inst] : T.inu[inst];
     const int c0 = part == 0 ? 0 : nq;
@@ -32,8 +32,8 @@ __global__ void scatterKernel(DevTables T, const int64_t* __restrict__ hostOff, 
     for (int k = threadIdx.x; k < cnt; k += blockDim.x) cols[base + (int64_t)(c0 + k) * stride] = packed[off + k];
 }
 __global__ void gatherKernel(DevTables T, const int64_t* __restrict__ hostOff, const double* __restrict__ cols,
-                             double* __restrict__ packed, int part) {
-    const int inst = blockIdx.x;
+                             double* __restrict__ packed, int part, int inst0) {
+    const int inst = inst0 + blockIdx.x;
     const int nq = T.inq[inst];
     const int cnt = part == 0 ? nq + T.inu[inst] : T.inu[inst];
     const int c0 = part == 0 ? 0 : nq;
@@ -123,16 +123,18 @@ cudaError_t launchNormalizeQuat(const DevTables& T, double* y, cudaStream_t s) {
 }
 
 cudaError_t launchScatter(const DevTables& T, const int64_t* hostOff, const double* packed, double* cols, int part,
-                          cudaStream_t s) {
-    if (T.ninst == 0) return cudaSuccess;
-    scatterKernel<<<T.ninst, 128, 0, s>>>(T, hostOff, packed, cols, part);
+                          cudaStream_t s, int inst0, int count) {
+    if (count < 0) count = T.ninst - inst0;
+    if (count <= 0) return cudaSuccess;
+    scatterKernel<<<count, 128, 0, s>>>(T, hostOff, packed, cols, part, inst0);
     return cudaGetLastError();
 }
 
 cudaError_t launchGather(const DevTables& T, const int64_t* hostOff, const double* cols, double* packed, int part,
-                         cudaStream_t s) {
-    if (T.ninst == 0) return cudaSuccess;
-    gatherKernel<<<T.ninst, 128, 0, s>>>(T, hostOff, cols, packed, part);
+                         cudaStream_t s, int inst0, int count) {
+    if (count < 0) count = T.ninst - inst0;
+    if (count <= 0) return cudaSuccess;
+    gatherKernel<<<count, 128, 0, s>>>(T, hostOff, cols, packed, part, inst0);
     return cudaGetLastError();
 }
 

@@ -33,11 +33,12 @@ cudaError_t launchRKMerson(const DevTables& T, const LaunchPlan& P, int precisio
                            const BatchBufs& B, int32_t* status, double h, int nsteps, double accuracy,
                            double consTol, int projectEveryStep, const Streams& s);
 cudaError_t launchNormalizeQuat(const DevTables& T, double* y, cudaStream_t s);
-// part 0 moves whole [q,u] records, part 1 only the u slots.
+// part 0 moves whole [q,u] records, part 1 only the u slots; instances
+// [inst0, inst0 + count) (count < 0: to the end).
 cudaError_t launchScatter(const DevTables& T, const int64_t* hostOff, const double* packed, double* cols, int part,
-                          cudaStream_t s);
+                          cudaStream_t s, int inst0 = 0, int count = -1);
 cudaError_t launchGather(const DevTables& T, const int64_t* hostOff, const double* cols, double* packed, int part,
-                         cudaStream_t s);
+                         cudaStream_t s, int inst0 = 0, int count = -1);
 
 // Per-segment launchers (k_r64.cu, k_r32c.cu, k_r32g.cu, k_rk64.cu,
 // k_rk32c.cu, k_rk32g.cu).

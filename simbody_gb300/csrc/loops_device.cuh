@@ -29,6 +29,15 @@
 //             one factorization, at most 7 iterations.
 // With localOnly a growing norm stops the iteration and undoes the last
 // step; a result worse than the entry state is restored.
+//
+// Unit constraint forces act on the loop bodies only, so the inward half of
+// every sweep is zero away from the loop bodies' paths to Ground (rows with
+// F_LOOPPATH), and the slot values the Gram columns, perr and verr need lie
+// on those paths: the sweeps, the kinematics of the projections and the
+// accumulator clears visit path rows only. The one sweep whose outward half
+// reaches every body (the constraint-force correction of udot) takes zero
+// eps off the path. Skipped rows would have contributed exact zeros, so the
+// results are the same as full sweeps.
 
 using SC64 = ScrStrided<double>;
 using V3d = V3<double>;
@@ -69,6 +78,7 @@ __device__ __noinline__ void loopKinematics(const LoopState& L) {
     for (int lb = 0; lb < nb; ++lb) {
         const int row = body0 + lb;
         const int info = T.info[row];
+        if (!(info & F_LOOPPATH)) continue;  // a path row's parent is a path row
         const int parent = T.parent[row];
         const int rec = T.srec[row];
         const Kin<double> P = parent < 0 ? groundKin<double>()
@@ -190,8 +200,8 @@ __device__ __forceinline__ void loopIn(const LoopState& L, int row, int rec, int
 //               (RigidBodyNodeSpec.cpp:517-552)
 //   kJacSweep:  du = the stored (weighted) values, V = V+ + H du
 template <int N, int KIND>
-__device__ __forceinline__ void loopOut(const LoopState& L, int rec, int n, bool hasParent, V3d& Aw, V3d& Av,
-                                        double* ud) {
+__device__ __forceinline__ void loopOut(const LoopState& L, int rec, int n, bool hasParent, bool onPath, V3d& Aw,
+                                        V3d& Av, double* ud) {
     const SC64& S = L.S;
     const int eDI = kRecH + 7 * N, eG = eDI + N * N, eEps = eG + 6 * N;
     const V3d l = ld3<double>(S, rec, kRecL);
@@ -199,7 +209,7 @@ __device__ __forceinline__ void loopOut(const LoopState& L, int rec, int n, bool
     const V3d Apv = hasParent ? Av + cross(Aw, l) : z3<double>();
     double eps[N];
 #pragma unroll
-    for (int j = 0; j < N; ++j) eps[j] = j < n ? S(rec, eEps + j) : 0.0;
+    for (int j = 0; j < N; ++j) eps[j] = j < n && onPath ? S(rec, eEps + j) : 0.0;
     Aw = Apw;
     Av = Apv;
 #pragma unroll
@@ -227,8 +237,9 @@ __device__ __noinline__ void loopIn6(const LoopState& L, int row, int rec, int i
     loopIn<6, KIND>(L, row, rec, 6, info, zw, zv);
 }
 template <int KIND>
-__device__ __noinline__ void loopOut6(const LoopState& L, int rec, bool hasParent, V3d& Aw, V3d& Av, double* ud) {
-    loopOut<6, KIND>(L, rec, 6, hasParent, Aw, Av, ud);
+__device__ __noinline__ void loopOut6(const LoopState& L, int rec, bool hasParent, bool onPath, V3d& Aw, V3d& Av,
+                                      double* ud) {
+    loopOut<6, KIND>(L, rec, 6, hasParent, onPath, Aw, Av, ud);
 }
 
 // Children's sums of the inward sweeps live in the z accumulator of the
@@ -240,7 +251,7 @@ __device__ __forceinline__ void loopZeroAcc(const LoopState& L) {
     const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
     for (int lb = 0; lb < nb; ++lb) {
         const int row = body0 + lb;
-        if (T.info[row] & F_MEMCHILD) {
+        if ((T.info[row] & (F_MEMCHILD | F_LOOPPATH)) == (F_MEMCHILD | F_LOOPPATH)) {
             st3<double>(L.S, T.srec[row], kRecZacc, z3<double>());
             st3<double>(L.S, T.srec[row], kRecZacc + 3, z3<double>());
         }
@@ -249,9 +260,10 @@ __device__ __forceinline__ void loopZeroAcc(const LoopState& L) {
 
 // One inward and one outward sweep over the instance driven by the applied
 // forces in the slot records. The outward result of each constrained body
-// goes to its slot (kSlotB); onBody(row, n, ud) sees every body's mobility
-// values. kJacSweep multiplies g by wt(row, j) between the halves.
-template <int NM, int KIND, class Wt, class OnBody>
+// goes to its slot (kSlotB); onBody(row, n, ud) sees the mobility values of
+// every path row (of every row with FULL_OUT). kJacSweep multiplies g by
+// wt(row, j) between the halves.
+template <int NM, int KIND, bool FULL_OUT = false, class Wt, class OnBody>
 __device__ __forceinline__ void loopSweep(const LoopState& L, const Wt& wt, const OnBody& onBody) {
     const DevTables& T = L.T;
     const SC64& S = L.S;
@@ -262,6 +274,10 @@ __device__ __forceinline__ void loopSweep(const LoopState& L, const Wt& wt, cons
         for (int lb = nb - 1; lb >= 0; --lb) {
             const int row = body0 + lb;
             const int info = T.info[row];
+            if (!(info & F_LOOPPATH)) {  // contributes zero
+                have = false;
+                continue;
+            }
             const int n = (info >> 4) & 15;
             const int rec = T.srec[row];
             V3d zw = z3<double>(), zv = z3<double>();
@@ -295,6 +311,8 @@ __device__ __forceinline__ void loopSweep(const LoopState& L, const Wt& wt, cons
         for (int lb = 0; lb < nb; ++lb) {
             const int row = body0 + lb;
             const int info = T.info[row];
+            const bool onPath = (info & F_LOOPPATH) != 0;
+            if (!FULL_OUT && !onPath) continue;  // a path row's parent is a path row
             const int n = (info >> 4) & 15;
             const int rec = T.srec[row];
             const int parent = T.parent[row];
@@ -306,8 +324,8 @@ __device__ __forceinline__ void loopSweep(const LoopState& L, const Wt& wt, cons
                 pv = ld3<double>(S, pr, 3);
             }
             double ud[6];
-            if (n == 6) loopOut6<KIND>(L, rec, hp, pw, pv, ud);
-            else loopOut<NM, KIND>(L, rec, n, hp, pw, pv, ud);
+            if (n == 6) loopOut6<KIND>(L, rec, hp, onPath, pw, pv, ud);
+            else loopOut<NM, KIND>(L, rec, n, hp, onPath, pw, pv, ud);
             onBody(row, n, ud);
             if (info & F_LOOPBODY) {
                 st3<double>(S, T.lrec[row], kSlotB, pw);
@@ -396,7 +414,7 @@ __device__ __noinline__ int loopForwardDynamics(const DevTables& T, int inst, co
     loopCholSolve(m, A, lam);
     loopClearForces(L);
     for (int c = 0; c < nc; ++c) loopAddConstraintForce(L, loopGeom(L, c), mk3(lam[3 * c], lam[3 * c + 1], lam[3 * c + 2]));
-    loopSweep<NM, kMInvSweep>(L, one, [&](int row, int n, const double* ud) {
+    loopSweep<NM, kMInvSweep, true>(L, one, [&](int row, int n, const double* ud) {
         const int uo = T.uoff[row];
         for (int i = 0; i < n; ++i) out.udot(uo + i, out.udotGet(uo + i) - ud[i]);
     });
@@ -456,7 +474,10 @@ __device__ __noinline__ bool loopProjectQ(const LoopState& L, double tol, bool l
     const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
     double perr[kMaxLoopEq], A[kMaxLoopEq * kMaxLoopEq];
     const double normOnEntry = loopPerr(L, perr);
-    for (int k = 0; k < nq; ++k) saveAt(L, k) = yAt(L, k);
+    for (int k = 0; k < nq; ++k) {
+        saveAt(L, k) = yAt(L, k);
+        deltaAt(L, k) = 0.0;  // rows off the loop paths never move
+    }
     const double tryFor = loopTryFor(tol);
     double achieved = normOnEntry, prev = normOnEntry;
     int its = 0;
@@ -532,7 +553,10 @@ __device__ __noinline__ bool loopProjectU(const LoopState& L, double tol, bool f
     const double normOnEntry = loopVerr(L, verr);
     if (normOnEntry > limit) return false;
     if (normOnEntry == 0 || (normOnEntry <= tol && !force)) return true;
-    for (int k = 0; k < nu; ++k) saveAt(L, nq + k) = yAt(L, nq + k);
+    for (int k = 0; k < nu; ++k) {
+        saveAt(L, nq + k) = yAt(L, nq + k);
+        deltaAt(L, nq + k) = 0.0;  // rows off the loop paths never move
+    }
     // E^2 with E = max(|u|, 1) frozen at entry
     auto wu = [&](int row, int j) -> double {
         const double a = fabs(saveAt(L, nq + T.uoff[row] + j));

@@ -88,6 +88,29 @@ int groupLanes(const sbg_topology_s& t) {
     return std::max(2, std::min(32, w >> kLanesShift));
 }
 
+// Relative GPU time of one RK-Merson step of a request, in serial body
+// visits per RHS on its driver:
+//   level-parallel driver  sum over levels of ceil(width / lanes)
+//   loop-closure driver    every body for the tree passes plus the loop-path
+//                          rows for each of the 3m+1 constraint sweeps, with
+//                          the FP64 one-thread driver's slowdown
+// A request's steps per tick are the server's chunk scaled by
+// kRefCost / cost, so that every request's chunk takes about the same time
+// and no request waits on a slower neighbour.
+constexpr double kRefCost = 8.0;          // the median request of the uneven-tree distribution
+constexpr double kLoopDriverWeight = 4.0;  // one FP64 thread per request vs. lanes in FP32
+double stepCost(const sbg_topology_s& t, bool loops, int G) {
+    if (!loops) {
+        double slots = 0;
+        for (int L = 0; L < t.nlevels; ++L) slots += (t.levStart[L + 1] - t.levStart[L] + G - 1) / G;
+        return slots;
+    }
+    int path = 0;
+    for (int r = 0; r < t.nb; ++r) path += (t.info[r] & F_LOOPPATH) != 0;
+    const int m = 3 * t.ncons;
+    return kLoopDriverWeight * (t.nb + (double)path * (3 * m + 1) / 3.0);
+}
+
 // Units of the pools per body row of a typical request (a tree of
 // 4..256 bodies with a Free root, Pin/Slider/Universal/Ball children, a
 // spring and a damper per mobility, 20% with loop closures): how the
@@ -166,7 +189,10 @@ struct sbg_server_s {
     char* hostUp[2] = {nullptr, nullptr};
     char* hostRes[2] = {nullptr, nullptr};
     cudaStream_t stream = nullptr, side = nullptr;
-    cudaEvent_t evFork = nullptr, evJoin = nullptr, evTick[2] = {nullptr, nullptr};
+    cudaEvent_t evFork = nullptr, evJoin = nullptr, evTick[2] = {nullptr, nullptr}, evBegin[2] = {nullptr, nullptr};
+    double gpuSeconds = 0;   // GPU time of the completed ticks
+    double hostSeconds = 0;  // time inside sbg_server_tick ...
+    double waitSeconds = 0;  // ... of which waiting for a tick in flight
     std::deque<TickRec> inflight;
     int64_t tick = 0;
     int64_t launches = 0;
@@ -188,6 +214,7 @@ struct sbg_server_s {
             if (hostUp[k]) cudaFreeHost(hostUp[k]);
             if (hostRes[k]) cudaFreeHost(hostRes[k]);
             if (evTick[k]) cudaEventDestroy(evTick[k]);
+            if (evBegin[k]) cudaEventDestroy(evBegin[k]);
         }
         if (evFork) cudaEventDestroy(evFork);
         if (evJoin) cudaEventDestroy(evJoin);
@@ -405,12 +432,19 @@ void harvest(sbg_server_s* s, const TickRec& tr) {
 int drainInflight(sbg_server_s* s, bool block, int32_t* ncompleted) {
     while (!s->inflight.empty()) {
         const TickRec& tr = s->inflight.front();
+        const auto w0 = std::chrono::steady_clock::now();
         cudaError_t e = block ? cudaEventSynchronize(s->evTick[tr.parity]) : cudaEventQuery(s->evTick[tr.parity]);
+        if (block) s->waitSeconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count();
         if (e == cudaErrorNotReady) {
             cudaGetLastError();
             return SBG_OK;
         }
         if (e != cudaSuccess) return cudaErr(e, "serving tick");
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, s->evBegin[tr.parity], s->evTick[tr.parity]) == cudaSuccess)
+            s->gpuSeconds += 1e-3 * ms;
+        else
+            cudaGetLastError();
         const int64_t before = s->completed;
         harvest(s, tr);
         if (ncompleted) *ncompleted += (int32_t)(s->completed - before);
@@ -513,7 +547,8 @@ int sbg_server_create(const sbg_server_config* cfg, sbg_server* out) {
     for (int k = 0; k < 2; ++k) {
         cudaError_t e = cudaMallocHost(&s->hostUp[k], (size_t)s->upCap);
         if (e == cudaSuccess) e = cudaMallocHost(&s->hostRes[k], (size_t)s->resCap);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->evTick[k], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreate(&s->evTick[k]);
+        if (e == cudaSuccess) e = cudaEventCreate(&s->evBegin[k]);
         if (e != cudaSuccess) return bail(cudaErr(e, "pinned staging"));
     }
     {
@@ -605,16 +640,27 @@ int sbg_server_submit(sbg_server s, sbg_topology topo, const double* y0, double 
         return setError(SBG_ERR_BUDGET, "request's state exceeds the server's result staging");
     r.id = s->nextId++;
     r.submitS = s->clock();
-    r.sched = s->sched.submit(r.id, fp, nsteps);
+    const double cost = stepCost(*topo, r.loops, r.G);
+    const int32_t chunk = (int32_t)std::max(1.0, std::min(16.0 * s->chunk, std::floor(s->chunk * kRefCost / cost)));
+    r.sched = s->sched.submit(r.id, fp, nsteps, chunk);
     s->byId[r.id] = r.sched;
     s->reqs.push_back(std::move(r));
     *id = s->reqs.back().id;
     return SBG_OK;
 }
 
+static int serverTick(sbg_server s, int32_t* ncompleted);
+
 int sbg_server_tick(sbg_server s, int32_t* ncompleted) {
     if (!s) return setError(SBG_ERR_INVALID, "null server");
     std::lock_guard<std::mutex> lock(s->mu);
+    const auto h0 = std::chrono::steady_clock::now();
+    const int rc = serverTick(s, ncompleted);
+    s->hostSeconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - h0).count();
+    return rc;
+}
+
+static int serverTick(sbg_server s, int32_t* ncompleted) {
     if (ncompleted) *ncompleted = 0;
     SBG_SCUDA(cudaSetDevice(s->device), "cudaSetDevice");
     // 1. results of finished ticks; keep at most one tick in flight while
@@ -703,6 +749,7 @@ int sbg_server_tick(sbg_server s, int32_t* ncompleted) {
     std::memcpy(st.host + postOff, st.post.data(), st.post.size() * sizeof(CopyDesc));
     // 5. enqueue the tick
     cudaStream_t m = s->stream;
+    SBG_SCUDA(cudaEventRecord(s->evBegin[parity], m), "tick event");
     SBG_SCUDA(cudaMemcpyAsync(s->devUp, st.host, (size_t)upBytes, cudaMemcpyHostToDevice, m), "tick upload");
     SBG_SCUDA(launchCopies(reinterpret_cast<const CopyDesc*>(s->devUp + preOff), (int)st.pre.size(), m), "tick scatter");
     ++s->launches;
@@ -815,6 +862,8 @@ int sbg_server_get_stats(sbg_server s, sbg_server_stats* out) {
     out->device_bytes = s->devBytes;
     out->max_slots = s->maxSlots;
     out->chunk_steps = s->chunk;
+    out->gpu_seconds = s->gpuSeconds;
+    out->host_seconds = s->hostSeconds - s->waitSeconds;
     for (int k = 0; k < kNumPools; ++k) {
         out->pool_capacity[k] = s->sched.pool(k).capacity();
         out->pool_in_use[k] = s->sched.pool(k).used();

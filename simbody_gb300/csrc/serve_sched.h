@@ -5,10 +5,13 @@
 // admission policy can be checked without a GPU.
 //
 // Continuous batching: every tick, each resident request advances by
-// min(chunk, remaining) fixed RK-Merson steps in the same launch as every
+// min(its chunk, remaining) fixed RK-Merson steps in the same launch as every
 // other resident request; a request whose last step falls in a tick retires
 // after it and its memory and slot go back to the pools, where the next
-// queued request (strict arrival order, no overtaking) can take them.
+// queued request (strict arrival order, no overtaking) can take them. A
+// request's chunk is the scheduler's default, or its own (the serving
+// runtime sizes it so that every request's chunk takes about the same time
+// on the GPU, so no request waits on a slower neighbour).
 #pragma once
 #include <cstdint>
 #include <deque>
@@ -86,6 +89,7 @@ struct SchedRequest {
     int64_t id = 0;
     Footprint fp;
     int32_t horizon = 0;     // steps requested
+    int32_t chunk = 0;       // steps per tick (0 = the scheduler's default)
     // set by the scheduler
     int32_t slot = -1;
     int64_t off[kNumPools] = {0, 0, 0, 0, 0};
@@ -121,11 +125,12 @@ public:
         return maxSlots_ > 0;
     }
     // Queue a request; returns its index in the request table.
-    int32_t submit(int64_t id, const Footprint& fp, int32_t horizon) {
+    int32_t submit(int64_t id, const Footprint& fp, int32_t horizon, int32_t chunk = 0) {
         SchedRequest r;
         r.id = id;
         r.fp = fp;
         r.horizon = horizon;
+        r.chunk = chunk;
         r.remaining = horizon;
         reqs_.push_back(r);
         queue_.push_back((int32_t)reqs_.size() - 1);
@@ -175,7 +180,8 @@ public:
         std::vector<int32_t> keep;
         for (int32_t i : active_) {
             SchedRequest& r = reqs_[i];
-            int32_t steps = r.remaining < chunk_ ? r.remaining : chunk_;
+            const int32_t c = r.chunk > 0 ? r.chunk : chunk_;
+            int32_t steps = r.remaining < c ? r.remaining : c;
             bool last = steps == r.remaining;
             if (last && finish && !finish(i)) {
                 if (steps <= 1) {  // nothing to run short of the last step: wait a tick

@@ -112,6 +112,21 @@ class Batch:
         N.check(N.engine_lib().sbg_realize_acceleration(self._h, _dptr(ydot), _iptr(status)))
         return ydot, status
 
+    def realize_acceleration_from(self, y: np.ndarray, ydot: np.ndarray | None = None,
+                                  status: np.ndarray | None = None):
+        """set_state(y) + realize_acceleration() in one call, with the copies
+        pipelined against the compute where the batch allows it."""
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        assert y.size == self.ny_total
+        if ydot is None:
+            ydot = np.empty(self.ny_total)
+        if status is None:
+            status = np.empty(self.ninst, dtype=np.int32)
+        assert ydot.dtype == np.float64 and ydot.size == self.ny_total and ydot.flags.c_contiguous
+        assert status.dtype == np.int32 and status.size == self.ninst and status.flags.c_contiguous
+        N.check(N.engine_lib().sbg_realize_acceleration_host(self._h, _dptr(y), _dptr(ydot), _iptr(status)))
+        return ydot, status
+
     def multiply_by_minv(self, f: np.ndarray) -> np.ndarray:
         f = np.ascontiguousarray(f, dtype=np.float64)
         assert f.size == self.u_offsets[-1]

@@ -113,3 +113,26 @@ def test_multiply_by_minv_fp64(engine):
     ref = O.multiply_by_minv(w.systems, w.nsys, w.instance_system[:64], b.y_offsets, y0, b.u_offsets, f)
     err = rel_err_per_instance(out, ref, b.u_offsets)
     assert err.max() <= 1e-12, err.max()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_pipelined_host_realize_equals_separate_calls(engine, precision):
+    """sbg_realize_acceleration_host (chunked upload / realize / download on
+    several streams) gives the bits of set_state + realize_acceleration, with
+    pageable and with page-locked host buffers."""
+    import torch
+
+    w = Workload(2, 4096)
+    b, y0 = engine_batch(w, precision)
+    b.set_state(y0)
+    ref, st0 = b.realize_acceleration()  # also tunes the batch
+    y1 = y0 * (1 + 1e-3 * np.random.default_rng(5).standard_normal(y0.size))
+    b.set_state(y1)
+    ref1, _ = b.realize_acceleration()
+    got, st = b.realize_acceleration_from(y0)
+    assert (st == 0).all() and np.array_equal(got, ref)
+    yp = torch.from_numpy(y1).pin_memory().numpy()
+    dp = torch.empty(b.ny_total, dtype=torch.float64).pin_memory().numpy()
+    sp = torch.empty(b.ninst, dtype=torch.int32).pin_memory().numpy()
+    got1, st1 = b.realize_acceleration_from(yp, dp, sp)
+    assert (st1 == 0).all() and np.array_equal(got1, ref1)
