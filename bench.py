@@ -34,6 +34,12 @@ sys.path.insert(0, str(ROOT))
 
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
+# DRAM bytes (read + write) of one launch of the mixed realize kernel on the
+# 65,536-instance 32-Ball workload, from an ncu capture of that launch
+# (profiles/realize_32ball_65536_ncu.md): the per-body scratch records
+# dominate it, against 235 MB of compulsory state I/O.
+TRAFFIC_BYTES_PER_LAUNCH = 1.807478e9 + 0.905554e9
+FP32_LANES = 152 * 128  # SMs x FP32 lanes per SM
 
 
 def _args():
@@ -60,6 +66,27 @@ def _dist():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     return rank, world
+
+
+def barrier() -> None:
+    """All replicas line up (multi-GPU runs: one process per GPU)."""
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.barrier()
+
+
+def max_over_ranks(x: float, device: str = "cuda") -> float:
+    """The slowest replica's value: a timed region ends when every rank is done.
+    Replicas run disjoint instances and exchange nothing else."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1):
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 # ------------------------------------------------------------------ clocks
@@ -154,6 +181,7 @@ def time_resident(b, steps: int, warmup: int):
         b.realize_acceleration_async()
     b.sync()
     torch.cuda.synchronize()
+    barrier()
     n0 = b.launch_count
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     start.record(stream)
@@ -162,6 +190,7 @@ def time_resident(b, steps: int, warmup: int):
     end.record(stream)
     end.synchronize()
     torch.cuda.synchronize()
+    barrier()
     return start.elapsed_time(end) / steps, b.launch_count - n0
 
 
@@ -370,12 +399,7 @@ def run_ours(args):
     bft.close()
     ms_e2e, e2e_launches, _ = time_e2e(bmx, y0, max(3, args.steps // 2), 1)
 
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([ms_mx], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_mx = float(t.item())
+    ms_mx = max_over_ranks(ms_mx)
     value = nb_total * world / (ms_mx * 1e-3)
     value64 = nb_total / (ms_64 * 1e-3)
     ny_total = b64.ny_total
@@ -410,10 +434,19 @@ def run_ours(args):
         "e2e": {"value": nb_total / (ms_e2e * 1e-3), "unit": "body-steps/s", "ms_per_step": ms_e2e,
                 "h2d_bytes_per_step": ny_total * 8, "d2h_bytes_per_step": ny_total * 8 + 4 * w.ninst},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind,
-                     "algorithmic_bytes": "16 B per state element: read [q,u] (f64), write [qdot,udot] (f64)"},
+                     "traffic": TRAFFIC_BYTES_PER_LAUNCH if w.ninst == 65536 else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this "
+                                       "kernel on this workload (profiles/realize_32ball_65536_ncu.md)",
+                     "dram_gbs_measured_traffic": (TRAFFIC_BYTES_PER_LAUNCH / (ms_mx * 1e-3) / 1e9
+                                                  if w.ninst == 65536 else None),
+                     "peak_kind": peak_kind,
+                     "algorithmic_bytes": "16 B per state element: read [q,u] (f64), write [qdot,udot] (f64) = "
+                                          f"{alg_bytes} B per launch"},
         "fp_work": {"flops_per_instance_fp64_algorithm": flops_inst,
-                    "achieved_tflops": flops_inst * w.ninst / (ms_mx * 1e-3) / 1e12},
+                    "achieved_tflops": flops_inst * w.ninst / (ms_mx * 1e-3) / 1e12,
+                    "fp32_peak_tflops_at_clock": FP32_LANES * 2 * (clk.summary()["sm_mhz"] or 2070.0) * 1e6 / 1e12,
+                    "note": "the 6x6 spatial recursions are scalar FP32 FMA work (no tensor-core contraction); "
+                            "the fraction of the FP32 peak is achieved / fp32_peak"},
         "gpu_launches": launches,
         "kernel_variant": bmx.kernel_variant,
         "clocks": clk.summary(),

@@ -118,6 +118,7 @@ ENGINE_API = {
     "sbg_server_drain": (C.c_int, [vp]),
     "sbg_server_result": (C.c_int, [vp, C.c_int64, dp, P(RequestInfo)]),
     "sbg_server_get_stats": (C.c_int, [vp, P(ServerStats)]),
+    "sbg_server_get_lane_stats": (C.c_int, [vp, C.c_int32, P(ServerStats)]),
     "sbg_server_clock": (C.c_double, [vp]),
     "sbg_serve_simulate": (C.c_int, [C.c_int32, i64p, ip, i64p, i64p, C.c_int32, C.c_int32, i64p, i64p, i64p]),
     "sbg_realize_acceleration_noalloc": (C.c_int, [vp, C.c_int32, vp, vp, vp, vp]),

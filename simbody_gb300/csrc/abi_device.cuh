@@ -909,11 +909,14 @@ __device__ __forceinline__ int rhsChain(const DevTables& T, int inst, const SC& 
 // lanes) share one instance; the bodies of a level are spread over the lanes;
 // a barrier separates levels; parents pull their children's contributions.
 // Returns SBG_INST_* bits (identical on every lane of the group).
-template <class R, int NM, bool REF, class Src, class Out>
+// LOOPS also writes the slot records of the loop bodies (rows nb + slot of S):
+// kinematics in pass 1, A_GB in pass 3.
+template <class R, int NM, bool REF, bool LOOPS = false, class Src, class Out>
 __device__ __noinline__ int rhsGroup(const DevTables& T, int inst, const ScrRows<R>& S, const Src& src, Out& out,
                                      int gl, int G, unsigned mask) {
     static_assert(!REF || std::is_same<R, float>::value, "refinement is for the FP32 recursion");
     const int body0 = T.ibody[inst];
+    const int nbI = T.inb[inst];
     const int* ls = T.levStart + T.ilev[inst];  // local row where each level starts (nlev + 1 entries)
     const int nlev = T.inlev[inst];
     const V3<R> g = mk3(R(T.grav[3 * inst]), R(T.grav[3 * inst + 1]), R(T.grav[3 * inst + 2]));
@@ -923,7 +926,10 @@ __device__ __noinline__ int rhsGroup(const DevTables& T, int inst, const ScrRows
             const int row = body0 + lb;
             const int parent = T.parent[row];
             const Kin<R> P = parent < 0 ? groundKin<R>() : loadKin<R>(S, parent);
-            storeKin(S, lb, body1<R, NM>(T, row, lb, S, src, out, g, P));
+            const Kin<R> K = body1<R, NM>(T, row, lb, S, src, out, g, P);
+            storeKin(S, lb, K);
+            if constexpr (LOOPS)
+                if (T.info[row] & F_LOOPBODY) storeKin(S, nbI + T.lslot[row], K);
         }
         __syncwarp(mask);
     }
@@ -953,6 +959,11 @@ __device__ __noinline__ int rhsGroup(const DevTables& T, int inst, const ScrRows
             if (n == 6) body3Free<R, REF>(T, row, lb, S, out, Ap, parent >= 0, A);
             else A = body3<R, NM, REF>(T, row, lb, n, S, out, Ap, parent >= 0);
             storeA3(S, lb, A, REF);
+            if constexpr (LOOPS)
+                if (T.info[row] & F_LOOPBODY) {
+                    st3<R>(S, nbI + T.lslot[row], kSlotA, A.w);
+                    st3<R>(S, nbI + T.lslot[row], kSlotA + 3, A.v);
+                }
         }
         __syncwarp(mask);
     }
@@ -1098,11 +1109,31 @@ __device__ __forceinline__ Slot groupSlot(const DevTables& T, int blk0) {
 template <class R, int NM, bool REF, bool GROUP, bool LOOPS = false, class Src, class Out>
 __device__ __forceinline__ int rhs(const DevTables& T, const Slot& s, R* scratch, const Src& src, Out& out) {
     if constexpr (LOOPS) {
-        static_assert(std::is_same<R, double>::value && !GROUP && !REF, "loop closures run the FP64 chain driver");
-        const ScrStrided<double> S{scratch + T.sbase[s.inst], (int)T.sstride[s.inst]};
-        int st = rhsChain<double, NM, false, true>(T, s.inst, S, src, out);
-        if (T.incons[s.inst] > 0) st |= loopForwardDynamics<NM>(T, s.inst, S, out);
-        return st;
+        static_assert(std::is_same<R, double>::value && !REF, "loop closures run in FP64");
+        double* rec0 = scratch + T.sbase[s.inst];
+        if constexpr (GROUP) {
+            // tree passes on the group's lanes; the multiplier solve and the
+            // constraint sweeps (loop paths only) on its first lane
+            const ScrRows<double> S{rec0, loopRows(T, s.inst)};
+            int st = rhsGroup<double, NM, false, true>(T, s.inst, S, src, out, s.gl, s.G, s.mask);
+            if (T.incons[s.inst] > 0) {
+                const LoopState L = loopStateRows(T, s.inst, rec0, nullptr, nullptr, nullptr, 0, 0);
+                int lst = 0;
+                if (s.gl == 0) lst = loopForwardDynamics<NM, true>(L, out);
+                __syncwarp(s.mask);
+                lst = (int)__reduce_or_sync(s.mask, (unsigned)lst);
+                if (!(lst & SBG_INST_CHOLESKY_FAIL)) loopCorrectionOutRows<NM>(L, out, s.gl, s.G, s.mask);
+                st |= lst;
+            }
+            return st;
+        } else {
+            const int sst = (int)T.sstride[s.inst];
+            const ScrStrided<double> S{rec0, sst};
+            int st = rhsChain<double, NM, false, true>(T, s.inst, S, src, out);
+            if (T.incons[s.inst] > 0)
+                st |= loopForwardDynamics<NM>(loopStateChain(T, s.inst, rec0, sst, nullptr, nullptr, nullptr, 0, 0), out);
+            return st;
+        }
     } else if constexpr (GROUP) {
         const ScrRows<R> S{scratch + T.sbase[s.inst], T.inb[s.inst]};
         return rhsGroup<R, NM, REF>(T, s.inst, S, src, out, s.gl, s.G, s.mask);
@@ -1206,13 +1237,31 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
         if (!groupAll<GROUP>(o.finite, s)) st |= SBG_INST_NONFINITE;
         if constexpr (GROUP) __syncwarp(s.mask);  // the next stage reads what other lanes wrote
     };
+    // The loop-closure state of this instance (either driver's layout; only
+    // instantiated with R = double); its projections run on the first lane
+    // of a group. The stage planes fB/fC are free outside a step.
+    auto loopState = [&]() {
+        double* rec0 = reinterpret_cast<double*>(scratch) + T.sbase[inst];
+        double* sv = reinterpret_cast<double*>(fB);
+        double* dl = reinterpret_cast<double*>(fC);
+        if constexpr (GROUP) return loopStateRows(T, inst, rec0, y, sv, dl, base, stride);
+        else return loopStateChain(T, inst, rec0, (int)T.sstride[inst], y, sv, dl, base, stride);
+    };
     // Integrator::initialize with loop closures: forced position and
-    // velocity projection (IntegratorRep.h:856-895); the buffers fB/fC are
-    // free outside a step.
+    // velocity projection (IntegratorRep.h:856-895).
+    auto loopLeaderOr = [&](int bits) {
+        if constexpr (GROUP) {
+            __syncwarp(s.mask);
+            return (int)__reduce_or_sync(s.mask, (unsigned)bits);
+        } else {
+            return bits;
+        }
+    };
     if constexpr (LOOPS)
         if (init && T.incons[inst] > 0) {
-            const LoopState L{T, inst, ScrStrided<double>{scratch + T.sbase[inst], (int)T.sstride[inst]}, y, fB, fC, base, stride};
-            st |= loopInitialize<NM>(L, consTol);
+            int lst = 0;
+            if (s.gl == 0) lst = loopInitialize<NM>(loopState(), consTol);
+            st |= loopLeaderOr(lst);
         }
     for (int step = 0; step < nst; ++step) {
         const double t1 = tc + h;
@@ -1296,9 +1345,10 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
             if (T.incons[inst] > 0) {
                 loopsDone = true;
                 if (errNorm <= 16 * accuracy) {
-                    const LoopState L{T, inst, ScrStrided<double>{scratch + T.sbase[inst], (int)T.sstride[inst]}, y, fB, fC, base, stride};
                     const double quatNorm = nquat > 0 ? sqrt(squat / nquat) : 0.0;
-                    st |= loopProjectStep<NM>(L, quatNorm, consTol, projLimit, pes);
+                    int lst = 0;
+                    if (s.gl == 0) lst = loopProjectStep<NM>(loopState(), quatNorm, consTol, projLimit, pes);
+                    st |= loopLeaderOr(lst);
                 }
             }
         if (!loopsDone && errNorm <= 16 * accuracy && nquat > 0) {

@@ -513,12 +513,15 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     std::copy(loopPos.begin(), loopPos.end(), order.begin() + b->nChain);
     std::copy(groupPos.begin(), groupPos.end(), order.begin() + b->nChain + b->nLoop);
     // slot records of the loop-closure topologies follow their body records
-    std::vector<int32_t> lrec(parent.size(), -1);
+    std::vector<int32_t> lrec(parent.size(), -1), lslot(parent.size(), -1);
     for (int k = 0; k < ntopo; ++k) {
         if (used[k] < 0) continue;
         const sbg_topology_s* t = topos[k];
         for (int r = 0; r < t->nb; ++r)
-            if (t->lslot[r] >= 0) lrec[rowBase[k] + r] = (int32_t)(recTotal[k] + (int64_t)t->lslot[r] * kSlotSize);
+            if (t->lslot[r] >= 0) {
+                lrec[rowBase[k] + r] = (int32_t)(recTotal[k] + (int64_t)t->lslot[r] * kSlotSize);
+                lslot[rowBase[k] + r] = t->lslot[r];
+            }
     }
     int64_t yOff = 0, sOff = 0, sOffLoop = 0;
     // tiles of 32 chain-driver instances (the chain segment, then the
@@ -614,6 +617,7 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     if ((rc = b->upload(&T.ccnt, ccnt, "children table"))) return bail(rc);
     if ((rc = b->upload(&T.clist, clist, "children table"))) return bail(rc);
     if ((rc = b->upload(&T.lrec, lrec, "loop table"))) return bail(rc);
+    if ((rc = b->upload(&T.lslot, lslot, "loop table"))) return bail(rc);
     if ((rc = b->upload(&T.lcons, lcons, "loop table"))) return bail(rc);
     if ((rc = b->upload(&T.lst, lst, "loop table"))) return bail(rc);
     if ((rc = b->upload(&T.icons, icons, "instance table"))) return bail(rc);

@@ -114,6 +114,7 @@ struct DevTables {
     const int32_t* lrec;     // per body row: slot record offset, -1 if none
     const int32_t* lcons;    // per constraint: local row of body 1, of body 2 (-1 = Ground)
     const double* lst;       // per constraint: station 1 (in body 1), station 2 (in body 2)
+    const int32_t* lslot;    // per body row: slot index of a loop body (-1 = none): level-parallel layout
     const int32_t* icons;    // per instance: first constraint
     const int32_t* incons;   // per instance: number of constraints
     // per-instance integration control (the serving loop; null in a batch,
@@ -136,6 +137,9 @@ struct LaunchPlan {
     int variant;  // 1: registers as needed; 4: at most 128 registers (FP32 only)
     int nLoop;    // order positions [nChain, nChain + nLoop): instances with loop closures (FP64 chain driver)
     int chainFirst;  // first order position of the chain segment launch (a sub-range of it: pipelined realize)
+    int groupFirst;  // first block of the level-parallel launch in the block table
+    int nLoopGroupBlocks;  // blocks [loopGroupFirst, +n): loop-closure instances on the level-parallel driver (FP64)
+    int loopGroupFirst;
 };
 
 }  // namespace sbg

@@ -39,4 +39,20 @@ void rkLoop(const KArgs& a, cudaStream_t s) {
             a.projectEveryStep);
 }
 
+// Loop-closure instances on the level-parallel driver (FP64): tree passes on
+// the lanes of each instance's group, the multiplier solve and projections on
+// its first lane. Blocks [loopGroupFirst, +nLoopGroupBlocks) of the block
+// table; scratch and stage planes as for the one-thread loop segment.
+void rkLoopGroup(const KArgs& a, cudaStream_t s) {
+    if (a.P->nLoopGroupBlocks <= 0) return;
+    rkMersonKernel<double, 3, false, true, 1, true><<<a.P->nLoopGroupBlocks, 128, 0, s>>>(
+        *a.T, a.P->loopGroupFirst, 0, a.ystate, a.time, static_cast<double*>(a.fbufLoop), a.fplane,
+        static_cast<double*>(a.scratchLoop), a.status, a.h, a.nsteps, a.accuracy, a.consTol, a.projectEveryStep);
+}
+void realizeLoopGroup(const KArgs& a, cudaStream_t s) {
+    if (a.P->nLoopGroupBlocks <= 0) return;
+    realizeKernel<double, 3, false, true, 1, true><<<a.P->nLoopGroupBlocks, 128, 0, s>>>(
+        *a.T, a.P->loopGroupFirst, 0, a.y, a.ydot, static_cast<double*>(a.scratchLoop), a.status);
+}
+
 }  // namespace sbg

@@ -5,7 +5,7 @@
 namespace sbg {
 
 template <bool REF, int MINB> static void go(const KArgs& a, cudaStream_t s) {
-    realizeKernel<float, 3, REF, true, MINB><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, 0, 0, a.y, a.ydot,
+    realizeKernel<float, 3, REF, true, MINB><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, a.P->groupFirst, 0, a.y, a.ydot,
                                                                                   static_cast<float*>(a.scratch), a.status);
 }
 
@@ -21,7 +21,7 @@ void minv32Chain(const KArgs& a, cudaStream_t s) {
     else minvKernel<float, 3, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.f, a.ydot, sc, a.status);
 }
 void minv32Group(const KArgs& a, cudaStream_t s) {
-    minvKernel<float, 3, true><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, 0, 0, a.y, a.f, a.ydot,
+    minvKernel<float, 3, true><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, a.P->groupFirst, 0, a.y, a.f, a.ydot,
                                                                    static_cast<float*>(a.scratch), a.status);
 }
 

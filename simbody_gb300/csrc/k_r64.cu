@@ -12,7 +12,7 @@ void realize64Chain(const KArgs& a, cudaStream_t s) {
     else realizeKernel<double, 3, false, false><<<nb, 128, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
 }
 void realize64Group(const KArgs& a, cudaStream_t s) {
-    realizeKernel<double, 3, false, true><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, 0, 0, a.y, a.ydot,
+    realizeKernel<double, 3, false, true><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, a.P->groupFirst, 0, a.y, a.ydot,
                                                                               static_cast<double*>(a.scratch), a.status);
 }
 void minv64Chain(const KArgs& a, cudaStream_t s) {
@@ -22,7 +22,7 @@ void minv64Chain(const KArgs& a, cudaStream_t s) {
     else minvKernel<double, 3, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.f, a.ydot, sc, a.status);
 }
 void minv64Group(const KArgs& a, cudaStream_t s) {
-    minvKernel<double, 3, true><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, 0, 0, a.y, a.f, a.ydot,
+    minvKernel<double, 3, true><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, a.P->groupFirst, 0, a.y, a.f, a.ydot,
                                                                     static_cast<double*>(a.scratch), a.status);
 }
 

@@ -6,7 +6,7 @@ namespace sbg {
 
 template <bool REF, int MINB> static void go(const KArgs& a, cudaStream_t s) {
     rkMersonKernel<float, 3, REF, true, MINB><<<a.P->nGroupBlocks, 128, 0, s>>>(
-        *a.T, 0, 0, a.ystate, a.time, static_cast<float*>(a.fbuf), a.fplane, static_cast<float*>(a.scratch), a.status,
+        *a.T, a.P->groupFirst, 0, a.ystate, a.time, static_cast<float*>(a.fbuf), a.fplane, static_cast<float*>(a.scratch), a.status,
         a.h, a.nsteps, a.accuracy, a.consTol, a.projectEveryStep);
 }
 

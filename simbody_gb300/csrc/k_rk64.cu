@@ -16,7 +16,7 @@ void rk64Chain(const KArgs& a, cudaStream_t s) {
 }
 void rk64Group(const KArgs& a, cudaStream_t s) {
     rkMersonKernel<double, 3, false, true><<<a.P->nGroupBlocks, 128, 0, s>>>(
-        *a.T, 0, 0, a.ystate, a.time, static_cast<double*>(a.fbuf), a.fplane, static_cast<double*>(a.scratch), a.status,
+        *a.T, a.P->groupFirst, 0, a.ystate, a.time, static_cast<double*>(a.fbuf), a.fplane, static_cast<double*>(a.scratch), a.status,
         a.h, a.nsteps, a.accuracy, a.consTol, a.projectEveryStep);
 }
 

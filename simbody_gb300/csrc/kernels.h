@@ -74,5 +74,7 @@ void rk32Group(const KArgs& a, bool refine, cudaStream_t s);
 void realizeLoop(const KArgs& a, cudaStream_t s);  // k_loops.cu
 void minvLoop(const KArgs& a, cudaStream_t s);
 void rkLoop(const KArgs& a, cudaStream_t s);
+void rkLoopGroup(const KArgs& a, cudaStream_t s);      // loop closures, level-parallel driver
+void realizeLoopGroup(const KArgs& a, cudaStream_t s);
 
 }  // namespace sbg

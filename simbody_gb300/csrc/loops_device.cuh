@@ -39,7 +39,16 @@
 // eps off the path. Skipped rows would have contributed exact zeros, so the
 // results are the same as full sweeps.
 
-using SC64 = ScrStrided<double>;
+// Loop-closure records through either driver's layout: element f of record
+// rec at rec * a + f * b, with (a, b) = (s, s) for the interleaved tiles of
+// the one-thread driver (stride s) and (1, P) for the field-major rows of the
+// level-parallel driver (P rows: the bodies, then the slot records).
+struct ScrGen {
+    double* p;
+    int a, b;
+    __device__ __forceinline__ double& operator()(int rec, int f) const { return p[rec * a + f * b]; }
+};
+using SC64 = ScrGen;
 using V3d = V3<double>;
 
 // One instance with loop closures inside a kernel. save/delta are column
@@ -53,7 +62,24 @@ struct LoopState {
     double* save;
     double* delta;
     int64_t base, stride;
+    bool rows;  // level-parallel layout: record = local row, slots after the bodies
+    int body0, nb;
+    // record of body row `row`, slot record of a loop body row
+    __device__ __forceinline__ int rec(int row) const { return rows ? row - body0 : T.srec[row]; }
+    __device__ __forceinline__ int slot(int row) const { return rows ? nb + T.lslot[row] : T.lrec[row]; }
 };
+// The state of instance `inst` over records at `scratch` (its record base):
+// one-thread layout with stride s, or the level-parallel layout.
+__device__ __forceinline__ LoopState loopStateChain(const DevTables& T, int inst, double* scratch, int s, double* y,
+                                                    double* save, double* delta, int64_t base, int64_t stride) {
+    return LoopState{T, inst, SC64{scratch, s, s}, y, save, delta, base, stride, false, T.ibody[inst], T.inb[inst]};
+}
+__device__ __forceinline__ int loopRows(const DevTables& T, int inst) { return T.inb[inst] + 2 * T.incons[inst]; }
+__device__ __forceinline__ LoopState loopStateRows(const DevTables& T, int inst, double* scratch, double* y,
+                                                   double* save, double* delta, int64_t base, int64_t stride) {
+    return LoopState{T, inst, SC64{scratch, 1, loopRows(T, inst)}, y, save, delta, base, stride, true,
+                     T.ibody[inst], T.inb[inst]};
+}
 
 struct NullOut {
     template <class R> __device__ __forceinline__ void qdot(int, R) {}
@@ -80,12 +106,12 @@ __device__ __noinline__ void loopKinematics(const LoopState& L) {
         const int info = T.info[row];
         if (!(info & F_LOOPPATH)) continue;  // a path row's parent is a path row
         const int parent = T.parent[row];
-        const int rec = T.srec[row];
+        const int rec = L.rec(row);
         const Kin<double> P = parent < 0 ? groundKin<double>()
-                              : (info & F_CARRY) ? carry : loadKin<double>(L.S, T.srec[body0 + parent]);
+                              : (info & F_CARRY) ? carry : loadKin<double>(L.S, L.rec(body0 + parent));
         carry = body1<double, NM>(T, row, rec, L.S, src, out, g, P);
         if (info & F_MEMCHILD) storeKin(L.S, rec, carry);
-        if (info & F_LOOPBODY) storeKin(L.S, T.lrec[row], carry);
+        if (info & F_LOOPBODY) storeKin(L.S, L.slot(row), carry);
     }
 }
 
@@ -98,8 +124,8 @@ __device__ __forceinline__ void loopSlots(const LoopState& L, int c, int& s1, in
     const DevTables& T = L.T;
     const int gc = T.icons[L.inst] + c, body0 = T.ibody[L.inst];
     const int r1 = T.lcons[2 * gc], r2 = T.lcons[2 * gc + 1];
-    s1 = r1 >= 0 ? T.lrec[body0 + r1] : -1;
-    s2 = r2 >= 0 ? T.lrec[body0 + r2] : -1;
+    s1 = r1 >= 0 ? L.slot(body0 + r1) : -1;
+    s2 = r2 >= 0 ? L.slot(body0 + r2) : -1;
 }
 
 __device__ __forceinline__ LoopGeom loopGeom(const LoopState& L, int c) {
@@ -169,7 +195,7 @@ __device__ __forceinline__ void loopIn(const LoopState& L, int row, int rec, int
     const SC64& S = L.S;
     const int eDI = kRecH + 7 * N, eG = eDI + N * N, eEps = eG + 6 * N;
     if (info & F_LOOPBODY) {
-        const int sl = L.T.lrec[row];
+        const int sl = L.slot(row);
         const V3d tw = ld3<double>(S, sl, kSlotF), tv = ld3<double>(S, sl, kSlotF + 3);
         if (KIND == kMInvSweep) { zw = zw - tw; zv = zv - tv; }
         else { zw = zw + tw; zv = zv + tv; }
@@ -252,93 +278,104 @@ __device__ __forceinline__ void loopZeroAcc(const LoopState& L) {
     for (int lb = 0; lb < nb; ++lb) {
         const int row = body0 + lb;
         if ((T.info[row] & (F_MEMCHILD | F_LOOPPATH)) == (F_MEMCHILD | F_LOOPPATH)) {
-            st3<double>(L.S, T.srec[row], kRecZacc, z3<double>());
-            st3<double>(L.S, T.srec[row], kRecZacc + 3, z3<double>());
+            st3<double>(L.S, L.rec(row), kRecZacc, z3<double>());
+            st3<double>(L.S, L.rec(row), kRecZacc + 3, z3<double>());
         }
     }
 }
 
-// One inward and one outward sweep over the instance driven by the applied
-// forces in the slot records. The outward result of each constrained body
-// goes to its slot (kSlotB); onBody(row, n, ud) sees the mobility values of
-// every path row (of every row with FULL_OUT). kJacSweep multiplies g by
-// wt(row, j) between the halves.
-template <int NM, int KIND, bool FULL_OUT = false, class Wt, class OnBody>
-__device__ __forceinline__ void loopSweep(const LoopState& L, const Wt& wt, const OnBody& onBody) {
+// Inward half of a sweep driven by the applied forces in the slot records
+// (path rows only: the others contribute zero). kJacSweep multiplies g by
+// wt(row, j) after the body's step.
+template <int NM, int KIND, class Wt>
+__device__ __forceinline__ void loopSweepIn(const LoopState& L, const Wt& wt) {
     const DevTables& T = L.T;
     const SC64& S = L.S;
     const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
-    {
-        V3d cw = z3<double>(), cv = z3<double>();
-        bool have = false;
-        for (int lb = nb - 1; lb >= 0; --lb) {
-            const int row = body0 + lb;
-            const int info = T.info[row];
-            if (!(info & F_LOOPPATH)) {  // contributes zero
-                have = false;
-                continue;
-            }
-            const int n = (info >> 4) & 15;
-            const int rec = T.srec[row];
-            V3d zw = z3<double>(), zv = z3<double>();
-            if (info & F_MEMCHILD) {
-                zw = ld3<double>(S, rec, kRecZacc);
-                zv = ld3<double>(S, rec, kRecZacc + 3);
-                st3<double>(S, rec, kRecZacc, z3<double>());
-                st3<double>(S, rec, kRecZacc + 3, z3<double>());
-            }
-            if (have) { zw = zw + cw; zv = zv + cv; }
-            if (n == 6) loopIn6<KIND>(L, row, rec, info, zw, zv);
-            else loopIn<NM, KIND>(L, row, rec, n, info, zw, zv);
-            if (KIND == kJacSweep) {
-                const int eEps = recEps(recN(n, NM));
-                for (int j = 0; j < n; ++j) S(rec, eEps + j) = S(rec, eEps + j) * wt(row, j);
-            }
-            const int parent = T.parent[row];
-            have = (info & F_CARRY) != 0;
-            if (have) {
-                cw = zw;
-                cv = zv;
-            } else if (parent >= 0) {
-                const int pr = T.srec[body0 + parent];
-                st3<double>(S, pr, kRecZacc, ld3<double>(S, pr, kRecZacc) + zw);
-                st3<double>(S, pr, kRecZacc + 3, ld3<double>(S, pr, kRecZacc + 3) + zv);
-            }
+    V3d cw = z3<double>(), cv = z3<double>();
+    bool have = false;
+    for (int lb = nb - 1; lb >= 0; --lb) {
+        const int row = body0 + lb;
+        const int info = T.info[row];
+        if (!(info & F_LOOPPATH)) {  // contributes zero
+            have = false;
+            continue;
+        }
+        const int n = (info >> 4) & 15;
+        const int rec = L.rec(row);
+        V3d zw = z3<double>(), zv = z3<double>();
+        if (info & F_MEMCHILD) {
+            zw = ld3<double>(S, rec, kRecZacc);
+            zv = ld3<double>(S, rec, kRecZacc + 3);
+            st3<double>(S, rec, kRecZacc, z3<double>());
+            st3<double>(S, rec, kRecZacc + 3, z3<double>());
+        }
+        if (have) { zw = zw + cw; zv = zv + cv; }
+        if (n == 6) loopIn6<KIND>(L, row, rec, info, zw, zv);
+        else loopIn<NM, KIND>(L, row, rec, n, info, zw, zv);
+        if (KIND == kJacSweep) {
+            const int eEps = recEps(recN(n, NM));
+            for (int j = 0; j < n; ++j) S(rec, eEps + j) = S(rec, eEps + j) * wt(row, j);
+        }
+        const int parent = T.parent[row];
+        have = (info & F_CARRY) != 0;
+        if (have) {
+            cw = zw;
+            cv = zv;
+        } else if (parent >= 0) {
+            const int pr = L.rec(body0 + parent);
+            st3<double>(S, pr, kRecZacc, ld3<double>(S, pr, kRecZacc) + zw);
+            st3<double>(S, pr, kRecZacc + 3, ld3<double>(S, pr, kRecZacc + 3) + zv);
         }
     }
-    {
-        V3d aw = z3<double>(), av = z3<double>();
-        for (int lb = 0; lb < nb; ++lb) {
-            const int row = body0 + lb;
-            const int info = T.info[row];
-            const bool onPath = (info & F_LOOPPATH) != 0;
-            if (!FULL_OUT && !onPath) continue;  // a path row's parent is a path row
-            const int n = (info >> 4) & 15;
-            const int rec = T.srec[row];
-            const int parent = T.parent[row];
-            const bool hp = parent >= 0;
-            V3d pw = aw, pv = av;
-            if (hp && !(info & F_CARRY)) {
-                const int pr = T.srec[body0 + parent];
-                pw = ld3<double>(S, pr, 0);
-                pv = ld3<double>(S, pr, 3);
-            }
-            double ud[6];
-            if (n == 6) loopOut6<KIND>(L, rec, hp, onPath, pw, pv, ud);
-            else loopOut<NM, KIND>(L, rec, n, hp, onPath, pw, pv, ud);
-            onBody(row, n, ud);
-            if (info & F_LOOPBODY) {
-                st3<double>(S, T.lrec[row], kSlotB, pw);
-                st3<double>(S, T.lrec[row], kSlotB + 3, pv);
-            }
-            if (info & F_MEMCHILD) {
-                st3<double>(S, rec, 0, pw);
-                st3<double>(S, rec, 3, pv);
-            }
-            aw = pw;
-            av = pv;
+}
+
+// Outward half. The outward result of each constrained body goes to its
+// slot (kSlotB); onBody(row, n, ud) sees the mobility values of every path
+// row (of every row with FULL_OUT, which take zero eps off the paths).
+template <int NM, int KIND, bool FULL_OUT, class OnBody>
+__device__ __forceinline__ void loopSweepOut(const LoopState& L, const OnBody& onBody) {
+    const DevTables& T = L.T;
+    const SC64& S = L.S;
+    const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
+    V3d aw = z3<double>(), av = z3<double>();
+    for (int lb = 0; lb < nb; ++lb) {
+        const int row = body0 + lb;
+        const int info = T.info[row];
+        const bool onPath = (info & F_LOOPPATH) != 0;
+        if (!FULL_OUT && !onPath) continue;  // a path row's parent is a path row
+        const int n = (info >> 4) & 15;
+        const int rec = L.rec(row);
+        const int parent = T.parent[row];
+        const bool hp = parent >= 0;
+        V3d pw = aw, pv = av;
+        if (hp && !(info & F_CARRY)) {
+            const int pr = L.rec(body0 + parent);
+            pw = ld3<double>(S, pr, 0);
+            pv = ld3<double>(S, pr, 3);
         }
+        double ud[6];
+        if (n == 6) loopOut6<KIND>(L, rec, hp, onPath, pw, pv, ud);
+        else loopOut<NM, KIND>(L, rec, n, hp, onPath, pw, pv, ud);
+        onBody(row, n, ud);
+        if (info & F_LOOPBODY) {
+            st3<double>(S, L.slot(row), kSlotB, pw);
+            st3<double>(S, L.slot(row), kSlotB + 3, pv);
+        }
+        if (info & F_MEMCHILD) {
+            st3<double>(S, rec, 0, pw);
+            st3<double>(S, rec, 3, pv);
+        }
+        aw = pw;
+        av = pv;
     }
+}
+
+// One inward and one outward sweep over the instance.
+template <int NM, int KIND, bool FULL_OUT = false, class Wt, class OnBody>
+__device__ __forceinline__ void loopSweep(const LoopState& L, const Wt& wt, const OnBody& onBody) {
+    loopSweepIn<NM, KIND>(L, wt);
+    loopSweepOut<NM, KIND, FULL_OUT>(L, onBody);
 }
 
 // Cholesky of the leading m x m block (row stride kMaxLoopEq), lower factor
@@ -393,10 +430,15 @@ __device__ __forceinline__ void loopGram(const LoopState& L, const Wt& wt, doubl
 }
 
 // Loop forward dynamics after the tree RHS (which left the tree udot in out
-// and A_GB in the slots). Returns SBG_INST_* bits.
-template <int NM, class Out>
-__device__ __noinline__ int loopForwardDynamics(const DevTables& T, int inst, const SC64& S, Out& out) {
-    const LoopState L{T, inst, S, nullptr, nullptr, nullptr, 0, 0};
+// and A_GB in the slots). Returns SBG_INST_* bits. With DEFER_OUT the
+// outward half of the final correction (udot -= M^-1 G^T lambda, every body)
+// is left to loopCorrectionOutRows, which the lanes of a group run level by
+// level.
+template <int NM, bool DEFER_OUT = false, class Out>
+__device__ __noinline__ int loopForwardDynamics(const LoopState& L, Out& out) {
+    const DevTables& T = L.T;
+    const int inst = L.inst;
+    const SC64& S = L.S;
     const int nc = T.incons[inst], m = 3 * nc;
     loopZeroAcc(L);
     double lam[kMaxLoopEq];
@@ -414,11 +456,49 @@ __device__ __noinline__ int loopForwardDynamics(const DevTables& T, int inst, co
     loopCholSolve(m, A, lam);
     loopClearForces(L);
     for (int c = 0; c < nc; ++c) loopAddConstraintForce(L, loopGeom(L, c), mk3(lam[3 * c], lam[3 * c + 1], lam[3 * c + 2]));
-    loopSweep<NM, kMInvSweep, true>(L, one, [&](int row, int n, const double* ud) {
-        const int uo = T.uoff[row];
-        for (int i = 0; i < n; ++i) out.udot(uo + i, out.udotGet(uo + i) - ud[i]);
-    });
+    if constexpr (DEFER_OUT) {
+        loopSweepIn<NM, kMInvSweep>(L, one);
+    } else {
+        loopSweep<NM, kMInvSweep, true>(L, one, [&](int row, int n, const double* ud) {
+            const int uo = T.uoff[row];
+            for (int i = 0; i < n; ++i) out.udot(uo + i, out.udotGet(uo + i) - ud[i]);
+        });
+    }
     return 0;
+}
+
+// The outward half of the constraint-force correction on the lanes of a
+// group (level-parallel layout): the same per-body step as the serial sweep,
+// a level at a time, parents' accelerations through their records.
+template <int NM, class Out>
+__device__ __forceinline__ void loopCorrectionOutRows(const LoopState& L, Out& out, int gl, int G, unsigned mask) {
+    const DevTables& T = L.T;
+    const SC64& S = L.S;
+    const int* ls = T.levStart + T.ilev[L.inst];
+    const int nlev = T.inlev[L.inst];
+    for (int lv = 0; lv < nlev; ++lv) {
+        for (int lb = ls[lv] + gl; lb < ls[lv + 1]; lb += G) {
+            const int row = L.body0 + lb;
+            const int info = T.info[row];
+            const int n = (info >> 4) & 15;
+            const int parent = T.parent[row];  // local row = record of the parent
+            const bool hp = parent >= 0;
+            V3d pw = z3<double>(), pv = z3<double>();
+            if (hp) {
+                pw = ld3<double>(S, parent, 0);
+                pv = ld3<double>(S, parent, 3);
+            }
+            double ud[6];
+            const bool onPath = (info & F_LOOPPATH) != 0;
+            if (n == 6) loopOut6<kMInvSweep>(L, lb, hp, onPath, pw, pv, ud);
+            else loopOut<NM, kMInvSweep>(L, lb, n, hp, onPath, pw, pv, ud);
+            const int uo = T.uoff[row];
+            for (int i = 0; i < n; ++i) out.udot(uo + i, out.udotGet(uo + i) - ud[i]);
+            st3<double>(S, lb, 0, pw);
+            st3<double>(S, lb, 3, pv);
+        }
+        __syncwarp(mask);
+    }
 }
 
 // ----------------------------------------------------------- projections

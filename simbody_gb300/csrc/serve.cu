@@ -11,8 +11,8 @@
 //                  forces, children, levels) and the FP64/FP32 parameters
 //   forces pool    mobility-force elements
 //   state pool     y = [q, u] (FP64) and the four RK stage planes
-//   scratch pools  per-body records of the level-parallel driver (R) and of
-//                  the FP64 loop-closure driver
+//   scratch pools  per-body records of the level-parallel driver, in the
+//                  server's precision and (loop closures) in FP64
 //   slots          per-request instance entries (the DevTables' instance
 //                  arrays), max_slots of them
 // Each tick (sbg_server_tick) the host
@@ -24,9 +24,10 @@
 //   4. enqueues on the server's stream: one host->device copy of a staging
 //      buffer (new requests' tables and states, this tick's control arrays),
 //      a copy kernel that scatters it into the arena, the RK-Merson kernels
-//      (level-parallel driver on a side stream, forked and joined; loop
-//      closures on the FP64 chain driver), a copy kernel that gathers the
-//      finished requests' states, and one device->host copy of them.
+//      (level-parallel driver for the trees on a side stream, forked and
+//      joined; FP64 level-parallel driver with the multiplier solve for the
+//      loop closures), a copy kernel that gathers the finished requests'
+//      states, and one device->host copy of them.
 // Requests that arrive while others are on the GPU join at the next tick,
 // into the slots and memory that finished requests gave back. A request's
 // arithmetic depends only on its own tables and state: the RK kernels carry
@@ -47,6 +48,7 @@
 #include <deque>
 #include <mutex>
 #include <new>
+#include <thread>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -91,24 +93,26 @@ int groupLanes(const sbg_topology_s& t) {
 // Relative GPU time of one RK-Merson step of a request, in serial body
 // visits per RHS on its driver:
 //   level-parallel driver  sum over levels of ceil(width / lanes)
-//   loop-closure driver    every body for the tree passes plus the loop-path
-//                          rows for each of the 3m+1 constraint sweeps, with
-//                          the FP64 one-thread driver's slowdown
+//   loop closures          the same tree passes in FP64, plus the loop-path
+//                          rows of the 2m+1 constraint sweeps and the
+//                          all-body correction, run on one lane
 // A request's steps per tick are the server's chunk scaled by
 // kRefCost / cost, so that every request's chunk takes about the same time
 // and no request waits on a slower neighbour.
 constexpr double kRefCost = 8.0;          // the median request of the uneven-tree distribution
-constexpr double kLoopDriverWeight = 4.0;  // one FP64 thread per request vs. lanes in FP32
+constexpr double kLoopDriverWeight = 3.0;  // FP64 lanes vs. FP32 lanes
 double stepCost(const sbg_topology_s& t, bool loops, int G) {
     if (!loops) {
         double slots = 0;
         for (int L = 0; L < t.nlevels; ++L) slots += (t.levStart[L + 1] - t.levStart[L] + G - 1) / G;
         return slots;
     }
+    double slots = 0;
+    for (int L = 0; L < t.nlevels; ++L) slots += (t.levStart[L + 1] - t.levStart[L] + G - 1) / G;
     int path = 0;
     for (int r = 0; r < t.nb; ++r) path += (t.info[r] & F_LOOPPATH) != 0;
     const int m = 3 * t.ncons;
-    return kLoopDriverWeight * (t.nb + (double)path * (3 * m + 1) / 3.0);
+    return kLoopDriverWeight * (slots + (double)path * (2 * m + 1) / 3.0 + t.nb / 3.0);
 }
 
 // Units of the pools per body row of a typical request (a tree of
@@ -145,7 +149,7 @@ struct ServeReq {
 };
 
 enum RowTable { R_PARENT = 0, R_INFO, R_QOFF, R_UOFF, R_SREC, R_FBEG, R_FCNT, R_LREC, R_CBEG, R_CCNT, R_CLIST, R_LEV,
-                kRowTables };
+                R_LSLOT, kRowTables };
 
 struct TickRec {
     int parity = 0;
@@ -154,7 +158,7 @@ struct TickRec {
 
 }  // namespace
 
-struct sbg_server_s {
+struct ServeLane {
     int precision = SBG_PRECISION_MIXED, device = 0;
     int64_t budget = 0;
     int32_t maxSlots = 0, chunk = 64;
@@ -206,7 +210,7 @@ struct sbg_server_s {
     double clock() const {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
-    ~sbg_server_s() {
+    ~ServeLane() {
         cudaSetDevice(device);
         if (stream) cudaStreamSynchronize(stream);
         for (void* p : bufs) cudaFree(p);
@@ -284,6 +288,7 @@ void buildImage(const sbg_topology_s& t, ServeReq& r, Footprint& fp) {
         at(R_FBEG, i) = t.fbeg[i];  // request-relative: + force base at admission
         at(R_FCNT, i) = t.fcnt[i];
         at(R_LREC, i) = t.lslot[i] >= 0 ? (int32_t)(recTotal + (int64_t)t.lslot[i] * kSlotSize) : -1;
+        at(R_LSLOT, i) = t.lslot[i];
         at(R_CBEG, i) = t.cbeg[i];  // request-relative: + row base at admission
         at(R_CCNT, i) = t.ccnt[i];
     }
@@ -298,7 +303,9 @@ void buildImage(const sbg_topology_s& t, ServeReq& r, Footprint& fp) {
     fp.units[kPoolRows] = rows;
     fp.units[kPoolForces] = r.nf;
     fp.units[kPoolState] = t.nq + t.nu;
-    if (r.loops) fp.units[kPoolLoopScratch] = recTotal + (int64_t)t.nslots * kSlotSize;
+    // level-parallel records: one row per body (loop closures: then the
+    // slot rows, 2 per constraint), FP64 for loop closures
+    if (r.loops) fp.units[kPoolLoopScratch] = (int64_t)(nb + 2 * t.ncons) * rowsRecordWidth(t, 3);
     else fp.units[kPoolScratch] = (int64_t)nb * rowsRecordWidth(t, 3);
 }
 
@@ -306,7 +313,7 @@ void buildImage(const sbg_topology_s& t, ServeReq& r, Footprint& fp) {
 // them to their device destinations (before the RK kernels), and the gather
 // descriptors that collect finished states (after them).
 struct Stager {
-    sbg_server_s* s;
+    ServeLane* s;
     char* host;
     int64_t cap, used = 0;
     std::vector<CopyDesc> pre, post;
@@ -357,7 +364,7 @@ int64_t imageBytes(const ServeReq& r, size_t rsz, int* ndesc) {
 }
 
 // Stage the tables, state and instance entries of an admitted request.
-void stageRequest(sbg_server_s* s, Stager& st, ServeReq& r, const SchedRequest& sr) {
+void stageRequest(ServeLane* s, Stager& st, ServeReq& r, const SchedRequest& sr) {
     const int rows = r.nb + 1;
     const int64_t row0 = sr.off[kPoolRows], f0 = sr.off[kPoolForces], y0 = sr.off[kPoolState];
     const int slot = sr.slot;
@@ -409,7 +416,7 @@ void stageRequest(sbg_server_s* s, Stager& st, ServeReq& r, const SchedRequest& 
 }
 
 // Copy finished requests out of the result buffer of a completed tick.
-void harvest(sbg_server_s* s, const TickRec& tr) {
+void harvest(ServeLane* s, const TickRec& tr) {
     const double now = s->clock();
     const char* base = s->hostRes[tr.parity];
     for (const auto& pr : tr.results) {
@@ -429,7 +436,7 @@ void harvest(sbg_server_s* s, const TickRec& tr) {
 }
 
 // Wait for (block) or poll the oldest in-flight tick; harvest it when done.
-int drainInflight(sbg_server_s* s, bool block, int32_t* ncompleted) {
+int drainInflight(ServeLane* s, bool block, int32_t* ncompleted) {
     while (!s->inflight.empty()) {
         const TickRec& tr = s->inflight.front();
         const auto w0 = std::chrono::steady_clock::now();
@@ -456,28 +463,19 @@ int drainInflight(sbg_server_s* s, bool block, int32_t* ncompleted) {
 
 }  // namespace
 
-extern "C" {
+namespace {
 
-int sbg_server_create(const sbg_server_config* cfg, sbg_server* out) {
-    if (!cfg || !out) return setError(SBG_ERR_INVALID, "null argument");
-    if (cfg->precision != SBG_PRECISION_FP64 && cfg->precision != SBG_PRECISION_MIXED &&
-        cfg->precision != SBG_PRECISION_MIXED_FAST)
-        return setError(SBG_ERR_INVALID, "unknown precision");
-    if (cfg->device_budget_bytes <= 0) return setError(SBG_ERR_INVALID, "the server needs a positive device budget");
-    if (cfg->max_slots < 0 || cfg->chunk_steps < 0) return setError(SBG_ERR_INVALID, "negative slot count or chunk");
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
-        cudaGetLastError();
-        return setError(SBG_ERR_NO_DEVICE, "no CUDA device available");
-    }
-    if (cfg->device < 0 || cfg->device >= ndev) return setError(SBG_ERR_INVALID, "bad device ordinal");
-    SBG_SCUDA(cudaSetDevice(cfg->device), "cudaSetDevice");
-    auto* s = new (std::nothrow) sbg_server_s();
+// One lane of the server: its own share of the budget (arena), slots,
+// scheduler, stream and tick cadence.
+int laneCreate(const sbg_server_config* cfg, int64_t budget, std::chrono::steady_clock::time_point t0,
+               ServeLane** out) {
+    auto* s = new (std::nothrow) ServeLane();
     if (!s) return setError(SBG_ERR_NOMEM, "out of host memory");
     auto bail = [&](int rc) { delete s; return rc; };
+    s->t0 = t0;
     s->precision = cfg->precision;
     s->device = cfg->device;
-    s->budget = cfg->device_budget_bytes;
+    s->budget = budget;
     s->maxSlots = cfg->max_slots > 0 ? cfg->max_slots : 65536;
     s->chunk = cfg->chunk_steps > 0 ? std::min(cfg->chunk_steps, kCtlSteps) : 64;
     const bool fp64 = s->precision == SBG_PRECISION_FP64;
@@ -486,7 +484,7 @@ int sbg_server_create(const sbg_server_config* cfg, sbg_server* out) {
     // Fixed part: slots, staging (device side), then the pools share the rest.
     const int64_t S = s->maxSlots;
     const int64_t slotBytes = S * (14 * 4 + 4 * 8 + (3 + 3 + 1) * 8 + kMaxLoopCons * (2 * 4 + 6 * 8)) + 2 * (S + 2) * 4;
-    s->upCap = std::max<int64_t>(4 << 20, std::min<int64_t>(64 << 20, s->budget / 16));
+    s->upCap = std::max<int64_t>(1 << 20, std::min<int64_t>(64 << 20, s->budget / 16));
     s->resCap = s->upCap;
     const int64_t fixed = slotBytes + s->upCap + s->resCap;
     if (fixed >= s->budget) return bail(setError(SBG_ERR_BUDGET, "device budget too small for the server's slots and staging"));
@@ -567,6 +565,7 @@ int sbg_server_create(const sbg_server_config* cfg, sbg_server* out) {
     T.fbeg = s->rowsI[R_FBEG];
     T.fcnt = s->rowsI[R_FCNT];
     T.lrec = s->rowsI[R_LREC];
+    T.lslot = s->rowsI[R_LSLOT];
     T.cbeg = s->rowsI[R_CBEG];
     T.ccnt = s->rowsI[R_CCNT];
     T.clist = s->rowsI[R_CLIST];
@@ -603,18 +602,9 @@ int sbg_server_create(const sbg_server_config* cfg, sbg_server* out) {
     return SBG_OK;
 }
 
-int sbg_server_destroy(sbg_server s) {
-    delete s;
-    return SBG_OK;
-}
-
-int sbg_server_submit(sbg_server s, sbg_topology topo, const double* y0, double t0, double h, int32_t nsteps,
-                      const sbg_integ_opts* opts, int64_t* id) {
-    if (!s || !topo || !y0 || !id) return setError(SBG_ERR_INVALID, "null argument");
-    if (!(h > 0) || !std::isfinite(h)) return setError(SBG_ERR_INVALID, "step size must be positive");
-    if (nsteps < 0 || nsteps > kCtlSteps) return setError(SBG_ERR_INVALID, "step count out of range");
-    if (topo->ncons > kMaxLoopCons)
-        return setError(SBG_ERR_UNSUPPORTED, "at most " + std::to_string(kMaxLoopCons) + " Ball loop closures per system");
+// Queue a request on a lane (the caller holds the lane's mutex).
+int laneSubmit(ServeLane* s, int64_t rid, sbg_topology topo, const double* y0, double t0, double h, int32_t nsteps,
+               const sbg_integ_opts* opts) {
     ServeReq r;
     Footprint fp;
     buildImage(*topo, r, fp);
@@ -630,7 +620,6 @@ int sbg_server_submit(sbg_server s, sbg_topology topo, const double* y0, double 
     }
     r.acc = acc;
     r.ctol = ctol > 0 ? ctol : acc / 10;
-    std::lock_guard<std::mutex> lock(s->mu);
     if (!s->sched.fitsEver(fp))
         return setError(SBG_ERR_BUDGET, "request needs more device memory than the server's budget provides");
     int nd = 0;
@@ -638,37 +627,37 @@ int sbg_server_submit(sbg_server s, sbg_topology topo, const double* y0, double 
         return setError(SBG_ERR_BUDGET, "request's tables exceed the server's upload staging");
     if ((int64_t)(r.nq + r.nu) * 8 + 16 > s->resCap)
         return setError(SBG_ERR_BUDGET, "request's state exceeds the server's result staging");
-    r.id = s->nextId++;
+    r.id = rid;
     r.submitS = s->clock();
     const double cost = stepCost(*topo, r.loops, r.G);
     const int32_t chunk = (int32_t)std::max(1.0, std::min(16.0 * s->chunk, std::floor(s->chunk * kRefCost / cost)));
     r.sched = s->sched.submit(r.id, fp, nsteps, chunk);
     s->byId[r.id] = r.sched;
     s->reqs.push_back(std::move(r));
-    *id = s->reqs.back().id;
     return SBG_OK;
 }
 
-static int serverTick(sbg_server s, int32_t* ncompleted);
+int laneIssue(ServeLane* s);
 
-int sbg_server_tick(sbg_server s, int32_t* ncompleted) {
-    if (!s) return setError(SBG_ERR_INVALID, "null server");
-    std::lock_guard<std::mutex> lock(s->mu);
-    const auto h0 = std::chrono::steady_clock::now();
-    const int rc = serverTick(s, ncompleted);
-    s->hostSeconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - h0).count();
+// One scheduling round of a lane. Results of finished ticks are collected;
+// a new tick is prepared only while at most one is in flight (its staging
+// buffers alternate by parity): with `block`, by waiting for the older one,
+// otherwise by returning at once (*issued = false).
+int laneTick(ServeLane* s, bool block, int32_t* ncompleted, bool* issued) {
+    *issued = false;
+    if (int rc = drainInflight(s, false, ncompleted)) return rc;
+    if (s->inflight.size() >= 2) {
+        if (!block) return SBG_OK;
+        if (int rc = drainInflight(s, true, ncompleted)) return rc;
+    }
+    if (s->inflight.size() >= 2) return setError(SBG_ERR_STATE, "serving ticks did not complete");
+    const int64_t tick0 = s->tick;
+    const int rc = laneIssue(s);
+    *issued = s->tick != tick0;
     return rc;
 }
 
-static int serverTick(sbg_server s, int32_t* ncompleted) {
-    if (ncompleted) *ncompleted = 0;
-    SBG_SCUDA(cudaSetDevice(s->device), "cudaSetDevice");
-    // 1. results of finished ticks; keep at most one tick in flight while
-    //    this one is prepared (its staging buffers alternate by parity)
-    if (int rc = drainInflight(s, false, ncompleted)) return rc;
-    if (s->inflight.size() >= 2)
-        if (int rc = drainInflight(s, true, ncompleted)) return rc;
-    if (s->inflight.size() >= 2) return setError(SBG_ERR_STATE, "serving ticks did not complete");
+int laneIssue(ServeLane* s) {
     const int parity = (int)(s->tick & 1);
     Stager st{s, s->hostUp[parity], s->upCap};
     const double now = s->clock();
@@ -695,29 +684,35 @@ static int serverTick(sbg_server s, int32_t* ncompleted) {
     });
     if (plan.empty() && admitted.empty()) return SBG_OK;
     s->peakResident = std::max<int64_t>(s->peakResident, (int64_t)plan.size());
-    // 4. control arrays: loop-closure requests first (FP64 chain driver),
-    //    then level-parallel requests by lanes per request, widest first
+    // 4. control arrays. Two level-parallel segments, each sorted by lanes
+    //    per request (widest first) and cut into 128-thread blocks of equal
+    //    lanes: loop-closure requests (FP64, blocks [0, nLoopBlocks)) and
+    //    the other trees (the server's precision, the blocks after them).
     std::vector<int32_t> loopIdx, grpIdx;
     for (const PlannedChunk& c : plan) (s->reqs[c.req].loops ? loopIdx : grpIdx).push_back((int32_t)(&c - plan.data()));
-    std::stable_sort(grpIdx.begin(), grpIdx.end(),
-                     [&](int32_t a, int32_t b) { return s->reqs[plan[a].req].G > s->reqs[plan[b].req].G; });
-    std::vector<int32_t> order;
+    auto byLanes = [&](int32_t a, int32_t b) { return s->reqs[plan[a].req].G > s->reqs[plan[b].req].G; };
+    std::stable_sort(loopIdx.begin(), loopIdx.end(), byLanes);
+    std::stable_sort(grpIdx.begin(), grpIdx.end(), byLanes);
+    std::vector<int32_t> order, blkFirst, blkG;
     order.reserve(plan.size());
-    for (int32_t k : loopIdx) order.push_back(s->sched.req(plan[k].req).slot);
-    std::vector<int32_t> blkFirst, blkG;
-    const int nLoop = (int)loopIdx.size();
-    for (size_t p = 0; p < grpIdx.size();) {
-        const int G = s->reqs[plan[grpIdx[p]].req].G;
-        size_t q = p;
-        while (q < grpIdx.size() && (int)(q - p) < 128 / G && s->reqs[plan[grpIdx[q]].req].G == G) ++q;
-        blkFirst.push_back(nLoop + (int32_t)p);
-        blkG.push_back(G);
-        p = q;
-    }
-    const int nGroupBlocks = (int)blkFirst.size();
-    blkFirst.push_back(nLoop + (int32_t)grpIdx.size());
+    auto segment = [&](const std::vector<int32_t>& idx) {
+        const int32_t pos0 = (int32_t)order.size();
+        for (size_t p = 0; p < idx.size();) {
+            const int G = s->reqs[plan[idx[p]].req].G;
+            size_t q = p;
+            while (q < idx.size() && (int)(q - p) < 128 / G && s->reqs[plan[idx[q]].req].G == G) ++q;
+            blkFirst.push_back(pos0 + (int32_t)p);
+            blkG.push_back(G);
+            p = q;
+        }
+        for (int32_t k : idx) order.push_back(s->sched.req(plan[k].req).slot);
+    };
+    segment(loopIdx);
+    const int nLoopBlocks = (int)blkFirst.size();
+    segment(grpIdx);
+    const int nGroupBlocks = (int)blkFirst.size() - nLoopBlocks;
+    blkFirst.push_back((int32_t)order.size());
     blkG.push_back(0);
-    for (int32_t k : grpIdx) order.push_back(s->sched.req(plan[k].req).slot);
     if (!order.empty()) st.put(order.data(), (int64_t)order.size() * 4, s->order);
     st.put(blkFirst.data(), (int64_t)blkFirst.size() * 4, s->blkFirst);
     st.put(blkG.data(), (int64_t)blkG.size() * 4, s->blkG);
@@ -754,7 +749,13 @@ static int serverTick(sbg_server s, int32_t* ncompleted) {
     SBG_SCUDA(launchCopies(reinterpret_cast<const CopyDesc*>(s->devUp + preOff), (int)st.pre.size(), m), "tick scatter");
     ++s->launches;
     if (!plan.empty()) {
-        const LaunchPlan P{0, nGroupBlocks, 3, 1, nLoop};
+        LaunchPlan P{};
+        P.nm = 3;
+        P.variant = 1;
+        P.nGroupBlocks = nGroupBlocks;
+        P.groupFirst = nLoopBlocks;
+        P.nLoopGroupBlocks = nLoopBlocks;
+        P.loopGroupFirst = 0;
         KArgs a{};
         a.T = &s->T;
         a.P = &P;
@@ -770,7 +771,7 @@ static int serverTick(sbg_server s, int32_t* ncompleted) {
         a.nsteps = 0;
         a.accuracy = 1e-3;
         a.consTol = 1e-4;
-        const bool both = nLoop > 0 && nGroupBlocks > 0;
+        const bool both = nLoopBlocks > 0 && nGroupBlocks > 0;
         cudaStream_t gs = both ? s->side : m;
         if (both) {
             SBG_SCUDA(cudaEventRecord(s->evFork, m), "fork");
@@ -781,8 +782,8 @@ static int serverTick(sbg_server s, int32_t* ncompleted) {
             else rk32Group(a, s->precision == SBG_PRECISION_MIXED, gs);
             ++s->launches;
         }
-        if (nLoop > 0) {
-            rkLoop(a, m);
+        if (nLoopBlocks > 0) {
+            rkLoopGroup(a, m);
             ++s->launches;
         }
         if (both) {
@@ -807,32 +808,150 @@ static int serverTick(sbg_server s, int32_t* ncompleted) {
     return SBG_OK;
 }
 
+bool laneIdle(const ServeLane* s) { return s->sched.queued() == 0 && s->sched.resident() == 0; }
+
+}  // namespace
+
+// The server: two lanes with independent tick cadences, so that requests of
+// very different cost per step do not wait on each other. Lane 0 runs the
+// trees without loop closures (level-parallel driver, the server's
+// precision), lane 1 the trees with Ball loop closures (FP64, multiplier
+// solve and projections). The budget is split between them in proportion
+// to their expected share of the arena.
+struct sbg_server_s {
+    ServeLane* lane[2] = {nullptr, nullptr};
+    std::mutex mu;
+    int64_t nextId = 1;
+    std::unordered_map<int64_t, int> laneOf;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    double hostSeconds = 0;  // inside sbg_server_tick ...
+    double pollSeconds = 0;  // ... of which waiting for a lane to free up
+    ~sbg_server_s() {
+        delete lane[0];
+        delete lane[1];
+    }
+    double clock() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+};
+
+constexpr double kLoopLaneShare = 0.35;  // of the budget
+
+extern "C" {
+
+int sbg_server_create(const sbg_server_config* cfg, sbg_server* out) {
+    if (!cfg || !out) return setError(SBG_ERR_INVALID, "null argument");
+    if (cfg->precision != SBG_PRECISION_FP64 && cfg->precision != SBG_PRECISION_MIXED &&
+        cfg->precision != SBG_PRECISION_MIXED_FAST)
+        return setError(SBG_ERR_INVALID, "unknown precision");
+    if (cfg->device_budget_bytes <= 0) return setError(SBG_ERR_INVALID, "the server needs a positive device budget");
+    if (cfg->max_slots < 0 || cfg->chunk_steps < 0) return setError(SBG_ERR_INVALID, "negative slot count or chunk");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return setError(SBG_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) return setError(SBG_ERR_INVALID, "bad device ordinal");
+    SBG_SCUDA(cudaSetDevice(cfg->device), "cudaSetDevice");
+    auto* s = new (std::nothrow) sbg_server_s();
+    if (!s) return setError(SBG_ERR_NOMEM, "out of host memory");
+    const int64_t loopBudget = (int64_t)(cfg->device_budget_bytes * kLoopLaneShare);
+    const int32_t slots = cfg->max_slots > 0 ? cfg->max_slots : 65536;
+    if (slots < 2) return setError(SBG_ERR_INVALID, "the server needs at least two slots (one per lane)");
+    const int32_t loopSlots = std::max(1, std::min(slots - 1, (int32_t)std::lround(slots * kLoopLaneShare)));
+    sbg_server_config c0 = *cfg, c1 = *cfg;
+    c0.max_slots = slots - loopSlots;
+    c1.max_slots = loopSlots;
+    int rc = laneCreate(&c0, cfg->device_budget_bytes - loopBudget, s->t0, &s->lane[0]);
+    if (rc == SBG_OK) rc = laneCreate(&c1, loopBudget, s->t0, &s->lane[1]);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return SBG_OK;
+}
+
+int sbg_server_destroy(sbg_server s) {
+    delete s;
+    return SBG_OK;
+}
+
+int sbg_server_submit(sbg_server s, sbg_topology topo, const double* y0, double t0, double h, int32_t nsteps,
+                      const sbg_integ_opts* opts, int64_t* id) {
+    if (!s || !topo || !y0 || !id) return setError(SBG_ERR_INVALID, "null argument");
+    if (!(h > 0) || !std::isfinite(h)) return setError(SBG_ERR_INVALID, "step size must be positive");
+    if (nsteps < 0 || nsteps > kCtlSteps) return setError(SBG_ERR_INVALID, "step count out of range");
+    if (topo->ncons > kMaxLoopCons)
+        return setError(SBG_ERR_UNSUPPORTED, "at most " + std::to_string(kMaxLoopCons) + " Ball loop closures per system");
+    std::lock_guard<std::mutex> lock(s->mu);
+    const int li = topo->ncons > 0 ? 1 : 0;
+    ServeLane* L = s->lane[li];
+    std::lock_guard<std::mutex> lk(L->mu);
+    const int64_t rid = s->nextId;
+    if (int rc = laneSubmit(L, rid, topo, y0, t0, h, nsteps, opts)) return rc;
+    ++s->nextId;
+    s->laneOf[rid] = li;
+    *id = rid;
+    return SBG_OK;
+}
+
+int sbg_server_tick(sbg_server s, int32_t* ncompleted) {
+    if (!s) return setError(SBG_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (ncompleted) *ncompleted = 0;
+    SBG_SCUDA(cudaSetDevice(s->lane[0]->device), "cudaSetDevice");
+    const auto h0 = std::chrono::steady_clock::now();
+    // Each lane issues its next tick when it can; if neither can (both have
+    // two ticks in flight), wait for whichever finishes first.
+    for (int round = 0;; ++round) {
+        bool any = false, work = false;
+        for (ServeLane* L : s->lane) {
+            std::lock_guard<std::mutex> lk(L->mu);
+            int32_t n = 0;
+            bool issued = false;
+            if (int rc = laneTick(L, false, &n, &issued)) return rc;
+            if (ncompleted) *ncompleted += n;
+            any |= issued || n > 0;
+            work |= !L->inflight.empty();  // waiting for a tick in flight can free a lane
+        }
+        if (any || !work) break;
+        const auto w0 = std::chrono::steady_clock::now();
+        std::this_thread::sleep_for(std::chrono::microseconds(round < 100 ? 20 : 200));
+        s->pollSeconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count();
+    }
+    s->hostSeconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - h0).count();
+    return SBG_OK;
+}
+
 int sbg_server_drain(sbg_server s) {
     if (!s) return setError(SBG_ERR_INVALID, "null server");
-    for (;;) {
-        int64_t ticks0 = 0;
-        {
+    for (ServeLane* L : s->lane) {
+        for (;;) {
             std::lock_guard<std::mutex> lock(s->mu);
-            ticks0 = s->tick;
-        }
-        int32_t n = 0;
-        if (int rc = sbg_server_tick(s, &n)) return rc;
-        std::lock_guard<std::mutex> lock(s->mu);
-        if (s->sched.queued() == 0 && s->sched.resident() == 0) {
-            if (int rc = drainInflight(s, true, nullptr)) return rc;
-            if (s->inflight.empty()) return SBG_OK;
-        } else if (s->tick == ticks0 && s->inflight.empty()) {
-            return setError(SBG_ERR_STATE, "serving made no progress: a queued request cannot be admitted");
+            std::lock_guard<std::mutex> lk(L->mu);
+            if (laneIdle(L)) {
+                if (int rc = drainInflight(L, true, nullptr)) return rc;
+                if (L->inflight.empty()) break;
+            }
+            int32_t n = 0;
+            bool issued = false;
+            if (int rc = laneTick(L, true, &n, &issued)) return rc;
+            if (!issued && L->inflight.empty() && !laneIdle(L))
+                return setError(SBG_ERR_STATE, "serving made no progress: a queued request cannot be admitted");
         }
     }
+    return SBG_OK;
 }
 
 int sbg_server_result(sbg_server s, int64_t id, double* y, sbg_request_info* info) {
     if (!s) return setError(SBG_ERR_INVALID, "null server");
-    std::lock_guard<std::mutex> lock(s->mu);
-    auto it = s->byId.find(id);
-    if (it == s->byId.end()) return setError(SBG_ERR_INVALID, "unknown request id");
-    const ServeReq& r = s->reqs[it->second];
+    std::lock_guard<std::mutex> lock0(s->mu);
+    auto li = s->laneOf.find(id);
+    if (li == s->laneOf.end()) return setError(SBG_ERR_INVALID, "unknown request id");
+    ServeLane* L = s->lane[li->second];
+    std::lock_guard<std::mutex> lock(L->mu);
+    auto it = L->byId.find(id);
+    if (it == L->byId.end()) return setError(SBG_ERR_INVALID, "unknown request id");
+    const ServeReq& r = L->reqs[it->second];
     if (info) {
         info->done = r.done ? 1 : 0;
         info->status = r.status;
@@ -850,23 +969,55 @@ int sbg_server_result(sbg_server s, int64_t id, double* y, sbg_request_info* inf
 
 int sbg_server_get_stats(sbg_server s, sbg_server_stats* out) {
     if (!s || !out) return setError(SBG_ERR_INVALID, "null argument");
-    std::lock_guard<std::mutex> lock(s->mu);
-    out->submitted = (int64_t)s->reqs.size();
-    out->completed = s->completed;
-    out->queued = (int64_t)s->sched.queued();
-    out->resident = (int64_t)s->sched.resident();
-    out->peak_resident = s->peakResident;
-    out->ticks = s->tick;
-    out->launches = s->launches;
-    out->body_steps = s->bodySteps;
-    out->device_bytes = s->devBytes;
-    out->max_slots = s->maxSlots;
-    out->chunk_steps = s->chunk;
-    out->gpu_seconds = s->gpuSeconds;
-    out->host_seconds = s->hostSeconds - s->waitSeconds;
+    std::lock_guard<std::mutex> lock0(s->mu);
+    std::memset(out, 0, sizeof *out);
+    double wait = 0;
+    for (ServeLane* L : s->lane) {
+        std::lock_guard<std::mutex> lock(L->mu);
+        out->submitted += (int64_t)L->reqs.size();
+        out->completed += L->completed;
+        out->queued += (int64_t)L->sched.queued();
+        out->resident += (int64_t)L->sched.resident();
+        out->peak_resident += L->peakResident;
+        out->ticks += L->tick;
+        out->launches += L->launches;
+        out->body_steps += L->bodySteps;
+        out->device_bytes += L->devBytes;
+        out->max_slots += L->maxSlots;
+        out->chunk_steps = L->chunk;
+        out->gpu_seconds += L->gpuSeconds;
+        wait += L->waitSeconds;
+        for (int k = 0; k < kNumPools; ++k) {
+            out->pool_capacity[k] += L->sched.pool(k).capacity();
+            out->pool_in_use[k] += L->sched.pool(k).used();
+        }
+    }
+    out->host_seconds = s->hostSeconds - wait - s->pollSeconds;
+    return SBG_OK;
+}
+
+int sbg_server_get_lane_stats(sbg_server s, int32_t lane, sbg_server_stats* out) {
+    if (!s || !out || lane < 0 || lane > 1) return setError(SBG_ERR_INVALID, "bad argument");
+    std::lock_guard<std::mutex> lock0(s->mu);
+    ServeLane* L = s->lane[lane];
+    std::lock_guard<std::mutex> lock(L->mu);
+    std::memset(out, 0, sizeof *out);
+    out->submitted = (int64_t)L->reqs.size();
+    out->completed = L->completed;
+    out->queued = (int64_t)L->sched.queued();
+    out->resident = (int64_t)L->sched.resident();
+    out->peak_resident = L->peakResident;
+    out->ticks = L->tick;
+    out->launches = L->launches;
+    out->body_steps = L->bodySteps;
+    out->device_bytes = L->devBytes;
+    out->max_slots = L->maxSlots;
+    out->chunk_steps = L->chunk;
+    out->gpu_seconds = L->gpuSeconds;
+    out->host_seconds = 0;
     for (int k = 0; k < kNumPools; ++k) {
-        out->pool_capacity[k] = s->sched.pool(k).capacity();
-        out->pool_in_use[k] = s->sched.pool(k).used();
+        out->pool_capacity[k] = L->sched.pool(k).capacity();
+        out->pool_in_use[k] = L->sched.pool(k).used();
     }
     return SBG_OK;
 }

@@ -71,6 +71,15 @@ class Server:
         d["pool_in_use"] = dict(zip(POOLS, list(st.pool_in_use)))
         return d
 
+    def lane_stats(self, lane: int) -> dict:
+        """Stats of one lane: 0 = trees, 1 = trees with loop closures."""
+        st = N.ServerStats()
+        N.check(N.engine_lib().sbg_server_get_lane_stats(self._h, int(lane), C.byref(st)))
+        d = {k: getattr(st, k) for k, _ in N.ServerStats._fields_ if not k.startswith("pool_")}
+        d["pool_capacity"] = dict(zip(POOLS, list(st.pool_capacity)))
+        d["pool_in_use"] = dict(zip(POOLS, list(st.pool_in_use)))
+        return d
+
     def clock(self) -> float:
         return float(N.engine_lib().sbg_server_clock(self._h))
 
