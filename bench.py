@@ -57,7 +57,7 @@ def _args():
     p.add_argument("--serve-seconds", type=float, default=3.0, help="arrival window of the serving stream (0 = skip)")
     p.add_argument("--serve-chunk", type=int, default=64)
     p.add_argument("--serve-budget-gb", type=float, default=40.0)
-    p.add_argument("--serve-deadline", type=float, default=90.0,
+    p.add_argument("--serve-deadline", type=float, default=100.0,
                    help="seconds after the first arrival at which unfinished requests are reported as censored")
     return p.parse_args()
 
@@ -316,16 +316,23 @@ def serving(seconds: float, chunk: int, budget_gb: float, cpu_sample_body_steps:
     t_end = srv.clock()
     lat, body_steps = np.empty(n), 0
     status_bad = censored = 0
+    status_bits = {}
     for i in range(n):
         inf = srv.info(ids[i])
         if inf["done"]:
             lat[i] = inf["done_s"] - (t_start + w.arrivals[i])
             body_steps += inf["nbodies"] * inf["nsteps"]
             status_bad += inf["status"] != 0
+            for bit, name in [(1, "nonfinite"), (2, "singular_d"), (4, "projection_failed"), (8, "cholesky_fail")]:
+                if inf["status"] & bit:
+                    status_bits[name] = status_bits.get(name, 0) + 1
         else:
             lat[i] = t_end - (t_start + w.arrivals[i])
             censored += 1
     st = srv.stats()
+    lanes = {name: {k: v for k, v in srv.lane_stats(li).items() if k in
+                    ("submitted", "completed", "peak_resident", "ticks", "gpu_seconds", "device_bytes")}
+             for li, name in [(0, "trees"), (1, "loop_closures")]}
     wall = t_end - t_start
     offered = body_steps / float(w.arrivals[-1])
     # CPU: requests run alone, one after another, on one core (the oracle)
@@ -345,7 +352,9 @@ def serving(seconds: float, chunk: int, budget_gb: float, cpu_sample_body_steps:
             "completed_requests_per_s": n / wall, "wall_s": wall, "max_queued": int(max_queue),
             "peak_resident": st["peak_resident"], "ticks": st["ticks"], "gpu_launches": st["launches"],
             "gpu_busy_fraction": st["gpu_seconds"] / wall, "host_tick_seconds": st["host_seconds"],
-            "requests_with_status": int(status_bad), "censored": int(censored), "deadline_s": deadline_s,
+            "requests_with_status": int(status_bad), "status_bits": status_bits, "censored": int(censored),
+            "deadline_s": deadline_s,
+            "lanes": lanes,
             "cpu_alone_sequential": {"requests": k, "body_steps_per_s": cpu_bs / max(cpu_t, 1e-9), "cores": 1,
                                      "kind": "port"}}
 

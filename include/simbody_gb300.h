@@ -285,6 +285,10 @@ typedef struct sbg_request_info {
     double  submit_s;   /* server clock (sbg_server_clock) at submission, */
     double  admit_s;    /* at admission (-1 while queued) and */
     double  done_s;     /* when the result reached the host (-1 before) */
+    int32_t attempts;   /* 2: the mixed-precision run failed (non-finite, singular
+                           D or failed projection) and the request was rerun
+                           from its initial state in FP64 */
+    int32_t reserved;
 } sbg_request_info;
 
 typedef struct sbg_server_stats {

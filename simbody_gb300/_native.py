@@ -66,7 +66,8 @@ class ServerConfig(C.Structure):
 
 class RequestInfo(C.Structure):
     _fields_ = [("done", C.c_int32), ("status", C.c_int32), ("nbodies", C.c_int32), ("nsteps", C.c_int32),
-                ("t", C.c_double), ("submit_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double)]
+                ("t", C.c_double), ("submit_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double),
+                ("attempts", C.c_int32), ("reserved", C.c_int32)]
 
 
 class ServerStats(C.Structure):

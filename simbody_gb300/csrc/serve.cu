@@ -146,6 +146,9 @@ struct ServeReq {
     bool done = false;
     double submitS = 0, admitS = -1, doneS = -1;
     int64_t steps = 0;
+    Footprint fp;
+    double cost = 0;       // estimated GPU time per step (stepCost)
+    int32_t attempts = 1;  // 2: rerun in FP64 after the mixed-precision run failed
 };
 
 enum RowTable { R_PARENT = 0, R_INFO, R_QOFF, R_UOFF, R_SREC, R_FBEG, R_FCNT, R_LREC, R_CBEG, R_CCNT, R_CLIST, R_LEV,
@@ -198,6 +201,8 @@ struct ServeLane {
     double hostSeconds = 0;  // time inside sbg_server_tick ...
     double waitSeconds = 0;  // ... of which waiting for a tick in flight
     std::deque<TickRec> inflight;
+    bool retryFailed = false;      // hand failed requests back for an FP64 rerun (mixed-precision tree lane)
+    std::vector<int32_t> retry;    // their indices in reqs
     int64_t tick = 0;
     int64_t launches = 0;
     // requests
@@ -426,6 +431,10 @@ void harvest(ServeLane* s, const TickRec& tr) {
         std::memcpy(r.y.data(), p, r.y.size() * 8);
         std::memcpy(&r.t, p + r.y.size() * 8, 8);
         std::memcpy(&r.status, p + r.y.size() * 8 + 8, 4);
+        if (s->retryFailed && (r.status & (SBG_INST_NONFINITE | SBG_INST_SINGULAR_D | SBG_INST_PROJECTION_FAILED))) {
+            s->retry.push_back(s->byId[pr.first]);  // rerun from y0 in FP64; not done yet
+            continue;
+        }
         r.done = true;
         r.doneS = now;
         r.y0.clear();
@@ -602,6 +611,24 @@ int laneCreate(const sbg_server_config* cfg, int64_t budget, std::chrono::steady
     return SBG_OK;
 }
 
+// Queue a request whose image, footprint and cost are set (the caller holds
+// the lane's mutex).
+int laneEnqueue(ServeLane* s, ServeReq&& r) {
+    if (!s->sched.fitsEver(r.fp))
+        return setError(SBG_ERR_BUDGET, "request needs more device memory than the server's budget provides");
+    int nd = 0;
+    if (imageBytes(r, s->rsz, &nd) + (int64_t)nd * (int64_t)sizeof(CopyDesc) + Stager::controlBytes(1) > s->upCap / 2)
+        return setError(SBG_ERR_BUDGET, "request's tables exceed the server's upload staging");
+    if ((int64_t)(r.nq + r.nu) * 8 + 16 > s->resCap)
+        return setError(SBG_ERR_BUDGET, "request's state exceeds the server's result staging");
+    const int32_t chunk =
+        (int32_t)std::max(1.0, std::min(16.0 * s->chunk, std::floor(s->chunk * kRefCost / std::max(r.cost, 1e-9))));
+    r.sched = s->sched.submit(r.id, r.fp, (int32_t)r.steps, chunk);
+    s->byId[r.id] = r.sched;
+    s->reqs.push_back(std::move(r));
+    return SBG_OK;
+}
+
 // Queue a request on a lane (the caller holds the lane's mutex).
 int laneSubmit(ServeLane* s, int64_t rid, sbg_topology topo, const double* y0, double t0, double h, int32_t nsteps,
                const sbg_integ_opts* opts) {
@@ -620,21 +647,11 @@ int laneSubmit(ServeLane* s, int64_t rid, sbg_topology topo, const double* y0, d
     }
     r.acc = acc;
     r.ctol = ctol > 0 ? ctol : acc / 10;
-    if (!s->sched.fitsEver(fp))
-        return setError(SBG_ERR_BUDGET, "request needs more device memory than the server's budget provides");
-    int nd = 0;
-    if (imageBytes(r, s->rsz, &nd) + (int64_t)nd * (int64_t)sizeof(CopyDesc) + Stager::controlBytes(1) > s->upCap / 2)
-        return setError(SBG_ERR_BUDGET, "request's tables exceed the server's upload staging");
-    if ((int64_t)(r.nq + r.nu) * 8 + 16 > s->resCap)
-        return setError(SBG_ERR_BUDGET, "request's state exceeds the server's result staging");
     r.id = rid;
     r.submitS = s->clock();
-    const double cost = stepCost(*topo, r.loops, r.G);
-    const int32_t chunk = (int32_t)std::max(1.0, std::min(16.0 * s->chunk, std::floor(s->chunk * kRefCost / cost)));
-    r.sched = s->sched.submit(r.id, fp, nsteps, chunk);
-    s->byId[r.id] = r.sched;
-    s->reqs.push_back(std::move(r));
-    return SBG_OK;
+    r.cost = stepCost(*topo, r.loops, r.G);
+    r.fp = fp;
+    return laneEnqueue(s, std::move(r));
 }
 
 int laneIssue(ServeLane* s);
@@ -835,6 +852,41 @@ struct sbg_server_s {
 
 constexpr double kLoopLaneShare = 0.35;  // of the budget
 
+// Requests whose mixed-precision run failed (non-finite, singular D, failed
+// projection) start again from their initial state in the FP64 lane, as the
+// reference's integrator restores the state and reports StepFailed
+// (AbstractIntegratorRep.cpp:426-431); their latency counts from the first
+// submission. Both lanes' mutexes are held by the caller.
+int moveRetries(sbg_server_s* s) {
+    ServeLane* A = s->lane[0];
+    ServeLane* B = s->lane[1];
+    for (int32_t i : A->retry) {
+        ServeReq& a = A->reqs[i];
+        ServeReq r;
+        r.id = a.id;
+        r.loops = true;  // the FP64 lane's level-parallel segment (no constraints: no loop work)
+        r.G = a.G;
+        r.nb = a.nb; r.nq = a.nq; r.nu = a.nu; r.nlevels = a.nlevels; r.nf = a.nf; r.ncons = a.ncons;
+        r.t0 = a.t0; r.h = a.h; r.acc = a.acc; r.ctol = a.ctol; r.pes = a.pes;
+        for (int k = 0; k < 3; ++k) r.grav[k] = a.grav[k];
+        r.rowsI = a.rowsI; r.par64 = a.par64; r.fkw = a.fkw; r.fcoef = a.fcoef; r.fq0 = a.fq0;
+        r.lcons = a.lcons; r.lst = a.lst; r.y0 = a.y0;
+        r.steps = a.steps;
+        r.submitS = a.submitS;
+        r.attempts = 2;
+        r.fp = a.fp;
+        r.fp.units[kPoolLoopScratch] = a.fp.units[kPoolScratch];  // same records, in FP64
+        r.fp.units[kPoolScratch] = 0;
+        r.cost = a.cost * kLoopDriverWeight;
+        if (int rc = laneEnqueue(B, std::move(r))) return rc;
+        s->laneOf[a.id] = 1;
+        a.y0.clear();
+        a.y0.shrink_to_fit();
+    }
+    A->retry.clear();
+    return SBG_OK;
+}
+
 extern "C" {
 
 int sbg_server_create(const sbg_server_config* cfg, sbg_server* out) {
@@ -866,6 +918,7 @@ int sbg_server_create(const sbg_server_config* cfg, sbg_server* out) {
         delete s;
         return rc;
     }
+    s->lane[0]->retryFailed = cfg->precision != SBG_PRECISION_FP64;
     *out = s;
     return SBG_OK;
 }
@@ -913,6 +966,12 @@ int sbg_server_tick(sbg_server s, int32_t* ncompleted) {
             any |= issued || n > 0;
             work |= !L->inflight.empty();  // waiting for a tick in flight can free a lane
         }
+        {
+            std::lock_guard<std::mutex> l0(s->lane[0]->mu);
+            std::lock_guard<std::mutex> l1(s->lane[1]->mu);
+            any |= !s->lane[0]->retry.empty();
+            if (int rc = moveRetries(s)) return rc;
+        }
         if (any || !work) break;
         const auto w0 = std::chrono::steady_clock::now();
         std::this_thread::sleep_for(std::chrono::microseconds(round < 100 ? 20 : 200));
@@ -924,7 +983,7 @@ int sbg_server_tick(sbg_server s, int32_t* ncompleted) {
 
 int sbg_server_drain(sbg_server s) {
     if (!s) return setError(SBG_ERR_INVALID, "null server");
-    for (ServeLane* L : s->lane) {
+    for (ServeLane* L : s->lane) {  // the tree lane first: its failures join the FP64 lane
         for (;;) {
             std::lock_guard<std::mutex> lock(s->mu);
             std::lock_guard<std::mutex> lk(L->mu);
@@ -938,6 +997,10 @@ int sbg_server_drain(sbg_server s) {
             if (!issued && L->inflight.empty() && !laneIdle(L))
                 return setError(SBG_ERR_STATE, "serving made no progress: a queued request cannot be admitted");
         }
+        std::lock_guard<std::mutex> lock(s->mu);
+        std::lock_guard<std::mutex> l0(s->lane[0]->mu);
+        std::lock_guard<std::mutex> l1(s->lane[1]->mu);
+        if (int rc = moveRetries(s)) return rc;
     }
     return SBG_OK;
 }
@@ -961,6 +1024,8 @@ int sbg_server_result(sbg_server s, int64_t id, double* y, sbg_request_info* inf
         info->submit_s = r.submitS;
         info->admit_s = r.admitS;
         info->done_s = r.doneS;
+        info->attempts = r.attempts;
+        info->reserved = 0;
     }
     if (!r.done) return info ? SBG_OK : setError(SBG_ERR_STATE, "request not finished");
     if (y) std::memcpy(y, r.y.data(), r.y.size() * 8);
@@ -972,9 +1037,9 @@ int sbg_server_get_stats(sbg_server s, sbg_server_stats* out) {
     std::lock_guard<std::mutex> lock0(s->mu);
     std::memset(out, 0, sizeof *out);
     double wait = 0;
+    out->submitted = s->nextId - 1;  // FP64 reruns are not new submissions
     for (ServeLane* L : s->lane) {
         std::lock_guard<std::mutex> lock(L->mu);
-        out->submitted += (int64_t)L->reqs.size();
         out->completed += L->completed;
         out->queued += (int64_t)L->sched.queued();
         out->resident += (int64_t)L->sched.resident();

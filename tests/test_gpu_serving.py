@@ -122,3 +122,23 @@ def test_request_larger_than_the_budget_is_rejected(engine, w5, topos):
     with pytest.raises(N.EngineError) as e:
         srv.submit(chain, chain.default_state(), 1e-3, 10)
     assert e.value.code == 4  # SBG_ERR_BUDGET
+
+
+def test_failed_mixed_request_is_rerun_in_fp64(engine, w5, topos):
+    """A mixed-precision request that ends non-finite is rerun from its
+    initial state in the FP64 lane (attempts == 2): here the state itself
+    holds a NaN, so the rerun fails too and reports it; its neighbours are
+    unaffected and keep attempts == 1."""
+    srv = Server("mixed", device_budget_bytes=1 << 30, chunk_steps=16)
+    i_bad, i_ok = 0, 1
+    assert w5.systems[int(w5.instance_system[i_bad])].nconstraints == 0
+    y_bad = w5.y0[w5.instance_slice(i_bad)].copy()
+    y_bad[2] = np.nan
+    rb = srv.submit(topos[i_bad], y_bad, w5.h, 20)
+    ro = srv.submit(topos[i_ok], w5.y0[w5.instance_slice(i_ok)], w5.h, 20)
+    srv.drain()
+    yb, ib = srv.result(rb)
+    yo, io = srv.result(ro)
+    assert ib["attempts"] == 2 and ib["status"] & N.INST_NONFINITE
+    assert io["attempts"] == 1 and io["status"] == 0 and np.isfinite(yo).all()
+    assert srv.stats()["submitted"] == 2
