@@ -66,7 +66,8 @@ enum : int {
 //  24  B[6]                      result of a unit-force sweep (acceleration
 //                                or velocity of the body origin)
 //  30  F[6]                      applied spatial force (torque, force) at Bo
-constexpr int kSlotA = 18, kSlotB = 24, kSlotF = 30, kSlotSize = 36;
+//  36  B[6] x 2, F[6] x 2         columns 1 and 2 of a three-column Gram sweep
+constexpr int kSlotA = 18, kSlotB = 24, kSlotF = 30, kSlotB3 = 36, kSlotF3 = 48, kSlotSize = 60;
 constexpr int kMaxLoopCons = 4;             // Ball constraints per instance
 constexpr int kMaxLoopEq = 3 * kMaxLoopCons;
 constexpr int F_MEMACC = F_MEMCHILD;

@@ -378,6 +378,232 @@ __device__ __forceinline__ void loopSweep(const LoopState& L, const Wt& wt, cons
     loopSweepOut<NM, KIND, FULL_OUT>(L, onBody);
 }
 
+// -------------------------------------------- three Gram columns per sweep
+// The three columns of one Ball constraint (unit forces along x, y, z at the
+// same two points) share one sweep: each row's data is loaded once and its
+// step runs once per column, with each column's arithmetic exactly that of
+// the single-column sweep. Column 0 keeps its values where the single-column
+// sweep does; columns 1 and 2 use fields the tree passes have finished with
+// (the next RHS or kinematics pass refills them):
+//   slot record   F_k (applied force), B_k (outward result)
+//   body record   eps_k, the z accumulator and the outward acceleration
+__device__ __forceinline__ int slotF(int k) { return k == 0 ? kSlotF : kSlotF3 + 6 * (k - 1); }
+__device__ __forceinline__ int slotB(int k) { return k == 0 ? kSlotB : kSlotB3 + 6 * (k - 1); }
+__device__ __forceinline__ int recEpsK(int eEps, int k) { return k == 0 ? eEps : kRecA + 6 * (k - 1); }
+__device__ __forceinline__ int recZaccK(int k) { return k == 0 ? kRecZacc : (k == 1 ? kRecPc : kRecPacc); }
+
+__device__ __forceinline__ void loopZeroAcc3(const LoopState& L) {
+    const DevTables& T = L.T;
+    const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
+    for (int lb = 0; lb < nb; ++lb) {
+        const int row = body0 + lb;
+        if ((T.info[row] & (F_MEMCHILD | F_LOOPPATH)) == (F_MEMCHILD | F_LOOPPATH))
+            for (int k = 0; k < 3; ++k) {
+                st3<double>(L.S, L.rec(row), recZaccK(k), z3<double>());
+                st3<double>(L.S, L.rec(row), recZaccK(k) + 3, z3<double>());
+            }
+    }
+}
+__device__ __forceinline__ void loopClearForces3(const LoopState& L) {
+    const int nc = L.T.incons[L.inst];
+    for (int c = 0; c < nc; ++c) {
+        int s1, s2;
+        loopSlots(L, c, s1, s2);
+        for (int k = 0; k < 3; ++k) {
+            if (s1 >= 0) { st3<double>(L.S, s1, slotF(k), z3<double>()); st3<double>(L.S, s1, slotF(k) + 3, z3<double>()); }
+            if (s2 >= 0) { st3<double>(L.S, s2, slotF(k), z3<double>()); st3<double>(L.S, s2, slotF(k) + 3, z3<double>()); }
+        }
+    }
+}
+__device__ __forceinline__ void loopAddForceK(const SC64& S, int slot, V3d r, V3d F, int k) {
+    if (slot < 0) return;
+    st3<double>(S, slot, slotF(k), ld3<double>(S, slot, slotF(k)) + cross(r, F));
+    st3<double>(S, slot, slotF(k) + 3, ld3<double>(S, slot, slotF(k) + 3) + F);
+}
+
+template <int N, int KIND>
+__device__ __forceinline__ void loopIn3(const LoopState& L, int row, int rec, int n, int info, V3d* zw, V3d* zv) {
+    const SC64& S = L.S;
+    const int eDI = kRecH + 7 * N, eG = eDI + N * N, eEps = eG + 6 * N;
+    if (info & F_LOOPBODY) {
+        const int sl = L.slot(row);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const V3d tw = ld3<double>(S, sl, slotF(k)), tv = ld3<double>(S, sl, slotF(k) + 3);
+            if (KIND == kMInvSweep) { zw[k] = zw[k] - tw; zv[k] = zv[k] - tv; }
+            else { zw[k] = zw[k] + tw; zv[k] = zv[k] + tv; }
+        }
+    }
+    V3d pw[3] = {zw[0], zw[1], zw[2]}, pv[3] = {zv[0], zv[1], zv[2]};
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        if (j < n) {
+            const V3d hw = ld3<double>(S, rec, kRecH + 6 * j), hv = ld3<double>(S, rec, kRecH + 6 * j + 3);
+            V3d gw = z3<double>(), gv = z3<double>();
+            if (KIND == kMInvSweep) { gw = ld3<double>(S, rec, eG + 6 * j); gv = ld3<double>(S, rec, eG + 6 * j + 3); }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const double d = dot(hw, zw[k]) + dot(hv, zv[k]);
+                if (KIND == kMInvSweep) {
+                    const double eps = -d;
+                    S(rec, recEpsK(eEps, k) + j) = eps;
+                    pw[k] = axpy(pw[k], eps, gw);
+                    pv[k] = axpy(pv[k], eps, gv);
+                } else {
+                    S(rec, recEpsK(eEps, k) + j) = d;
+                }
+            }
+        }
+    }
+    const V3d l = ld3<double>(S, rec, kRecL);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        zw[k] = pw[k] + cross(l, pv[k]);
+        zv[k] = pv[k];
+    }
+}
+
+template <int N, int KIND>
+__device__ __forceinline__ void loopOut3(const LoopState& L, int rec, int n, bool hasParent, V3d* Aw, V3d* Av) {
+    const SC64& S = L.S;
+    const int eDI = kRecH + 7 * N, eG = eDI + N * N, eEps = eG + 6 * N;
+    const V3d l = ld3<double>(S, rec, kRecL);
+    V3d Apw[3], Apv[3];
+    double eps[3][N];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        Apw[k] = hasParent ? Aw[k] : z3<double>();
+        Apv[k] = hasParent ? Av[k] + cross(Aw[k], l) : z3<double>();
+#pragma unroll
+        for (int j = 0; j < N; ++j) eps[k][j] = j < n ? S(rec, recEpsK(eEps, k) + j) : 0.0;
+        Aw[k] = Apw[k];
+        Av[k] = Apv[k];
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        if (i < n) {
+            const V3d hw = ld3<double>(S, rec, kRecH + 6 * i), hv = ld3<double>(S, rec, kRecH + 6 * i + 3);
+            V3d gw = z3<double>(), gv = z3<double>();
+            if (KIND == kMInvSweep) { gw = ld3<double>(S, rec, eG + 6 * i); gv = ld3<double>(S, rec, eG + 6 * i + 3); }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                double s;
+                if (KIND == kMInvSweep) {
+                    s = 0.0;
+#pragma unroll
+                    for (int c = 0; c < N; ++c)
+                        if (c < n) s = s + S(rec, eDI + i * N + c) * eps[k][c];
+                    s = s - (dot(gw, Apw[k]) + dot(gv, Apv[k]));
+                } else {
+                    s = eps[k][i];
+                }
+                Aw[k] = axpy(Aw[k], s, hw);
+                Av[k] = axpy(Av[k], s, hv);
+            }
+        }
+    }
+}
+
+template <int KIND>
+__device__ __noinline__ void loopIn36(const LoopState& L, int row, int rec, int info, V3d* zw, V3d* zv) {
+    loopIn3<6, KIND>(L, row, rec, 6, info, zw, zv);
+}
+template <int KIND>
+__device__ __noinline__ void loopOut36(const LoopState& L, int rec, bool hasParent, V3d* Aw, V3d* Av) {
+    loopOut3<6, KIND>(L, rec, 6, hasParent, Aw, Av);
+}
+
+// The three-column sweep over the loop-path rows: inward, then outward with
+// the constrained bodies' results in their slots (B_k).
+template <int NM, int KIND, class Wt>
+__device__ __forceinline__ void loopSweep3(const LoopState& L, const Wt& wt) {
+    const DevTables& T = L.T;
+    const SC64& S = L.S;
+    const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
+    {
+        V3d cw[3], cv[3];
+        bool have = false;
+        for (int lb = nb - 1; lb >= 0; --lb) {
+            const int row = body0 + lb;
+            const int info = T.info[row];
+            if (!(info & F_LOOPPATH)) {
+                have = false;
+                continue;
+            }
+            const int n = (info >> 4) & 15;
+            const int rec = L.rec(row);
+            V3d zw[3], zv[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                zw[k] = z3<double>();
+                zv[k] = z3<double>();
+                if (info & F_MEMCHILD) {
+                    zw[k] = ld3<double>(S, rec, recZaccK(k));
+                    zv[k] = ld3<double>(S, rec, recZaccK(k) + 3);
+                    st3<double>(S, rec, recZaccK(k), z3<double>());
+                    st3<double>(S, rec, recZaccK(k) + 3, z3<double>());
+                }
+                if (have) { zw[k] = zw[k] + cw[k]; zv[k] = zv[k] + cv[k]; }
+            }
+            if (n == 6) loopIn36<KIND>(L, row, rec, info, zw, zv);
+            else loopIn3<NM, KIND>(L, row, rec, n, info, zw, zv);
+            if (KIND == kJacSweep) {
+                const int eEps = recEps(recN(n, NM));
+                for (int k = 0; k < 3; ++k)
+                    for (int j = 0; j < n; ++j)
+                        S(rec, recEpsK(eEps, k) + j) = S(rec, recEpsK(eEps, k) + j) * wt(row, j);
+            }
+            const int parent = T.parent[row];
+            have = (info & F_CARRY) != 0;
+            if (have) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) { cw[k] = zw[k]; cv[k] = zv[k]; }
+            } else if (parent >= 0) {
+                const int pr = L.rec(body0 + parent);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    st3<double>(S, pr, recZaccK(k), ld3<double>(S, pr, recZaccK(k)) + zw[k]);
+                    st3<double>(S, pr, recZaccK(k) + 3, ld3<double>(S, pr, recZaccK(k) + 3) + zv[k]);
+                }
+            }
+        }
+    }
+    {
+        V3d aw[3], av[3];
+        for (int k = 0; k < 3; ++k) { aw[k] = z3<double>(); av[k] = z3<double>(); }
+        for (int lb = 0; lb < nb; ++lb) {
+            const int row = body0 + lb;
+            const int info = T.info[row];
+            if (!(info & F_LOOPPATH)) continue;
+            const int n = (info >> 4) & 15;
+            const int rec = L.rec(row);
+            const int parent = T.parent[row];
+            const bool hp = parent >= 0;
+            V3d pw[3], pv[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { pw[k] = aw[k]; pv[k] = av[k]; }
+            if (hp && !(info & F_CARRY)) {
+                const int pr = L.rec(body0 + parent);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) { pw[k] = ld3<double>(S, pr, 6 * k); pv[k] = ld3<double>(S, pr, 6 * k + 3); }
+            }
+            if (n == 6) loopOut36<KIND>(L, rec, hp, pw, pv);
+            else loopOut3<NM, KIND>(L, rec, n, hp, pw, pv);
+            if (info & F_LOOPBODY)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    st3<double>(S, L.slot(row), slotB(k), pw[k]);
+                    st3<double>(S, L.slot(row), slotB(k) + 3, pv[k]);
+                }
+            if (info & F_MEMCHILD)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) { st3<double>(S, rec, 6 * k, pw[k]); st3<double>(S, rec, 6 * k + 3, pv[k]); }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { aw[k] = pw[k]; av[k] = pv[k]; }
+        }
+    }
+}
+
 // Cholesky of the leading m x m block (row stride kMaxLoopEq), lower factor
 // in place; then the two triangular solves.
 __device__ __forceinline__ bool loopCholFactor(int m, double* A) {
@@ -408,23 +634,30 @@ __device__ __forceinline__ void loopCholSolve(int m, const double* A, double* b)
     }
 }
 
-// Column j of G W G^T (kJacSweep) or G M^-1 G^T (kMInvSweep) for every j.
+// Column j of G W G^T (kJacSweep) or G M^-1 G^T (kMInvSweep) for every j,
+// three columns (one constraint) per sweep.
 template <int NM, int KIND, class Wt>
 __device__ __forceinline__ void loopGram(const LoopState& L, const Wt& wt, double* A) {
-    const int nc = L.T.incons[L.inst], m = 3 * nc;
-    auto none = [](int, int, const double*) {};
-    for (int j = 0; j < m; ++j) {
-        loopClearForces(L);
-        V3d e = z3<double>();
-        if (j % 3 == 0) e.x = 1.0; else if (j % 3 == 1) e.y = 1.0; else e.z = 1.0;
-        loopAddConstraintForce(L, loopGeom(L, j / 3), e);
-        loopSweep<NM, KIND>(L, wt, none);
+    const int nc = L.T.incons[L.inst];
+    loopZeroAcc3(L);  // the accumulators of columns 1 and 2 held tree-pass values
+    for (int c = 0; c < nc; ++c) {
+        loopClearForces3(L);
+        const LoopGeom Gc = loopGeom(L, c);
+        for (int k = 0; k < 3; ++k) {
+            V3d e = z3<double>();
+            if (k == 0) e.x = 1.0; else if (k == 1) e.y = 1.0; else e.z = 1.0;
+            loopAddForceK(L.S, Gc.s2, Gc.r2, e, k);
+            loopAddForceK(L.S, Gc.s1, Gc.r1, -e, k);
+        }
+        loopSweep3<NM, KIND>(L, wt);
         for (int i = 0; i < nc; ++i) {
             const LoopGeom G = loopGeom(L, i);
-            const V3d d = slotPoint(L.S, G.s2, kSlotB, G.r2) - slotPoint(L.S, G.s1, kSlotB, G.r1);
-            A[(3 * i + 0) * kMaxLoopEq + j] = d.x;
-            A[(3 * i + 1) * kMaxLoopEq + j] = d.y;
-            A[(3 * i + 2) * kMaxLoopEq + j] = d.z;
+            for (int k = 0; k < 3; ++k) {
+                const V3d d = slotPoint(L.S, G.s2, slotB(k), G.r2) - slotPoint(L.S, G.s1, slotB(k), G.r1);
+                A[(3 * i + 0) * kMaxLoopEq + 3 * c + k] = d.x;
+                A[(3 * i + 1) * kMaxLoopEq + 3 * c + k] = d.y;
+                A[(3 * i + 2) * kMaxLoopEq + 3 * c + k] = d.z;
+            }
         }
     }
 }
