@@ -54,10 +54,10 @@ def _args():
     p.add_argument("--arm", default="all", choices=["all", "mixed", "fp64"],
                    help="profiling aid: time only this form's realize (no e2e, no CPU baseline)")
     p.add_argument("--no-trajectories", action="store_true")
-    p.add_argument("--serve-seconds", type=float, default=3.0, help="arrival window of the serving stream (0 = skip)")
+    p.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window of the serving stream (0 = skip)")
     p.add_argument("--serve-chunk", type=int, default=64)
     p.add_argument("--serve-budget-gb", type=float, default=40.0)
-    p.add_argument("--serve-deadline", type=float, default=100.0,
+    p.add_argument("--serve-deadline", type=float, default=90.0,
                    help="seconds after the first arrival at which unfinished requests are reported as censored")
     return p.parse_args()
 
@@ -284,30 +284,37 @@ def trajectories():
     return out
 
 
-def serving(seconds: float, chunk: int, budget_gb: float, cpu_sample_body_steps: float, deadline_s: float):
-    """The serving stream: Poisson arrivals at 2,000 requests/s for
-    `seconds`, trees from the uneven-batch distribution, horizons
-    log-uniform in [100, 10000] steps, 20% with 1-4 Ball loop closures;
-    continuous batching with a device budget. Latency = time the result
-    reached the host - scheduled arrival. Requests still running
-    `deadline_s` after the first arrival are reported as censored: their
-    latency enters the percentiles as the time waited so far (a lower
-    bound), and `censored` says how many there were."""
+def serving(seconds: float, chunk: int, budget_gb: float, cpu_sample_body_steps: float, deadline_s: float,
+            rate: float = 2000.0, trees_only: bool = False):
+    """The serving stream: Poisson arrivals at `rate` requests/s (2,000 in
+    the configuration) for `seconds`, trees from the uneven-batch
+    distribution, horizons log-uniform in [100, 10000] steps, 20% with 1-4
+    Ball loop closures (none with `trees_only`); continuous batching with a
+    device budget. Latency = time the result reached the host - scheduled
+    arrival. Requests still running `deadline_s` after the first arrival are
+    reported as censored: their latency enters the percentiles as the time
+    waited so far (a lower bound), and `censored` says how many there were."""
     from oracle import oracle as O
     from simbody_gb300 import Server, Topology, Workload
 
-    n = int(round(2000 * seconds))
-    w = Workload(5, n)
-    topos = [Topology(w.systems[int(w.instance_system[i])], keepalive=w) for i in range(n)]
+    want = int(round(rate * seconds))
+    w = Workload(5, int(want * (1.3 if trees_only else 1.0)) + 8)
+    keep = [i for i in range(w.ninst) if not (trees_only and w.systems[int(w.instance_system[i])].nconstraints)]
+    keep = keep[:want]
+    n = len(keep)
+    # the workload's arrivals are a 2,000/s Poisson stream: rescaled to `rate`
+    arrivals = np.array([w.arrivals[i] for i in keep]) * (2000.0 / rate)
+    arrivals -= arrivals[0] - w.arrivals[0] * (2000.0 / rate)
+    topos = [Topology(w.systems[int(w.instance_system[i])], keepalive=w) for i in keep]
     srv = Server("mixed", device_budget_bytes=int(budget_gb * (1 << 30)), chunk_steps=chunk)
     ids = np.zeros(n, dtype=np.int64)
     t_start = srv.clock()
     nxt, max_queue = 0, 0
     while nxt < n:
         now = srv.clock() - t_start
-        while nxt < n and w.arrivals[nxt] <= now:
-            i = nxt
-            ids[i] = srv.submit(topos[i], w.y0[w.instance_slice(i)], w.h, int(w.horizons[i]))
+        while nxt < n and arrivals[nxt] <= now:
+            i = keep[nxt]
+            ids[nxt] = srv.submit(topos[nxt], w.y0[w.instance_slice(i)], w.h, int(w.horizons[i]))
             nxt += 1
         srv.tick()
         max_queue = max(max_queue, srv.stats()["queued"])
@@ -320,38 +327,42 @@ def serving(seconds: float, chunk: int, budget_gb: float, cpu_sample_body_steps:
     for i in range(n):
         inf = srv.info(ids[i])
         if inf["done"]:
-            lat[i] = inf["done_s"] - (t_start + w.arrivals[i])
+            lat[i] = inf["done_s"] - (t_start + arrivals[i])
             body_steps += inf["nbodies"] * inf["nsteps"]
             status_bad += inf["status"] != 0
             for bit, name in [(1, "nonfinite"), (2, "singular_d"), (4, "projection_failed"), (8, "cholesky_fail")]:
                 if inf["status"] & bit:
                     status_bits[name] = status_bits.get(name, 0) + 1
         else:
-            lat[i] = t_end - (t_start + w.arrivals[i])
+            lat[i] = t_end - (t_start + arrivals[i])
             censored += 1
     st = srv.stats()
     lanes = {name: {k: v for k, v in srv.lane_stats(li).items() if k in
                     ("submitted", "completed", "peak_resident", "ticks", "gpu_seconds", "device_bytes")}
              for li, name in [(0, "trees"), (1, "loop_closures")]}
     wall = t_end - t_start
-    offered = body_steps / float(w.arrivals[-1])
+    nbod = w.nbodies()
+    offered = float(sum(int(nbod[i]) * int(w.horizons[i]) for i in keep)) / float(arrivals[-1])
     # CPU: requests run alone, one after another, on one core (the oracle)
     cpu_t, cpu_bs, k = 0.0, 0, 0
     while k < n and cpu_bs < cpu_sample_body_steps:
+        i = keep[k]
         t0 = time.perf_counter()
-        O.rk_workload(w, w.h, int(w.horizons[k]), instances=[k], nthreads=1)
+        O.rk_workload(w, w.h, int(w.horizons[i]), instances=[i], nthreads=1)
         cpu_t += time.perf_counter() - t0
-        cpu_bs += int(w.nbodies()[k]) * int(w.horizons[k])
+        cpu_bs += int(nbod[i]) * int(w.horizons[i])
         k += 1
     srv.close()
-    return {"requests": n, "arrival_rate_per_s": 2000, "arrival_window_s": float(w.arrivals[-1]),
+    return {"requests": n, "arrival_rate_per_s": rate, "arrival_window_s": float(arrivals[-1]),
+            "requests_with_loop_closures": int(sum(w.systems[int(w.instance_system[i])].nconstraints > 0
+                                                   for i in keep)),
             "precision": "mixed", "chunk_steps": chunk, "device_budget_bytes": st["device_bytes"],
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "mean": float(lat.mean()), "max": float(lat.max())},
             "throughput_body_steps_per_s": body_steps / wall, "offered_body_steps_per_s": offered,
-            "completed_requests_per_s": n / wall, "wall_s": wall, "max_queued": int(max_queue),
+            "completed_requests_per_s": (n - censored) / wall, "wall_s": wall, "max_queued": int(max_queue),
             "peak_resident": st["peak_resident"], "ticks": st["ticks"], "gpu_launches": st["launches"],
-            "gpu_busy_fraction": st["gpu_seconds"] / wall, "host_tick_seconds": st["host_seconds"],
+            "host_tick_seconds": st["host_seconds"],
             "requests_with_status": int(status_bad), "status_bits": status_bits, "censored": int(censored),
             "deadline_s": deadline_s,
             "lanes": lanes,
@@ -476,6 +487,14 @@ def run_ours(args):
                                         args.serve_deadline)
         except Exception as e:  # noqa: BLE001
             result["serving"] = {"error": repr(e)}
+        # the tree lane alone at a rate it sustains (the loop-closure lane
+        # saturates far below 2,000 req/s; see the loop lane's numbers above)
+        try:
+            result["serving_trees_sustained"] = serving(args.serve_seconds * 4, args.serve_chunk,
+                                                        args.serve_budget_gb, 0, args.serve_deadline,
+                                                        rate=500.0, trees_only=True)
+        except Exception as e:  # noqa: BLE001
+            result["serving_trees_sustained"] = {"error": repr(e)}
     if rank == 0:
         print(json.dumps(result))
     if world > 1:
