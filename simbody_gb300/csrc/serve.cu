@@ -44,6 +44,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -82,12 +83,19 @@ using namespace sbg;
 
 namespace {
 
-constexpr int kLanesShift = 1;  // G = pow2ceil(widest level) >> 1, in [2, 32]
+// Lanes per request: G = pow2ceil(widest level) >> shift, in [2, 32].
+int lanesShift() {
+    static const int shift = [] {
+        const char* v = std::getenv("SBG_SERVE_LANES_SHIFT");  // tuning override
+        return v ? std::max(0, std::min(3, std::atoi(v))) : 0;  // all lanes: latency over throughput
+    }();
+    return shift;
+}
 
 int groupLanes(const sbg_topology_s& t) {
     int w = 1;
     while (w < t.maxLevelWidth) w <<= 1;
-    return std::max(2, std::min(32, w >> kLanesShift));
+    return std::max(2, std::min(32, w >> lanesShift()));
 }
 
 // Relative GPU time of one RK-Merson step of a request, in serial body
