@@ -339,7 +339,7 @@ def serving(seconds: float, chunk: int, budget_gb: float, cpu_sample_body_steps:
     st = srv.stats()
     lanes = {name: {k: v for k, v in srv.lane_stats(li).items() if k in
                     ("submitted", "completed", "peak_resident", "ticks", "gpu_seconds", "device_bytes")}
-             for li, name in [(0, "trees"), (1, "loop_closures")]}
+             for li, name in [(0, "trees"), (1, "fp64_cheaper"), (2, "fp64_costlier")]}
     wall = t_end - t_start
     nbod = w.nbodies()
     offered = float(sum(int(nbod[i]) * int(w.horizons[i]) for i in keep)) / float(arrivals[-1])

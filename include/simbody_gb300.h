@@ -257,11 +257,14 @@ int sbg_batch_group_lanes_shift(sbg_batch batch);
  * after their tick and queued ones (strict arrival order) take their slots
  * and memory. The server allocates its whole device budget once, at
  * creation (device arena split into table, state and scratch pools); a
- * request is admitted only while its share fits. Requests with loop
- * closures (FP64, far more work per step) run in a lane of their own, with
- * its own share of the budget and slots (35 %) and its own tick cadence, so
- * the other requests never wait on them. A request's result does not
- * depend on which other requests share its ticks. */
+ * request is admitted only while its share fits. The server runs three
+ * lanes, each with its own share of the budget and slots and its own tick
+ * cadence, so that requests never wait on much costlier ones: lane 0 the
+ * trees without loop closures (the server's precision), lanes 1 and 2 in
+ * FP64 the trees with loop closures, split by estimated cost per step.
+ * A mixed-precision request that fails is rerun from its initial state in
+ * FP64 (sbg_request_info.attempts). A request's result does not depend on
+ * which other requests share its ticks. */
 typedef struct sbg_server_s* sbg_server;
 
 typedef struct sbg_server_config {
@@ -269,7 +272,7 @@ typedef struct sbg_server_config {
                                      closures always run in FP64 */
     int32_t device;               /* CUDA device ordinal */
     int64_t device_budget_bytes;  /* device memory the server holds (> 0) */
-    int32_t max_slots;            /* resident requests at most (0 = 65536; >= 2) */
+    int32_t max_slots;            /* resident requests at most (0 = 65536; >= 3) */
     int32_t chunk_steps;          /* RK steps per tick of a request of median
                                      cost (0 = 64); each request's own chunk
                                      scales with the inverse of its estimated
@@ -321,7 +324,8 @@ int sbg_server_drain(sbg_server server);
  * info given, an unfinished request returns SBG_OK and done = 0. */
 int sbg_server_result(sbg_server server, int64_t request_id, double* y, sbg_request_info* info);
 int sbg_server_get_stats(sbg_server server, sbg_server_stats* stats);
-/* The same for one lane: 0 = trees, 1 = trees with loop closures. */
+/* The same for one lane: 0 = trees, 1 / 2 = FP64 lanes (loop closures and
+ * reruns; cheaper / costlier per step). */
 int sbg_server_get_lane_stats(sbg_server server, int32_t lane, sbg_server_stats* stats);
 /* Seconds since the server was created: the clock of sbg_request_info. */
 double sbg_server_clock(sbg_server server);

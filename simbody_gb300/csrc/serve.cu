@@ -501,7 +501,7 @@ int laneCreate(const sbg_server_config* cfg, int64_t budget, std::chrono::steady
     // Fixed part: slots, staging (device side), then the pools share the rest.
     const int64_t S = s->maxSlots;
     const int64_t slotBytes = S * (14 * 4 + 4 * 8 + (3 + 3 + 1) * 8 + kMaxLoopCons * (2 * 4 + 6 * 8)) + 2 * (S + 2) * 4;
-    s->upCap = std::max<int64_t>(1 << 20, std::min<int64_t>(64 << 20, s->budget / 16));
+    s->upCap = std::max<int64_t>(512 << 10, std::min<int64_t>(64 << 20, s->budget / 16));
     s->resCap = s->upCap;
     const int64_t fixed = slotBytes + s->upCap + s->resCap;
     if (fixed >= s->budget) return bail(setError(SBG_ERR_BUDGET, "device budget too small for the server's slots and staging"));
@@ -837,14 +837,21 @@ bool laneIdle(const ServeLane* s) { return s->sched.queued() == 0 && s->sched.re
 
 }  // namespace
 
-// The server: two lanes with independent tick cadences, so that requests of
-// very different cost per step do not wait on each other. Lane 0 runs the
-// trees without loop closures (level-parallel driver, the server's
-// precision), lane 1 the trees with Ball loop closures (FP64, multiplier
-// solve and projections). The budget is split between them in proportion
-// to their expected share of the arena.
+// The server: lanes with independent tick cadences, so that requests of very
+// different cost per step do not wait on each other (a tick lasts at least
+// one step of its costliest request). Lane 0 runs the trees without loop
+// closures (level-parallel driver, the server's precision); lanes 1 and 2
+// run in FP64 the trees with Ball loop closures (multiplier solve and
+// projections) and the reruns of failed mixed-precision requests, split by
+// estimated cost per step at kSplitCost. The budget and the slots are split
+// in proportion to the lanes' expected share of the arena.
+constexpr int kLanes = 3;
+constexpr double kLaneShare[kLanes] = {0.65, 0.20, 0.15};
+constexpr double kSplitCost = 200.0;  // stepCost units: about the median loop-closure request
+int fp64Lane(double cost) { return cost <= kSplitCost ? 1 : 2; }
+
 struct sbg_server_s {
-    ServeLane* lane[2] = {nullptr, nullptr};
+    ServeLane* lane[kLanes] = {nullptr, nullptr, nullptr};
     std::mutex mu;
     int64_t nextId = 1;
     std::unordered_map<int64_t, int> laneOf;
@@ -852,22 +859,18 @@ struct sbg_server_s {
     double hostSeconds = 0;  // inside sbg_server_tick ...
     double pollSeconds = 0;  // ... of which waiting for a lane to free up
     ~sbg_server_s() {
-        delete lane[0];
-        delete lane[1];
+        for (ServeLane* L : lane) delete L;
     }
     double clock() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
 };
-
-constexpr double kLoopLaneShare = 0.35;  // of the budget
 
 // Requests whose mixed-precision run failed (non-finite, singular D, failed
 // projection) start again from their initial state in the FP64 lane, as the
 // reference's integrator restores the state and reports StepFailed
 // (AbstractIntegratorRep.cpp:426-431); their latency counts from the first
-// submission. Both lanes' mutexes are held by the caller.
+// submission. Every lane's mutex is held by the caller.
 int moveRetries(sbg_server_s* s) {
     ServeLane* A = s->lane[0];
-    ServeLane* B = s->lane[1];
     for (int32_t i : A->retry) {
         ServeReq& a = A->reqs[i];
         ServeReq r;
@@ -886,8 +889,9 @@ int moveRetries(sbg_server_s* s) {
         r.fp.units[kPoolLoopScratch] = a.fp.units[kPoolScratch];  // same records, in FP64
         r.fp.units[kPoolScratch] = 0;
         r.cost = a.cost * kLoopDriverWeight;
-        if (int rc = laneEnqueue(B, std::move(r))) return rc;
-        s->laneOf[a.id] = 1;
+        const int li = fp64Lane(r.cost);
+        if (int rc = laneEnqueue(s->lane[li], std::move(r))) return rc;
+        s->laneOf[a.id] = li;
         a.y0.clear();
         a.y0.shrink_to_fit();
     }
@@ -913,18 +917,23 @@ int sbg_server_create(const sbg_server_config* cfg, sbg_server* out) {
     SBG_SCUDA(cudaSetDevice(cfg->device), "cudaSetDevice");
     auto* s = new (std::nothrow) sbg_server_s();
     if (!s) return setError(SBG_ERR_NOMEM, "out of host memory");
-    const int64_t loopBudget = (int64_t)(cfg->device_budget_bytes * kLoopLaneShare);
     const int32_t slots = cfg->max_slots > 0 ? cfg->max_slots : 65536;
-    if (slots < 2) return setError(SBG_ERR_INVALID, "the server needs at least two slots (one per lane)");
-    const int32_t loopSlots = std::max(1, std::min(slots - 1, (int32_t)std::lround(slots * kLoopLaneShare)));
-    sbg_server_config c0 = *cfg, c1 = *cfg;
-    c0.max_slots = slots - loopSlots;
-    c1.max_slots = loopSlots;
-    int rc = laneCreate(&c0, cfg->device_budget_bytes - loopBudget, s->t0, &s->lane[0]);
-    if (rc == SBG_OK) rc = laneCreate(&c1, loopBudget, s->t0, &s->lane[1]);
-    if (rc) {
+    if (slots < kLanes) {
         delete s;
-        return rc;
+        return setError(SBG_ERR_INVALID, "the server needs at least " + std::to_string(kLanes) + " slots (one per lane)");
+    }
+    int32_t left = slots;
+    int64_t budgetLeft = cfg->device_budget_bytes;
+    for (int li = kLanes - 1; li >= 0; --li) {  // lane 0 takes what the others leave
+        sbg_server_config c = *cfg;
+        c.max_slots = li == 0 ? left : std::max(1, std::min(left - li, (int32_t)std::lround(slots * kLaneShare[li])));
+        const int64_t budget = li == 0 ? budgetLeft : (int64_t)(cfg->device_budget_bytes * kLaneShare[li]);
+        left -= c.max_slots;
+        budgetLeft -= budget;
+        if (int rc = laneCreate(&c, budget, s->t0, &s->lane[li])) {
+            delete s;
+            return rc;
+        }
     }
     s->lane[0]->retryFailed = cfg->precision != SBG_PRECISION_FP64;
     *out = s;
@@ -944,7 +953,8 @@ int sbg_server_submit(sbg_server s, sbg_topology topo, const double* y0, double 
     if (topo->ncons > kMaxLoopCons)
         return setError(SBG_ERR_UNSUPPORTED, "at most " + std::to_string(kMaxLoopCons) + " Ball loop closures per system");
     std::lock_guard<std::mutex> lock(s->mu);
-    const int li = topo->ncons > 0 ? 1 : 0;
+    const bool loops = topo->ncons > 0;
+    const int li = loops ? fp64Lane(stepCost(*topo, true, groupLanes(*topo))) : 0;
     ServeLane* L = s->lane[li];
     std::lock_guard<std::mutex> lk(L->mu);
     const int64_t rid = s->nextId;
@@ -977,6 +987,7 @@ int sbg_server_tick(sbg_server s, int32_t* ncompleted) {
         {
             std::lock_guard<std::mutex> l0(s->lane[0]->mu);
             std::lock_guard<std::mutex> l1(s->lane[1]->mu);
+            std::lock_guard<std::mutex> l2(s->lane[2]->mu);
             any |= !s->lane[0]->retry.empty();
             if (int rc = moveRetries(s)) return rc;
         }
@@ -991,7 +1002,7 @@ int sbg_server_tick(sbg_server s, int32_t* ncompleted) {
 
 int sbg_server_drain(sbg_server s) {
     if (!s) return setError(SBG_ERR_INVALID, "null server");
-    for (ServeLane* L : s->lane) {  // the tree lane first: its failures join the FP64 lane
+    for (ServeLane* L : s->lane) {  // the tree lane first: its failures join the FP64 lanes
         for (;;) {
             std::lock_guard<std::mutex> lock(s->mu);
             std::lock_guard<std::mutex> lk(L->mu);
@@ -1008,6 +1019,7 @@ int sbg_server_drain(sbg_server s) {
         std::lock_guard<std::mutex> lock(s->mu);
         std::lock_guard<std::mutex> l0(s->lane[0]->mu);
         std::lock_guard<std::mutex> l1(s->lane[1]->mu);
+        std::lock_guard<std::mutex> l2(s->lane[2]->mu);
         if (int rc = moveRetries(s)) return rc;
     }
     return SBG_OK;
@@ -1070,7 +1082,7 @@ int sbg_server_get_stats(sbg_server s, sbg_server_stats* out) {
 }
 
 int sbg_server_get_lane_stats(sbg_server s, int32_t lane, sbg_server_stats* out) {
-    if (!s || !out || lane < 0 || lane > 1) return setError(SBG_ERR_INVALID, "bad argument");
+    if (!s || !out || lane < 0 || lane >= kLanes) return setError(SBG_ERR_INVALID, "bad argument");
     std::lock_guard<std::mutex> lock0(s->mu);
     ServeLane* L = s->lane[lane];
     std::lock_guard<std::mutex> lock(L->mu);

@@ -72,7 +72,9 @@ class Server:
         return d
 
     def lane_stats(self, lane: int) -> dict:
-        """Stats of one lane: 0 = trees, 1 = trees with loop closures."""
+        """Stats of one lane: 0 = trees, 1 / 2 = the FP64 lanes (loop closures
+        and reruns of failed mixed-precision requests; cheaper / costlier per
+        step)."""
         st = N.ServerStats()
         N.check(N.engine_lib().sbg_server_get_lane_stats(self._h, int(lane), C.byref(st)))
         d = {k: getattr(st, k) for k, _ in N.ServerStats._fields_ if not k.startswith("pool_")}

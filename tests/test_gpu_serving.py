@@ -90,7 +90,7 @@ def test_server_matches_batch_integration(engine, w5, topos, precision, tol):
 
 def test_small_budget_limits_residency_not_results(engine, w5, topos):
     big = run(Server("mixed", device_budget_bytes=1 << 30, chunk_steps=16), w5, topos, range(NREQ))
-    small = Server("mixed", device_budget_bytes=16 << 20, max_slots=6, chunk_steps=16)
+    small = Server("mixed", device_budget_bytes=48 << 20, max_slots=6, chunk_steps=16)
     res = run(small, w5, topos, range(NREQ))
     st = small.stats()
     assert st["peak_resident"] <= 6 and st["completed"] == NREQ
@@ -101,14 +101,14 @@ def test_small_budget_limits_residency_not_results(engine, w5, topos):
 
 
 def test_request_larger_than_the_budget_is_rejected(engine, w5, topos):
-    srv = Server("mixed", device_budget_bytes=12 << 20, max_slots=4)
+    srv = Server("mixed", device_budget_bytes=48 << 20, max_slots=4)
     big = max(range(NREQ), key=lambda i: topos[i].nbodies)
-    # fill nothing; a budget this small still has room for one tree...
+    # a small budget still has room for the largest tree of the stream...
     srv.submit(topos[big], w5.y0[w5.instance_slice(big)], w5.h, 3)
     srv.drain()
     assert srv.result(1) is not None
-    # ...but a 4096-body chain does not fit it
-    n = 4096
+    # ...but a 20,000-body chain does not fit it
+    n = 20000
     bodies = (N.BodyDesc * n)()
     for k in range(n):
         b = bodies[k]
