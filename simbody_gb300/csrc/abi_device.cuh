@@ -911,8 +911,8 @@ __device__ __forceinline__ int rhsChain(const DevTables& T, int inst, const SC& 
 // Returns SBG_INST_* bits (identical on every lane of the group).
 // LOOPS also writes the slot records of the loop bodies (rows nb + slot of S):
 // kinematics in pass 1, A_GB in pass 3.
-template <class R, int NM, bool REF, bool LOOPS = false, class Src, class Out>
-__device__ __noinline__ int rhsGroup(const DevTables& T, int inst, const ScrRows<R>& S, const Src& src, Out& out,
+template <class R, int NM, bool REF, bool LOOPS = false, class SC, class Src, class Out>
+__device__ __noinline__ int rhsGroup(const DevTables& T, int inst, const SC& S, const Src& src, Out& out,
                                      int gl, int G, unsigned mask) {
     static_assert(!REF || std::is_same<R, float>::value, "refinement is for the FP32 recursion");
     const int body0 = T.ibody[inst];
@@ -1114,7 +1114,9 @@ __device__ __forceinline__ int rhs(const DevTables& T, const Slot& s, R* scratch
         if constexpr (GROUP) {
             // tree passes on the group's lanes; the multiplier solve and the
             // constraint sweeps (loop paths only) on its first lane
-            const ScrRows<double> S{rec0, loopRows(T, s.inst)};
+            // record-major rows (the first lane's serial loop work touches a
+            // few records many times: they stay in L1)
+            const ScrGen S{rec0, (int)T.sstride[s.inst], 1};
             int st = rhsGroup<double, NM, false, true>(T, s.inst, S, src, out, s.gl, s.G, s.mask);
             if (T.incons[s.inst] > 0) {
                 const LoopState L = loopStateRows(T, s.inst, rec0, nullptr, nullptr, nullptr, 0, 0);

@@ -41,8 +41,9 @@
 
 // Loop-closure records through either driver's layout: element f of record
 // rec at rec * a + f * b, with (a, b) = (s, s) for the interleaved tiles of
-// the one-thread driver (stride s) and (1, P) for the field-major rows of the
-// level-parallel driver (P rows: the bodies, then the slot records).
+// the one-thread driver (stride s) and (W, 1) for the record-major rows of
+// the level-parallel driver (record width W; the bodies, then the slot
+// records).
 struct ScrGen {
     double* p;
     int a, b;
@@ -74,10 +75,13 @@ __device__ __forceinline__ LoopState loopStateChain(const DevTables& T, int inst
                                                     double* save, double* delta, int64_t base, int64_t stride) {
     return LoopState{T, inst, SC64{scratch, s, s}, y, save, delta, base, stride, false, T.ibody[inst], T.inb[inst]};
 }
+// The level-parallel layout of an instance with loop closures: one record
+// per row (the bodies, then 2 slot records per constraint), record-major
+// with the record width in T.sstride (element f of row r at r * W + f).
 __device__ __forceinline__ int loopRows(const DevTables& T, int inst) { return T.inb[inst] + 2 * T.incons[inst]; }
 __device__ __forceinline__ LoopState loopStateRows(const DevTables& T, int inst, double* scratch, double* y,
                                                    double* save, double* delta, int64_t base, int64_t stride) {
-    return LoopState{T, inst, SC64{scratch, 1, loopRows(T, inst)}, y, save, delta, base, stride, true,
+    return LoopState{T, inst, SC64{scratch, (int)T.sstride[inst], 1}, y, save, delta, base, stride, true,
                      T.ibody[inst], T.inb[inst]};
 }
 

@@ -136,6 +136,7 @@ struct ServeReq {
     bool loops = false;
     int32_t G = 2;
     int nb = 0, nq = 0, nu = 0, nlevels = 0, nf = 0, ncons = 0;
+    int64_t recW = 0;            // record width of the level-parallel layout
     double t0 = 0, h = 0, acc = 1e-3, ctol = 1e-4;
     bool pes = false;
     double grav[3] = {0, 0, 0};
@@ -318,8 +319,9 @@ void buildImage(const sbg_topology_s& t, ServeReq& r, Footprint& fp) {
     fp.units[kPoolState] = t.nq + t.nu;
     // level-parallel records: one row per body (loop closures: then the
     // slot rows, 2 per constraint), FP64 for loop closures
-    if (r.loops) fp.units[kPoolLoopScratch] = (int64_t)(nb + 2 * t.ncons) * rowsRecordWidth(t, 3);
-    else fp.units[kPoolScratch] = (int64_t)nb * rowsRecordWidth(t, 3);
+    r.recW = rowsRecordWidth(t, 3);
+    if (r.loops) fp.units[kPoolLoopScratch] = (int64_t)(nb + 2 * t.ncons) * r.recW;
+    else fp.units[kPoolScratch] = (int64_t)nb * r.recW;
 }
 
 // Upload staging of one tick: raw bytes plus the copy descriptors that move
@@ -409,6 +411,8 @@ void stageRequest(ServeLane* s, Stager& st, ServeReq& r, const SchedRequest& sr)
     const int32_t ib = (int32_t)row0, nb = r.nb, nq = r.nq, nu = r.nu, nlev = r.nlevels,
                   ic = slot * kMaxLoopCons, nc = r.ncons, zero = 0;
     const int64_t yb = y0, one = 1, sb = r.loops ? sr.off[kPoolLoopScratch] : sr.off[kPoolScratch];
+    // FP64 lanes: record-major rows of width recW; trees: field-major (sstride unused)
+    const int64_t sst = r.loops ? r.recW : 1;
     const double par[3] = {r.h, r.acc, r.ctol};
     st.put(&ib, 4, s->ibody + slot);
     st.put(&nb, 4, s->inb + slot);
@@ -421,7 +425,7 @@ void stageRequest(ServeLane* s, Stager& st, ServeReq& r, const SchedRequest& sr)
     st.put(&yb, 8, s->ybase + slot);
     st.put(&one, 8, s->ystride + slot);
     st.put(&sb, 8, s->sbase + slot);
-    st.put(&one, 8, s->sstride + slot);
+    st.put(&sst, 8, s->sstride + slot);
     st.put(r.grav, 24, s->grav + 3 * (int64_t)slot);
     st.put(par, 24, s->iparam + 3 * (int64_t)slot);
     st.put(&r.t0, 8, s->time + slot);
@@ -878,6 +882,7 @@ int moveRetries(sbg_server_s* s) {
         r.loops = true;  // the FP64 lane's level-parallel segment (no constraints: no loop work)
         r.G = a.G;
         r.nb = a.nb; r.nq = a.nq; r.nu = a.nu; r.nlevels = a.nlevels; r.nf = a.nf; r.ncons = a.ncons;
+        r.recW = a.recW;
         r.t0 = a.t0; r.h = a.h; r.acc = a.acc; r.ctol = a.ctol; r.pes = a.pes;
         for (int k = 0; k < 3; ++k) r.grav[k] = a.grav[k];
         r.rowsI = a.rowsI; r.par64 = a.par64; r.fkw = a.fkw; r.fcoef = a.fcoef; r.fq0 = a.fq0;
