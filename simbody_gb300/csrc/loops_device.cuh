@@ -44,11 +44,12 @@
 // the one-thread driver (stride s) and (W, 1) for the record-major rows of
 // the level-parallel driver (record width W; the bodies, then the slot
 // records).
-struct ScrGen {
-    double* p;
+template <class R> struct ScrGenT {
+    R* p;
     int a, b;
-    __device__ __forceinline__ double& operator()(int rec, int f) const { return p[rec * a + f * b]; }
+    __device__ __forceinline__ R& operator()(int rec, int f) const { return p[rec * a + f * b]; }
 };
+using ScrGen = ScrGenT<double>;
 using SC64 = ScrGen;
 using V3d = V3<double>;
 

@@ -411,7 +411,9 @@ void stageRequest(ServeLane* s, Stager& st, ServeReq& r, const SchedRequest& sr)
     const int32_t ib = (int32_t)row0, nb = r.nb, nq = r.nq, nu = r.nu, nlev = r.nlevels,
                   ic = slot * kMaxLoopCons, nc = r.ncons, zero = 0;
     const int64_t yb = y0, one = 1, sb = r.loops ? sr.off[kPoolLoopScratch] : sr.off[kPoolScratch];
-    // FP64 lanes: record-major rows of width recW; trees: field-major (sstride unused)
+    // FP64 lanes: record-major rows of width recW (lane 0's serial loop work
+    // revisits few records); trees: field-major, coalesced across the lanes
+    // of a level (measured faster for them), sstride unused
     const int64_t sst = r.loops ? r.recW : 1;
     const double par[3] = {r.h, r.acc, r.ctol};
     st.put(&ib, 4, s->ibody + slot);
