@@ -1105,7 +1105,7 @@ __device__ __forceinline__ Slot groupSlot(const DevTables& T, int blk0) {
 #include "loops_device.cuh"
 
 // One RHS of the instance owned by slot s, through either driver; LOOPS adds
-// the Ball loop-closure multipliers (FP64 chain driver).
+// the Ball loop-closure multipliers (FP64; one-thread or level-parallel driver).
 template <class R, int NM, bool REF, bool GROUP, bool LOOPS = false, class Src, class Out>
 __device__ __forceinline__ int rhs(const DevTables& T, const Slot& s, R* scratch, const Src& src, Out& out) {
     if constexpr (LOOPS) {

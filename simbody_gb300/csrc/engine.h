@@ -1,5 +1,5 @@
 // engine.h -- device-side table layout shared by the host runtime (capi.cpp)
-// and the CUDA kernels (abi_kernels.cu).
+// and the CUDA kernels (abi_device.cuh and the k_*.cu instantiations).
 //
 // HBM layout of a batch
 //   Body table (one row per mobilized body of every distinct topology, bodies
@@ -59,7 +59,7 @@ enum : int {
                            // constraint force reaches on its way to the base
 };
 
-// Loop closures (Constraint::Ball), FP64 chain driver only. Each body named
+// Loop closures (Constraint::Ball), FP64 only. Each body named
 // by a constraint has a slot record after the body records of its instance:
 //   0  R_GB[9] p_GB[3] V_GB[6]   from the position/velocity pass
 //  18  A_GB[6]                   tree acceleration (pass 3)

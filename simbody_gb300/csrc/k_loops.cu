@@ -1,4 +1,4 @@
-// k_loops.cu -- kernels of the loop-closure segment: FP64 chain driver with
+// k_loops.cu -- kernels of the loop-closure segments (FP64): the one-thread driver with
 // Constraint::Ball multipliers (realize, RK-Merson with projections) and the
 // tree M^-1 of those instances.
 #include "abi_device.cuh"
@@ -42,7 +42,8 @@ void rkLoop(const KArgs& a, cudaStream_t s) {
 // Loop-closure instances on the level-parallel driver (FP64): tree passes on
 // the lanes of each instance's group, the multiplier solve and projections on
 // its first lane. Blocks [loopGroupFirst, +nLoopGroupBlocks) of the block
-// table; scratch and stage planes as for the one-thread loop segment.
+// table; FP64 scratch and stage planes, records record-major (width in
+// T.sstride).
 void rkLoopGroup(const KArgs& a, cudaStream_t s) {
     if (a.P->nLoopGroupBlocks <= 0) return;
     rkMersonKernel<double, 3, false, true, 1, true><<<a.P->nLoopGroupBlocks, 128, 0, s>>>(

@@ -1,4 +1,4 @@
-// kernels.h -- host-callable launchers of the CUDA kernels (abi_kernels.cu).
+// kernels.h -- host-callable launchers of the CUDA kernels (k_*.cu, serve.cu).
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
