@@ -136,3 +136,54 @@ def test_pipelined_host_realize_equals_separate_calls(engine, precision):
     sp = torch.empty(b.ninst, dtype=torch.int32).pin_memory().numpy()
     got1, st1 = b.realize_acceleration_from(yp, dp, sp)
     assert (st1 == 0).all() and np.array_equal(got1, ref1)
+
+
+def test_full_size_ball_chain_fp64_matches_oracle(engine):
+    """The headline workload at its full size (65,536 32-Ball chains): every
+    instance's FP64 udot against the oracle, and the mixed form within 1e-5."""
+    w = Workload(2, 65536)
+    b, y0 = engine_batch(w, "fp64")
+    b.set_state(y0)
+    ydot, st = b.realize_acceleration()
+    ref, rst = O.realize_workload(w, nthreads=O.hardware_threads())
+    assert (st == 0).all() and (rst == 0).all()
+    err = rel_err_per_instance(ydot, ref, b.y_offsets)
+    assert err.max() <= 1e-12, err.max()
+    bm, _ = engine_batch(w, "mixed")
+    bm.set_state(y0)
+    dm, _ = bm.realize_acceleration()
+    nq = 128
+    errs = [np.linalg.norm(dm[o + nq:e] - ydot[o + nq:e]) / np.linalg.norm(ydot[o + nq:e])
+            for o, e in zip(b.y_offsets[:-1:97], b.y_offsets[1::97])]
+    assert max(errs) <= 1e-5, max(errs)
+
+
+def test_largest_tree_single_instance_matches_oracle(engine):
+    """One instance of the largest tree of the uneven distribution (the
+    level-parallel driver alone on the GPU)."""
+    w = Workload(4, 400)
+    i = int(np.argmax(w.nbodies()))
+    assert w.nbodies()[i] >= 200
+    for prec, tol in (("fp64", 1e-12), ("mixed", 1e-5)):
+        b, y0 = engine_batch(w, prec, instances=[i])
+        b.set_state(y0)
+        ydot, st = b.realize_acceleration()
+        ref, _ = O.realize_workload(w, [i])
+        assert st[0] == 0
+        err = np.linalg.norm(ydot - ref) / np.linalg.norm(ref)
+        assert err <= tol, (prec, err)
+
+
+def test_empty_batch(engine):
+    """A batch of no instances: every operation is a no-op."""
+    from simbody_gb300 import Batch
+    from simbody_gb300.engine import Topology
+
+    w = Workload(1, 1)
+    t = Topology(w.systems[0], keepalive=w)
+    b = Batch([t], np.zeros(0, dtype=np.int32), precision="mixed")
+    assert b.ninst == 0 and b.ny_total == 0
+    b.set_state(np.zeros(0))
+    ydot, st = b.realize_acceleration()
+    assert ydot.size == 0 and st.size == 0
+    b.rk_merson_fixed(1e-3, 3)

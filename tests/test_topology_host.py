@@ -1,0 +1,93 @@
+"""Host-side topology flattening (sbg_topology_create): the validation the
+reference performs when a System is built (SimbodyMatterSubsystemRep.cpp:
+256-330, MobilizedBody/Force/Constraint constructors), the state sizes and
+the default state. No GPU is needed for any of it."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from simbody_gb300 import _native as N
+from simbody_gb300.engine import Topology
+
+
+def chain(n, mob=N.SBG_PIN):
+    bodies = (N.BodyDesc * n)()
+    for k in range(n):
+        b = bodies[k]
+        b.parent, b.mobilizer, b.mass = k, mob, 1.0
+        b.unit_inertia[0] = b.unit_inertia[1] = b.unit_inertia[2] = 1.0
+        for j in (0, 4, 8):
+            b.X_PF[j] = b.X_BM[j] = 1.0
+        b.X_BM[10] = 0.5
+    return bodies
+
+
+def make(bodies, n, forces=None, nf=0, cons=None, nc=0):
+    return N.SystemDesc(n, nf, nc, 0, (C.c_double * 3)(0, -9.8, 0), bodies, forces, cons)
+
+
+def create(desc):
+    h = C.c_void_p()
+    rc = N.engine_lib().sbg_topology_create(C.byref(desc), C.byref(h))
+    if rc == 0:
+        N.engine_lib().sbg_topology_destroy(h)
+    return rc, (N.engine_lib().sbg_last_error() or b"").decode()
+
+
+@pytest.mark.parametrize("mob,nq,nu,nquat", [(N.SBG_PIN, 1, 1, 0), (N.SBG_SLIDER, 1, 1, 0),
+                                              (N.SBG_UNIVERSAL, 2, 2, 0), (N.SBG_BALL, 4, 3, 1),
+                                              (N.SBG_FREE, 7, 6, 1)])
+def test_sizes_and_default_state(mob, nq, nu, nquat):
+    b = chain(3, mob)
+    t = Topology(make(b, 3), keepalive=b)
+    assert (t.nq, t.nu, t.nbodies, t.nlevels, t.nquaternions) == (3 * nq, 3 * nu, 3, 3, 3 * nquat)
+    y = t.default_state()
+    # quaternions start at the identity (RigidBodyNodeSpec_Ball.h:405-415), all else zero
+    expect = np.zeros(3 * (nq + nu))
+    if nquat:
+        expect[[k * nq for k in range(3)]] = 1.0
+    assert np.array_equal(y, expect)
+
+
+def test_levels_of_a_branched_tree():
+    b = chain(5)
+    b[1].parent = 1
+    b[2].parent = 1  # bodies 2 and 3 hang off body 1
+    b[3].parent = 3
+    b[4].parent = 0  # a second root
+    t = Topology(make(b, 5), keepalive=b)
+    assert t.nlevels == 3
+
+
+@pytest.mark.parametrize("field,value,msg", [("parent", 2, "parent must precede"), ("parent", -1, "parent must precede"),
+                                             ("mobilizer", 7, "unknown mobilizer"), ("mass", 0.0, "mass must be positive"),
+                                             ("mass", float("nan"), "mass must be positive")])
+def test_invalid_bodies_are_rejected(field, value, msg):
+    b = chain(3)
+    setattr(b[1], field, value)
+    rc, err = create(make(b, 3))
+    assert rc == 1 and msg in err  # SBG_ERR_INVALID
+
+
+def test_invalid_forces_and_constraints_are_rejected():
+    b = chain(3)
+    f = (N.MobilityForceDesc * 1)()
+    f[0].kind, f[0].body, f[0].which, f[0].coef = 0, 2, 1, 10.0  # a Pin has one mobility: which = 1 is out of range
+    assert create(make(b, 3, f, 1))[0] == 1
+    f[0].which, f[0].body = 0, 4  # no body 4
+    assert create(make(b, 3, f, 1))[0] == 1
+    f[0].body, f[0].kind = 2, 5  # unknown kind
+    assert create(make(b, 3, f, 1))[0] == 1
+    c = (N.BallConstraintDesc * 1)()
+    c[0].body1, c[0].body2 = 2, 2  # a body constrained to itself
+    assert create(make(b, 3, None, 0, c, 1))[0] == 1
+    assert create(N.SystemDesc(0, 0, 0, 0, (C.c_double * 3)(0, 0, 0), None, None, None))[0] == 1
+
+
+def test_largest_serving_tree_flattens():
+    b = chain(256, N.SBG_BALL)
+    for k in range(2, 256):
+        b[k].parent = (k * 7919 + 3) % (k + 1)  # any earlier body: a random-looking tree
+    t = Topology(make(b, 256), keepalive=b)
+    assert t.nbodies == 256 and t.nq == 1024 and t.nu == 768
