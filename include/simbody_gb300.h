@@ -212,6 +212,42 @@ int sbg_realize_acceleration_host(sbg_batch batch, const double* y, double* ydot
  * f and out are packed like the u parts of y (nu values per instance). */
 int sbg_multiply_by_minv(sbg_batch batch, const double* f, double* out);
 
+/* Tree operators on the batch's current state, for every instance. They run
+ * in FP64 whatever the batch's precision and ignore the systems' own forces
+ * and constraints, as the reference's do. Packing:
+ *   u-like arrays (mobility forces, udot, residuals, M x, ~J F): nu values
+ *     per instance, like the u parts of y;
+ *   body arrays: one entry per mobilized body (Ground excluded) in the order
+ *     of the system description's bodies, instances one after another
+ *     (nbodies entries each). A SpatialVec entry is 6 values (angular then
+ *     linear: moment and force, or angular and linear velocity /
+ *     acceleration), expressed in Ground at the body origin. A spatial
+ *     inertia entry is 10 values: mass, the mass center measured from the
+ *     body origin (3), and the unit inertia about the body origin (xx yy zz
+ *     xy xz yz), all in Ground.
+ * status (may be NULL) gets one SBG_INST_* word per instance (NONFINITE for
+ * a non-finite result). Synchronous. */
+
+/* SimbodyMatterSubsystem::calcResidualForceIgnoringConstraints(state,
+ * appliedMobilityForces, appliedBodyForces, knownUdot, residualMobilityForces)
+ * (Simbody/include/simbody/internal/SimbodyMatterSubsystem.h:2234):
+ * residual = M udot + C(q,u) - f_applied - ~J F_applied (inverse dynamics,
+ * Stage::Velocity). Any of the three inputs may be NULL: all zero, as a
+ * zero-length Vector is for the reference. */
+int sbg_calc_residual_force(sbg_batch batch, const double* mobility_forces, const double* body_forces,
+                            const double* known_udot, double* residual, int32_t* status);
+/* SimbodyMatterSubsystem::multiplyByM(state, a, Ma) (SimbodyMatterSubsystem.h:1262). */
+int sbg_multiply_by_m(sbg_batch batch, const double* a, double* Ma, int32_t* status);
+/* SimbodyMatterSubsystem::multiplyBySystemJacobian(state, u, Ju)
+ * (SimbodyMatterSubsystem.h:554): Ju is a body array of SpatialVecs. */
+int sbg_multiply_by_system_jacobian(sbg_batch batch, const double* u, double* Ju, int32_t* status);
+/* SimbodyMatterSubsystem::multiplyBySystemJacobianTranspose(state, F_G, f)
+ * (SimbodyMatterSubsystem.h:646): F_G is a body array of SpatialVecs. */
+int sbg_multiply_by_system_jacobian_transpose(sbg_batch batch, const double* F_G, double* f, int32_t* status);
+/* SimbodyMatterSubsystem::calcCompositeBodyInertias(state, R)
+ * (SimbodyMatterSubsystem.h:2323): R is a body array of spatial inertias. */
+int sbg_calc_composite_body_inertias(sbg_batch batch, double* R, int32_t* status);
+
 /* RungeKuttaMersonIntegrator with setFixedStepSize(h), initialize(state) and
  * stepTo(t0 + nsteps*h) looped until reached (RungeKuttaMersonIntegrator.cpp:86-140,
  * AbstractIntegratorRep.cpp:137-207, 341-577), for every instance, on the

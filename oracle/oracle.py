@@ -31,6 +31,10 @@ def lib() -> C.CDLL:
         L.oracle_minv_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, i64p, dp, dp, C.c_int32]
         L.oracle_rk_merson_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, dp, C.c_double, C.c_int32,
                                              C.c_double, C.c_double, C.c_int32, ip, i64p, C.c_int32]
+        L.oracle_tree_op_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, i64p, i64p, C.c_int32, dp, dp,
+                                           dp, dp, C.c_int32]
+        L.oracle_system_forces_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, i64p, i64p, dp, dp,
+                                                 C.c_int32]
         L.oracle_count_realize.argtypes = [sd, dp, i64p]
         L.oracle_time_realize.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, dp, C.c_int32, C.c_int32]
         L.oracle_time_realize.restype = C.c_double
@@ -86,6 +90,42 @@ def multiply_by_minv(systems, nsys, sys_of, y_off, y, u_off, f, nthreads=0):
                                    _d(np.ascontiguousarray(y)), _l(np.ascontiguousarray(u_off)), _d(f), _d(out),
                                    nthreads))
     return out
+
+
+TREE_OPS = {"residual": 0, "mv": 1, "jv": 2, "jtf": 3, "composite": 4}
+
+
+def tree_op(systems, nsys, sys_of, y_off, y, u_off, b_off, op, x=None, fmob=None, fbody=None, nthreads=0):
+    """One of the O(n) tree operators (TREE_OPS) per instance. u-like arrays
+    are packed at u_off; body arrays hold 6 values (10 for composite
+    inertias) per body at b_off (bodies before each instance)."""
+    sys_of = np.ascontiguousarray(sys_of, dtype=np.int32)
+    u_off = np.ascontiguousarray(u_off, dtype=np.int64)
+    b_off = np.ascontiguousarray(b_off, dtype=np.int64)
+    k = TREE_OPS[op]
+    n = len(sys_of)
+    nout = {2: 6 * int(b_off[n]), 4: 10 * int(b_off[n])}.get(k, int(u_off[n]))
+    out = np.empty(nout)
+    keep = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None for a in (x, fmob, fbody)]
+    ptr = [None if a is None else _d(a) for a in keep]
+    _check(lib().oracle_tree_op_batch(systems, nsys, _i(sys_of), n, _l(np.ascontiguousarray(y_off)),
+                                      _d(np.ascontiguousarray(y)), _l(u_off), _l(b_off), k, ptr[0], ptr[1], ptr[2],
+                                      _d(out), nthreads))
+    return out
+
+
+def system_forces(systems, nsys, sys_of, y_off, y, u_off, b_off, nthreads=0):
+    """(mobility forces, body forces) of the systems' own force elements."""
+    sys_of = np.ascontiguousarray(sys_of, dtype=np.int32)
+    u_off = np.ascontiguousarray(u_off, dtype=np.int64)
+    b_off = np.ascontiguousarray(b_off, dtype=np.int64)
+    n = len(sys_of)
+    fm = np.empty(int(u_off[n]))
+    fb = np.empty(6 * int(b_off[n]))
+    _check(lib().oracle_system_forces_batch(systems, nsys, _i(sys_of), n, _l(np.ascontiguousarray(y_off)),
+                                            _d(np.ascontiguousarray(y)), _l(u_off), _l(b_off), _d(fm), _d(fb),
+                                            nthreads))
+    return fm, fb
 
 
 def rk_merson(systems, nsys, sys_of, y_off, y, h, nsteps, t=None, accuracy=0.0, cons_tol=0.0,

@@ -674,6 +674,90 @@ int oracle_rk_merson_batch(const sbg_system_desc* systems, int32_t nsys, const i
     return 0;
 }
 
+// Tree operators for a batch (body arrays: b_off[i] = bodies before instance
+// i; SpatialVecs take 6 values per body, spatial inertias 10):
+//   op 0  calcResidualForceIgnoringConstraints: out(u) = M x + C(q,u) - fmob - ~J Fbody
+//   op 1  multiplyByM: out(u) = M x
+//   op 2  multiplyBySystemJacobian: out(6 per body) = J x
+//   op 3  multiplyBySystemJacobianTranspose: out(u) = ~J Fbody
+//   op 4  calcCompositeBodyInertias: out(10 per body)
+// fmob and Fbody may be NULL (zero); x may be NULL for ops 0 and 1 (zero).
+int oracle_tree_op_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
+                         const int64_t* y_off, const double* y, const int64_t* u_off, const int64_t* b_off,
+                         int32_t op, const double* x, const double* fmob, const double* Fbody, double* out,
+                         int32_t nthreads) {
+    if (op < 0 || op > 4) return setErr("unknown tree operator");
+    std::vector<Topology> topo(nsys);
+    for (int s = 0; s < nsys; ++s) {
+        const char* e = nullptr;
+        if (!buildTopology(systems[s], topo[s], &e)) return setErr(e);
+    }
+    parallelFor(ninst, nthreads, [&](int i, int) {
+        const Topology& t = topo[sys_of[i]];
+        Work<double> w;
+        w.resize(t);
+        const double* q = y + y_off[i];
+        realizePosition(t, q, w);
+        std::vector<double> zero(t.nu, 0.0);
+        const double* xi = x ? x + u_off[i] : zero.data();
+        const double* Fi = Fbody ? Fbody + 6 * b_off[i] : nullptr;
+        const double* fi = fmob ? fmob + u_off[i] : nullptr;
+        switch (op) {
+        case 0:
+            realizeVelocity(t, q, q + t.nq, w, (double*)nullptr);
+            accelerationsOutward(t, w, xi, true);
+            forcesInward(t, w, 0, Fi, fi, out + u_off[i]);
+            break;
+        case 1:
+            accelerationsOutward(t, w, xi, false);
+            forcesInward(t, w, 1, (const double*)nullptr, (const double*)nullptr, out + u_off[i]);
+            break;
+        case 2: {
+            accelerationsOutward(t, w, xi, false);
+            double* o = out + 6 * b_off[i];
+            for (int bi = 1; bi <= t.nb; ++bi)
+                for (int k = 0; k < 3; ++k) { o[6 * (bi - 1) + k] = w.c[bi].Aw[k]; o[6 * (bi - 1) + 3 + k] = w.c[bi].Av[k]; }
+            break;
+        }
+        case 3:
+            forcesInward(t, w, 2, Fi, (const double*)nullptr, out + u_off[i]);
+            break;
+        default:
+            compositeInertias(t, w, out + 10 * b_off[i]);
+            break;
+        }
+    });
+    return 0;
+}
+
+// The forces of each system's own force elements at its state: Force::Gravity
+// body forces (6 per body, moment and force in Ground) and the mobility
+// springs and dampers (nu per instance), as realize(Dynamics) accumulates them.
+int oracle_system_forces_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
+                               const int64_t* y_off, const double* y, const int64_t* u_off, const int64_t* b_off,
+                               double* fmob, double* Fbody, int32_t nthreads) {
+    std::vector<Topology> topo(nsys);
+    for (int s = 0; s < nsys; ++s) {
+        const char* e = nullptr;
+        if (!buildTopology(systems[s], topo[s], &e)) return setErr(e);
+    }
+    parallelFor(ninst, nthreads, [&](int i, int) {
+        const Topology& t = topo[sys_of[i]];
+        Work<double> w;
+        w.resize(t);
+        const double* q = y + y_off[i];
+        realizePosition(t, q, w);
+        calcForces(t, q, q + t.nq, w);
+        for (int k = 0; k < t.nu; ++k) fmob[u_off[i] + k] = w.f[k];
+        for (int bi = 1; bi <= t.nb; ++bi)
+            for (int k = 0; k < 3; ++k) {
+                Fbody[6 * (b_off[i] + bi - 1) + k] = w.c[bi].Fw[k];
+                Fbody[6 * (b_off[i] + bi - 1) + 3 + k] = w.c[bi].Fv[k];
+            }
+    });
+    return 0;
+}
+
 // Exact operation counts of one realize(Acceleration) of one instance with
 // the counting scalar: counts[0]=add/sub, [1]=mul, [2]=div, [3]=sqrt,
 // [4]=sin/cos, [5]=abs/compare.

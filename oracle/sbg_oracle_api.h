@@ -17,6 +17,13 @@ int oracle_rk_merson_batch(const sbg_system_desc* systems, int32_t nsys, const i
                            const int64_t* y_off, double* y, double* t, double h, int32_t nsteps, double accuracy,
                            double consTol, int32_t projectEveryStep, int32_t* status, int64_t* nproj,
                            int32_t nthreads);
+int oracle_tree_op_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
+                         const int64_t* y_off, const double* y, const int64_t* u_off, const int64_t* b_off,
+                         int32_t op, const double* x, const double* fmob, const double* Fbody, double* out,
+                         int32_t nthreads);
+int oracle_system_forces_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
+                               const int64_t* y_off, const double* y, const int64_t* u_off, const int64_t* b_off,
+                               double* fmob, double* Fbody, int32_t nthreads);
 int oracle_count_realize(const sbg_system_desc* d, const double* y, int64_t* counts);
 double oracle_time_realize(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
                            const int64_t* y_off, const double* y, double* ydot, int32_t nreps, int32_t nthreads);

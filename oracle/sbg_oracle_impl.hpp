@@ -392,6 +392,114 @@ template <class R> void multiplyByMInv(const Topology& t, Work<R>& w, const R* f
         }
 }
 
+// ------------------------------------------------------- tree operators
+// Body accelerations from a u-like vector x, base to tip:
+//   calcBodyAccelerationsFromUdotOutward (RigidBodyNodeSpec.cpp:566-582):
+//     A = ~Phi A_parent + H x + a (coriolis = true, Stage::Velocity);
+//   multiplyByMPass1Outward (:658-669), multiplyBySystemJacobian (:762-775):
+//     A = ~Phi A_parent + H x (coriolis = false, Stage::Position).
+template <class R> void accelerationsOutward(const Topology& t, Work<R>& w, const R* x, bool coriolis) {
+    w.c[0].Aw = zero3<R>(); w.c[0].Av = zero3<R>();
+    for (const auto& lev : t.levels)
+        for (int bi : lev) {
+            const Body& b = t.b[bi];
+            BodyCache<R>& c = w.c[bi];
+            const BodyCache<R>& pc = w.c[b.parent];
+            const V3<R> Apw = pc.Aw;
+            const V3<R> Apv = pc.Av + cross(pc.Aw, c.l);
+            V3<R> hw = zero3<R>(), hv = zero3<R>();
+            for (int j = 0; j < b.nu; ++j) { hw = hw + x[b.uoff + j] * c.Hw[j]; hv = hv + x[b.uoff + j] * c.Hv[j]; }
+            c.Aw = Apw + hw;
+            c.Av = Apv + hv;
+            if (coriolis) { c.Aw = c.Aw + c.aw; c.Av = c.Av + c.av; }
+        }
+}
+
+// Tip-to-base force sweep F = own + sum over children of Phi_c F_c, then
+// tau = ~H F - f (f may be null). The body's own term is
+//   kind 0  Mk A + b - F_applied   calcInverseDynamicsPass2Inward (RigidBodyNodeSpec.cpp:611-642)
+//   kind 1  Mk A                   multiplyByMPass2Inward (:675-697)
+//   kind 2  F_applied              multiplyBySystemJacobianTranspose (:795-818)
+// with Mk A = m (G A_w + p x A_v, A_v - p x A_w) (MassProperties.h:1071-1072).
+// F_applied holds 6 values (moment, force) per mobilized body in body order
+// (may be null: zero).
+template <class R> void forcesInward(const Topology& t, Work<R>& w, int kind, const R* F_applied, const R* f, R* tau) {
+    for (int li = (int)t.levels.size() - 1; li >= 0; --li)
+        for (int bi : t.levels[li]) {
+            const Body& b = t.b[bi];
+            BodyCache<R>& c = w.c[bi];
+            V3<R> Fw = zero3<R>(), Fv = zero3<R>();
+            if (kind != 2) {
+                Fw = c.m * (c.Gi * c.Aw + cross(c.pc, c.Av));
+                Fv = c.m * (c.Av - cross(c.pc, c.Aw));
+                if (kind == 0) { Fw = Fw + c.bw; Fv = Fv + c.bv; }
+            }
+            if (F_applied) {
+                const R* Fb = F_applied + 6 * (bi - 1);
+                const V3<R> aw = v3<R>(Fb[0], Fb[1], Fb[2]), av = v3<R>(Fb[3], Fb[4], Fb[5]);
+                if (kind == 2) { Fw = Fw + aw; Fv = Fv + av; }
+                else { Fw = Fw - aw; Fv = Fv - av; }
+            }
+            for (int ch : b.children) {  // Phi*F = (F_w + l % F_v, F_v)
+                const BodyCache<R>& cc = w.c[ch];
+                Fw = Fw + (cc.zw + cross(cc.l, cc.zv));
+                Fv = Fv + cc.zv;
+            }
+            c.zw = Fw; c.zv = Fv;
+            for (int j = 0; j < b.nu; ++j) {
+                R s = dot(c.Hw[j], Fw) + dot(c.Hv[j], Fv);
+                if (f) s = s - f[b.uoff + j];
+                tau[b.uoff + j] = s;
+            }
+        }
+}
+
+// Unit inertia of a unit point mass at p (UnitInertia::pointMassAt,
+// MassProperties.h:866-867, element order of Inertia::pointMassAt :458-466).
+template <class R> inline S33<R> pointMassUnit(const V3<R>& p) {
+    const R xx = p[0] * p[0], yy = p[1] * p[1], zz = p[2] * p[2];
+    return s33<R>(yy + zz, -p[0] * p[1], xx + zz, -p[0] * p[2], -p[1] * p[2], xx + yy);
+}
+// Spatial inertia (m, p = mass center from the origin, G = unit inertia about
+// the origin), all in Ground.
+template <class R> struct SpatialInertia {
+    R m;
+    V3<R> p;
+    S33<R> G;
+};
+// SpatialInertia::shiftInPlace (MassProperties.h:1110-1116): origin OF -> OF + S.
+template <class R> inline SpatialInertia<R> siShift(SpatialInertia<R> s, const V3<R>& S) {
+    s.G = s.G - pointMassUnit(s.p);
+    const V3<R> pNew = s.p - S;
+    s.G = s.G + pointMassUnit(pNew);
+    s.p = pNew;
+    return s;
+}
+// SpatialInertia::operator+= (MassProperties.h:1037-1044).
+template <class R> inline void siAdd(SpatialInertia<R>& a, const SpatialInertia<R>& b) {
+    const R mtot = a.m + b.m, oom = R(1) / mtot;
+    a.p = oom * (a.m * a.p + b.m * b.p);
+    a.G = oom * (a.m * a.G + b.m * b.G);
+    a.m = mtot;
+}
+// calcCompositeBodyInertias (SimbodyMatterSubsystemRep.cpp:5196-5205),
+// RigidBodyNode::calcCompositeBodyInertiasInward (RigidBodyNode.cpp:232-243):
+// R = Mk_G + sum over children of R_c.shift(-l_c). out: 10 values per body
+// (m, p[3], G xx yy zz xy xz yz), body order.
+template <class R> void compositeInertias(const Topology& t, const Work<R>& w, R* out) {
+    std::vector<SpatialInertia<R>> Rb(t.nb + 1);
+    for (int li = (int)t.levels.size() - 1; li >= 0; --li)
+        for (int bi : t.levels[li]) {
+            const BodyCache<R>& c = w.c[bi];
+            SpatialInertia<R> r{c.m, c.pc, c.Gi};
+            for (int ch : t.b[bi].children) siAdd(r, siShift(Rb[ch], -w.c[ch].l));
+            Rb[bi] = r;
+            R* o = out + 10 * (bi - 1);
+            o[0] = r.m; o[1] = r.p[0]; o[2] = r.p[1]; o[3] = r.p[2];
+            o[4] = r.G.xx; o[5] = r.G.yy; o[6] = r.G.zz; o[7] = r.G.yx; o[8] = r.G.zx; o[9] = r.G.zy;
+        }
+}
+
 // Full realize(Stage::Acceleration) of one unconstrained instance:
 // ydot = [qdot, udot]. Returns false on a singular D.
 template <class R> bool realizeAcceleration(const Topology& t, const R* y, Work<R>& w, R* ydot) {

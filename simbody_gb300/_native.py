@@ -103,6 +103,11 @@ ENGINE_API = {
     "sbg_realize_acceleration": (C.c_int, [vp, dp, ip]),
     "sbg_realize_acceleration_host": (C.c_int, [vp, dp, dp, ip]),
     "sbg_multiply_by_minv": (C.c_int, [vp, dp, dp]),
+    "sbg_calc_residual_force": (C.c_int, [vp, dp, dp, dp, dp, ip]),
+    "sbg_multiply_by_m": (C.c_int, [vp, dp, dp, ip]),
+    "sbg_multiply_by_system_jacobian": (C.c_int, [vp, dp, dp, ip]),
+    "sbg_multiply_by_system_jacobian_transpose": (C.c_int, [vp, dp, dp, ip]),
+    "sbg_calc_composite_body_inertias": (C.c_int, [vp, dp, ip]),
     "sbg_rk_merson_fixed": (C.c_int, [vp, C.c_double, C.c_int32, P(IntegOpts), ip]),
     "sbg_batch_stream": (vp, [vp]),
     "sbg_realize_acceleration_async": (C.c_int, [vp]),

@@ -81,6 +81,7 @@ struct sbg_batch_s {
     cudaStream_t stream = nullptr;
     std::vector<int32_t> instTopo;
     std::vector<int64_t> hostYOff, hostUOff;  // packed host offsets (n+1)
+    std::vector<int64_t> hostBOff;            // bodies before each instance (n+1)
     int64_t nyTotal = 0, nuTotal = 0, colElems = 0;
     std::vector<DevBuf> bufs;
     int64_t devBytes = 0;
@@ -118,6 +119,14 @@ struct sbg_batch_s {
     cudaEvent_t evT0 = nullptr, evT1 = nullptr;
     bool tuned = false;
     cudaGraphExec_t realizeGraph = nullptr;  // captured after tuning
+    // tree operators (allocated on first use): FP64 scratch for a batch whose
+    // own scratch is FP32, device operands and results in the host packing,
+    // their pinned host staging, and the per-instance packing offsets
+    void* opsScratch = nullptr;
+    double* opsDev = nullptr;
+    double* opsHost = nullptr;
+    int64_t opsElems = 0;
+    int64_t* dHostBOff = nullptr;
 
     Streams streams() const { return Streams{stream, stream2, evFork, evJoin}; }
     LaunchPlan plan() const { return LaunchPlan{nChain, nGroupBlocks, nm, variant == 0 ? 1 : variant, nLoop}; }
@@ -157,6 +166,7 @@ struct sbg_batch_s {
         if (device >= 0) cudaSetDevice(device);
         for (auto& b : bufs) cudaFree(b.p);
         if (hostPinned) cudaFreeHost(hostPinned);
+        if (opsHost) cudaFreeHost(opsHost);
         if (realizeGraph) cudaGraphExecDestroy(realizeGraph);
         if (evFork) cudaEventDestroy(evFork);
         if (evT0) cudaEventDestroy(evT0);
@@ -296,6 +306,7 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
         t->qoff.push_back(qo[bi]);
         t->uoff.push_back(uo[bi]);
         t->srec.push_back((int32_t)rec);
+        t->bodyOfRow.push_back(bi - 1);
         rec += scratchRecordSize(n);
         t->fbeg.push_back((int32_t)t->fkw.size());
         t->fcnt.push_back((int32_t)fOf[bi].size());
@@ -424,7 +435,7 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     // distinct topologies used, concatenated body tables
     std::vector<int> used(ntopo, -1);
     std::vector<int64_t> recTotal(ntopo, 0);
-    std::vector<int32_t> parent, info, qoff, uoff, srec, fbeg, fcnt, fkw;
+    std::vector<int32_t> parent, info, qoff, uoff, srec, fbeg, fcnt, fkw, bidx;
     std::vector<double> par, fcoef, fq0;
     std::vector<int32_t> rowBase(ntopo, 0);
     for (int i = 0; i < ninst; ++i) {
@@ -438,6 +449,7 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
         info.insert(info.end(), t->info.begin(), t->info.end());
         qoff.insert(qoff.end(), t->qoff.begin(), t->qoff.end());
         uoff.insert(uoff.end(), t->uoff.begin(), t->uoff.end());
+        bidx.insert(bidx.end(), t->bodyOfRow.begin(), t->bodyOfRow.end());
         const std::vector<int32_t> pr = paddedRecords(*t, nm, &recTotal[k]);
         srec.insert(srec.end(), pr.begin(), pr.end());
         for (int32_t fb : t->fbeg) fbeg.push_back(fb + fOff);
@@ -476,6 +488,7 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     }
     b->hostYOff.assign(ninst + 1, 0);
     b->hostUOff.assign(ninst + 1, 0);
+    b->hostBOff.assign(ninst + 1, 0);
     // Trees with fewer bodies run one per thread (their lanes would mostly
     // idle or diverge in a group); larger trees with wide levels get a group.
     int groupMinBodies = 48;
@@ -492,6 +505,7 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
         for (int k = 0; k < 3; ++k) grav[3 * i + k] = t->gravity[k];
         b->hostYOff[i + 1] = b->hostYOff[i] + t->nq + t->nu;
         b->hostUOff[i + 1] = b->hostUOff[i] + t->nu;
+        b->hostBOff[i + 1] = b->hostBOff[i] + t->nb;
         if (t->ncons > 0) loopPos.push_back(i);
         else if (t->chain || t->maxLevelWidth <= 2 || t->nb < groupMinBodies) chainPos.push_back(i);
         else groupPos.push_back(i);
@@ -591,6 +605,7 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     if ((rc = b->upload(&T.qoff, qoff, "body table"))) return bail(rc);
     if ((rc = b->upload(&T.uoff, uoff, "body table"))) return bail(rc);
     if ((rc = b->upload(&T.srec, srec, "body table"))) return bail(rc);
+    if ((rc = b->upload(&T.bidx, bidx, "body table"))) return bail(rc);
     if ((rc = b->upload(&T.fbeg, fbeg, "body table"))) return bail(rc);
     if ((rc = b->upload(&T.fcnt, fcnt, "body table"))) return bail(rc);
     if ((rc = b->upload(&T.par64, par, "parameters"))) return bail(rc);
@@ -936,6 +951,92 @@ int sbg_multiply_by_minv(sbg_batch b, const double* f, double* outp) {
     SBG_CUDA(cudaStreamSynchronize(b->stream), "M^-1");
     std::memcpy(outp, b->hostPinned, bytes);
     return SBG_OK;
+}
+
+// ------------------------------------------------------------ tree operators
+// Device operands of a tree operator in the host packing: x [nu] | fmob [nu] |
+// fbody [6 nb] | out [max(nu, 10 nb)], mirrored in pinned host memory.
+static int ensureTreeOps(sbg_batch b) {
+    const int64_t nu = b->nuTotal, nbT = b->hostBOff[b->ninst];
+    const int64_t need = 2 * nu + 6 * nbT + std::max<int64_t>(nu, 10 * nbT);
+    if (b->opsDev && b->opsElems >= need) return SBG_OK;
+    int rc;
+    void* p = nullptr;
+    if (b->precision != SBG_PRECISION_FP64 && !b->opsScratch && b->scratchElems > 0) {
+        if ((rc = b->alloc(&b->opsScratch, b->scratchElems * sizeof(double), "tree-operator scratch"))) return rc;
+    }
+    if ((rc = b->alloc(&p, std::max<int64_t>(need, 1) * sizeof(double), "tree-operator operands"))) return rc;
+    b->opsDev = static_cast<double*>(p);
+    const int64_t* dOff = nullptr;
+    if ((rc = b->upload(&dOff, b->hostBOff, "offsets"))) return rc;
+    b->dHostBOff = const_cast<int64_t*>(dOff);
+    cudaError_t e = cudaMallocHost(&b->opsHost, std::max<int64_t>(need, 1) * sizeof(double));
+    if (e != cudaSuccess) {
+        b->opsHost = nullptr;
+        return cudaFail(e, "cudaMallocHost");
+    }
+    b->opsElems = need;
+    return SBG_OK;
+}
+
+static int runTreeOp(sbg_batch b, int kind, const double* x, const double* fmob, const double* fbody, double* out,
+                     int32_t* status) {
+    if (!b || !out) return fail(SBG_ERR_INVALID, "null argument");
+    if (!b->stateSet) return fail(SBG_ERR_STATE, "no state has been set");
+    SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    if (int rc = ensureTreeOps(b)) return rc;
+    const int64_t nu = b->nuTotal, nbT = b->hostBOff[b->ninst];
+    double* dX = b->opsDev;
+    double* dF = dX + nu;
+    double* dB = dF + nu;
+    double* dOut = dB + 6 * nbT;
+    const int64_t nOut = kind == OP_JV ? 6 * nbT : (kind == OP_COMPOSITE ? 10 * nbT : nu);
+    double* hX = b->opsHost;
+    auto up = [&](const double* src, double* dDst, int64_t n, const char* what) -> int {
+        if (!src || n == 0) return SBG_OK;
+        double* h = hX + (dDst - b->opsDev);
+        std::memcpy(h, src, n * sizeof(double));
+        SBG_CUDA(cudaMemcpyAsync(dDst, h, n * sizeof(double), cudaMemcpyHostToDevice, b->stream), what);
+        return SBG_OK;
+    };
+    if (int rc = up(x, dX, nu, "operand upload")) return rc;
+    if (int rc = up(fmob, dF, nu, "mobility force upload")) return rc;
+    if (int rc = up(fbody, dB, 6 * nbT, "body force upload")) return rc;
+    OpIO io{kind, x ? dX : nullptr, fmob ? dF : nullptr, fbody ? dB : nullptr, dOut, b->dHostUOff, b->dHostBOff};
+    double* sc = b->precision == SBG_PRECISION_FP64 ? static_cast<double*>(b->scratch)
+                                                     : static_cast<double*>(b->opsScratch);
+    SBG_CUDA(launchTreeOp(b->T, b->plan(), io, b->y, sc, static_cast<double*>(b->scratchLoop), b->status, b->stream),
+             "tree-operator kernel launch");
+    b->launches += b->segments();
+    double* hOut = hX + (dOut - b->opsDev);
+    if (nOut > 0)
+        SBG_CUDA(cudaMemcpyAsync(hOut, dOut, nOut * sizeof(double), cudaMemcpyDeviceToHost, b->stream), "result download");
+    if (status && b->ninst > 0)
+        SBG_CUDA(cudaMemcpyAsync(status, b->status, b->ninst * sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream),
+                 "status download");
+    SBG_CUDA(cudaStreamSynchronize(b->stream), "tree operator");
+    std::memcpy(out, hOut, nOut * sizeof(double));
+    return SBG_OK;
+}
+
+int sbg_calc_residual_force(sbg_batch b, const double* mobility_forces, const double* body_forces,
+                            const double* known_udot, double* residual, int32_t* status) {
+    return runTreeOp(b, OP_RESIDUAL, known_udot, mobility_forces, body_forces, residual, status);
+}
+int sbg_multiply_by_m(sbg_batch b, const double* a, double* Ma, int32_t* status) {
+    if (!a) return fail(SBG_ERR_INVALID, "null argument");
+    return runTreeOp(b, OP_MV, a, nullptr, nullptr, Ma, status);
+}
+int sbg_multiply_by_system_jacobian(sbg_batch b, const double* u, double* Ju, int32_t* status) {
+    if (!u) return fail(SBG_ERR_INVALID, "null argument");
+    return runTreeOp(b, OP_JV, u, nullptr, nullptr, Ju, status);
+}
+int sbg_multiply_by_system_jacobian_transpose(sbg_batch b, const double* F_G, double* f, int32_t* status) {
+    if (!F_G) return fail(SBG_ERR_INVALID, "null argument");
+    return runTreeOp(b, OP_JTF, nullptr, nullptr, F_G, f, status);
+}
+int sbg_calc_composite_body_inertias(sbg_batch b, double* R, int32_t* status) {
+    return runTreeOp(b, OP_COMPOSITE, nullptr, nullptr, nullptr, R, status);
 }
 
 int sbg_rk_merson_fixed_async(sbg_batch b, double h, int32_t nsteps, const sbg_integ_opts* opts) {

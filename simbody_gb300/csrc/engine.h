@@ -116,6 +116,7 @@ struct DevTables {
     const int32_t* lcons;    // per constraint: local row of body 1, of body 2 (-1 = Ground)
     const double* lst;       // per constraint: station 1 (in body 1), station 2 (in body 2)
     const int32_t* lslot;    // per body row: slot index of a loop body (-1 = none): level-parallel layout
+    const int32_t* bidx;     // per body row: index of the body in its system description (tree operators)
     const int32_t* icons;    // per instance: first constraint
     const int32_t* incons;   // per instance: number of constraints
     // per-instance integration control (the serving loop; null in a batch,

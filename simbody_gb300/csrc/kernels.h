@@ -32,6 +32,23 @@ cudaError_t launchMInv(const DevTables& T, const LaunchPlan& P, int precision, c
 cudaError_t launchRKMerson(const DevTables& T, const LaunchPlan& P, int precision, double* y, double* time,
                            const BatchBufs& B, int32_t* status, double h, int nsteps, double accuracy,
                            double consTol, int projectEveryStep, const Streams& s);
+// Tree operators (k_ops.cu, ops_device.cuh). Operands in the host packing:
+// u-like arrays nu values per instance at uoff[inst]; body arrays one entry
+// per mobilized body, in descriptor body order, from boff[inst] (6 values per
+// SpatialVec, 10 per spatial inertia). scratch is FP64 scratch laid out like
+// the batch's own (its element offsets), scratchLoop the loop segment's.
+enum : int { OP_RESIDUAL = 0, OP_MV = 1, OP_JV = 2, OP_JTF = 3, OP_COMPOSITE = 4 };
+struct OpIO {
+    int kind;
+    const double* x;      // udot / a / u-like vector (null = zero)
+    const double* fmob;   // applied mobility forces (null = zero)
+    const double* fbody;  // applied body forces in Ground (null = zero)
+    double* out;
+    const int64_t* uoff;
+    const int64_t* boff;
+};
+cudaError_t launchTreeOp(const DevTables& T, const LaunchPlan& P, const OpIO& io, const double* y, double* scratch,
+                         double* scratchLoop, int32_t* status, cudaStream_t s);
 cudaError_t launchNormalizeQuat(const DevTables& T, double* y, cudaStream_t s);
 // part 0 moves whole [q,u] records, part 1 only the u slots; instances
 // [inst0, inst0 + count) (count < 0: to the end).

@@ -14,6 +14,7 @@ struct sbg_topology_s {
     int maxNonFreeDof = 0;
     int64_t recSize = 0;                 // scratch elements per instance
     std::vector<int32_t> parent, info, qoff, uoff, srec, fbeg, fcnt;
+    std::vector<int32_t> bodyOfRow;             // descriptor index (0-based) of each row
     std::vector<int32_t> levStart;              // nlevels + 1 local rows
     std::vector<int32_t> cbeg, ccnt, clist;     // children (local rows) per row
     int maxLevelWidth = 0;

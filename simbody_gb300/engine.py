@@ -6,6 +6,12 @@ Simbody calls (paths relative to the Simbody source tree):
   set_state / get_state      State::updY / getY       (State.h:962-1034)
   realize_acceleration       System::realize(s, Stage::Acceleration) + getYDot
   multiply_by_minv           SimbodyMatterSubsystem::multiplyByMInv (.h:1343)
+  calc_residual_force        ...::calcResidualForceIgnoringConstraints (.h:2234)
+  multiply_by_m              ...::multiplyByM (.h:1262)
+  multiply_by_system_jacobian / _transpose
+                             ...::multiplyBySystemJacobian(Transpose) (.h:554, 646)
+  calc_composite_body_inertias
+                             ...::calcCompositeBodyInertias (.h:2323)
   rk_merson_fixed            RungeKuttaMersonIntegrator, setFixedStepSize(h),
                              initialize, stepTo(t0 + n h)
 """
@@ -84,6 +90,8 @@ class Batch:
         self.nq = nqs
         self.nu = nus
         self.u_offsets = np.concatenate([[0], np.cumsum(nus)]).astype(np.int64)
+        nbs = np.array([self.topologies[k].nbodies for k in self.instance_topology], dtype=np.int64)
+        self.body_offsets = np.concatenate([[0], np.cumsum(nbs)]).astype(np.int64)
 
     # -- state
     def set_state(self, y: np.ndarray, t: np.ndarray | None = None) -> None:
@@ -133,6 +141,65 @@ class Batch:
         out = np.empty_like(f)
         N.check(N.engine_lib().sbg_multiply_by_minv(self._h, _dptr(f), _dptr(out)))
         return out
+
+    # -- tree operators (FP64 whatever the precision; body arrays: one entry
+    #    per mobilized body in description order, instances one after another)
+    def _uvec(self, a, name):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        assert a.size == self.u_offsets[-1], f"{name}: {a.size} values for {self.u_offsets[-1]} mobilities"
+        return a
+
+    def _bvec(self, a, name):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        assert a.size == 6 * self.body_offsets[-1], f"{name}: {a.size} values for {self.body_offsets[-1]} bodies"
+        return a
+
+    @staticmethod
+    def _opt(a):
+        return None if a is None else _dptr(a)
+
+    def calc_residual_force(self, mobility_forces=None, body_forces=None, known_udot=None):
+        """Inverse dynamics: M udot + C(q,u) - f - ~J F per instance; any input
+        may be None (zero). Returns (residual, status)."""
+        f = self._uvec(mobility_forces, "mobility_forces")
+        F = self._bvec(body_forces, "body_forces")
+        x = self._uvec(known_udot, "known_udot")
+        out = np.empty(self.u_offsets[-1])
+        st = np.empty(self.ninst, dtype=np.int32)
+        N.check(N.engine_lib().sbg_calc_residual_force(self._h, self._opt(f), self._opt(F), self._opt(x), _dptr(out),
+                                                       _iptr(st)))
+        return out, st
+
+    def multiply_by_m(self, a):
+        a = self._uvec(a, "a")
+        out = np.empty(self.u_offsets[-1])
+        st = np.empty(self.ninst, dtype=np.int32)
+        N.check(N.engine_lib().sbg_multiply_by_m(self._h, _dptr(a), _dptr(out), _iptr(st)))
+        return out, st
+
+    def multiply_by_system_jacobian(self, u):
+        u = self._uvec(u, "u")
+        out = np.empty(6 * self.body_offsets[-1])
+        st = np.empty(self.ninst, dtype=np.int32)
+        N.check(N.engine_lib().sbg_multiply_by_system_jacobian(self._h, _dptr(u), _dptr(out), _iptr(st)))
+        return out, st
+
+    def multiply_by_system_jacobian_transpose(self, F_G):
+        F = self._bvec(F_G, "F_G")
+        out = np.empty(self.u_offsets[-1])
+        st = np.empty(self.ninst, dtype=np.int32)
+        N.check(N.engine_lib().sbg_multiply_by_system_jacobian_transpose(self._h, _dptr(F), _dptr(out), _iptr(st)))
+        return out, st
+
+    def calc_composite_body_inertias(self):
+        out = np.empty(10 * self.body_offsets[-1])
+        st = np.empty(self.ninst, dtype=np.int32)
+        N.check(N.engine_lib().sbg_calc_composite_body_inertias(self._h, _dptr(out), _iptr(st)))
+        return out, st
 
     def rk_merson_fixed(self, h: float, nsteps: int, accuracy: float = 0.0, constraint_tolerance: float = 0.0,
                         project_every_step: bool = False) -> np.ndarray:
