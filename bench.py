@@ -172,6 +172,49 @@ def cpu_baseline(w, seconds: float, instances: int):
             "sample": f"{n} instances x {reps} realize(Acceleration) passes, {t:.1f} s wall"}
 
 
+# ------------------------------------------------------------- tree operators
+def tree_operators(b, w, y0, reps: int, cpu_instances: int):
+    """The tree operators on the headline workload (FP64 in every batch
+    precision): device time of the kernels (CUDA events on the batch stream,
+    copies excluded), the same through the public API with host buffers, and
+    the oracle port on the host cores for a sample of the instances."""
+    from oracle import oracle as O
+
+    nu, nb = int(b.u_offsets[-1]), int(b.body_offsets[-1])
+    rng = np.random.default_rng(0)
+    x, f, F = rng.standard_normal(nu), rng.standard_normal(nu), rng.standard_normal(6 * nb)
+    calls = {"residual": (lambda: b.calc_residual_force(f, F, x), dict(x=x, fmob=f, fbody=F)),
+             "mv": (lambda: b.multiply_by_m(x), dict(x=x)),
+             "jv": (lambda: b.multiply_by_system_jacobian(x), dict(x=x)),
+             "jtf": (lambda: b.multiply_by_system_jacobian_transpose(F), dict(fbody=F)),
+             "composite": (lambda: b.calc_composite_body_inertias(), {})}
+    n = min(cpu_instances, b.ninst)
+    threads = O.hardware_threads()
+    out = {"unit": "body-ops/s", "instances": b.ninst, "bodies": nb,
+           "cpu_sample": f"oracle port, {n} instances, {threads} threads"}
+    for name, (fn, kw) in calls.items():
+        fn()
+        dev, wall = [], []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            _, st = fn()
+            wall.append(time.perf_counter() - t0)
+            dev.append(b.last_operator_ms())
+        assert (st == 0).all()
+        dev_ms, wall_ms = float(np.median(dev)), float(np.median(wall)) * 1e3
+        sub = {k: (v[: int(b.u_offsets[n])] if k in ("x", "fmob") else v[: 6 * int(b.body_offsets[n])])
+               for k, v in kw.items()}
+        t0 = time.perf_counter()
+        O.tree_op(w.systems, w.nsys, w.instance_system[:n], b.y_offsets[: n + 1], y0[: int(b.y_offsets[n])],
+                  b.u_offsets[: n + 1], b.body_offsets[: n + 1], name, nthreads=threads, **sub)
+        cpu_s = time.perf_counter() - t0
+        nbs = int(b.body_offsets[n])
+        out[name] = {"device_ms": dev_ms, "device_body_ops_per_s": nb / (dev_ms * 1e-3),
+                     "api_ms": wall_ms, "api_body_ops_per_s": nb / (wall_ms * 1e-3),
+                     "cpu_body_ops_per_s": nbs / cpu_s}
+    return out
+
+
 # ------------------------------------------------------------------ GPU arm
 def time_resident(b, steps: int, warmup: int):
     import torch
@@ -473,6 +516,10 @@ def run_ours(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, min(args.instances, 65536))
+    try:
+        result["tree_operators"] = tree_operators(bmx, w, y0, 5, 8192)
+    except Exception as e:  # noqa: BLE001
+        result["tree_operators"] = {"error": repr(e)}
     b64.close()
     bmx.close()
     # the extra sections never keep the headline line from being printed

@@ -247,6 +247,9 @@ int sbg_multiply_by_system_jacobian_transpose(sbg_batch batch, const double* F_G
 /* SimbodyMatterSubsystem::calcCompositeBodyInertias(state, R)
  * (SimbodyMatterSubsystem.h:2323): R is a body array of spatial inertias. */
 int sbg_calc_composite_body_inertias(sbg_batch batch, double* R, int32_t* status);
+/* Device time in milliseconds of the kernels of the batch's last tree
+ * operator call (its copies excluded), from CUDA events on the batch's stream. */
+int sbg_batch_last_operator_ms(sbg_batch batch, double* ms);
 
 /* RungeKuttaMersonIntegrator with setFixedStepSize(h), initialize(state) and
  * stepTo(t0 + nsteps*h) looped until reached (RungeKuttaMersonIntegrator.cpp:86-140,

@@ -108,6 +108,7 @@ ENGINE_API = {
     "sbg_multiply_by_system_jacobian": (C.c_int, [vp, dp, dp, ip]),
     "sbg_multiply_by_system_jacobian_transpose": (C.c_int, [vp, dp, dp, ip]),
     "sbg_calc_composite_body_inertias": (C.c_int, [vp, dp, ip]),
+    "sbg_batch_last_operator_ms": (C.c_int, [vp, dp]),
     "sbg_rk_merson_fixed": (C.c_int, [vp, C.c_double, C.c_int32, P(IntegOpts), ip]),
     "sbg_batch_stream": (vp, [vp]),
     "sbg_realize_acceleration_async": (C.c_int, [vp]),

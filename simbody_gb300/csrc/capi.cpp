@@ -127,6 +127,7 @@ struct sbg_batch_s {
     double* opsHost = nullptr;
     int64_t opsElems = 0;
     int64_t* dHostBOff = nullptr;
+    cudaEvent_t evOp0 = nullptr, evOp1 = nullptr;  // bracket the last tree operator's kernels
 
     Streams streams() const { return Streams{stream, stream2, evFork, evJoin}; }
     LaunchPlan plan() const { return LaunchPlan{nChain, nGroupBlocks, nm, variant == 0 ? 1 : variant, nLoop}; }
@@ -171,6 +172,8 @@ struct sbg_batch_s {
         if (evFork) cudaEventDestroy(evFork);
         if (evT0) cudaEventDestroy(evT0);
         if (evT1) cudaEventDestroy(evT1);
+        if (evOp0) cudaEventDestroy(evOp0);
+        if (evOp1) cudaEventDestroy(evOp1);
         if (evJoin) cudaEventDestroy(evJoin);
         if (stream2) cudaStreamDestroy(stream2);
         for (int k = 1; k < 4; ++k)
@@ -976,6 +979,10 @@ static int ensureTreeOps(sbg_batch b) {
         return cudaFail(e, "cudaMallocHost");
     }
     b->opsElems = need;
+    if (!b->evOp0) {
+        SBG_CUDA(cudaEventCreate(&b->evOp0), "event");
+        SBG_CUDA(cudaEventCreate(&b->evOp1), "event");
+    }
     return SBG_OK;
 }
 
@@ -1005,8 +1012,10 @@ static int runTreeOp(sbg_batch b, int kind, const double* x, const double* fmob,
     OpIO io{kind, x ? dX : nullptr, fmob ? dF : nullptr, fbody ? dB : nullptr, dOut, b->dHostUOff, b->dHostBOff};
     double* sc = b->precision == SBG_PRECISION_FP64 ? static_cast<double*>(b->scratch)
                                                      : static_cast<double*>(b->opsScratch);
+    SBG_CUDA(cudaEventRecord(b->evOp0, b->stream), "event");
     SBG_CUDA(launchTreeOp(b->T, b->plan(), io, b->y, sc, static_cast<double*>(b->scratchLoop), b->status, b->stream),
              "tree-operator kernel launch");
+    SBG_CUDA(cudaEventRecord(b->evOp1, b->stream), "event");
     b->launches += b->segments();
     double* hOut = hX + (dOut - b->opsDev);
     if (nOut > 0)
@@ -1016,6 +1025,15 @@ static int runTreeOp(sbg_batch b, int kind, const double* x, const double* fmob,
                  "status download");
     SBG_CUDA(cudaStreamSynchronize(b->stream), "tree operator");
     std::memcpy(out, hOut, nOut * sizeof(double));
+    return SBG_OK;
+}
+
+int sbg_batch_last_operator_ms(sbg_batch b, double* ms) {
+    if (!b || !ms) return fail(SBG_ERR_INVALID, "null argument");
+    if (!b->evOp0) return fail(SBG_ERR_STATE, "no tree operator has run");
+    float t = 0.f;
+    SBG_CUDA(cudaEventElapsedTime(&t, b->evOp0, b->evOp1), "event");
+    *ms = t;
     return SBG_OK;
 }
 

@@ -201,6 +201,12 @@ class Batch:
         N.check(N.engine_lib().sbg_calc_composite_body_inertias(self._h, _dptr(out), _iptr(st)))
         return out, st
 
+    def last_operator_ms(self) -> float:
+        """Device time of the last tree operator's kernels (copies excluded)."""
+        ms = C.c_double()
+        N.check(N.engine_lib().sbg_batch_last_operator_ms(self._h, C.byref(ms)))
+        return ms.value
+
     def rk_merson_fixed(self, h: float, nsteps: int, accuracy: float = 0.0, constraint_tolerance: float = 0.0,
                         project_every_step: bool = False) -> np.ndarray:
         opts = N.IntegOpts(accuracy, constraint_tolerance, int(project_every_step), 0)

@@ -73,6 +73,7 @@ def test_tree_operators_match_oracle(engine, config, n, precision):
     R, st = b.calc_composite_body_inertias()
     assert (st == 0).all()
     assert _per_instance_rel(R, ref("composite"), bo10).max() <= 1e-12
+    assert b.last_operator_ms() > 0.0
 
 
 def test_tree_operators_leave_the_state_and_realize_untouched(engine):
