@@ -296,9 +296,14 @@ def trajectories():
         b.set_state(y0)
         ms, launches = time_rk(b, w.h, w.nsteps)
         y, _ = b.get_state()
+        _, st = b.get_ydot()
         body_steps = int(w.nbodies().sum()) * w.nsteps
         rec = {"precision": prec, "instances": w.ninst, "steps": w.nsteps, "h": w.h, "ms": ms,
-               "body_steps_per_s": body_steps / (ms * 1e-3), "gpu_launches": launches}
+               "body_steps_per_s": body_steps / (ms * 1e-3), "gpu_launches": launches,
+               # instances that reached a state where the mixed refinement
+               # reported an ill-conditioned M (SBG_INST_ILL_CONDITIONED)
+               "ill_conditioned_instances": int(((st & 32) != 0).sum()),
+               "other_status_nonzero": int(((st & ~32) != 0).sum())}
         if n_ref:
             idx = np.arange(n_ref)
             r, yr0 = engine_batch(w, "fp64", instances=idx)
@@ -365,7 +370,7 @@ def serving(seconds: float, chunk: int, budget_gb: float, cpu_sample_body_steps:
         srv.tick()
     t_end = srv.clock()
     lat, body_steps = np.empty(n), 0
-    status_bad = censored = 0
+    status_bad = censored = fp64_steps = reruns = 0
     status_bits = {}
     for i in range(n):
         inf = srv.info(ids[i])
@@ -373,6 +378,8 @@ def serving(seconds: float, chunk: int, budget_gb: float, cpu_sample_body_steps:
             lat[i] = inf["done_s"] - (t_start + arrivals[i])
             body_steps += inf["nbodies"] * inf["nsteps"]
             status_bad += inf["status"] != 0
+            fp64_steps += inf["fp64_steps"]
+            reruns += inf["attempts"] == 2
             for bit, name in [(1, "nonfinite"), (2, "singular_d"), (4, "projection_failed"), (8, "cholesky_fail")]:
                 if inf["status"] & bit:
                     status_bits[name] = status_bits.get(name, 0) + 1
@@ -407,6 +414,7 @@ def serving(seconds: float, chunk: int, budget_gb: float, cpu_sample_body_steps:
             "peak_resident": st["peak_resident"], "ticks": st["ticks"], "gpu_launches": st["launches"],
             "host_tick_seconds": st["host_seconds"],
             "requests_with_status": int(status_bad), "status_bits": status_bits, "censored": int(censored),
+            "requests_switched_to_fp64": int(fp64_steps), "requests_rerun_in_fp64": int(reruns),
             "deadline_s": deadline_s,
             "lanes": lanes,
             "cpu_alone_sequential": {"requests": k, "body_steps_per_s": cpu_bs / max(cpu_t, 1e-9), "cores": 1,
@@ -491,6 +499,7 @@ def run_ours(args):
         "fp64": {"value": value64, "ms_per_step": ms_64, "speedup_mixed_over_fp64": value / value64},
         "fp32_unrefined": {"value": nb_total / (ms_ft * 1e-3), "ms_per_step": ms_ft,
                            "udot_rel_err_max": float(err_ft.max())},
+        "fp64_fallback_instances": bmx.fallback_count(),
         "udot_rel_err": {"max": float(err.max()), "p99": float(np.quantile(err, 0.99)), "mean": float(err.mean()),
                          "definition": "per instance ||udot_mixed - udot_fp64||_2 / ||udot_fp64||_2"},
         "status_nonzero": int((stmx != 0).sum() + (st64 != 0).sum()),

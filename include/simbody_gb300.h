@@ -74,6 +74,15 @@ typedef enum sbg_precision {
 #define SBG_INST_PROJECTION_FAILED  4   /* quaternion/constraint projection refused */
 #define SBG_INST_CHOLESKY_FAIL      8   /* G M^-1 G^T not positive definite */
 #define SBG_INST_TIMEOUT           16   /* persistent kernel hit its iteration budget */
+/* Mixed form only: at some RHS of this instance the refinement correction was
+ * larger than 1e-4 of udot, i.e. the FP32 factorisation of M was too poorly
+ * conditioned for the mixed form's 1e-5 bar. sbg_realize_acceleration never
+ * reports it: it recomputes such instances in FP64. The server's mixed lane
+ * never reports it either: it continues the request in FP64. A mixed batch
+ * integration (sbg_rk_merson_fixed) reports it and carries on in mixed
+ * precision; rerun the instance in an FP64 batch for a result within FP64
+ * parity. */
+#define SBG_INST_ILL_CONDITIONED   32
 
 /* One mobilized body, numbered 1..nbodies in MobilizedBodyIndex order (Ground
  * is 0); parent < own index, as Simbody requires
@@ -250,6 +259,10 @@ int sbg_calc_composite_body_inertias(sbg_batch batch, double* R, int32_t* status
 /* Device time in milliseconds of the kernels of the batch's last tree
  * operator call (its copies excluded), from CUDA events on the batch's stream. */
 int sbg_batch_last_operator_ms(sbg_batch batch, double* ms);
+/* Mixed batches: how many instance realizations so far were recomputed in
+ * FP64 because the refinement reported an ill-conditioned M (see
+ * SBG_INST_ILL_CONDITIONED); 0 for other precisions. Synchronous. */
+int sbg_batch_fallback_count(sbg_batch batch, int64_t* n);
 
 /* RungeKuttaMersonIntegrator with setFixedStepSize(h), initialize(state) and
  * stepTo(t0 + nsteps*h) looped until reached (RungeKuttaMersonIntegrator.cpp:86-140,
@@ -330,7 +343,10 @@ typedef struct sbg_request_info {
     int32_t attempts;   /* 2: the mixed-precision run failed (non-finite, singular
                            D or failed projection) and the request was rerun
                            from its initial state in FP64 */
-    int32_t reserved;
+    int32_t fp64_steps; /* 1: a mixed-precision request reached a state where
+                           the mixed form's refinement could not meet its bar
+                           (SBG_INST_ILL_CONDITIONED) and took its remaining
+                           steps in FP64 */
 } sbg_request_info;
 
 typedef struct sbg_server_stats {

@@ -67,7 +67,7 @@ class ServerConfig(C.Structure):
 class RequestInfo(C.Structure):
     _fields_ = [("done", C.c_int32), ("status", C.c_int32), ("nbodies", C.c_int32), ("nsteps", C.c_int32),
                 ("t", C.c_double), ("submit_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double),
-                ("attempts", C.c_int32), ("reserved", C.c_int32)]
+                ("attempts", C.c_int32), ("fp64_steps", C.c_int32)]
 
 
 class ServerStats(C.Structure):
@@ -109,6 +109,7 @@ ENGINE_API = {
     "sbg_multiply_by_system_jacobian_transpose": (C.c_int, [vp, dp, dp, ip]),
     "sbg_calc_composite_body_inertias": (C.c_int, [vp, dp, ip]),
     "sbg_batch_last_operator_ms": (C.c_int, [vp, dp]),
+    "sbg_batch_fallback_count": (C.c_int, [vp, i64p]),
     "sbg_rk_merson_fixed": (C.c_int, [vp, C.c_double, C.c_int32, P(IntegOpts), ip]),
     "sbg_batch_stream": (vp, [vp]),
     "sbg_realize_acceleration_async": (C.c_int, [vp]),

@@ -777,6 +777,7 @@ __device__ __forceinline__ A3<float> body5(const DevTables& T, int row, int rec,
                 if (k < n) s = s + S(rec, eDI + i * N + k) * eps[k];
             const float d = s - (dot(ld3<float>(S, rec, eG + 6 * i), Apw) + dot(ld3<float>(S, rec, eG + 6 * i + 3), Apv));
             out.udot(uo + i, S(rec, eU0 + i) + d);
+            out.note(S(rec, eU0 + i), d);
             A.w = axpy(A.w, d, ld3<float>(S, rec, kRecH + 6 * i));
             A.v = axpy(A.v, d, ld3<float>(S, rec, kRecH + 6 * i + 3));
         }
@@ -1010,11 +1011,15 @@ struct YSrc {
     __device__ __forceinline__ double q(int k) const { return y[base + (int64_t)k * stride]; }
     __device__ __forceinline__ double u(int k) const { return y[base + (int64_t)(nq + k) * stride]; }
 };
+// umax / dmax: largest |udot0| and |refinement correction| seen by body5
+// (mixed form), for the ill-conditioning test.
 struct YdOut {
     double* yd;
     int64_t base, stride;
     int nq;
     bool finite = true;
+    float umax = 0.f, dmax = 0.f;
+    __device__ __forceinline__ void note(float u0, float d) { umax = fmaxf(umax, fabsf(u0)); dmax = fmaxf(dmax, fabsf(d)); }
     template <class R> __device__ __forceinline__ void qdot(int k, R v) {
         yd[base + (int64_t)k * stride] = double(v);
         finite &= isfinite(v);
@@ -1076,6 +1081,8 @@ template <class F> struct FOut {
     int64_t base, stride;
     int nq;
     bool finite = true;
+    float umax = 0.f, dmax = 0.f;
+    __device__ __forceinline__ void note(float u0, float d) { umax = fmaxf(umax, fabsf(u0)); dmax = fmaxf(dmax, fabsf(d)); }
     template <class R> __device__ __forceinline__ void qdot(int k, R v) { f[base + (int64_t)k * stride] = F(v); finite &= isfinite(v); }
     template <class R> __device__ __forceinline__ void udot(int k, R v) { f[base + (int64_t)(nq + k) * stride] = F(v); finite &= isfinite(v); }
     __device__ __forceinline__ double udotGet(int k) const { return double(f[base + (int64_t)(nq + k) * stride]); }
@@ -1103,6 +1110,20 @@ __device__ __forceinline__ Slot groupSlot(const DevTables& T, int blk0) {
 }
 
 #include "loops_device.cuh"
+
+// Mixed form: SBG_INST_ILL_CONDITIONED when the refinement correction exceeds
+// kIllConditioned of udot0 (max-norms over the instance, i.e. over the lanes
+// of its group). The correction is about cond(M) times the FP32 rounding, so
+// a large one means the FP32 factorisation is too poor for the mixed form's
+// accuracy bar. Non-negative floats order like their bit patterns.
+template <bool GROUP, class Out> __device__ __forceinline__ int illConditioned(const Out& out, const Slot& s) {
+    float um = out.umax, dm = out.dmax;
+    if constexpr (GROUP) {
+        um = __uint_as_float(__reduce_max_sync(s.mask, __float_as_uint(um)));
+        dm = __uint_as_float(__reduce_max_sync(s.mask, __float_as_uint(dm)));
+    }
+    return dm > kIllConditioned * um ? SBG_INST_ILL_CONDITIONED : 0;
+}
 
 // One RHS of the instance owned by slot s, through either driver; LOOPS adds
 // the Ball loop-closure multipliers (FP64; one-thread or level-parallel driver).
@@ -1138,10 +1159,14 @@ __device__ __forceinline__ int rhs(const DevTables& T, const Slot& s, R* scratch
         }
     } else if constexpr (GROUP) {
         const ScrRows<R> S{scratch + T.sbase[s.inst], T.inb[s.inst]};
-        return rhsGroup<R, NM, REF>(T, s.inst, S, src, out, s.gl, s.G, s.mask);
+        int st = rhsGroup<R, NM, REF>(T, s.inst, S, src, out, s.gl, s.G, s.mask);
+        if constexpr (REF) st |= illConditioned<true>(out, s);
+        return st;
     } else {
         const ScrTiled<R> S{scratch + T.sbase[s.inst]};
-        return rhsChain<R, NM, REF>(T, s.inst, S, src, out);
+        int st = rhsChain<R, NM, REF>(T, s.inst, S, src, out);
+        if constexpr (REF) st |= illConditioned<false>(out, s);
+        return st;
     }
 }
 
@@ -1161,6 +1186,34 @@ __global__ void __launch_bounds__(BS, MINB) realizeKernel(DevTables T, int first
     int st = rhs<R, NM, REF, GROUP, LOOPS>(T, s, scratch, src, out);
     if (!groupAll<GROUP>(out.finite, s)) st |= SBG_INST_NONFINITE;
     if (s.gl == 0) status[s.inst] = st;
+}
+
+// Mixed form: the instances of a segment (order positions [first, first +
+// count)) whose refinement reported an ill-conditioned M are recomputed in
+// FP64 on the FP64 mirror of their records, one thread per instance (the
+// level-parallel layout with a single lane). The other threads return at
+// once. T.fallbacks counts the recomputed instances.
+template <int NM, bool GROUP>
+__global__ void __launch_bounds__(128) realizeFallbackKernel(DevTables T, int first, int count,
+                                                             const double* __restrict__ y, double* __restrict__ ydot,
+                                                             int32_t* __restrict__ status) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int inst = T.order[first + t];
+    if (!(status[inst] & SBG_INST_ILL_CONDITIONED)) return;
+    YSrc src{y, T.ybase[inst], T.ystride[inst], T.inq[inst]};
+    YdOut out{ydot, T.ybase[inst], T.ystride[inst], T.inq[inst]};
+    int st;
+    if constexpr (GROUP) {
+        const ScrRows<double> S{T.scratch64 + T.sbase[inst], T.inb[inst]};
+        st = rhsGroup<double, NM, false>(T, inst, S, src, out, 0, 1, 1u << (threadIdx.x & 31));
+    } else {
+        const ScrTiled<double> S{T.scratch64 + T.sbase[inst]};
+        st = rhsChain<double, NM, false>(T, inst, S, src, out);
+    }
+    if (!out.finite) st |= SBG_INST_NONFINITE;
+    status[inst] = st;
+    atomicAdd(T.fallbacks, 1ULL);
 }
 
 template <class R, int NM, bool GROUP>
@@ -1189,6 +1242,35 @@ __device__ __forceinline__ void normalizeQuatAt(double* y, int64_t base, int64_t
 __device__ __forceinline__ double groupSum(double v, const Slot& s) {
     for (int off = s.G >> 1; off > 0; off >>= 1) v += __shfl_xor_sync(s.mask, v, off);
     return v;
+}
+
+// One RK-Merson stage RHS of a level-parallel instance of the mixed form,
+// out of line (the kernel keeps a single call site): the mixed RHS, then,
+// once the refinement reports an ill-conditioned M and `fallback` allows it,
+// the FP64 RHS on the FP64 mirror of the records from then on (*rhs64).
+// Returns the status bits (kStFp64 when it switched); *finite reports the
+// derivatives.
+template <int NM, class R>
+__device__ __noinline__ int stageRhsMixedGroup(const DevTables& T, const Slot& s, R* scratch, bool fallback,
+                                               bool* rhs64, const double* y, const R* f0, const R* a, const R* b,
+                                               int64_t base, int64_t stride, int nq, int stg, double c, R* dst,
+                                               bool* finite) {
+    StageSrc<R> src{y, f0, a, b, base, stride, nq, stg, c};
+    FOut<R> o{dst, base, stride, nq};
+    int r = 0;
+    if (!*rhs64) {
+        r = rhs<R, NM, true, true>(T, s, scratch, src, o);
+        if (!(fallback && (r & SBG_INST_ILL_CONDITIONED))) {
+            *finite = o.finite;
+            return r;
+        }
+        *rhs64 = true;
+        o.finite = true;
+        r = kStFp64;
+    }
+    r |= rhs<double, NM, false, true>(T, s, T.scratch64, src, o);
+    *finite = o.finite;
+    return r;
 }
 
 template <class R, int NM, bool REF, bool GROUP, int MINB = 1, bool LOOPS = false, int BS = 128>
@@ -1232,10 +1314,24 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
         }
     }
     const double projLimit = fmax(2 * consTol, sqrt(consTol));
+    // Mixed form in the server's lane: once the refinement reports an
+    // ill-conditioned M, the instance's RHS runs in FP64 on the FP64 mirror of
+    // its records for the rest of the request (kStFp64 in its status word
+    // keeps that across launches). A batch has no per-instance control: it
+    // keeps SBG_INST_ILL_CONDITIONED in the status and stays mixed.
+    const bool fallback = REF && GROUP && T.ictl && T.scratch64;
+    bool rhs64 = fallback && (st & kStFp64);
     auto stage = [&](int stg, double c, const R* a, const R* b, R* dst) {
         StageSrc<R> src{y, f0, a, b, base, stride, nq, stg, c};
         FOut<R> o{dst, base, stride, nq};
-        st |= rhs<R, NM, REF, GROUP, LOOPS>(T, s, scratch, src, o);
+        if constexpr (REF && GROUP) {
+            bool fin = true;
+            st |= stageRhsMixedGroup<NM, R>(T, s, scratch, fallback, &rhs64, y, f0, a, b, base, stride, nq, stg, c,
+                                            dst, &fin);
+            o.finite = fin;
+        } else {
+            st |= rhs<R, NM, REF, GROUP, LOOPS>(T, s, scratch, src, o);
+        }
         if (!groupAll<GROUP>(o.finite, s)) st |= SBG_INST_NONFINITE;
         if constexpr (GROUP) __syncwarp(s.mask);  // the next stage reads what other lanes wrote
     };

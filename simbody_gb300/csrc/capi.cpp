@@ -133,6 +133,11 @@ struct sbg_batch_s {
     LaunchPlan plan() const { return LaunchPlan{nChain, nGroupBlocks, nm, variant == 0 ? 1 : variant, nLoop}; }
     BatchBufs bufsArg() const { return BatchBufs{scratch, scratchLoop, fbuf, fbufLoop, colElems}; }
     int segments() const { return (nChain > 0) + (nLoop > 0) + (nGroupBlocks > 0); }
+    // kernels of one realize: the segments, and in the mixed form the FP64
+    // recomputation pass after the chain and the level-parallel segment
+    int realizeLaunches() const {
+        return segments() + (T.scratch64 ? (nChain > 0) + (nGroupBlocks > 0) : 0);
+    }
 
     // Lanes per instance of the group segment: blocks of 128 threads hold
     // 128/G instances of equal G (the order is sorted by widest level, so G is
@@ -672,6 +677,16 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     if ((rc = b->alloc(&p, std::max<int64_t>(b->nyTotal, 1) * sizeof(double), "staging"))) return bail(rc);
     b->staging = static_cast<double*>(p);
     if ((rc = b->alloc(&b->scratch, std::max<int64_t>(b->scratchElems, 1) * rsz, "scratch"))) return bail(rc);
+    if (precision == SBG_PRECISION_MIXED && b->scratchElems > 0) {
+        // FP64 mirror of the scratch for the instances whose refinement
+        // reports an ill-conditioned M, and the count of those recomputed
+        if ((rc = b->alloc(&p, b->scratchElems * sizeof(double), "FP64 scratch mirror"))) return bail(rc);
+        T.scratch64 = static_cast<double*>(p);
+        if ((rc = b->alloc(&p, sizeof(unsigned long long), "fallback counter"))) return bail(rc);
+        T.fallbacks = static_cast<unsigned long long*>(p);
+        const cudaError_t ez = cudaMemset(p, 0, sizeof(unsigned long long));
+        if (ez != cudaSuccess) return bail(cudaFail(ez, "fallback counter"));
+    }
     if ((rc = b->alloc(&b->fbuf, 4 * std::max<int64_t>(b->colElems, 1) * rsz, "stage derivatives"))) return bail(rc);
     if (b->nLoop > 0) {
         if ((rc = b->alloc(&b->scratchLoop, scratchLoopElems * sizeof(double), "loop scratch"))) return bail(rc);
@@ -769,7 +784,7 @@ static int timePlan(sbg_batch b, float* ms) {
     SBG_CUDA(cudaEventRecord(b->evT1, b->stream), "tuner");
     SBG_CUDA(cudaEventSynchronize(b->evT1), "tuner");
     SBG_CUDA(cudaEventElapsedTime(ms, b->evT0, b->evT1), "tuner");
-    b->launches += 5 * b->segments();
+    b->launches += 5 * b->realizeLaunches();
     return SBG_OK;
 }
 
@@ -830,7 +845,7 @@ int sbg_realize_acceleration_async(sbg_batch b) {
         if (e != cudaSuccess) return cudaFail(e, "graph instantiate");
     }
     SBG_CUDA(cudaGraphLaunch(b->realizeGraph, b->stream), "realize graph launch");
-    b->launches += b->segments();
+    b->launches += b->realizeLaunches();
     return SBG_OK;
 }
 
@@ -923,7 +938,7 @@ int sbg_realize_acceleration_host(sbg_batch b, const double* y, double* ydot, in
         if (stPinned)
             SBG_CUDA(cudaMemcpyAsync(status + i0, b->status + i0, (i1 - i0) * sizeof(int32_t), cudaMemcpyDeviceToHost,
                                      st), "status download");
-        b->launches += 3;
+        b->launches += 3 + (b->T.scratch64 ? 1 : 0);
     }
     for (int k = 1; k < nstreams; ++k) {
         SBG_CUDA(cudaEventRecord(b->pipeEv[k], b->pipe[k]), "pipeline");
@@ -966,7 +981,8 @@ static int ensureTreeOps(sbg_batch b) {
     int rc;
     void* p = nullptr;
     if (b->precision != SBG_PRECISION_FP64 && !b->opsScratch && b->scratchElems > 0) {
-        if ((rc = b->alloc(&b->opsScratch, b->scratchElems * sizeof(double), "tree-operator scratch"))) return rc;
+        if (b->T.scratch64) b->opsScratch = b->T.scratch64;  // the mixed form's FP64 mirror has the layout
+        else if ((rc = b->alloc(&b->opsScratch, b->scratchElems * sizeof(double), "tree-operator scratch"))) return rc;
     }
     if ((rc = b->alloc(&p, std::max<int64_t>(need, 1) * sizeof(double), "tree-operator operands"))) return rc;
     b->opsDev = static_cast<double*>(p);
@@ -1025,6 +1041,18 @@ static int runTreeOp(sbg_batch b, int kind, const double* x, const double* fmob,
                  "status download");
     SBG_CUDA(cudaStreamSynchronize(b->stream), "tree operator");
     std::memcpy(out, hOut, nOut * sizeof(double));
+    return SBG_OK;
+}
+
+int sbg_batch_fallback_count(sbg_batch b, int64_t* n) {
+    if (!b || !n) return fail(SBG_ERR_INVALID, "null argument");
+    *n = 0;
+    if (!b->T.fallbacks) return SBG_OK;
+    SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    unsigned long long v = 0;
+    SBG_CUDA(cudaStreamSynchronize(b->stream), "fallback count");
+    SBG_CUDA(cudaMemcpy(&v, b->T.fallbacks, sizeof(v), cudaMemcpyDeviceToHost), "fallback count");
+    *n = (int64_t)v;
     return SBG_OK;
 }
 

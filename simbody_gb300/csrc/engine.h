@@ -117,6 +117,12 @@ struct DevTables {
     const double* lst;       // per constraint: station 1 (in body 1), station 2 (in body 2)
     const int32_t* lslot;    // per body row: slot index of a loop body (-1 = none): level-parallel layout
     const int32_t* bidx;     // per body row: index of the body in its system description (tree operators)
+    // FP64 mirror of the scratch with the same element offsets (mixed batches
+    // and the server's mixed lane; null otherwise): where the mixed form's
+    // refinement reports an ill-conditioned M the RHS is recomputed in FP64
+    // on these records.
+    double* scratch64;
+    unsigned long long* fallbacks;  // instances recomputed in FP64 by realize (cumulative; null = none)
     const int32_t* icons;    // per instance: first constraint
     const int32_t* incons;   // per instance: number of constraints
     // per-instance integration control (the serving loop; null in a batch,
@@ -127,6 +133,12 @@ struct DevTables {
 constexpr int kCtlSteps = (1 << 24) - 1;
 constexpr int kCtlInit = 1 << 30;                // first launch: Integrator::initialize projections
 constexpr int kCtlProjectEveryStep = 1 << 29;    // Integrator::setProjectEveryStep(true)
+// Status-word bit kept across a request's launches in the server: its RHS
+// runs in FP64 from now on (stripped before the status is reported).
+constexpr int kStFp64 = 1 << 30;
+// The mixed form's refinement trusts its FP32 factorisation while the
+// correction stays within this fraction of udot (max-norms).
+constexpr float kIllConditioned = 1e-4f;
 
 // How one batch operation is launched: order positions [0, nChain) run the
 // chain driver (one thread per instance, width nm), the next nLoop positions

@@ -24,8 +24,12 @@ template <bool REF> static void pick(const KArgs& a, cudaStream_t s) {
 }
 
 void realize32Chain(const KArgs& a, bool refine, cudaStream_t s) {
-    if (refine) pick<true>(a, s);
-    else pick<false>(a, s);
+    if (refine) {
+        pick<true>(a, s);
+        realizeFallback(a, false, s);
+    } else {
+        pick<false>(a, s);
+    }
 }
 
 }  // namespace sbg

@@ -10,7 +10,10 @@ template <bool REF, int MINB> static void go(const KArgs& a, cudaStream_t s) {
 }
 
 void realize32Group(const KArgs& a, bool refine, cudaStream_t s) {
-    if (refine) { if (a.P->variant >= 4) go<true, 4>(a, s); else go<true, 1>(a, s); }
+    if (refine) {
+        if (a.P->variant >= 4) go<true, 4>(a, s); else go<true, 1>(a, s);
+        realizeFallback(a, true, s);
+    }
     else { if (a.P->variant >= 4) go<false, 4>(a, s); else go<false, 1>(a, s); }
 }
 

@@ -88,6 +88,9 @@ void rk64Chain(const KArgs& a, cudaStream_t s);
 void rk64Group(const KArgs& a, cudaStream_t s);
 void rk32Chain(const KArgs& a, bool refine, cudaStream_t s);
 void rk32Group(const KArgs& a, bool refine, cudaStream_t s);
+// FP64 recomputation of the instances the mixed realize flagged
+// SBG_INST_ILL_CONDITIONED (k_fallback.cu); a no-op without T.scratch64.
+void realizeFallback(const KArgs& a, bool group, cudaStream_t s);
 void realizeLoop(const KArgs& a, cudaStream_t s);  // k_loops.cu
 void minvLoop(const KArgs& a, cudaStream_t s);
 void rkLoop(const KArgs& a, cudaStream_t s);

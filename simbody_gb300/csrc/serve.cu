@@ -158,6 +158,7 @@ struct ServeReq {
     Footprint fp;
     double cost = 0;       // estimated GPU time per step (stepCost)
     int32_t attempts = 1;  // 2: rerun in FP64 after the mixed-precision run failed
+    int32_t fp64Steps = 0; // 1: its RHS switched to FP64 (an ill-conditioned M)
 };
 
 enum RowTable { R_PARENT = 0, R_INFO, R_QOFF, R_UOFF, R_SREC, R_FBEG, R_FCNT, R_LREC, R_CBEG, R_CCNT, R_CLIST, R_LEV,
@@ -191,6 +192,7 @@ struct ServeLane {
     void* fbuf = nullptr;
     void* fbufLoop = nullptr;
     void* scratch = nullptr;
+    double* scratch64 = nullptr;  // mixed lane: FP64 mirror of scratch (same offsets)
     double* scratchLoop = nullptr;
     // slots
     int32_t *ibody = nullptr, *inb = nullptr, *inq = nullptr, *inu = nullptr, *ilev = nullptr, *inlev = nullptr,
@@ -271,7 +273,7 @@ int64_t bytesPerUnit(int k, size_t rsz, bool fp64) {
     case kPoolRows: return kRowTables * 4 + kParamStride * (fp64 ? 8 : 8 + 4);
     case kPoolForces: return 4 + 2 * 8 + 2 * 4;
     case kPoolState: return 8 + 4 * (int64_t)rsz + (fp64 ? 0 : 4 * 8);
-    case kPoolScratch: return (int64_t)rsz;
+    case kPoolScratch: return (int64_t)rsz + (fp64 ? 0 : 8);  // mixed: + the FP64 mirror
     default: return 8;
     }
 }
@@ -445,6 +447,8 @@ void harvest(ServeLane* s, const TickRec& tr) {
         std::memcpy(r.y.data(), p, r.y.size() * 8);
         std::memcpy(&r.t, p + r.y.size() * 8, 8);
         std::memcpy(&r.status, p + r.y.size() * 8 + 8, 4);
+        if (r.status & kStFp64) r.fp64Steps = 1;
+        r.status &= ~kStFp64;
         if (s->retryFailed && (r.status & (SBG_INST_NONFINITE | SBG_INST_SINGULAR_D | SBG_INST_PROJECTION_FAILED))) {
             s->retry.push_back(s->byId[pr.first]);  // rerun from y0 in FP64; not done yet
             continue;
@@ -550,6 +554,7 @@ int laneCreate(const sbg_server_config* cfg, int64_t budget, std::chrono::steady
         float* p = nullptr;
         if ((rc = s->alloc(&p, s->cap[kPoolScratch], "scratch"))) return bail(rc);
         s->scratch = p;
+        if ((rc = s->alloc(&s->scratch64, s->cap[kPoolScratch], "FP64 scratch mirror"))) return bail(rc);
     }
     if ((rc = s->alloc(&s->scratchLoop, s->cap[kPoolLoopScratch], "loop scratch"))) return bail(rc);
     int32_t** i32[] = {&s->ibody, &s->inb, &s->inq, &s->inu, &s->ilev, &s->inlev, &s->icons, &s->incons,
@@ -621,6 +626,7 @@ int laneCreate(const sbg_server_config* cfg, int64_t budget, std::chrono::steady
     T.incons = s->incons;
     T.ictl = s->ictl;
     T.iparam = s->iparam;
+    T.scratch64 = s->scratch64;
     *out = s;
     return SBG_OK;
 }
@@ -1052,7 +1058,7 @@ int sbg_server_result(sbg_server s, int64_t id, double* y, sbg_request_info* inf
         info->admit_s = r.admitS;
         info->done_s = r.doneS;
         info->attempts = r.attempts;
-        info->reserved = 0;
+        info->fp64_steps = r.fp64Steps;
     }
     if (!r.done) return info ? SBG_OK : setError(SBG_ERR_STATE, "request not finished");
     if (y) std::memcpy(y, r.y.data(), r.y.size() * 8);

@@ -201,6 +201,13 @@ class Batch:
         N.check(N.engine_lib().sbg_calc_composite_body_inertias(self._h, _dptr(out), _iptr(st)))
         return out, st
 
+    def fallback_count(self) -> int:
+        """Mixed batches: realizations recomputed in FP64 so far (an
+        ill-conditioned M; SBG_INST_ILL_CONDITIONED)."""
+        n = C.c_int64()
+        N.check(N.engine_lib().sbg_batch_fallback_count(self._h, C.byref(n)))
+        return n.value
+
     def last_operator_ms(self) -> float:
         """Device time of the last tree operator's kernels (copies excluded)."""
         ms = C.c_double()
