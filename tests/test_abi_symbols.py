@@ -37,3 +37,28 @@ def test_abi_version_and_no_device_here():
 def test_struct_layouts_match_header():
     assert C.sizeof(N.BodyDesc) == 280
     assert C.sizeof(N.SystemDesc) == 64
+
+
+def test_batch_entry_points_refuse_a_null_batch_without_touching_the_device():
+    """Argument checks come before any CUDA call, so they hold on a machine
+    without a GPU: a null batch is SBG_ERR_INVALID with a message."""
+    from simbody_gb300.build import build_engine
+
+    build_engine()
+    lib = N.engine_lib()
+    d = (C.c_double * 4)()
+    i32 = (C.c_int32 * 4)()
+    i64 = C.c_int64()
+    calls = {
+        "sbg_calc_residual_force": (None, d, d, d, d, i32),
+        "sbg_multiply_by_m": (None, d, d, i32),
+        "sbg_multiply_by_system_jacobian": (None, d, d, i32),
+        "sbg_multiply_by_system_jacobian_transpose": (None, d, d, i32),
+        "sbg_calc_composite_body_inertias": (None, d, i32),
+        "sbg_multiply_by_minv": (None, d, d),
+        "sbg_batch_fallback_count": (None, C.byref(i64)),
+        "sbg_batch_last_operator_ms": (None, d),
+    }
+    for name, args in calls.items():
+        assert getattr(lib, name)(*args) == 1, name  # SBG_ERR_INVALID
+        assert lib.sbg_last_error(), name
