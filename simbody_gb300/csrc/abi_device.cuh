@@ -16,7 +16,12 @@
 // residual r = f - tau(udot0) and runs the first M^-1 pass on it, pass 5 (base
 // to tip) applies udot = udot0 + M^-1 r with the FP32 factorization. This
 // takes the relative udot error of an FP32 recursion (up to ~1e-4 on random
-// trees) to the few-1e-6 level set by the FP32 kinematics.
+// trees) to the few-1e-6 level set by the FP32 kinematics, as long as M is
+// well conditioned. Where the correction exceeds 1e-4 of udot (an
+// ill-conditioned M, the FP32 factorisation too poor for the refinement to
+// converge) the instance is flagged SBG_INST_ILL_CONDITIONED and, in a
+// realize or the server's mixed lane, recomputed in FP64 on an FP64 mirror
+// of its records.
 //
 // Two mappings drive the same per-body code:
 //   chain driver  one thread per instance walks its rows in order; along a

@@ -35,7 +35,9 @@ constexpr int kMaxDof = 6;
 //  18  pc[3] Gi[6] l[3] a[6] bF[6]
 //  42  Pacc: M[6] J[6] F[9], zacc[6]      (pass 2 accumulators)
 //      reused after pass 2: [42,54) F_df (double-float inverse-dynamics force),
-//      [54,60) z2acc (refinement M^-1 accumulator)
+//      [54,60) z2acc (refinement M^-1 accumulator); the tree operators
+//      (ops_device.cuh) keep A [42,48) and F [48,54), or a composite inertia
+//      [42,52), there
 //  69  H[6n] f[n] DI[n*n] G[6n] eps[n] udot0[n]
 #ifdef __CUDACC__
 #define SBG_HD __host__ __device__
