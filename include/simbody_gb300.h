@@ -218,7 +218,10 @@ int sbg_realize_acceleration_host(sbg_batch batch, const double* y, double* ydot
 
 /* SimbodyMatterSubsystem::multiplyByMInv(state, f, MInvf)
  * (Simbody/include/simbody/internal/SimbodyMatterSubsystem.h:1343):
- * f and out are packed like the u parts of y (nu values per instance). */
+ * f and out are packed like the u parts of y (nu values per instance). It
+ * runs in the batch's precision; a mixed batch uses the FP32 recursion
+ * without refinement, whose relative error grows with the condition number
+ * of M. An FP64 batch gives the reference's result to 1e-12. */
 int sbg_multiply_by_minv(sbg_batch batch, const double* f, double* out);
 
 /* Tree operators on the batch's current state, for every instance. They run
