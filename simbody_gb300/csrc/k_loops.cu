@@ -1,6 +1,7 @@
-// k_loops.cu -- kernels of the loop-closure segments (FP64): the one-thread driver with
-// Constraint::Ball multipliers (realize, RK-Merson with projections) and the
-// tree M^-1 of those instances.
+// k_loops.cu -- kernels of the loop-closure segments (FP64): realize with
+// Constraint::Ball multipliers and the tree M^-1 of those instances on the
+// one-thread driver, and the level-parallel driver's realize and RK-Merson
+// (the one-thread RK-Merson is in k_rkloops.cu).
 #include "abi_device.cuh"
 
 namespace sbg {
@@ -23,20 +24,6 @@ void minvLoop(const KArgs& a, cudaStream_t s) {
         minvKernel<double, 1, false><<<nb, 128, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.f, a.ydot, sc, a.status);
     else
         minvKernel<double, 3, false><<<nb, 128, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.f, a.ydot, sc, a.status);
-}
-
-void rkLoop(const KArgs& a, cudaStream_t s) {
-    double* sc = static_cast<double*>(a.scratchLoop);
-    double* fb = static_cast<double*>(a.fbufLoop);
-    const int first = a.P->nChain, nb = loopBlocks(*a.P);
-    if (a.P->nm == 1)
-        rkMersonKernel<double, 1, false, false, 1, true><<<nb, 128, 0, s>>>(
-            *a.T, first, a.P->nLoop, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.nsteps, a.accuracy, a.consTol,
-            a.projectEveryStep);
-    else
-        rkMersonKernel<double, 3, false, false, 1, true><<<nb, 128, 0, s>>>(
-            *a.T, first, a.P->nLoop, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.nsteps, a.accuracy, a.consTol,
-            a.projectEveryStep);
 }
 
 // Loop-closure instances on the level-parallel driver (FP64): tree passes on

@@ -1,35 +1,13 @@
 // k_r32c.cu -- realize(Acceleration) kernel instantiations, FP32 recursions,
-// chain driver (refine = double-float residual refinement). Occupancy
-// variants: 1 = 128-thread blocks with every register the code wants; 4 =
-// 128-thread blocks, at most 128 registers (4 blocks per SM); 7 = 64-thread
-// blocks, at most 144 registers (7 blocks per SM), which keeps a batch of
-// 65,536 one-thread instances in a single balanced wave over 152 SMs.
-#include "abi_device.cuh"
+// chain driver: the dispatch and the unrefined form (the refined form, with
+// its FP64 recomputation pass, is in k_r32cr.cu).
+#include "r32c_launch.cuh"
 
 namespace sbg {
 
-template <bool REF, int MINB, int BS> static void go(const KArgs& a, cudaStream_t s) {
-    const int nb = (a.P->nChain + BS - 1) / BS;
-    float* sc = static_cast<float*>(a.scratch);
-    if (a.P->nm == 1)
-        realizeKernel<float, 1, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
-    else
-        realizeKernel<float, 3, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
-}
-
-template <bool REF> static void pick(const KArgs& a, cudaStream_t s) {
-    if (a.P->variant == 4) go<REF, 4, 128>(a, s);
-    else if (a.P->variant == 7) go<REF, 7, 64>(a, s);
-    else go<REF, 1, 128>(a, s);
-}
-
 void realize32Chain(const KArgs& a, bool refine, cudaStream_t s) {
-    if (refine) {
-        pick<true>(a, s);
-        realizeFallback(a, false, s);
-    } else {
-        pick<false>(a, s);
-    }
+    if (refine) realize32ChainRefined(a, s);
+    else r32ChainPick<false>(a, s);
 }
 
 }  // namespace sbg

@@ -94,6 +94,7 @@ void realizeFallback(const KArgs& a, bool group, cudaStream_t s);
 void realizeLoop(const KArgs& a, cudaStream_t s);  // k_loops.cu
 void minvLoop(const KArgs& a, cudaStream_t s);
 void rkLoop(const KArgs& a, cudaStream_t s);
+void rkLoopWidth1(const KArgs& a, cudaStream_t s);  // k_rkloops1.cu: rkLoop for batch width 1
 void rkLoopGroup(const KArgs& a, cudaStream_t s);      // loop closures, level-parallel driver
 void realizeLoopGroup(const KArgs& a, cudaStream_t s);
 
