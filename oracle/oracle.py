@@ -35,6 +35,11 @@ def lib() -> C.CDLL:
                                            dp, dp, C.c_int32]
         L.oracle_system_forces_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, i64p, i64p, dp, dp,
                                                  C.c_int32]
+        L.oracle_rk_merson_adaptive_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, dp, C.c_double,
+                                                      C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                                      C.c_int32, C.c_int32, ip, i64p, C.c_int32]
+        L.oracle_adjust_step_size.argtypes = [C.c_double, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double,
+                                              dp]
         L.oracle_count_realize.argtypes = [sd, dp, i64p]
         L.oracle_time_realize.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, dp, C.c_int32, C.c_int32]
         L.oracle_time_realize.restype = C.c_double
@@ -139,6 +144,31 @@ def rk_merson(systems, nsys, sys_of, y_off, y, h, nsteps, t=None, accuracy=0.0, 
                                         _d(y), _d(tt), float(h), int(nsteps), accuracy, cons_tol,
                                         int(project_every_step), _i(st), C.byref(npj), nthreads))
     return y, tt, st, npj.value
+
+
+def rk_merson_adaptive(systems, nsys, sys_of, y_off, y, t_final, t=None, h_init=0.0, h_min=0.0, h_max=0.0,
+                       accuracy=0.0, cons_tol=0.0, project_every_step=False, max_steps=1_000_000, nthreads=0):
+    """Error-controlled RK-Merson to t_final (instances without constraints).
+    Returns (y, t, status, stats) with stats[i] = (accepted, rejected)."""
+    sys_of = np.ascontiguousarray(sys_of, dtype=np.int32)
+    y = np.array(y, dtype=np.float64, copy=True)
+    tt = np.zeros(len(sys_of)) if t is None else np.array(t, dtype=np.float64, copy=True)
+    st = np.empty(len(sys_of), dtype=np.int32)
+    stats = np.zeros((len(sys_of), 2), dtype=np.int64)
+    _check(lib().oracle_rk_merson_adaptive_batch(systems, nsys, _i(sys_of), len(sys_of),
+                                                 _l(np.ascontiguousarray(y_off)), _d(y), _d(tt), float(t_final),
+                                                 float(h_init), float(h_min), float(h_max), float(accuracy),
+                                                 float(cons_tol), int(project_every_step), int(max_steps), _i(st),
+                                                 _l(stats), nthreads))
+    return y, tt, st, stats
+
+
+def adjust_step_size(err, h, accuracy=1e-3, err_order=4, limited=False, h_min=0.0, h_max=0.0):
+    """The step-size controller alone: (success, new h)."""
+    hh = C.c_double(h)
+    ok = lib().oracle_adjust_step_size(float(err), int(err_order), int(limited), float(accuracy), float(h_min),
+                                       float(h_max), C.byref(hh))
+    return bool(ok), hh.value
 
 
 def count_realize(system_ptr, y):

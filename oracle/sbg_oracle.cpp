@@ -556,6 +556,137 @@ int rkMerson(const Topology& t, double* y, double* time, double h, int nsteps, c
     return status;
 }
 
+// ======================================================= variable step
+// AbstractIntegratorRep::adjustStepSize (AbstractIntegratorRep.cpp:448-502):
+// the next step size from the error norm of the step just attempted (order
+// errOrder). Returns whether the step succeeded: the new size is not smaller.
+// hMin / hMax <= 0: no user limit (the reference's -1).
+bool adjustStepSize(double err, int errOrder, bool hWasArtificiallyLimited, double accuracy, double hMin,
+                    double hMax, double& h) {
+    const double Safety = 0.9, MinShrink = 0.1, MaxGrow = 5, HysteresisLow = 0.9, HysteresisHigh = 1.2;
+    double hNew;
+    if (!std::isfinite(err)) hNew = MinShrink * h;
+    else if (err == 0) hNew = MaxGrow * h;
+    else hNew = Safety * h * std::pow(accuracy / err, 1 / double(errOrder));
+    if (hNew > h && (hWasArtificiallyLimited || hNew < HysteresisHigh * h)) hNew = h;
+    if (hNew < h) {
+        if (err <= accuracy) hNew = h;
+        else hNew = std::min(hNew, HysteresisLow * h);
+    }
+    hNew = std::min(hNew, MaxGrow * h);
+    hNew = std::max(hNew, MinShrink * h);
+    if (hMin > 0) hNew = std::max(hNew, hMin);
+    if (hMax > 0) hNew = std::min(hNew, hMax);
+    const bool success = hNew >= h;
+    h = hNew;
+    return success;
+}
+
+// Error-controlled RK-Merson for an instance without constraints:
+// Integrator::setFinalTime(tFinal), initialize(state) (quaternions
+// normalized), then stepTo(tFinal) until reached. The first step size is the
+// system timescale / 10 = 0.01 (AbstractIntegratorRep.cpp:41-49,
+// SystemGutsRep.h:50) unless hInit > 0. Each internal step
+// (AbstractIntegratorRep.cpp:513-577) picks t1 against tMax = tFinal,
+// attempts the RK-Merson step (the stages and yErr as in rkMerson), projects
+// when errNorm <= 2^4 accuracy: quaternions are normalized when their RMS error
+// exceeds consTol (or projectEveryStep), removing the radial component of
+// their error estimate (RigidBodyNodeSpec_Ball.h:417-434); an RMS error above
+// max(2 consTol, sqrt(consTol)) fails the attempt (errNorm = infinity). The
+// error norm after projection decides through adjustStepSize; a failed
+// attempt restores y and retries with the smaller step. Returns SBG_INST_*
+// bits; SBG_INST_TIMEOUT when maxSteps accepted steps did not reach tFinal or
+// the step size no longer advances time.
+int rkMersonAdaptive(const Topology& t, double* y, double* time, double tFinal, double hInit, double hMin,
+                     double hMax, const IntegOpts& o, Work<double>& w, int maxSteps, int64_t* accepted,
+                     int64_t* rejected) {
+    const int ny = t.nq + t.nu;
+    int status = 0;
+    std::vector<double> y0(ny), f0(ny), fa(ny), fb(ny), ysave(ny), ytmp(ny), yerr(ny), uScale(t.nu);
+    auto rhs = [&](const double* yy, double* f) {
+        if (!realizeAcceleration(t, yy, w, f)) status |= SBG_INST_SINGULAR_D;
+    };
+    normalizeQuaternions(t, y);
+    double h = hInit > 0 ? hInit : 0.1 / 10;
+    if (hMin > 0) h = std::max(h, hMin);
+    if (hMax > 0) h = std::min(h, hMax);
+    const double projLimit = std::max(2 * o.consTol, std::sqrt(o.consTol));
+    double tc = *time;
+    int64_t nAcc = 0, nRej = 0;
+    while (tc < tFinal) {
+        if (nAcc >= maxSteps) { status |= SBG_INST_TIMEOUT; break; }
+        const double t0 = tc;
+        for (int i = 0; i < ny; ++i) y0[i] = y[i];
+        for (int i = 0; i < t.nu; ++i) {  // calcRelativeScaling (IntegratorRep.h:644-655), w = 1
+            const double vi = std::abs(y0[t.nq + i]);
+            uScale[i] = vi > 1 ? 1 / vi : 1.0;
+        }
+        rhs(y0.data(), f0.data());
+        double t1 = t0;
+        for (;;) {
+            bool limited = false;
+            if (tFinal < t0 + 0.95 * h) { limited = true; t1 = tFinal; }
+            else if (tFinal > t0 + 1.001 * h) t1 = t0 + h;
+            else t1 = tFinal;
+            if (!(t1 > t0)) { status |= SBG_INST_TIMEOUT; break; }
+            const double hs = t1 - t0;
+            const double h3 = hs / 3, h6 = hs / 6, h8 = hs / 8, h2 = hs / 2;
+            for (int i = 0; i < ny; ++i) ytmp[i] = y0[i] + h3 * f0[i];
+            rhs(ytmp.data(), fa.data());  // f1
+            for (int i = 0; i < ny; ++i) ytmp[i] = y0[i] + h6 * (f0[i] + fa[i]);
+            rhs(ytmp.data(), fa.data());  // f2
+            for (int i = 0; i < ny; ++i) ytmp[i] = y0[i] + h8 * (f0[i] + 3 * fa[i]);
+            rhs(ytmp.data(), fb.data());  // f3
+            for (int i = 0; i < ny; ++i) ysave[i] = y0[i] + h2 * ((f0[i] - 3 * fa[i]) + 4 * fb[i]);
+            rhs(ysave.data(), fa.data());  // f4
+            for (int i = 0; i < ny; ++i) y[i] = y0[i] + h6 * ((f0[i] + 4 * fb[i]) + fa[i]);
+            for (int i = 0; i < ny; ++i) yerr[i] = 0.2 * std::abs(y[i] - ysave[i]);
+            double errNorm = errorNorm(t, y, yerr.data(), uScale.data());
+            if (errNorm <= 16 * o.accuracy) {  // attemptDAEStep (AbstractIntegratorRep.cpp:158-199)
+                double sq = 0;
+                int nqt = 0;
+                for (int bi = 1; bi <= t.nb; ++bi) {
+                    const Body& b = t.b[bi];
+                    if (b.type != SBG_BALL && b.type != SBG_FREE) continue;
+                    const double* qq = y + b.qoff;
+                    const double e = std::sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]) - 1;
+                    sq += e * e;
+                    ++nqt;
+                }
+                const double quatNorm = nqt ? std::sqrt(sq / nqt) : 0.0;
+                if (quatNorm > projLimit) {
+                    errNorm = HUGE_VAL;  // the step did not converge
+                } else if (quatNorm > o.consTol || o.projectEveryStep) {
+                    for (int bi = 1; bi <= t.nb; ++bi) {
+                        const Body& b = t.b[bi];
+                        if (b.type != SBG_BALL && b.type != SBG_FREE) continue;
+                        double* qq = y + b.qoff;
+                        double* qe = yerr.data() + b.qoff;
+                        const double n = std::sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);
+                        for (int k = 0; k < 4; ++k) qq[k] = qq[k] / n;
+                        const double d = qe[0] * qq[0] + qe[1] * qq[1] + qe[2] * qq[2] + qe[3] * qq[3];
+                        for (int k = 0; k < 4; ++k) qe[k] = qe[k] - d * qq[k];
+                    }
+                    errNorm = errorNorm(t, y, yerr.data(), uScale.data());
+                }
+            }
+            if (adjustStepSize(errNorm, 4, limited, o.accuracy, hMin, hMax, h)) break;
+            ++nRej;
+            for (int i = 0; i < ny; ++i) y[i] = y0[i];
+            if (nRej > 64 * (int64_t)maxSteps) { status |= SBG_INST_TIMEOUT; break; }
+        }
+        if (status & SBG_INST_TIMEOUT) break;
+        for (int i = 0; i < ny; ++i)
+            if (!std::isfinite(y[i])) status |= SBG_INST_NONFINITE;
+        tc = t1;
+        ++nAcc;
+    }
+    *time = tc;
+    if (accepted) *accepted = nAcc;
+    if (rejected) *rejected = nRej;
+    return status;
+}
+
 }  // namespace sbgo
 
 // ===================================================================== C API
@@ -756,6 +887,46 @@ int oracle_system_forces_batch(const sbg_system_desc* systems, int32_t nsys, con
             }
     });
     return 0;
+}
+
+// Error-controlled RK-Merson to tFinal for every instance (no constraints;
+// rkMersonAdaptive). hInit / hMin / hMax <= 0: the reference's defaults.
+// stats (may be NULL): accepted and rejected steps, 2 per instance.
+int oracle_rk_merson_adaptive_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of,
+                                    int32_t ninst, const int64_t* y_off, double* y, double* t, double tFinal,
+                                    double hInit, double hMin, double hMax, double accuracy, double consTol,
+                                    int32_t projectEveryStep, int32_t maxSteps, int32_t* status, int64_t* stats,
+                                    int32_t nthreads) {
+    std::vector<Topology> topo(nsys);
+    for (int s = 0; s < nsys; ++s) {
+        const char* e = nullptr;
+        if (!buildTopology(systems[s], topo[s], &e)) return setErr(e);
+    }
+    for (int i = 0; i < ninst; ++i)
+        if (!topo[sys_of[i]].constraints.empty())
+            return setErr("variable-step integration of loop closures is not restated");
+    IntegOpts o;
+    if (accuracy > 0) o.accuracy = accuracy;
+    o.consTol = consTol > 0 ? consTol : o.accuracy / 10;
+    o.projectEveryStep = projectEveryStep != 0;
+    parallelFor(ninst, nthreads, [&](int i, int) {
+        const Topology& tp = topo[sys_of[i]];
+        Work<double> w;
+        w.resize(tp);
+        double tt = t ? t[i] : 0.0;
+        int64_t acc = 0, rej = 0;
+        const int st = rkMersonAdaptive(tp, y + y_off[i], &tt, tFinal, hInit, hMin, hMax, o, w, maxSteps, &acc, &rej);
+        if (t) t[i] = tt;
+        if (status) status[i] = st;
+        if (stats) { stats[2 * i] = acc; stats[2 * i + 1] = rej; }
+    });
+    return 0;
+}
+
+// Step-size controller alone (adjustStepSize), for its unit tests.
+int oracle_adjust_step_size(double err, int32_t errOrder, int32_t limited, double accuracy, double hMin, double hMax,
+                            double* h) {
+    return adjustStepSize(err, errOrder, limited != 0, accuracy, hMin, hMax, *h) ? 1 : 0;
 }
 
 // Exact operation counts of one realize(Acceleration) of one instance with

@@ -24,6 +24,13 @@ int oracle_tree_op_batch(const sbg_system_desc* systems, int32_t nsys, const int
 int oracle_system_forces_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
                                const int64_t* y_off, const double* y, const int64_t* u_off, const int64_t* b_off,
                                double* fmob, double* Fbody, int32_t nthreads);
+int oracle_rk_merson_adaptive_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of,
+                                    int32_t ninst, const int64_t* y_off, double* y, double* t, double tFinal,
+                                    double hInit, double hMin, double hMax, double accuracy, double consTol,
+                                    int32_t projectEveryStep, int32_t maxSteps, int32_t* status, int64_t* stats,
+                                    int32_t nthreads);
+int oracle_adjust_step_size(double err, int32_t errOrder, int32_t limited, double accuracy, double hMin, double hMax,
+                            double* h);
 int oracle_count_realize(const sbg_system_desc* d, const double* y, int64_t* counts);
 double oracle_time_realize(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
                            const int64_t* y_off, const double* y, double* ydot, int32_t nreps, int32_t nthreads);
