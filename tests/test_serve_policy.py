@@ -65,3 +65,27 @@ def test_request_that_never_fits_is_rejected():
     with pytest.raises(N.EngineError) as e:
         simulate(units, [10], [0], [10, 10, 100, 10, 10], max_slots=4, chunk_steps=8)
     assert e.value.code == 4  # SBG_ERR_BUDGET
+
+
+@pytest.mark.parametrize("seed", [5, 6, 7])
+def test_mixed_sizes_never_overcommit_a_pool_and_all_finish(seed):
+    """Requests of very different footprints against small pools: at every
+    tick the resident requests' units fit every pool, admission stays in
+    arrival order, and every request finishes with its own number of chunks."""
+    rng = np.random.default_rng(seed)
+    n, chunk = 150, 8
+    cap = np.array([400, 300, 500, 2000, 700], dtype=np.int64)
+    units = np.stack([rng.integers(1, c // 3, size=n) for c in cap], axis=1).astype(np.int64)
+    hz = rng.integers(1, 120, size=n)
+    arr = np.sort(rng.integers(0, 60, size=n))
+    adm, done, peak = simulate(units, hz, arr, cap, max_slots=32, chunk_steps=chunk)
+    assert (adm >= arr).all() and (np.diff(adm) >= 0).all()
+    assert (done - adm + 1 >= np.array([chunks(int(h), chunk) for h in hz])).all()
+    T = int(done.max()) + 1
+    use = np.zeros((T, 5), dtype=np.int64)
+    occ = np.zeros(T, dtype=int)
+    for k in range(n):
+        use[adm[k]:done[k] + 1] += units[k]
+        occ[adm[k]:done[k] + 1] += 1
+    assert (use <= cap).all()
+    assert occ.max() <= 32 and peak <= 32
