@@ -18,7 +18,6 @@ a device->host copy of [qdot, udot] and the status words.
 from __future__ import annotations
 
 import argparse
-import ctypes as C
 import json
 import os
 import subprocess

@@ -4,7 +4,6 @@ Simbody's articulated-body recursions and fixed-step RK-Merson driver
 from __future__ import annotations
 
 import ctypes as C
-import os
 from pathlib import Path
 
 import numpy as np
