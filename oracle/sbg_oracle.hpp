@@ -8,9 +8,16 @@
 // Parity status: pinned against the reference's own known-answer tests
 // (TestMassMatrix.cpp M*M^-1 = I and udot = M^-1 f at u = 0, TestForces.cpp
 // spring/damper closed forms and RK-Merson energy conservation,
-// TestConstraints.cpp Ball errors) restated in tests/, and against a
+// TestConstraints.cpp Ball errors) restated in tests/, against golden vectors
+// recorded from a build of the reference (tests/golden/reference_vectors.npz:
+// realize, M^-1 f and RK-Merson states of the seeded workloads) and against a
 // trajectory value recorded from the reference itself (double pendulum,
-// instance 0 of the 1024-instance workload, y(1 s)).
+// instance 0 of the 1024-instance workload, y(1 s)). The tree operators
+// (inverse dynamics, M x, J x, ~J F, composite inertias) are pinned through
+// the identities the reference's TestMassMatrix.cpp checks, on the golden
+// states and the golden M^-1 f and udot. The error-controlled RK-Merson is
+// pinned through its fixed-limit case, which reproduces the golden
+// fixed-step states.
 //
 // Every routine follows the reference formulas and evaluation order closely
 // and cites the reference file:line (paths relative to the Simbody source
