@@ -62,3 +62,24 @@ def test_batch_entry_points_refuse_a_null_batch_without_touching_the_device():
     for name, args in calls.items():
         assert getattr(lib, name)(*args) == 1, name  # SBG_ERR_INVALID
         assert lib.sbg_last_error(), name
+
+
+def test_header_is_plain_c_and_cxx(tmp_path):
+    """The boundary header compiles as C99 (what a cgo / N-API / ctypes
+    binding sees) and as C++ (the drop-in surface), warnings as errors."""
+    import shutil
+    import subprocess
+
+    gcc, gxx = shutil.which("gcc"), shutil.which("g++")
+    if not gcc or not gxx:
+        import pytest
+        pytest.skip("no host C/C++ compiler")
+    src_c = tmp_path / "use.c"
+    src_c.write_text('#include "simbody_gb300.h"\nint main(void) { return sbg_abi_version() == SBG_ABI_VERSION ? 0 : 1; }\n')
+    src_cc = tmp_path / "use.cc"
+    src_cc.write_text(src_c.read_text())
+    inc = str(ROOT / "include")
+    for cc, src, std in ((gcc, src_c, "-std=c99"), (gxx, src_cc, "-std=c++17")):
+        r = subprocess.run([cc, std, "-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only", "-I", inc, str(src)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
