@@ -22,6 +22,7 @@ INST_SINGULAR_D = 2
 INST_PROJECTION_FAILED = 4
 INST_CHOLESKY_FAIL = 8
 INST_TIMEOUT = 16
+INST_ILL_CONDITIONED = 32  # mixed form: the FP32 factorisation of M too poor for the refinement
 
 STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "BUDGET", 5: "STATE", 6: "UNSUPPORTED",
                 7: "NO_DEVICE"}

@@ -83,3 +83,11 @@ def test_header_is_plain_c_and_cxx(tmp_path):
         r = subprocess.run([cc, std, "-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only", "-I", inc, str(src)],
                            capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def test_status_bits_match_the_header():
+    text = (ROOT / "include" / "simbody_gb300.h").read_text()
+    defines = dict(re.findall(r"#define SBG_(INST_[A-Z_]+)\s+(\d+)", text))
+    assert len(defines) >= 7
+    for name, value in defines.items():
+        assert getattr(N, name) == int(value), name
