@@ -144,7 +144,13 @@ typedef struct sbg_integ_opts {
     double  accuracy;
     double  constraint_tolerance;
     int32_t project_every_step;   /* Integrator::setProjectEveryStep */
-    int32_t reserved;
+    /* 0: the call starts with Integrator::initialize(state) (quaternions
+     * normalised; with loop closures, forced position and velocity
+     * projections). Nonzero: it continues the integration the previous
+     * integration call on this batch left, as a second Integrator::stepTo()
+     * does (AbstractIntegratorRep.cpp:341-421); SBG_ERR_STATE if the state was
+     * set since or nothing has been integrated. */
+    int32_t continue_integration;
 } sbg_integ_opts;
 
 typedef struct sbg_batch_config {
@@ -268,12 +274,35 @@ int sbg_batch_last_operator_ms(sbg_batch batch, double* ms);
 int sbg_batch_fallback_count(sbg_batch batch, int64_t* n);
 
 /* RungeKuttaMersonIntegrator with setFixedStepSize(h), initialize(state) and
- * stepTo(t0 + nsteps*h) looped until reached (RungeKuttaMersonIntegrator.cpp:86-140,
+ * exactly nsteps internal steps of h (stepTo looped with
+ * setReturnEveryInternalStep; RungeKuttaMersonIntegrator.cpp:86-140,
  * AbstractIntegratorRep.cpp:137-207, 341-577), for every instance, on the
  * batch's current device state, which is advanced in place. status (may be
- * NULL) gets the OR of SBG_INST_* words per instance. opts may be NULL. */
+ * NULL) gets the OR of SBG_INST_* words per instance. opts may be NULL; with
+ * opts->continue_integration the call continues the previous one. */
 int sbg_rk_merson_fixed(sbg_batch batch, double h, int32_t nsteps,
                         const sbg_integ_opts* opts, int32_t* status);
+/* Integrator::stepTo(t_report) of a fixed-step RungeKuttaMersonIntegrator
+ * with setAllowInterpolation(false), so tMax = t_report
+ * (AbstractIntegratorRep.cpp:229-240): every instance steps from its current
+ * time; each step ends at t0 + h unless t_report lies within 0.95 h (a
+ * shortened last step) or within 1.001 h (t_report itself) of t0
+ * (AbstractIntegratorRep.cpp:536-544). An instance already at t_report does
+ * not move. Without opts->continue_integration the call begins with
+ * Integrator::initialize; with it, stepTo(0.5) then stepTo(1.0) gives the
+ * reference's two-call trajectory. SBG_INST_TIMEOUT if time stops advancing. */
+int sbg_rk_merson_step_to(sbg_batch batch, double h, double t_report,
+                          const sbg_integ_opts* opts, int32_t* status);
+
+/* State::getQDotDot() at Stage::Acceleration (SimbodyMatterSubsystem
+ * calcQDotDot over the mobilizers): Pin/Slider/Universal qdotdot = udot; a
+ * Ball or Free quaternion gets N(q) udot_w + NDot(q,qdot) w computed as
+ * Rotation::convertAngVelDotToQuaternionDotDot (RigidBodyNodeSpec_Ball.h:355-390,
+ * RigidBodyNodeSpec_Free.h:418-455, Rotation.h:1006-1013), a Free body's
+ * translation its udot. qdotdot gets nq values per instance, back to back in
+ * instance order. Formed from the state and the udot of the last realize,
+ * which must be of the current state (SBG_ERR_STATE otherwise). Synchronous. */
+int sbg_batch_get_qdotdot(sbg_batch batch, double* qdotdot);
 
 /* ------------------------------------------- device-resident (timing) path */
 
@@ -285,6 +314,9 @@ int sbg_realize_acceleration_async(sbg_batch batch);
 /* RK Merson on the resident state, asynchronous on the batch stream. */
 int sbg_rk_merson_fixed_async(sbg_batch batch, double h, int32_t nsteps,
                               const sbg_integ_opts* opts);
+/* sbg_rk_merson_step_to, asynchronous on the batch stream. */
+int sbg_rk_merson_step_to_async(sbg_batch batch, double h, double t_report,
+                                const sbg_integ_opts* opts);
 /* Copy the resident ydot / status of the last realize to host (synchronous). */
 int sbg_batch_get_ydot(sbg_batch batch, double* ydot, int32_t* status);
 int sbg_batch_sync(sbg_batch batch);
@@ -410,10 +442,14 @@ int sbg_serve_simulate(int32_t n, const int64_t* units, const int32_t* horizons,
  * topology tables in fixed device arrays: at most 256 bodies and 4096
  * mobility-force elements); larger topologies are rejected with
  * SBG_ERR_INVALID. Runs asynchronously on `stream` (a cudaStream_t, NULL =
- * default stream) of the current device. The first call on a device looks up
- * the arrays' device addresses, so make it before any stream capture. All
- * calls share the arrays: calls that overlap on the GPU race. Message of the
- * last failure: sbg_noalloc_last_error(). */
+ * default stream) of the current device. The first call on a device does the
+ * set-up: it looks up the arrays' device addresses (cudaGetSymbolAddress), and
+ * with CUDA's lazy module loading that is also when the driver loads this
+ * module and creates its fixed arrays (about 16.3 MiB), so that first call can
+ * fail with SBG_ERR_CUDA if the device has no memory left. Make it at start-up,
+ * before any stream capture; later calls allocate nothing. All calls share
+ * the arrays, which keep the last call's contents: calls that overlap on the
+ * GPU race. Message of the last failure: sbg_noalloc_last_error(). */
 int sbg_realize_acceleration_noalloc(sbg_topology topology, int32_t ninstances,
                                      const double* y, double* ydot,
                                      int32_t* status, void* stream);

@@ -19,6 +19,7 @@
 #ifndef SIMBODY_GB300_HPP_
 #define SIMBODY_GB300_HPP_
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <stdexcept>

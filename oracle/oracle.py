@@ -30,6 +30,10 @@ def lib() -> C.CDLL:
         L.oracle_minv_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, i64p, dp, dp, C.c_int32]
         L.oracle_rk_merson_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, dp, C.c_double, C.c_int32,
                                              C.c_double, C.c_double, C.c_int32, ip, i64p, C.c_int32]
+        L.oracle_rk_merson_run_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, dp, C.c_double,
+                                                 C.c_int32, C.c_double, C.c_int32, C.c_double, C.c_double,
+                                                 C.c_int32, ip, C.c_int32]
+        L.oracle_qdotdot_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, dp, i64p, dp]
         L.oracle_tree_op_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, i64p, i64p, C.c_int32, dp, dp,
                                            dp, dp, C.c_int32]
         L.oracle_system_forces_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, i64p, i64p, dp, dp,
@@ -143,6 +147,33 @@ def rk_merson(systems, nsys, sys_of, y_off, y, h, nsteps, t=None, accuracy=0.0, 
                                         _d(y), _d(tt), float(h), int(nsteps), accuracy, cons_tol,
                                         int(project_every_step), _i(st), C.byref(npj), nthreads))
     return y, tt, st, npj.value
+
+
+def rk_merson_run(systems, nsys, sys_of, y_off, y, h, nsteps=-1, t_report=0.0, t=None, initialize=True,
+                  accuracy=0.0, cons_tol=0.0, project_every_step=False, nthreads=0):
+    """One call of the fixed-step integrator: nsteps >= 0 steps of h, or
+    (nsteps < 0) stepTo(t_report) with interpolation off; initialize=False
+    continues the integration (y, t) describe. Returns (y, t, status)."""
+    sys_of = np.ascontiguousarray(sys_of, dtype=np.int32)
+    y = np.array(y, dtype=np.float64, copy=True)
+    tt = np.zeros(len(sys_of)) if t is None else np.array(t, dtype=np.float64, copy=True)
+    st = np.empty(len(sys_of), dtype=np.int32)
+    _check(lib().oracle_rk_merson_run_batch(systems, nsys, _i(sys_of), len(sys_of), _l(np.ascontiguousarray(y_off)),
+                                            _d(y), _d(tt), float(h), int(nsteps), float(t_report), int(initialize),
+                                            accuracy, cons_tol, int(project_every_step), _i(st), nthreads))
+    return y, tt, st
+
+
+def qdotdot(systems, nsys, sys_of, y_off, y, ydot, q_off):
+    """State::getQDotDot() from a realized y and its ydot; nq values per
+    instance at q_off[i]."""
+    sys_of = np.ascontiguousarray(sys_of, dtype=np.int32)
+    q_off = np.ascontiguousarray(q_off, dtype=np.int64)
+    out = np.zeros(int(q_off[-1]))
+    _check(lib().oracle_qdotdot_batch(systems, nsys, _i(sys_of), len(sys_of), _l(np.ascontiguousarray(y_off)),
+                                      _d(np.ascontiguousarray(y)), _d(np.ascontiguousarray(ydot)), _l(q_off),
+                                      _d(out)))
+    return out
 
 
 def rk_merson_adaptive(systems, nsys, sys_of, y_off, y, t_final, t=None, h_init=0.0, h_min=0.0, h_max=0.0,

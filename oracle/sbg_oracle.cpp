@@ -457,6 +457,9 @@ static bool projectULoops(const Topology& t, const double* q, double* u, Work<do
     return true;
 }
 
+int rkMersonRun(const Topology& t, double* y, double* time, double h, int nsteps, double tReport, bool initialize,
+                const IntegOpts& o, Work<double>& w, int64_t* nProjections);
+
 // One instance: Integrator::initialize (Integrator.cpp:333-377, which forces a
 // projection: quaternions are normalized) then nsteps fixed RK-Merson steps
 // (RungeKuttaMersonIntegrator.cpp:86-140, AbstractIntegratorRep.cpp:137-207,
@@ -464,6 +467,23 @@ static bool projectULoops(const Topology& t, const double* q, double* u, Work<do
 // with interpolation allowed) with stage step hs = t1 - t.
 int rkMerson(const Topology& t, double* y, double* time, double h, int nsteps, const IntegOpts& o, Work<double>& w,
              int64_t* nProjections) {
+    return rkMersonRun(t, y, time, h, nsteps, 0.0, true, o, w, nProjections);
+}
+
+// One call of the fixed-step integrator. initialize: Integrator::initialize
+// first (as above); otherwise the integration continues from y and *time as
+// the previous call left them -- a second Integrator::stepTo() on the same
+// integrator: the first stage derivative is recomputed from y, which is what
+// the reference's realizeStateDerivatives at the top of the main loop does
+// (AbstractIntegratorRep.cpp:395-404), and nothing is normalized or projected
+// at entry. nsteps >= 0: exactly nsteps steps of h (tMax = infinity).
+// nsteps < 0: stepTo(tReport) with setAllowInterpolation(false), i.e. tMax =
+// tReport (AbstractIntegratorRep.cpp:229-240): each step's t1 follows
+// takeOneStep (:536-544) -- tReport when it lies within 0.95 h of t0, t0 + h
+// when it lies beyond 1.001 h, else tReport -- until t reaches tReport; with
+// a fixed step size adjustStepSize keeps h for the next step (min = max = h).
+int rkMersonRun(const Topology& t, double* y, double* time, double h, int nsteps, double tReport, bool initialize,
+                const IntegOpts& o, Work<double>& w, int64_t* nProjections) {
     const int ny = t.nq + t.nu;
     const bool loops = !t.constraints.empty();
     int status = 0;
@@ -472,27 +492,39 @@ int rkMerson(const Topology& t, double* y, double* time, double h, int nsteps, c
         int st = loops ? realizeAccelerationLoops(t, yy, w, f) : (realizeAcceleration(t, yy, w, f) ? 0 : SBG_INST_SINGULAR_D);
         status |= st;
     };
-    // initialize: ForceProjection
-    // ForceProjection, not LocalOnly, no projection limit (IntegratorRep.h:856-895):
-    // with loops at least one Newton iteration runs unless perr is exactly 0.
-    std::vector<double> perr0;
-    if (loops) perrAt(t, y, w, perr0);
-    if (!loops || normRMSv(perr0) == 0) normalizeQuaternions(t, y);
-    else if (!projectQNewton(t, y, w, o.consTol, false)) status |= SBG_INST_PROJECTION_FAILED;
-    if (loops) {
-        if (!projectULoops(t, y, y + t.nq, w, o.consTol, true, HUGE_VAL, false))
-            status |= SBG_INST_PROJECTION_FAILED;
+    if (initialize) {
+        // initialize: ForceProjection, not LocalOnly, no projection limit
+        // (IntegratorRep.h:856-895): with loops at least one Newton iteration
+        // runs unless perr is exactly 0.
+        std::vector<double> perr0;
+        if (loops) perrAt(t, y, w, perr0);
+        if (!loops || normRMSv(perr0) == 0) normalizeQuaternions(t, y);
+        else if (!projectQNewton(t, y, w, o.consTol, false)) status |= SBG_INST_PROJECTION_FAILED;
+        if (loops) {
+            if (!projectULoops(t, y, y + t.nq, w, o.consTol, true, HUGE_VAL, false))
+                status |= SBG_INST_PROJECTION_FAILED;
+        }
     }
     double tc = *time;
-    for (int step = 0; step < nsteps; ++step) {
+    for (int step = 0;; ++step) {
         const double t0 = tc;
+        double t1;
+        if (nsteps >= 0) {
+            if (step >= nsteps) break;
+            t1 = t0 + h;
+        } else {
+            if (!(t0 < tReport)) break;
+            if (tReport < t0 + 0.95 * h) t1 = tReport;
+            else if (tReport > t0 + 1.001 * h) t1 = t0 + h;
+            else t1 = tReport;
+            if (!(t1 > t0)) { status |= SBG_INST_TIMEOUT; break; }
+        }
         for (int i = 0; i < ny; ++i) y0[i] = y[i];
         for (int i = 0; i < t.nu; ++i) {  // calcRelativeScaling (IntegratorRep.h:644-655), w = 1
             const double vi = std::abs(y0[t.nq + i]);
             uScale[i] = vi > 1 ? 1 / vi : 1.0;
         }
         rhs(y0.data(), f0.data());
-        const double t1 = t0 + h;
         const double hs = t1 - t0;
         const double h3 = hs / 3, h6 = hs / 6, h8 = hs / 8, h2 = hs / 2;
         for (int i = 0; i < ny; ++i) ytmp[i] = y0[i] + h3 * f0[i];
@@ -802,6 +834,51 @@ int oracle_rk_merson_batch(const sbg_system_desc* systems, int32_t nsys, const i
         np += p;
     });
     if (nproj) *nproj = np.load();
+    return 0;
+}
+
+// One integration call per instance (rkMersonRun): nsteps >= 0 steps of h, or
+// nsteps < 0 stepTo(t_report) with interpolation off; initialize = 0
+// continues the integration y and t describe.
+int oracle_rk_merson_run_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
+                               const int64_t* y_off, double* y, double* t, double h, int32_t nsteps, double t_report,
+                               int32_t initialize, double accuracy, double consTol, int32_t projectEveryStep,
+                               int32_t* status, int32_t nthreads) {
+    std::vector<Topology> topo(nsys);
+    for (int s = 0; s < nsys; ++s) {
+        const char* e = nullptr;
+        if (!buildTopology(systems[s], topo[s], &e)) return setErr(e);
+    }
+    IntegOpts o;
+    if (accuracy > 0) o.accuracy = accuracy;
+    o.consTol = consTol > 0 ? consTol : o.accuracy / 10;
+    o.projectEveryStep = projectEveryStep != 0;
+    parallelFor(ninst, nthreads, [&](int i, int) {
+        const Topology& tp = topo[sys_of[i]];
+        Work<double> w;
+        w.resize(tp);
+        double tt = t ? t[i] : 0.0;
+        const int st = rkMersonRun(tp, y + y_off[i], &tt, h, nsteps, t_report, initialize != 0, o, w, nullptr);
+        if (t) t[i] = tt;
+        if (status) status[i] = st;
+    });
+    return 0;
+}
+
+// State::getQDotDot() after realize(Acceleration) for a batch: y and ydot in
+// the [q,u] packing at y_off[i], qdotdot nq values per instance at q_off[i].
+int oracle_qdotdot_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
+                         const int64_t* y_off, const double* y, const double* ydot, const int64_t* q_off,
+                         double* qdotdot) {
+    std::vector<Topology> topo(nsys);
+    for (int s = 0; s < nsys; ++s) {
+        const char* e = nullptr;
+        if (!buildTopology(systems[s], topo[s], &e)) return setErr(e);
+    }
+    for (int i = 0; i < ninst; ++i) {
+        const Topology& tp = topo[sys_of[i]];
+        calcQDotDot(tp, y + y_off[i], ydot + y_off[i] + tp.nq, qdotdot + q_off[i]);
+    }
     return 0;
 }
 

@@ -17,6 +17,13 @@ int oracle_rk_merson_batch(const sbg_system_desc* systems, int32_t nsys, const i
                            const int64_t* y_off, double* y, double* t, double h, int32_t nsteps, double accuracy,
                            double consTol, int32_t projectEveryStep, int32_t* status, int64_t* nproj,
                            int32_t nthreads);
+int oracle_rk_merson_run_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
+                               const int64_t* y_off, double* y, double* t, double h, int32_t nsteps, double t_report,
+                               int32_t initialize, double accuracy, double consTol, int32_t projectEveryStep,
+                               int32_t* status, int32_t nthreads);
+int oracle_qdotdot_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
+                         const int64_t* y_off, const double* y, const double* ydot, const int64_t* q_off,
+                         double* qdotdot);
 int oracle_tree_op_batch(const sbg_system_desc* systems, int32_t nsys, const int32_t* sys_of, int32_t ninst,
                          const int64_t* y_off, const double* y, const int64_t* u_off, const int64_t* b_off,
                          int32_t op, const double* x, const double* fmob, const double* Fbody, double* out,

@@ -514,4 +514,45 @@ template <class R> bool realizeAcceleration(const Topology& t, const R* y, Work<
     return ok;
 }
 
+// qdotdot = N(q) udot + NDot(q, qdot) u per mobilizer, the quantity
+// State::getQDotDot() returns at Stage::Acceleration
+// (SimbodyMatterSubsystemRep.cpp calcQDotDot over the nodes):
+//   Pin, Slider, Universal  q = angles/displacement with qdot = u, so
+//                           qdotdot = udot (RigidBodyNodeSpec.h calcQDotDot)
+//   Ball (quaternion)       convertAngVelDotToQuaternionDotDot(q, w_FM, b_FM)
+//                           = N(q) b + (-1/4 |w|^2) q with the unnormalized q
+//                           (RigidBodyNodeSpec_Ball.h:355-390,
+//                           Rotation.h:1006-1013)
+//   Free                    the quaternion part as Ball, then the translational
+//                           udot (RigidBodyNodeSpec_Free.h:418-455)
+template <class R> void calcQDotDot(const Topology& t, const R* y, const R* udot, R* qdotdot) {
+    const R* q = y;
+    const R* u = y + t.nq;
+    for (int bi = 1; bi <= t.nb; ++bi) {
+        const Body& b = t.b[bi];
+        const R* qq = q + b.qoff;
+        const R* ub = u + b.uoff;
+        const R* bd = udot + b.uoff;
+        R* o = qdotdot + b.qoff;
+        if (b.type != SBG_BALL && b.type != SBG_FREE) {
+            for (int k = 0; k < b.nu; ++k) o[k] = bd[k];
+            continue;
+        }
+        // Rotation.h: calcUnnormalizedNForQuaternion is 0.5 * the rows below;
+        // N b is a row-by-row product (Mat43 * Vec3)
+        const R e0 = R(0.5) * qq[0], e1 = R(0.5) * qq[1], e2 = R(0.5) * qq[2], e3 = R(0.5) * qq[3];
+        const R Nb0 = -e1 * bd[0] + -e2 * bd[1] + -e3 * bd[2];
+        const R Nb1 = e0 * bd[0] + e3 * bd[1] + -e2 * bd[2];
+        const R Nb2 = -e3 * bd[0] + e0 * bd[1] + e1 * bd[2];
+        const R Nb3 = e2 * bd[0] + -e1 * bd[1] + e0 * bd[2];
+        const R s = R(-0.25) * (ub[0] * ub[0] + ub[1] * ub[1] + ub[2] * ub[2]);
+        o[0] = Nb0 + s * qq[0];
+        o[1] = Nb1 + s * qq[1];
+        o[2] = Nb2 + s * qq[2];
+        o[3] = Nb3 + s * qq[3];
+        if (b.type == SBG_FREE)
+            for (int k = 0; k < 3; ++k) o[4 + k] = bd[3 + k];
+    }
+}
+
 }  // namespace sbgo

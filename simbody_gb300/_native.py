@@ -53,7 +53,7 @@ class SystemDesc(C.Structure):
 
 class IntegOpts(C.Structure):
     _fields_ = [("accuracy", C.c_double), ("constraint_tolerance", C.c_double),
-                ("project_every_step", C.c_int32), ("reserved", C.c_int32)]
+                ("project_every_step", C.c_int32), ("continue_integration", C.c_int32)]
 
 
 class BatchConfig(C.Structure):
@@ -115,8 +115,11 @@ ENGINE_API = {
     "sbg_batch_stream": (vp, [vp]),
     "sbg_realize_acceleration_async": (C.c_int, [vp]),
     "sbg_rk_merson_fixed_async": (C.c_int, [vp, C.c_double, C.c_int32, P(IntegOpts)]),
+    "sbg_rk_merson_step_to": (C.c_int, [vp, C.c_double, C.c_double, P(IntegOpts), ip]),
+    "sbg_rk_merson_step_to_async": (C.c_int, [vp, C.c_double, C.c_double, P(IntegOpts)]),
     "sbg_batch_get_ydot": (C.c_int, [vp, dp, ip]),
     "sbg_batch_sync": (C.c_int, [vp]),
+    "sbg_batch_get_qdotdot": (C.c_int, [vp, dp]),
     "sbg_batch_launch_count": (C.c_int64, [vp]),
     "sbg_batch_kernel_variant": (C.c_int, [vp]),
     "sbg_batch_group_lanes_shift": (C.c_int, [vp]),

@@ -1282,7 +1282,7 @@ template <class R, int NM, bool REF, bool GROUP, int MINB = 1, bool LOOPS = fals
 __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int first, int count, double* __restrict__ y,
                                                             double* __restrict__ time, R* __restrict__ fbuf,
                                                             int64_t fplane, R* __restrict__ scratch,
-                                                            int32_t* __restrict__ status, double h, int nsteps,
+                                                            int32_t* __restrict__ status, double h, StepCtl sc,
                                                             double accuracy, double consTol, int projectEveryStep) {
     const Slot s = GROUP ? groupSlot(T, first) : chainSlot(T, first, count);
     if (s.inst < 0) return;
@@ -1298,8 +1298,9 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
     double tc = time[inst];
     // Per-instance control (serving): this launch's steps, whether it starts
     // the integration, the instance's own step size and tolerances.
-    int nst = nsteps;
-    bool init = true, pes = projectEveryStep != 0;
+    int nst = sc.nsteps;
+    const double tStop = sc.tStop;
+    bool init = sc.init != 0, pes = projectEveryStep != 0;
     if (T.ictl) {
         const int c = T.ictl[inst];
         nst = c & kCtlSteps;
@@ -1366,8 +1367,23 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
             if (s.gl == 0) lst = loopInitialize<NM>(loopState(), consTol);
             st |= loopLeaderOr(lst);
         }
-    for (int step = 0; step < nst; ++step) {
-        const double t1 = tc + h;
+    for (int step = 0;; ++step) {
+        // t1 of this step (StepCtl): a fixed count of full steps, or
+        // takeOneStep's choice against tMax = tStop (AbstractIntegratorRep.cpp:536-544)
+        double t1;
+        if (nst >= 0) {
+            if (step >= nst) break;
+            t1 = tc + h;
+        } else {
+            if (!(tc < tStop)) break;
+            if (tStop < tc + 0.95 * h) t1 = tStop;
+            else if (tStop > tc + 1.001 * h) t1 = tc + h;
+            else t1 = tStop;
+            if (!(t1 > tc) || step >= kMaxStepsPerCall) {  // time no longer advances
+                st |= SBG_INST_TIMEOUT;
+                break;
+            }
+        }
         const double hs = t1 - tc;
         stage(0, 0.0, fA, fB, f0);      // f0 = f(y0)
         stage(1, hs / 3, fA, fB, fA);   // f1 -> fA

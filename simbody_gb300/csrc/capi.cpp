@@ -94,6 +94,7 @@ struct sbg_batch_s {
     int32_t* status = nullptr;
     int64_t* dHostYOff = nullptr;
     int64_t* dHostUOff = nullptr;
+    int64_t* dHostQOff = nullptr;  // qdotdot packing: nq values per instance
     double* staging = nullptr;  // packed device staging (nyTotal)
     void* scratch = nullptr;
     void* fbuf = nullptr;       // RK stage derivatives, 4 planes
@@ -103,6 +104,8 @@ struct sbg_batch_s {
     int64_t scratchElems = 0;
     double* hostPinned = nullptr;  // pinned host staging (nyTotal)
     bool stateSet = false;
+    bool integrating = false;  // an integration has run since the state was last set: it can be continued
+    bool realized = false;     // ydot holds the realize of the current state (qdotdot can be formed)
     int64_t launches = 0;
     // mapping
     int nChain = 0;                       // order positions of the chain segment
@@ -661,6 +664,12 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     b->dHostYOff = const_cast<int64_t*>(dOff);
     if ((rc = b->upload(&dOff, b->hostUOff, "offsets"))) return bail(rc);
     b->dHostUOff = const_cast<int64_t*>(dOff);
+    {
+        std::vector<int64_t> qo(ninst + 1);
+        for (int i = 0; i <= ninst; ++i) qo[i] = b->hostYOff[i] - b->hostUOff[i];
+        if ((rc = b->upload(&dOff, qo, "offsets"))) return bail(rc);
+        b->dHostQOff = const_cast<int64_t*>(dOff);
+    }
 
     const size_t rsz = precision == SBG_PRECISION_FP64 ? sizeof(double) : sizeof(float);
     void* p = nullptr;
@@ -749,6 +758,8 @@ int sbg_batch_set_state(sbg_batch b, const double* t, const double* y) {
     }
     SBG_CUDA(cudaStreamSynchronize(b->stream), "state upload");
     b->stateSet = true;
+    b->integrating = false;
+    b->realized = false;
     return SBG_OK;
 }
 
@@ -846,6 +857,7 @@ int sbg_realize_acceleration_async(sbg_batch b) {
     }
     SBG_CUDA(cudaGraphLaunch(b->realizeGraph, b->stream), "realize graph launch");
     b->launches += b->realizeLaunches();
+    b->realized = true;
     return SBG_OK;
 }
 
@@ -950,6 +962,8 @@ int sbg_realize_acceleration_host(sbg_batch b, const double* y, double* ydot, in
     SBG_CUDA(cudaStreamSynchronize(b->stream), "pipelined realize");
     if (!dstPinned) std::memcpy(ydot, b->hostPinned, bytes);
     b->stateSet = true;
+    b->integrating = false;
+    b->realized = true;
     return SBG_OK;
 }
 
@@ -963,6 +977,7 @@ int sbg_multiply_by_minv(sbg_batch b, const double* f, double* outp) {
     SBG_CUDA(launchScatter(b->T, b->dHostUOff, b->staging, b->fcol, 1, b->stream), "force scatter");
     SBG_CUDA(launchMInv(b->T, b->plan(), b->precision, b->y, b->fcol, b->ydot, b->bufsArg(), b->status, b->streams()),
              "M^-1 kernel launch");
+    b->realized = false;  // the result went to the derivative columns
     SBG_CUDA(launchGather(b->T, b->dHostUOff, b->ydot, b->staging, 1, b->stream), "result gather");
     b->launches += 2 + b->segments();
     SBG_CUDA(cudaMemcpyAsync(b->hostPinned, b->staging, bytes, cudaMemcpyDeviceToHost, b->stream), "result download");
@@ -1085,35 +1100,80 @@ int sbg_calc_composite_body_inertias(sbg_batch b, double* R, int32_t* status) {
     return runTreeOp(b, OP_COMPOSITE, nullptr, nullptr, nullptr, R, status);
 }
 
-int sbg_rk_merson_fixed_async(sbg_batch b, double h, int32_t nsteps, const sbg_integ_opts* opts) {
+// One integration call: Integrator::initialize (unless the options continue
+// the previous call's integration), then the steps StepCtl describes.
+static int rkMersonCall(sbg_batch b, double h, int32_t nsteps, double tStop, const sbg_integ_opts* opts) {
     if (!b) return fail(SBG_ERR_INVALID, "null batch");
     if (!b->stateSet) return fail(SBG_ERR_STATE, "no state has been set");
     if (!(h > 0) || !std::isfinite(h)) return fail(SBG_ERR_INVALID, "step size must be positive");
-    if (nsteps < 0) return fail(SBG_ERR_INVALID, "negative step count");
+    if (nsteps < 0 && !std::isfinite(tStop)) return fail(SBG_ERR_INVALID, "report time must be finite");
     double acc = 1e-3, ctol = -1;
     int pes = 0;
+    bool cont = false;
     if (opts) {
         if (opts->accuracy > 0) acc = opts->accuracy;
         if (opts->constraint_tolerance > 0) ctol = opts->constraint_tolerance;
         pes = opts->project_every_step;
+        cont = opts->continue_integration != 0;
     }
     if (ctol <= 0) ctol = acc / 10;
+    if (cont && !b->integrating)
+        return fail(SBG_ERR_STATE, "no integration to continue: the state was set since, or none has run");
     SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
     if (int rc = tuneVariant(b)) return rc;  // realize leaves the state untouched
     SBG_CUDA(cudaMemsetAsync(b->status, 0, std::max(b->ninst, 1) * sizeof(int32_t), b->stream), "status reset");
-    SBG_CUDA(launchNormalizeQuat(b->T, b->y, b->stream), "initialize");
-    SBG_CUDA(launchRKMerson(b->T, b->plan(), b->precision, b->y, b->time, b->bufsArg(), b->status, h, nsteps, acc, ctol,
+    if (!cont) {
+        SBG_CUDA(launchNormalizeQuat(b->T, b->y, b->stream), "initialize");
+        ++b->launches;
+    }
+    const StepCtl step{nsteps, cont ? 0 : 1, tStop};
+    SBG_CUDA(launchRKMerson(b->T, b->plan(), b->precision, b->y, b->time, b->bufsArg(), b->status, h, step, acc, ctol,
                             pes, b->streams()),
              "RK-Merson kernel launch");
-    b->launches += 1 + b->segments();
+    b->launches += b->segments();
+    b->integrating = true;
+    b->realized = false;
     return SBG_OK;
+}
+
+static int rkMersonFinish(sbg_batch b, int32_t* status) {
+    SBG_CUDA(cudaStreamSynchronize(b->stream), "RK-Merson");
+    if (status) SBG_CUDA(cudaMemcpy(status, b->status, b->ninst * sizeof(int32_t), cudaMemcpyDeviceToHost), "status download");
+    return SBG_OK;
+}
+
+int sbg_rk_merson_fixed_async(sbg_batch b, double h, int32_t nsteps, const sbg_integ_opts* opts) {
+    if (nsteps < 0) return fail(SBG_ERR_INVALID, "negative step count");
+    return rkMersonCall(b, h, nsteps, 0.0, opts);
 }
 
 int sbg_rk_merson_fixed(sbg_batch b, double h, int32_t nsteps, const sbg_integ_opts* opts, int32_t* status) {
     int rc = sbg_rk_merson_fixed_async(b, h, nsteps, opts);
     if (rc) return rc;
-    SBG_CUDA(cudaStreamSynchronize(b->stream), "RK-Merson");
-    if (status) SBG_CUDA(cudaMemcpy(status, b->status, b->ninst * sizeof(int32_t), cudaMemcpyDeviceToHost), "status download");
+    return rkMersonFinish(b, status);
+}
+
+int sbg_rk_merson_step_to_async(sbg_batch b, double h, double t_report, const sbg_integ_opts* opts) {
+    return rkMersonCall(b, h, -1, t_report, opts);
+}
+
+int sbg_rk_merson_step_to(sbg_batch b, double h, double t_report, const sbg_integ_opts* opts, int32_t* status) {
+    int rc = sbg_rk_merson_step_to_async(b, h, t_report, opts);
+    if (rc) return rc;
+    return rkMersonFinish(b, status);
+}
+
+int sbg_batch_get_qdotdot(sbg_batch b, double* qdotdot) {
+    if (!b || !qdotdot) return fail(SBG_ERR_INVALID, "null argument");
+    if (!b->realized) return fail(SBG_ERR_STATE, "the current state has not been realized through Acceleration");
+    SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    const int64_t nqT = b->nyTotal - b->nuTotal;
+    SBG_CUDA(launchQDotDot(b->T, b->dHostQOff, b->y, b->ydot, b->staging, b->stream), "qdotdot kernel launch");
+    ++b->launches;
+    SBG_CUDA(cudaMemcpyAsync(b->hostPinned, b->staging, nqT * sizeof(double), cudaMemcpyDeviceToHost, b->stream),
+             "qdotdot download");
+    SBG_CUDA(cudaStreamSynchronize(b->stream), "qdotdot");
+    std::memcpy(qdotdot, b->hostPinned, nqT * sizeof(double));
     return SBG_OK;
 }
 

@@ -35,7 +35,7 @@ void rkLoopGroup(const KArgs& a, cudaStream_t s) {
     if (a.P->nLoopGroupBlocks <= 0) return;
     rkMersonKernel<double, 3, false, true, 1, true><<<a.P->nLoopGroupBlocks, 128, 0, s>>>(
         *a.T, a.P->loopGroupFirst, 0, a.ystate, a.time, static_cast<double*>(a.fbufLoop), a.fplane,
-        static_cast<double*>(a.scratchLoop), a.status, a.h, a.nsteps, a.accuracy, a.consTol, a.projectEveryStep);
+        static_cast<double*>(a.scratchLoop), a.status, a.h, a.step, a.accuracy, a.consTol, a.projectEveryStep);
 }
 void realizeLoopGroup(const KArgs& a, cudaStream_t s) {
     if (a.P->nLoopGroupBlocks <= 0) return;

@@ -7,7 +7,7 @@ namespace sbg {
 template <bool REF, int MINB> static void go(const KArgs& a, cudaStream_t s) {
     rkMersonKernel<float, 3, REF, true, MINB><<<a.P->nGroupBlocks, 128, 0, s>>>(
         *a.T, a.P->groupFirst, 0, a.ystate, a.time, static_cast<float*>(a.fbuf), a.fplane, static_cast<float*>(a.scratch), a.status,
-        a.h, a.nsteps, a.accuracy, a.consTol, a.projectEveryStep);
+        a.h, a.step, a.accuracy, a.consTol, a.projectEveryStep);
 }
 
 void rk32Group(const KArgs& a, bool refine, cudaStream_t s) {

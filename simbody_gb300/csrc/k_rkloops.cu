@@ -18,7 +18,7 @@ void rkLoop(const KArgs& a, cudaStream_t s) {
     double* fb = static_cast<double*>(a.fbufLoop);
     const int first = a.P->nChain, nb = loopBlocks(*a.P);
     rkMersonKernel<double, 3, false, false, 1, true><<<nb, 128, 0, s>>>(
-        *a.T, first, a.P->nLoop, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.nsteps, a.accuracy, a.consTol,
+        *a.T, first, a.P->nLoop, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.step, a.accuracy, a.consTol,
         a.projectEveryStep);
 }
 

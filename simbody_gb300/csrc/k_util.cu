@@ -20,6 +20,52 @@ __global__ void normalizeQuatKernel(DevTables T, double* __restrict__ y) {
     }
 }
 
+// State::getQDotDot() at Stage::Acceleration from the resident state and the
+// last realize's udot, into the host packing (nq values per instance from
+// qHost[inst]): qdotdot = udot for Pin/Slider/Universal; for the quaternion
+// of a Ball or Free body N(q) udot_w - |w|^2/4 q with the unnormalized q
+// (Rotation.h:1006-1013: convertAngVelDotToQuaternionDotDot), then the Free
+// body's translational udot (RigidBodyNodeSpec_Ball.h:355-390,
+// RigidBodyNodeSpec_Free.h:418-455). One thread per instance.
+__global__ void qdotdotKernel(DevTables T, const int64_t* __restrict__ qHost, const double* __restrict__ y,
+                              const double* __restrict__ ydot, double* __restrict__ out) {
+    const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+    if (inst >= T.ninst) return;
+    const int64_t base = T.ybase[inst], stride = T.ystride[inst];
+    const int nq = T.inq[inst], body0 = T.ibody[inst], nb = T.inb[inst];
+    double* o = out + qHost[inst];
+    auto Y = [&](int k) { return y[base + (int64_t)k * stride]; };
+    auto UD = [&](int k) { return ydot[base + (int64_t)(nq + k) * stride]; };
+    for (int lb = 0; lb < nb; ++lb) {
+        const int row = body0 + lb;
+        const int type = T.info[row] & 15, n = (T.info[row] >> 4) & 15;
+        const int qo = T.qoff[row], uo = T.uoff[row];
+        if (type != T_BALL && type != T_FREE) {
+            for (int k = 0; k < n; ++k) o[qo + k] = UD(uo + k);
+            continue;
+        }
+        const double q0 = Y(qo), q1 = Y(qo + 1), q2 = Y(qo + 2), q3 = Y(qo + 3);
+        const double w0 = Y(nq + uo), w1 = Y(nq + uo + 1), w2 = Y(nq + uo + 2);
+        const double b0 = UD(uo), b1 = UD(uo + 1), b2 = UD(uo + 2);
+        const double e0 = 0.5 * q0, e1 = 0.5 * q1, e2 = 0.5 * q2, e3 = 0.5 * q3;
+        const double s = -0.25 * (w0 * w0 + w1 * w1 + w2 * w2);
+        o[qo + 0] = (-e1 * b0 + -e2 * b1 + -e3 * b2) + s * q0;
+        o[qo + 1] = (e0 * b0 + e3 * b1 + -e2 * b2) + s * q1;
+        o[qo + 2] = (-e3 * b0 + e0 * b1 + e1 * b2) + s * q2;
+        o[qo + 3] = (e2 * b0 + -e1 * b1 + e0 * b2) + s * q3;
+        if (type == T_FREE)
+            for (int k = 0; k < 3; ++k) o[qo + 4 + k] = UD(uo + 3 + k);
+    }
+}
+
+cudaError_t launchQDotDot(const DevTables& T, const int64_t* qHost, const double* y, const double* ydot, double* out,
+                          cudaStream_t s) {
+    const int threads = 128, blocks = (T.ninst + threads - 1) / threads;
+    if (blocks == 0) return cudaSuccess;
+    qdotdotKernel<<<blocks, threads, 0, s>>>(T, qHost, y, ydot, out);
+    return cudaGetLastError();
+}
+
 // Pack/unpack between the host's per-instance packing and the columns.
 // part 0: all of [q,u]; part 1: the u slots only (nu values per instance).
 __global__ void scatterKernel(DevTables T, const int64_t* __restrict__ hostOff, const double* __restrict__ packed,
@@ -101,10 +147,10 @@ cudaError_t launchMInv(const DevTables& T, const LaunchPlan& P, int precision, c
 }
 
 cudaError_t launchRKMerson(const DevTables& T, const LaunchPlan& P, int precision, double* y, double* time,
-                           const BatchBufs& B, int32_t* status, double h, int nsteps, double accuracy,
+                           const BatchBufs& B, int32_t* status, double h, StepCtl step, double accuracy,
                            double consTol, int projectEveryStep, const Streams& s) {
     KArgs a = baseArgs(T, P, B, status);
-    a.ystate = y; a.time = time; a.h = h; a.nsteps = nsteps; a.accuracy = accuracy; a.consTol = consTol;
+    a.ystate = y; a.time = time; a.h = h; a.step = step; a.accuracy = accuracy; a.consTol = consTol;
     a.projectEveryStep = projectEveryStep;
     auto loops = [&](cudaStream_t st) { rkLoop(a, st); };
     if (precision == SBG_PRECISION_FP64)

@@ -15,6 +15,25 @@ struct Streams {
     cudaEvent_t fork, join;
 };
 
+// How far one RK-Merson call steps (RungeKuttaMersonIntegrator with a fixed
+// step size, AbstractIntegratorRep.cpp:341-577):
+//   nsteps >= 0  exactly nsteps steps of h (t1 = t0 + h; tMax = infinity)
+//   nsteps <  0  Integrator::stepTo(tStop) with interpolation off
+//                (setAllowInterpolation(false): tMax = tStop). Each step picks
+//                t1 by takeOneStep's rule (:536-544): tStop when it lies within
+//                0.95 h, t0 + h when it lies beyond 1.001 h, else tStop; the
+//                call ends once t reaches tStop.
+//   init         Integrator::initialize first: quaternions normalised (the
+//                caller's launch) and, with loop closures, the forced
+//                position and velocity projections; 0 continues the
+//                integration where the previous call left it.
+struct StepCtl {
+    int nsteps;
+    int init;
+    double tStop;
+};
+constexpr int kMaxStepsPerCall = 1 << 30;
+
 // precision: SBG_PRECISION_FP64, _MIXED (FP32 recursions + double-float
 // residual refinement) or _MIXED_FAST (FP32 recursions only).
 // Buffers of a batch the launchers need besides the tables.
@@ -30,7 +49,7 @@ cudaError_t launchRealize(const DevTables& T, const LaunchPlan& P, int precision
 cudaError_t launchMInv(const DevTables& T, const LaunchPlan& P, int precision, const double* y, const double* f,
                        double* out, const BatchBufs& B, int32_t* status, const Streams& s);
 cudaError_t launchRKMerson(const DevTables& T, const LaunchPlan& P, int precision, double* y, double* time,
-                           const BatchBufs& B, int32_t* status, double h, int nsteps, double accuracy,
+                           const BatchBufs& B, int32_t* status, double h, StepCtl step, double accuracy,
                            double consTol, int projectEveryStep, const Streams& s);
 // Tree operators (k_ops.cu, ops_device.cuh). Operands in the host packing:
 // u-like arrays nu values per instance at uoff[inst]; body arrays one entry
@@ -50,12 +69,17 @@ struct OpIO {
 cudaError_t launchTreeOp(const DevTables& T, const LaunchPlan& P, const OpIO& io, const double* y, double* scratch,
                          double* scratchLoop, int32_t* status, cudaStream_t s);
 cudaError_t launchNormalizeQuat(const DevTables& T, double* y, cudaStream_t s);
+// qdotdot of every instance from the resident y and ydot, nq values per
+// instance at qHost[inst] of out.
+cudaError_t launchQDotDot(const DevTables& T, const int64_t* qHost, const double* y, const double* ydot, double* out,
+                          cudaStream_t s);
 // part 0 moves whole [q,u] records, part 1 only the u slots; instances
 // [inst0, inst0 + count) (count < 0: to the end).
 cudaError_t launchScatter(const DevTables& T, const int64_t* hostOff, const double* packed, double* cols, int part,
                           cudaStream_t s, int inst0 = 0, int count = -1);
 cudaError_t launchGather(const DevTables& T, const int64_t* hostOff, const double* cols, double* packed, int part,
                          cudaStream_t s, int inst0 = 0, int count = -1);
+
 
 // Per-segment launchers (k_r64.cu, k_r32c.cu, k_r32g.cu, k_rk64.cu,
 // k_rk32c.cu, k_rk32g.cu).
@@ -74,7 +98,8 @@ struct KArgs {
     void* fbufLoop;      // FP64 stage derivatives of the loop-closure segment
     int32_t* status;
     double h, accuracy, consTol;
-    int nsteps, projectEveryStep;
+    StepCtl step;
+    int projectEveryStep;
 };
 void realize64Chain(const KArgs& a, cudaStream_t s);
 void realize64Group(const KArgs& a, cudaStream_t s);

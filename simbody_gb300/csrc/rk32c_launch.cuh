@@ -13,11 +13,11 @@ template <bool REF, int MINB, int BS> static void rk32ChainGo(const KArgs& a, cu
     float* sc = static_cast<float*>(a.scratch);
     if (a.P->nm == 1)
         rkMersonKernel<float, 1, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(
-            *a.T, 0, a.P->nChain, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.nsteps, a.accuracy, a.consTol,
+            *a.T, 0, a.P->nChain, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.step, a.accuracy, a.consTol,
             a.projectEveryStep);
     else
         rkMersonKernel<float, 3, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(
-            *a.T, 0, a.P->nChain, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.nsteps, a.accuracy, a.consTol,
+            *a.T, 0, a.P->nChain, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.step, a.accuracy, a.consTol,
             a.projectEveryStep);
 }
 

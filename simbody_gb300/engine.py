@@ -215,10 +215,21 @@ class Batch:
         return ms.value
 
     def rk_merson_fixed(self, h: float, nsteps: int, accuracy: float = 0.0, constraint_tolerance: float = 0.0,
-                        project_every_step: bool = False) -> np.ndarray:
-        opts = N.IntegOpts(accuracy, constraint_tolerance, int(project_every_step), 0)
+                        project_every_step: bool = False, continue_integration: bool = False) -> np.ndarray:
+        """nsteps fixed RK-Merson steps of h; Integrator::initialize first
+        unless continue_integration."""
+        opts = N.IntegOpts(accuracy, constraint_tolerance, int(project_every_step), int(continue_integration))
         st = np.empty(self.ninst, dtype=np.int32)
         N.check(N.engine_lib().sbg_rk_merson_fixed(self._h, float(h), int(nsteps), C.byref(opts), _iptr(st)))
+        return st
+
+    def rk_merson_step_to(self, h: float, t_report: float, accuracy: float = 0.0, constraint_tolerance: float = 0.0,
+                          project_every_step: bool = False, continue_integration: bool = False) -> np.ndarray:
+        """Integrator::stepTo(t_report) with a fixed step h and interpolation
+        off (the last step shortened to land on t_report)."""
+        opts = N.IntegOpts(accuracy, constraint_tolerance, int(project_every_step), int(continue_integration))
+        st = np.empty(self.ninst, dtype=np.int32)
+        N.check(N.engine_lib().sbg_rk_merson_step_to(self._h, float(h), float(t_report), C.byref(opts), _iptr(st)))
         return st
 
     # -- device-resident timing path
@@ -237,6 +248,12 @@ class Batch:
         st = np.empty(self.ninst, dtype=np.int32)
         N.check(N.engine_lib().sbg_batch_get_ydot(self._h, _dptr(ydot), _iptr(st)))
         return ydot, st
+
+    def get_qdotdot(self) -> np.ndarray:
+        """State::getQDotDot() of the last realize: nq values per instance."""
+        out = np.empty(int(self.y_offsets[-1] - self.u_offsets[-1]))
+        N.check(N.engine_lib().sbg_batch_get_qdotdot(self._h, _dptr(out)))
+        return out
 
     def sync(self) -> None:
         N.check(N.engine_lib().sbg_batch_sync(self._h))

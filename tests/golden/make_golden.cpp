@@ -12,6 +12,12 @@
 //                           or cons_tol when it is nonzero (tight tolerances
 //                           make the in-step projections run), stepped for
 //                           exactly nsteps steps
+//   qdd                     s.getQDotDot() after the realize above
+// and, into a second file, integrator continuation records: with
+// setFixedStepSize(h) and setAllowInterpolation(false), after initialize(s)
+//   mode 0  stepTo(t_mid); stepTo(t_end)     (a second call continues)
+//   mode 1  stepTo(t_end)
+//   mode 2  stepTo(t_end + 0.3 h)            (a shortened last step)
 // Reference calls used (paths relative to the Simbody source tree):
 //   MobilizedBody::{Pin,Slider,Universal,Ball,Free} (Simbody/include/simbody/internal/MobilizedBody_*.h)
 //   Force::Gravity, Force::MobilityLinearSpring/Damper (Simbody/include/simbody/internal/Force*.h)
@@ -20,7 +26,10 @@
 //
 // Output: one binary file of records
 //   int64 cfg, inst, ny, nu, nsteps, status   double h, t_rk, cons_tol
-//   double y0[ny], ydot[ny], f[nu], minv_f[nu], y_rk[ny]
+//   double y0[ny], ydot[ny], f[nu], minv_f[nu], y_rk[ny], qdd[ny - nu]
+// and a second of continuation records
+//   int64 cfg, inst, ny, mode, status, nsteps_taken   double h, t_mid, t_end, t_out
+//   double y0[ny], y_out[ny]
 #include "Simbody.h"
 
 #include <cmath>
@@ -94,12 +103,14 @@ void put(FILE* fp, const void* p, size_t bytes) {
 }  // namespace
 
 int main(int argc, char** argv) {
-    if (argc < 2) {
-        fprintf(stderr, "usage: make_golden OUT.bin\n");
+    if (argc < 3) {
+        fprintf(stderr, "usage: make_golden OUT.bin CONT.bin\n");
         return 2;
     }
     FILE* fp = fopen(argv[1], "wb");
     if (!fp) return 1;
+    FILE* fc = fopen(argv[2], "wb");
+    if (!fc) return 1;
     struct Sel { int cfg, ninst, nsteps; double h; std::vector<int> pick; double consTol; };
     // cfg 5 draws 1-4 Ball loops for about one request in five; the
     // instances listed are ones that carry loops and ones that do not.
@@ -147,6 +158,8 @@ int main(int argc, char** argv) {
             std::vector<double> ydot(ny), f(nu), minv(nu), yrk(ny);
             m.sys.realize(st, Stage::Acceleration);
             for (int k = 0; k < ny; ++k) ydot[k] = st.getYDot()[k];
+            std::vector<double> qdd(ny - nu);
+            for (int k = 0; k < ny - nu; ++k) qdd[k] = st.getQDotDot()[k];
             Vector fv((int)nu), out;
             for (int k = 0; k < nu; ++k) fv[k] = f[k] = std::cos(0.7 * k + 0.3 * i + s.cfg);
             m.matter.multiplyByMInv(st, fv, out);
@@ -176,11 +189,80 @@ int main(int argc, char** argv) {
             put(fp, f.data(), nu * 8);
             put(fp, minv.data(), nu * 8);
             put(fp, yrk.data(), ny * 8);
+            put(fp, qdd.data(), (ny - nu) * 8);
             ++written;
         }
         sbg_workload_destroy(w);
     }
     fclose(fp);
-    printf("%d records\n", written);
+
+    // integrator continuation: one or two stepTo calls, interpolation off
+    struct ContSel { int cfg, ninst; double h, tMid, tEnd; std::vector<int> pick; };
+    const ContSel cont[] = {
+        {1, 8, 1e-3, 0.5, 1.0, {0, 1}},
+        {2, 4, 5e-4, 0.005, 0.01, {0, 1}},
+        {3, 6, 5e-4, 0.005, 0.01, {0, 1}},
+        {4, 8, 5e-4, 0.005, 0.01, {2, 3}},
+        {5, 64, 5e-4, 0.005, 0.01, {}},
+    };
+    int contWritten = 0;
+    for (const ContSel& c : cont) {
+        sbg_workload w;
+        if (sbg_workload_create(c.cfg, c.ninst, &w)) {
+            fprintf(stderr, "workload %d: %s\n", c.cfg, sbg_workload_last_error());
+            return 1;
+        }
+        const sbg_system_desc* systems = sbg_workload_systems(w);
+        const int32_t* isys = sbg_workload_instance_system(w);
+        const int64_t* yo = sbg_workload_y_offsets(w);
+        const double* y0 = sbg_workload_y0(w);
+        std::vector<int> pick = c.pick;
+        if (pick.empty()) {  // config 5: two requests with loop closures, one without
+            int withLoops = 0, without = 0;
+            for (int i = 0; i < c.ninst; ++i) {
+                const bool loops = systems[isys[i]].nconstraints > 0;
+                if (loops && withLoops < 2) { pick.push_back(i); ++withLoops; }
+                if (!loops && without < 1) { pick.push_back(i); ++without; }
+            }
+        }
+        for (int i : pick) {
+            const sbg_system_desc& d = systems[isys[i]];
+            Model m(d);
+            const int64_t ny = yo[i + 1] - yo[i];
+            for (int mode = 0; mode < 3; ++mode) {
+                int64_t status = 0, taken = 0;
+                std::vector<double> yout(ny, 0.0);
+                double tout = 0;
+                try {
+                    State s2 = m.sys.getDefaultState();
+                    for (int k = 0; k < ny; ++k) s2.updY()[k] = y0[yo[i] + k];
+                    RungeKuttaMersonIntegrator integ(m.sys);
+                    integ.setFixedStepSize(c.h);
+                    integ.setAllowInterpolation(false);
+                    integ.initialize(s2);
+                    auto to = [&](double t) { while (integ.getTime() < t) integ.stepTo(t); };
+                    if (mode == 0) { to(c.tMid); to(c.tEnd); }
+                    else if (mode == 1) to(c.tEnd);
+                    else to(c.tEnd + 0.3 * c.h);
+                    for (int k = 0; k < ny; ++k) yout[k] = integ.getState().getY()[k];
+                    tout = integ.getTime();
+                    taken = integ.getNumStepsTaken();
+                } catch (const std::exception& e) {
+                    fprintf(stderr, "cfg %d inst %d mode %d: integrator failed: %s\n", c.cfg, i, mode, e.what());
+                    status = 1;
+                }
+                const int64_t hdr[6] = {c.cfg, i, ny, mode, status, taken};
+                const double hd[4] = {c.h, c.tMid, c.tEnd, tout};
+                put(fc, hdr, sizeof hdr);
+                put(fc, hd, sizeof hd);
+                put(fc, &y0[yo[i]], ny * 8);
+                put(fc, yout.data(), ny * 8);
+                ++contWritten;
+            }
+        }
+        sbg_workload_destroy(w);
+    }
+    fclose(fc);
+    printf("%d records, %d continuation records\n", written, contWritten);
     return 0;
 }

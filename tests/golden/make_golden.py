@@ -9,8 +9,15 @@ driver make_golden.cpp is compiled against them, run on the seeded workloads
 
   cfg, inst, ny, nu, nsteps, status, h, t_rk,    one entry per record
   cons_tol (0 = the integrator's default)
-  y_off, u_off                                   offsets into the flat arrays
-  y0, ydot, y_rk (by y_off); f, minv_f (by u_off)
+  y_off, u_off, q_off                            offsets into the flat arrays
+  y0, ydot, y_rk (by y_off); f, minv_f (by u_off); qdd (by q_off)
+
+and the integrator continuation records (setAllowInterpolation(false)), one
+per instance and mode (0: stepTo(t_mid); stepTo(t_end), 1: stepTo(t_end),
+2: stepTo(t_end + 0.3 h)):
+
+  c_cfg, c_inst, c_ny, c_mode, c_status, c_steps, c_h, c_t_mid, c_t_end,
+  c_t_out, c_y_off; c_y0, c_y_out (by c_y_off)
 
 The vectors are committed; the tests only read the .npz.
 """
@@ -48,7 +55,7 @@ def read_records(path: Path) -> dict:
         pos += 24
         cfg, inst, ny, nu, nsteps, status = (int(v) for v in hdr)
         arrs = {}
-        for name, n in (("y0", ny), ("ydot", ny), ("f", nu), ("minv_f", nu), ("y_rk", ny)):
+        for name, n in (("y0", ny), ("ydot", ny), ("f", nu), ("minv_f", nu), ("y_rk", ny), ("qdd", ny - nu)):
             arrs[name] = np.frombuffer(raw, dtype=np.float64, count=n, offset=pos).copy()
             pos += 8 * n
         recs.append(dict(cfg=cfg, inst=inst, ny=ny, nu=nu, nsteps=nsteps, status=status, h=h, t_rk=t, cons_tol=ctol, **arrs))
@@ -56,10 +63,34 @@ def read_records(path: Path) -> dict:
                                                  "cons_tol")}
     out["y_off"] = np.concatenate([[0], np.cumsum(out["ny"])]).astype(np.int64)
     out["u_off"] = np.concatenate([[0], np.cumsum(out["nu"])]).astype(np.int64)
+    out["q_off"] = np.concatenate([[0], np.cumsum(out["ny"] - out["nu"])]).astype(np.int64)
     for k in ("y0", "ydot", "y_rk"):
         out[k] = np.concatenate([r[k] for r in recs])
-    for k in ("f", "minv_f"):
+    for k in ("f", "minv_f", "qdd"):
         out[k] = np.concatenate([r[k] for r in recs])
+    return out
+
+
+def read_continuation(path: Path) -> dict:
+    raw = path.read_bytes()
+    pos = 0
+    recs = []
+    while pos < len(raw):
+        cfg, inst, ny, mode, status, steps = (int(v) for v in np.frombuffer(raw, dtype=np.int64, count=6, offset=pos))
+        pos += 48
+        h, tmid, tend, tout = np.frombuffer(raw, dtype=np.float64, count=4, offset=pos)
+        pos += 32
+        y0 = np.frombuffer(raw, dtype=np.float64, count=ny, offset=pos).copy()
+        pos += 8 * ny
+        yout = np.frombuffer(raw, dtype=np.float64, count=ny, offset=pos).copy()
+        pos += 8 * ny
+        recs.append(dict(cfg=cfg, inst=inst, ny=ny, mode=mode, status=status, steps=steps, h=h, t_mid=tmid,
+                         t_end=tend, t_out=tout, y0=y0, y_out=yout))
+    out = {"c_" + k: np.array([r[k] for r in recs])
+           for k in ("cfg", "inst", "ny", "mode", "status", "steps", "h", "t_mid", "t_end", "t_out")}
+    out["c_y_off"] = np.concatenate([[0], np.cumsum(out["c_ny"])]).astype(np.int64)
+    out["c_y0"] = np.concatenate([r["y0"] for r in recs])
+    out["c_y_out"] = np.concatenate([r["y_out"] for r in recs])
     return out
 
 
@@ -82,8 +113,10 @@ def main() -> int:
                 f"-Wl,-rpath,{a.simbody_lib}", str(wl), f"-Wl,-rpath,{OUT}"]
         subprocess.run(cmd, check=True)
         binf = Path(td) / "records.bin"
-        subprocess.run([str(exe), str(binf)], check=True, env={"OPENBLAS_NUM_THREADS": "1"})
+        conf = Path(td) / "cont.bin"
+        subprocess.run([str(exe), str(binf), str(conf)], check=True, env={"OPENBLAS_NUM_THREADS": "1"})
         data = read_records(binf)
+        data.update(read_continuation(conf))
     np.savez_compressed(a.out, **data)
     print(f"wrote {a.out}: {len(data['cfg'])} records")
     return 0

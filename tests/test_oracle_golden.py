@@ -110,3 +110,63 @@ def test_tight_tolerance_records_project_in_steps(gold, workloads):
                                        cons_tol=float(gold["cons_tol"][r]))
         done += nproj > 0
     assert done >= 3
+
+
+def test_qdotdot_matches_reference(gold, workloads):
+    """State::getQDotDot() recorded after realize(Acceleration): the oracle's
+    calcQDotDot from the recorded ydot, every mobilizer type (quaternion
+    second derivatives of Ball and Free bodies included)."""
+    for r, cfg, inst, ys, _ in _records(gold):
+        w = workloads[cfg]
+        qs = slice(int(gold["q_off"][r]), int(gold["q_off"][r + 1]))
+        y0, yd = gold["y0"][ys], gold["ydot"][ys]
+        qdd = O.qdotdot(w.systems, w.nsys, w.instance_system[[inst]], np.array([0, len(y0)]), y0, yd,
+                        np.array([0, qs.stop - qs.start]))
+        assert _rel(qdd, gold["qdd"][qs]) <= 1e-13, (cfg, inst, _rel(qdd, gold["qdd"][qs]))
+
+
+def _cont_records(g):
+    for r in range(len(g["c_cfg"])):
+        ys = slice(int(g["c_y_off"][r]), int(g["c_y_off"][r + 1]))
+        yield r, int(g["c_cfg"][r]), int(g["c_inst"][r]), int(g["c_mode"][r]), ys
+
+
+def oracle_continuation(w, inst, mode, h, t_mid, t_end, y0):
+    """The oracle driven as the continuation records were: initialize, then
+    stepTo(t_mid); stepTo(t_end) (mode 0), stepTo(t_end) (1) or
+    stepTo(t_end + 0.3 h) (2), interpolation off."""
+    off = np.array([0, len(y0)])
+    so = w.instance_system[[inst]]
+    if mode == 0:
+        y, t, st = O.rk_merson_run(w.systems, w.nsys, so, off, y0, h, t_report=t_mid)
+        y, t, st2 = O.rk_merson_run(w.systems, w.nsys, so, off, y, h, t_report=t_end, t=t, initialize=False)
+        return y, t, st | st2
+    target = t_end if mode == 1 else t_end + 0.3 * h
+    return O.rk_merson_run(w.systems, w.nsys, so, off, y0, h, t_report=target)
+
+
+def test_integrator_continuation_matches_reference(gold, workloads):
+    """Integrator::stepTo twice on one integrator, once, and to a time that
+    is not a whole number of steps (setAllowInterpolation(false): the last
+    step is shortened): the oracle's continuation against the reference's
+    records, final time exactly and state to 1e-11."""
+    for r, cfg, inst, mode, ys in _cont_records(gold):
+        assert gold["c_status"][r] == 0
+        w = workloads[cfg]
+        assert np.array_equal(w.y0[w.instance_slice(inst)], gold["c_y0"][ys])
+        y, t, st = oracle_continuation(w, inst, mode, float(gold["c_h"][r]), float(gold["c_t_mid"][r]),
+                                       float(gold["c_t_end"][r]), gold["c_y0"][ys])
+        assert st[0] == 0
+        assert t[0] == gold["c_t_out"][r], (cfg, inst, mode, t[0], gold["c_t_out"][r])
+        assert _rel(y, gold["c_y_out"][ys]) <= 1e-11, (cfg, inst, mode, _rel(y, gold["c_y_out"][ys]))
+
+
+def test_continuation_records_cover_loops_and_quaternions(gold, workloads):
+    """The continuation records include quaternion bodies (a re-initialize
+    would renormalize them) and loop closures (it would re-project)."""
+    quats = loops = 0
+    for r, cfg, inst, mode, ys in _cont_records(gold):
+        d = workloads[cfg].systems[int(workloads[cfg].instance_system[inst])]
+        quats += any(d.bodies[k].mobilizer in (3, 4) for k in range(d.nbodies))
+        loops += d.nconstraints > 0
+    assert quats >= 6 and loops >= 2

@@ -73,6 +73,45 @@ def test_noalloc_matches_regular_entry_point_twice(engine):
     assert _rel(got2, got1) > 1e-6  # the inputs really differed
 
 
+def _one_topology_batch(w, inst, n, seed):
+    """n states of instance inst's topology: its seeded state plus noise."""
+    from simbody_gb300.engine import Batch
+
+    k = int(w.instance_system[inst])
+    topo = Topology(w.systems[k], keepalive=w)
+    y0 = w.y0[w.instance_slice(inst)]
+    rng = np.random.default_rng(seed)
+    y = np.tile(y0, n) + rng.normal(scale=0.05, size=n * y0.size)
+    b = Batch([topo], np.zeros(n, dtype=np.int32), precision="fp64")
+    return topo, b, y
+
+
+@pytest.mark.parametrize("config,inst,n", [
+    (3, 0, 1500),    # branched tree, Free base: 6-wide Free records, children pushed into a parent's record
+    (3, 5, 1500),    # another random tree
+    (1, 0, 20000),   # two-Pin chain: one-mobility records; more instances than the scratch holds at once
+])
+def test_noalloc_matches_regular_on_trees_and_pin_chains(engine, config, inst, n):
+    """Two calls in a row on one topology of a workload, against the regular
+    entry point. The instance counts exceed what the 16 MiB scratch holds at
+    once, so the kernel's threads loop over several instances each."""
+    pytest.importorskip("torch")
+    w = Workload(config, max(inst + 1, 8))
+    topo, b, y = _one_topology_batch(w, inst, n, seed=config * 100 + inst)
+    assert topo.nbodies > 1
+    for call in range(2):
+        yy = y if call == 0 else y + 0.01 * np.sin(np.arange(y.size))
+        b.set_state(yy)
+        ref, rst = b.realize_acceleration()
+        got, st = _noalloc(topo, n, yy)
+        assert (st == rst).all()
+        assert (st == 0).mean() > 0.99
+        ok = st == 0
+        ny = y.size // n
+        e = np.abs(got - ref).reshape(n, ny)[ok].max() / np.abs(ref.reshape(n, ny)[ok]).max()
+        assert e <= TOL, (call, e)
+
+
 def test_noalloc_rejects_oversized_topology(engine):
     bodies = (N.BodyDesc * 300)()
     for i in range(300):
