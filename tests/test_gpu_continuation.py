@@ -72,7 +72,8 @@ def test_step_to_matches_reference_records(engine, gold):
 @pytest.mark.parametrize("config,n", [(2, 64), (3, 64), (4, 32), (5, 64)])
 def test_step_to_matches_oracle(engine, config, n):
     w = Workload(config, n)
-    h, t_mid, t_end = w.h, 7 * w.h, 15.5 * w.h
+    h = w.h if w.h > 0 else 5e-4  # the Ball-chain workload is realize-only
+    t_mid, t_end = 7 * h, 15.5 * h
     for mode in (0, 2):
         b, y, t, st = _engine_continuation(w, mode, h, t_mid, t_end)
         off = b.y_offsets
