@@ -74,14 +74,13 @@ typedef enum sbg_precision {
 #define SBG_INST_PROJECTION_FAILED  4   /* quaternion/constraint projection refused */
 #define SBG_INST_CHOLESKY_FAIL      8   /* G M^-1 G^T not positive definite */
 #define SBG_INST_TIMEOUT           16   /* persistent kernel hit its iteration budget */
-/* Mixed form only: at some RHS of this instance the refinement correction was
- * larger than 1e-4 of udot, i.e. the FP32 factorisation of M was too poorly
- * conditioned for the mixed form's 1e-5 bar. sbg_realize_acceleration never
- * reports it: it recomputes such instances in FP64. The server's mixed lane
- * never reports it either: it continues the request in FP64. A mixed batch
- * integration (sbg_rk_merson_fixed) reports it and carries on in mixed
- * precision; rerun the instance in an FP64 batch for a result within FP64
- * parity. */
+/* Mixed form, internal: at some RHS of this instance the refinement
+ * correction was larger than a set fraction of udot (1e-4 in a realize, 1e-5
+ * in an integration), i.e. the FP32 factorisation of M was too poorly
+ * conditioned for the mixed form's 1e-5 bar. No entry point reports it:
+ * sbg_realize_acceleration recomputes such instances in FP64; a mixed batch
+ * integration takes that step and the next 15 of the instance in FP64; the
+ * server's mixed lane continues the request in FP64. */
 #define SBG_INST_ILL_CONDITIONED   32
 
 /* One mobilized body, numbered 1..nbodies in MobilizedBodyIndex order (Ground

@@ -1121,13 +1121,15 @@ __device__ __forceinline__ Slot groupSlot(const DevTables& T, int blk0) {
 // of its group). The correction is about cond(M) times the FP32 rounding, so
 // a large one means the FP32 factorisation is too poor for the mixed form's
 // accuracy bar. Non-negative floats order like their bit patterns.
-template <bool GROUP, class Out> __device__ __forceinline__ int illConditioned(const Out& out, const Slot& s) {
+template <bool GROUP, class Out>
+__device__ __forceinline__ int illConditioned(const DevTables& T, const Out& out, const Slot& s) {
     float um = out.umax, dm = out.dmax;
     if constexpr (GROUP) {
         um = __uint_as_float(__reduce_max_sync(s.mask, __float_as_uint(um)));
         dm = __uint_as_float(__reduce_max_sync(s.mask, __float_as_uint(dm)));
     }
-    return dm > kIllConditioned * um ? SBG_INST_ILL_CONDITIONED : 0;
+    const float tol = (T.fbList || T.ictl) ? kIllConditionedStep : kIllConditioned;
+    return dm > tol * um ? SBG_INST_ILL_CONDITIONED : 0;
 }
 
 // One RHS of the instance owned by slot s, through either driver; LOOPS adds
@@ -1165,12 +1167,12 @@ __device__ __forceinline__ int rhs(const DevTables& T, const Slot& s, R* scratch
     } else if constexpr (GROUP) {
         const ScrRows<R> S{scratch + T.sbase[s.inst], T.inb[s.inst]};
         int st = rhsGroup<R, NM, REF>(T, s.inst, S, src, out, s.gl, s.G, s.mask);
-        if constexpr (REF) st |= illConditioned<true>(out, s);
+        if constexpr (REF) st |= illConditioned<true>(T, out, s);
         return st;
     } else {
         const ScrTiled<R> S{scratch + T.sbase[s.inst]};
         int st = rhsChain<R, NM, REF>(T, s.inst, S, src, out);
-        if constexpr (REF) st |= illConditioned<false>(out, s);
+        if constexpr (REF) st |= illConditioned<false>(T, out, s);
         return st;
     }
 }
@@ -1278,15 +1280,44 @@ __device__ __noinline__ int stageRhsMixedGroup(const DevTables& T, const Slot& s
     return r;
 }
 
-template <class R, int NM, bool REF, bool GROUP, int MINB = 1, bool LOOPS = false, int BS = 128>
+// Group g of kFbLanes lanes of the FP64 list kernel: the g-th instance in
+// FP64 mode at this launch.
+__device__ __forceinline__ Slot listSlot(const DevTables& T, int launch) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = t / kFbLanes, lane = threadIdx.x & 31;
+    const int* list = T.fbList + (int64_t)(launch & 1) * T.ninst;
+    const unsigned mask = ((1u << kFbLanes) - 1u) << (lane & ~(kFbLanes - 1));
+    return Slot{g < T.fbCount[launch & 1] ? list[g] : -1, t % kFbLanes, kFbLanes, mask};
+}
+
+// One-step launches of a mixed batch integration: the instance's mode at the
+// next launch (written by this launch's owner of the instance only); FP64
+// puts it on the next list.
+__device__ __forceinline__ void fbNext(const DevTables& T, int launch, int inst, bool fp64) {
+    const int k = (launch + 1) & 1;
+    T.fbMode[(int64_t)k * T.ninst + inst] = fp64 ? 1 : 0;
+    if (fp64) T.fbList[(int64_t)k * T.ninst + atomicAdd(T.fbCount + k, 1)] = inst;
+}
+
+// LIST: the FP64 steps of the instances in FP64 mode during the one-step
+// launches of a mixed batch integration (R = double, kFbLanes lanes per
+// instance through the level-parallel driver, scratch = FP64 records in the
+// level-parallel layout at T.sbase, fbuf = the FP64 stage planes).
+template <class R, int NM, bool REF, bool GROUP, int MINB = 1, bool LOOPS = false, int BS = 128, bool LIST = false>
 __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int first, int count, double* __restrict__ y,
                                                             double* __restrict__ time, R* __restrict__ fbuf,
                                                             int64_t fplane, R* __restrict__ scratch,
                                                             int32_t* __restrict__ status, double h, StepCtl sc,
                                                             double accuracy, double consTol, int projectEveryStep) {
-    const Slot s = GROUP ? groupSlot(T, first) : chainSlot(T, first, count);
+    static_assert(!LIST || (std::is_same<R, double>::value && !REF && GROUP && !LOOPS), "the FP64 list is level-parallel FP64");
+    const Slot s = LIST ? listSlot(T, sc.launch) : GROUP ? groupSlot(T, first) : chainSlot(T, first, count);
     if (s.inst < 0) return;
     const int inst = s.inst;
+    // One-step launches of a mixed batch integration: an instance in FP64 mode
+    // is the list kernel's at this launch.
+    const bool split = !LIST && REF && T.fbList != nullptr;
+    if (split && T.fbMode[(int64_t)(sc.launch & 1) * T.ninst + inst]) return;
+    bool toFp64 = false;  // split: this launch's mixed step met an ill-conditioned M
     const int64_t base = T.ybase[inst], stride = T.ystride[inst];
     const int nq = T.inq[inst], nu = T.inu[inst];
     const int body0 = T.ibody[inst], nb = T.inb[inst];
@@ -1300,6 +1331,7 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
     // the integration, the instance's own step size and tolerances.
     int nst = sc.nsteps;
     const double tStop = sc.tStop;
+    const int maxSteps = sc.maxSteps > 0 ? sc.maxSteps : kMaxStepsPerCall;
     bool init = sc.init != 0, pes = projectEveryStep != 0;
     if (T.ictl) {
         const int c = T.ictl[inst];
@@ -1371,6 +1403,8 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
         // t1 of this step (StepCtl): a fixed count of full steps, or
         // takeOneStep's choice against tMax = tStop (AbstractIntegratorRep.cpp:536-544)
         double t1;
+        if (step >= maxSteps) break;
+        if (T.stepsLeft && T.stepsLeft[inst] <= 0) break;  // one-step launches: this instance is done
         if (nst >= 0) {
             if (step >= nst) break;
             t1 = tc + h;
@@ -1390,6 +1424,15 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
         stage(2, hs / 6, fA, fB, fB);   // f2 -> fB (input uses f1 in fA)
         stage(3, hs / 8, fB, fB, fC);   // f3 -> fC (input uses f2 in fB)
         stage(4, hs / 2, fB, fC, fA);   // f4 -> fA (ysave input uses f2, f3)
+        if (split && (st & SBG_INST_ILL_CONDITIONED)) {
+            // The step met an ill-conditioned M: leave y and t as they were;
+            // the FP64 list kernel takes this step at the next launch, and
+            // the next few.
+            st &= ~SBG_INST_ILL_CONDITIONED;
+            toFp64 = true;
+            if (s.gl == 0) T.fbLeft[inst] = kFp64Steps;
+            break;
+        }
         // y1 = y0 + h/6 (f0 + 4 f3 + f4); yerr = 0.2 |y1 - ysave|; error norm
         // (RungeKuttaMersonIntegrator.cpp:124-139, IntegratorRep.h:454-523).
         // Each lane of a group takes every G-th body.
@@ -1483,6 +1526,14 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
         }
         if constexpr (GROUP) __syncwarp(s.mask);
         tc = t1;
+        if (s.gl == 0) {
+            if (T.stepsLeft) --T.stepsLeft[inst];
+            if constexpr (LIST) --T.fbLeft[inst];
+        }
+    }
+    if (s.gl == 0) {
+        if constexpr (LIST) fbNext(T, sc.launch, inst, T.fbLeft[inst] > 0);
+        else if (split) fbNext(T, sc.launch, inst, toFp64);
     }
     if (s.gl == 0) {
         time[inst] = tc;

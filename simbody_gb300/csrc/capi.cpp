@@ -131,6 +131,19 @@ struct sbg_batch_s {
     int64_t opsElems = 0;
     int64_t* dHostBOff = nullptr;
     cudaEvent_t evOp0 = nullptr, evOp1 = nullptr;  // bracket the last tree operator's kernels
+    // one-step launches of a mixed batch integration (allocated on first use)
+    std::vector<int64_t> rowsElems;   // FP64 level-parallel record elements per instance (0: loop closures)
+    int32_t* fbList = nullptr;        // 2 x ninst
+    int32_t* fbCount = nullptr;       // 2, then the unfinished count
+    int32_t* fbMode = nullptr;        // 2 x ninst
+    int32_t* fbLeft = nullptr;
+    int32_t* stepsLeft = nullptr;
+    int64_t fbLaunch = 0;             // one-step launches of the integration so far (continued calls go on)
+    double* fbuf64 = nullptr;
+    int64_t* rowsBase = nullptr;
+    double* rows = nullptr;
+    cudaStream_t fbStream = nullptr;
+    cudaEvent_t fbFork = nullptr, fbJoin = nullptr;
 
     Streams streams() const { return Streams{stream, stream2, evFork, evJoin}; }
     LaunchPlan plan() const { return LaunchPlan{nChain, nGroupBlocks, nm, variant == 0 ? 1 : variant, nLoop}; }
@@ -183,6 +196,9 @@ struct sbg_batch_s {
         if (evOp0) cudaEventDestroy(evOp0);
         if (evOp1) cudaEventDestroy(evOp1);
         if (evJoin) cudaEventDestroy(evJoin);
+        if (fbFork) cudaEventDestroy(fbFork);
+        if (fbJoin) cudaEventDestroy(fbJoin);
+        if (fbStream) cudaStreamDestroy(fbStream);
         if (stream2) cudaStreamDestroy(stream2);
         for (int k = 1; k < 4; ++k)
             if (pipe[k]) cudaStreamDestroy(pipe[k]);
@@ -517,6 +533,7 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
         b->hostYOff[i + 1] = b->hostYOff[i] + t->nq + t->nu;
         b->hostUOff[i + 1] = b->hostUOff[i] + t->nu;
         b->hostBOff[i + 1] = b->hostBOff[i] + t->nb;
+        b->rowsElems.push_back(t->ncons > 0 ? 0 : (int64_t)t->nb * rowsRecordWidth(*t, 3));
         if (t->ncons > 0) loopPos.push_back(i);
         else if (t->chain || t->maxLevelWidth <= 2 || t->nb < groupMinBodies) chainPos.push_back(i);
         else groupPos.push_back(i);
@@ -1100,6 +1117,127 @@ int sbg_calc_composite_body_inertias(sbg_batch b, double* R, int32_t* status) {
     return runTreeOp(b, OP_COMPOSITE, nullptr, nullptr, nullptr, R, status);
 }
 
+// The number of steps takeOneStep's rule takes from t0 to tStop with step h
+// (AbstractIntegratorRep.cpp:536-544), as the RK kernels apply it.
+static int64_t stepsToReach(double t0, double tStop, double h) {
+    int64_t n = 0;
+    double tc = t0;
+    while (tc < tStop && n < kMaxStepsPerCall) {
+        double t1;
+        if (tStop < tc + 0.95 * h) t1 = tStop;
+        else if (tStop > tc + 1.001 * h) t1 = tc + h;
+        else t1 = tStop;
+        if (!(t1 > tc)) break;
+        tc = t1;
+        ++n;
+    }
+    return n;
+}
+
+// Buffers of the one-step launches of a mixed batch integration (allocated
+// on first use): the two FP64-mode lists and their lengths, the per-instance
+// FP64 modes and step counters, the FP64 stage planes, FP64 records of the
+// level-parallel layout for the list kernel, its stream and events.
+static int ensureFallbackSteps(sbg_batch b) {
+    if (b->fbList) return SBG_OK;
+    void* p = nullptr;
+    int rc;
+    const int64_t n = b->ninst;
+    if ((rc = b->alloc(&p, 2 * n * sizeof(int32_t), "FP64 lists"))) return rc;
+    b->fbList = static_cast<int32_t*>(p);
+    if ((rc = b->alloc(&p, 4 * sizeof(int32_t), "FP64 list lengths"))) return rc;
+    b->fbCount = static_cast<int32_t*>(p);
+    if ((rc = b->alloc(&p, 2 * n * sizeof(int32_t), "FP64 modes"))) return rc;
+    b->fbMode = static_cast<int32_t*>(p);
+    if ((rc = b->alloc(&p, n * sizeof(int32_t), "FP64 step counters"))) return rc;
+    b->fbLeft = static_cast<int32_t*>(p);
+    if ((rc = b->alloc(&p, n * sizeof(int32_t), "step counters"))) return rc;
+    b->stepsLeft = static_cast<int32_t*>(p);
+    if ((rc = b->alloc(&p, 4 * std::max<int64_t>(b->colElems, 1) * sizeof(double), "FP64 stage derivatives")))
+        return rc;
+    b->fbuf64 = static_cast<double*>(p);
+    std::vector<int64_t> base(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) base[i + 1] = base[i] + b->rowsElems[i];
+    if ((rc = b->alloc(&p, std::max<int64_t>(base[n], 1) * sizeof(double), "FP64 level-parallel records"))) return rc;
+    b->rows = static_cast<double*>(p);
+    const int64_t* dBase = nullptr;
+    if ((rc = b->upload(&dBase, base, "FP64 record offsets"))) return rc;
+    b->rowsBase = const_cast<int64_t*>(dBase);
+    SBG_CUDA(cudaStreamCreateWithFlags(&b->fbStream, cudaStreamNonBlocking), "stream");
+    SBG_CUDA(cudaEventCreateWithFlags(&b->fbFork, cudaEventDisableTiming), "event");
+    SBG_CUDA(cudaEventCreateWithFlags(&b->fbJoin, cudaEventDisableTiming), "event");
+    return SBG_OK;
+}
+
+// A mixed batch integration as one-step launches. At launch L the mixed
+// kernels step the instances in mixed mode while the FP64 list kernel, on its
+// own stream, steps those in FP64 mode; an instance whose mixed step meets an
+// ill-conditioned M keeps its state and takes that step in FP64 at launch
+// L + 1, so it ends one launch behind the others for each such event.
+// Launches go on until every instance has taken its steps (nsteps >= 0) or
+// reached tStop.
+static int rkMersonMixedSteps(sbg_batch b, double h, int32_t nsteps, double tStop, bool cont, double acc, double ctol,
+                              int pes) {
+    if (int rc = ensureFallbackSteps(b)) return rc;
+    DevTables Tk = b->T;
+    Tk.fbList = b->fbList;
+    Tk.fbCount = b->fbCount;
+    Tk.fbMode = b->fbMode;
+    Tk.fbLeft = b->fbLeft;
+    Tk.stepsLeft = nsteps >= 0 ? b->stepsLeft : nullptr;
+    Tk.fbuf64 = b->fbuf64;
+    const int n = b->ninst;
+    if (!cont) {  // a new integration: every instance starts in mixed mode
+        SBG_CUDA(cudaMemsetAsync(b->fbMode, 0, 2 * (size_t)n * sizeof(int32_t), b->stream), "FP64 modes");
+        SBG_CUDA(cudaMemsetAsync(b->fbLeft, 0, n * sizeof(int32_t), b->stream), "FP64 modes");
+        SBG_CUDA(cudaMemsetAsync(b->fbCount, 0, 2 * sizeof(int32_t), b->stream), "FP64 lists");
+        b->fbLaunch = 0;
+    }
+    int64_t target = nsteps;
+    if (nsteps >= 0) {
+        SBG_CUDA(launchFillInt(b->stepsLeft, n, nsteps, b->stream), "step counters");
+    } else {
+        // steps to tStop from the earliest instance time, by the kernels' rule
+        std::vector<double> t0(n);
+        SBG_CUDA(cudaMemcpyAsync(t0.data(), b->time, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream),
+                 "time download");
+        SBG_CUDA(cudaStreamSynchronize(b->stream), "time download");
+        target = stepsToReach(*std::min_element(t0.begin(), t0.end()), tStop, h);
+    }
+    const LaunchPlan P = b->plan();
+    const int64_t limit = 2 * target + 64;
+    int64_t L = 0;
+    for (;;) {
+        for (; L < target; ++L) {
+            const int li = (int)((b->fbLaunch + L) & ((1 << 30) - 1));  // only its parity matters
+            SBG_CUDA(cudaMemsetAsync(b->fbCount + ((li + 1) & 1), 0, sizeof(int32_t), b->stream), "FP64 list reset");
+            SBG_CUDA(cudaEventRecord(b->fbFork, b->stream), "fork");
+            SBG_CUDA(cudaStreamWaitEvent(b->fbStream, b->fbFork, 0), "fork");
+            const StepCtl step{nsteps >= 0 ? 1 : -1, (!cont && L == 0) ? 1 : 0, tStop, 1, li};
+            SBG_CUDA(launchRKMerson(Tk, P, b->precision, b->y, b->time, b->bufsArg(), b->status, h, step, acc, ctol, pes,
+                                    b->streams()),
+                     "RK-Merson kernel launch");
+            SBG_CUDA(launchRKFp64List(Tk, P, b->y, b->time, b->status, h, step, acc, ctol, pes, b->colElems, b->rowsBase,
+                                      b->rows, b->fbStream),
+                     "FP64 list kernel launch");
+            SBG_CUDA(cudaEventRecord(b->fbJoin, b->fbStream), "join");
+            SBG_CUDA(cudaStreamWaitEvent(b->stream, b->fbJoin, 0), "join");
+            b->launches += b->segments() + 1;
+        }
+        SBG_CUDA(launchCountUnfinished(n, Tk.stepsLeft, b->time, b->status, tStop, b->fbCount + 2, b->stream),
+                 "unfinished count");
+        int32_t left = 0;
+        SBG_CUDA(cudaMemcpyAsync(&left, b->fbCount + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream),
+                 "unfinished count");
+        SBG_CUDA(cudaStreamSynchronize(b->stream), "unfinished count");
+        if (left == 0) break;
+        if (L >= limit) return fail(SBG_ERR_CUDA, "mixed integration did not finish its steps");
+        target = L + 4;
+    }
+    b->fbLaunch += L;
+    return SBG_OK;
+}
+
 // One integration call: Integrator::initialize (unless the options continue
 // the previous call's integration), then the steps StepCtl describes.
 static int rkMersonCall(sbg_batch b, double h, int32_t nsteps, double tStop, const sbg_integ_opts* opts) {
@@ -1126,11 +1264,16 @@ static int rkMersonCall(sbg_batch b, double h, int32_t nsteps, double tStop, con
         SBG_CUDA(launchNormalizeQuat(b->T, b->y, b->stream), "initialize");
         ++b->launches;
     }
-    const StepCtl step{nsteps, cont ? 0 : 1, tStop};
-    SBG_CUDA(launchRKMerson(b->T, b->plan(), b->precision, b->y, b->time, b->bufsArg(), b->status, h, step, acc, ctol,
-                            pes, b->streams()),
-             "RK-Merson kernel launch");
-    b->launches += b->segments();
+    if (b->precision == SBG_PRECISION_MIXED && b->ninst > 0) {
+        // one step per launch: steps that meet an ill-conditioned M are taken in FP64
+        if (int rc = rkMersonMixedSteps(b, h, nsteps, tStop, cont, acc, ctol, pes)) return rc;
+    } else {
+        const StepCtl step{nsteps, cont ? 0 : 1, tStop, 0, 0};
+        SBG_CUDA(launchRKMerson(b->T, b->plan(), b->precision, b->y, b->time, b->bufsArg(), b->status, h, step, acc,
+                                ctol, pes, b->streams()),
+                 "RK-Merson kernel launch");
+        b->launches += b->segments();
+    }
     b->integrating = true;
     b->realized = false;
     return SBG_OK;

@@ -131,7 +131,28 @@ struct DevTables {
     // whose instances share the launch's step count, step size and options)
     const int32_t* ictl;     // steps of this launch | kCtl* flags
     const double* iparam;    // h, accuracy, constraint tolerance (3 per instance)
+    // One-step launches of a mixed batch integration (null otherwise). At
+    // launch L an instance is in FP64 mode when fbMode[(L & 1) * ninst + i]
+    // is set: the FP64 list kernel steps it (it is on fbList[L & 1], length
+    // fbCount[L & 1]) while the mixed kernels, concurrently, step the others.
+    // Each launch's owner of an instance writes its mode for launch L + 1 and
+    // puts it on the next list if FP64. An instance whose mixed step meets an
+    // ill-conditioned M leaves its state as it was (it falls one step behind)
+    // and takes that step and the next kFp64Steps - 1 in FP64 (fbLeft counts
+    // them). stepsLeft counts the steps an instance still has to take in a
+    // fixed-count call (null for stepTo).
+    int32_t* fbList;         // 2 x ninst
+    int32_t* fbCount;        // 2
+    int32_t* fbMode;         // 2 x ninst
+    int32_t* fbLeft;         // per instance
+    int32_t* stepsLeft;      // per instance
+    double* fbuf64;          // FP64 stage derivatives of the FP64-mode instances (4 planes)
 };
+// FP64 steps an instance takes, from the step whose mixed RHS met an
+// ill-conditioned M, before it tries the mixed form again.
+constexpr int kFp64Steps = 16;
+// Lanes per instance of the FP64 list kernel (level-parallel driver).
+constexpr int kFbLanes = 8;
 constexpr int kCtlSteps = (1 << 24) - 1;
 constexpr int kCtlInit = 1 << 30;                // first launch: Integrator::initialize projections
 constexpr int kCtlProjectEveryStep = 1 << 29;    // Integrator::setProjectEveryStep(true)
@@ -139,8 +160,12 @@ constexpr int kCtlProjectEveryStep = 1 << 29;    // Integrator::setProjectEveryS
 // runs in FP64 from now on (stripped before the status is reported).
 constexpr int kStFp64 = 1 << 30;
 // The mixed form's refinement trusts its FP32 factorisation while the
-// correction stays within this fraction of udot (max-norms).
+// correction stays within this fraction of udot (max-norms): 1e-4 in a
+// realize, where a flagged instance costs an FP64 recomputation after the
+// mixed pass, and 1e-5 in an integration (batch steps and the server), whose
+// FP64 steps overlap the mixed ones.
 constexpr float kIllConditioned = 1e-4f;
+constexpr float kIllConditionedStep = 1e-5f;
 
 // How one batch operation is launched: order positions [0, nChain) run the
 // chain driver (one thread per instance, width nm), the next nLoop positions

@@ -1,6 +1,7 @@
-// k_fallback.cu -- FP64 recomputation of the mixed realize's ill-conditioned
-// instances (realizeFallbackKernel), one launch per segment after its mixed
-// kernel on the same stream.
+// k_fallback.cu -- FP64 work of the mixed form's ill-conditioned instances:
+// the realize's recomputation (realizeFallbackKernel, one launch per segment
+// after its mixed kernel on the same stream) and the FP64 steps of a mixed
+// batch integration (rkFp64List).
 #include "abi_device.cuh"
 
 namespace sbg {
@@ -21,6 +22,21 @@ void realizeFallback(const KArgs& a, bool group, cudaStream_t s) {
             realizeFallbackKernel<3, false><<<(count + 127) / 128, 128, 0, s>>>(*a.T, a.P->chainFirst, count, a.y,
                                                                                a.ydot, a.status);
     }
+}
+
+// The FP64 steps of the instances in FP64 mode at a one-step launch of a
+// mixed batch integration: rkMersonKernel with LIST, kFbLanes lanes per
+// instance through the level-parallel driver on FP64 records of that layout
+// (rowsBase per instance into rows). The grid covers every instance; groups
+// past the list's length return at once.
+void rkFp64List(const KArgs& a, const int64_t* rowsBase, double* rows, cudaStream_t s) {
+    DevTables T = *a.T;
+    if (!T.fbList || T.ninst <= 0) return;
+    T.sbase = rowsBase;
+    const int nb = (int)(((int64_t)T.ninst * kFbLanes + 127) / 128);
+    rkMersonKernel<double, 3, false, true, 1, false, 128, true><<<nb, 128, 0, s>>>(
+        T, 0, 0, a.ystate, a.time, T.fbuf64, a.fplane, rows, a.status, a.h, a.step, a.accuracy, a.consTol,
+        a.projectEveryStep);
 }
 
 }  // namespace sbg

@@ -161,6 +161,44 @@ cudaError_t launchRKMerson(const DevTables& T, const LaunchPlan& P, int precisio
                     [&](cudaStream_t st) { rk32Group(a, ref, st); });
 }
 
+cudaError_t launchRKFp64List(const DevTables& T, const LaunchPlan& P, double* y, double* time, int32_t* status,
+                             double h, StepCtl step, double accuracy, double consTol, int projectEveryStep,
+                             int64_t fplane, const int64_t* rowsBase, double* rows, cudaStream_t s) {
+    KArgs a{};
+    a.T = &T; a.P = &P; a.ystate = y; a.time = time; a.status = status; a.h = h; a.step = step;
+    a.accuracy = accuracy; a.consTol = consTol; a.projectEveryStep = projectEveryStep; a.fplane = fplane;
+    rkFp64List(a, rowsBase, rows, s);
+    return cudaGetLastError();
+}
+
+__global__ void fillIntKernel(int32_t* __restrict__ p, int n, int v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+cudaError_t launchFillInt(int32_t* p, int n, int v, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    fillIntKernel<<<(n + 255) / 256, 256, 0, s>>>(p, n, v);
+    return cudaGetLastError();
+}
+
+// Instances of a one-step integration call that have steps left (stepsLeft
+// > 0; with stepsLeft null: time < tStop and no TIMEOUT status).
+__global__ void countUnfinishedKernel(int n, const int32_t* __restrict__ stepsLeft, const double* __restrict__ time,
+                                      const int32_t* __restrict__ status, double tStop, int32_t* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool left = false;
+    if (i < n) left = stepsLeft ? stepsLeft[i] > 0 : (time[i] < tStop && !(status[i] & SBG_INST_TIMEOUT));
+    const unsigned b = __ballot_sync(0xffffffffu, left);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(out, __popc(b));
+}
+cudaError_t launchCountUnfinished(int n, const int32_t* stepsLeft, const double* time, const int32_t* status,
+                                  double tStop, int32_t* out, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(int32_t), s);
+    if (e != cudaSuccess || n <= 0) return e;
+    countUnfinishedKernel<<<(n + 255) / 256, 256, 0, s>>>(n, stepsLeft, time, status, tStop, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launchNormalizeQuat(const DevTables& T, double* y, cudaStream_t s) {
     const int threads = 128, blocks = (T.ninst + threads - 1) / threads;
     if (blocks == 0) return cudaSuccess;

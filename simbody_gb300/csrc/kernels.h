@@ -27,10 +27,15 @@ struct Streams {
 //                caller's launch) and, with loop closures, the forced
 //                position and velocity projections; 0 continues the
 //                integration where the previous call left it.
+//   maxSteps     > 0: at most this many steps in this launch (the one-step
+//                launches of a mixed batch integration)
+//   launch       index of this one-step launch (only its parity is used)
 struct StepCtl {
     int nsteps;
     int init;
     double tStop;
+    int maxSteps;
+    int launch;
 };
 constexpr int kMaxStepsPerCall = 1 << 30;
 
@@ -121,6 +126,17 @@ void minvLoop(const KArgs& a, cudaStream_t s);
 void rkLoop(const KArgs& a, cudaStream_t s);
 void rkLoopWidth1(const KArgs& a, cudaStream_t s);  // k_rkloops1.cu: rkLoop for batch width 1
 void rkLoopGroup(const KArgs& a, cudaStream_t s);      // loop closures, level-parallel driver
+// One FP64 RK-Merson step for each instance in FP64 mode at this launch
+// (T.fbList[launch & 1]), kFbLanes lanes per instance on FP64 records of the
+// level-parallel layout at rowsBase (k_fallback.cu).
+void rkFp64List(const KArgs& a, const int64_t* rowsBase, double* rows, cudaStream_t s);
+cudaError_t launchRKFp64List(const DevTables& T, const LaunchPlan& P, double* y, double* time, int32_t* status,
+                             double h, StepCtl step, double accuracy, double consTol, int projectEveryStep,
+                             int64_t fplane, const int64_t* rowsBase, double* rows, cudaStream_t s);
+cudaError_t launchFillInt(int32_t* p, int n, int v, cudaStream_t s);
+// *out = instances with steps left in a one-step integration call
+cudaError_t launchCountUnfinished(int n, const int32_t* stepsLeft, const double* time, const int32_t* status,
+                                  double tStop, int32_t* out, cudaStream_t s);
 void realizeLoopGroup(const KArgs& a, cudaStream_t s);
 
 }  // namespace sbg

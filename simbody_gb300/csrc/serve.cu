@@ -805,7 +805,7 @@ int laneIssue(ServeLane* s) {
         a.scratchLoop = s->scratchLoop;
         a.status = s->status;
         a.h = 0;
-        a.step = StepCtl{0, 0, 0.0};  // per instance from ictl/iparam
+        a.step = StepCtl{0, 0, 0.0, 0, 0};  // per instance from ictl/iparam
         a.accuracy = 1e-3;
         a.consTol = 1e-4;
         const bool both = nLoopBlocks > 0 && nGroupBlocks > 0;

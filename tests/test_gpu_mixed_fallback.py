@@ -3,20 +3,24 @@
 FP32 recursions plus one double-float refinement step reach the 1e-5 udot bar
 only while the FP32 factorisation of M is good enough. Along random-tree
 trajectories M becomes ill-conditioned often enough that the refinement
-correction grows to the size of udot itself. The kernels detect this: a
-correction above 1e-4 of udot sets SBG_INST_ILL_CONDITIONED. Then:
+correction grows to the size of udot itself. The kernels detect this from the
+size of the correction. Then:
   * a mixed realize recomputes those instances in FP64 (status 0, counted by
-    sbg_batch_fallback_count);
+    sbg_batch_fallback_count); threshold 1e-4 of udot;
+  * a mixed batch integration takes the step in FP64, and the next 15 of that
+    instance; threshold 1e-5;
   * the server's mixed lane continues such a request in FP64
-    (info fp64_steps = 1, status 0);
-  * a mixed batch integration reports the bit.
+    (info fp64_steps = 1, status 0); threshold 1e-5.
 
-The states come from FP64 integrations of the serving stream's trees (2,000
-steps), where such states are common. A CPU emulation of the mixed RHS along
-those trajectories flagged 18 % of the states; the unflagged ones stayed
-within 2.2e-5 (a floor set by the FP32 kinematics, which the correction does
-not see). So the bar here is: every instance within 3e-5, and 99 % within
-1e-5.
+Along FP64 trajectories of the random-tree and uneven workloads (108,000
+states sampled on a GB300) a 1e-5 threshold flagged 14-17 % of the states and
+left none above 1e-5; 1e-4 flagged 3-4 % and let three states per workload
+through, up to 3.5e-5 (their error comes from the FP32 position kinematics,
+which the correction does not see).
+
+The states here come from FP64 integrations of the serving stream's trees
+(2,000 steps), where such states are common. The bar is the mixed form's:
+every instance within 1e-5.
 """
 import numpy as np
 import pytest
@@ -26,7 +30,6 @@ from simbody_gb300.engine import Topology
 
 pytestmark = pytest.mark.gpu
 
-ILL = 32
 
 
 def _udot(d, b):
@@ -56,17 +59,43 @@ def test_mixed_realize_falls_back_to_fp64_on_ill_conditioned_states(engine, tree
     assert (s64 == 0).all() and (smx == 0).all()
     assert bmx.fallback_count() > 0
     err = np.array([np.linalg.norm(a - r) / np.linalg.norm(r) for a, r in zip(_udot(dmx, bmx), _udot(d64, b64))])
-    assert err.max() <= 3e-5, err.max()
-    assert np.mean(err <= 1e-5) >= 0.99, np.sort(err)[-5:]
+    assert err.max() <= 1e-5, np.sort(err)[-5:]
 
 
-def test_mixed_batch_integration_reports_ill_conditioning(engine, trees):
+def test_mixed_batch_integration_takes_ill_conditioned_steps_in_fp64(engine, trees):
+    """From ill-conditioned states a mixed batch integration takes the
+    affected steps in FP64: no instance reports the bit, every instance ends
+    at the same time as the FP64 integration, within the mixed bar of it, and
+    two calls of 15 steps give the bits of one call of 30."""
     w, idx, y = trees
     bmx, _ = engine_batch(w, "mixed", instances=idx)
+    b64, _ = engine_batch(w, "fp64", instances=idx)
     bmx.set_state(y)
-    st = bmx.rk_merson_fixed(w.h, 1)
-    assert (st & ~(ILL | 4) == 0).all()
-    assert (st & ILL).any()
+    b64.set_state(y)
+    st = bmx.rk_merson_fixed(w.h, 30)
+    s64 = b64.rk_merson_fixed(w.h, 30)
+    assert (st & ~4 == 0).all() and (s64 & ~4 == 0).all()
+    ym, tm = bmx.get_state()
+    y64, t64 = b64.get_state()
+    np.testing.assert_array_equal(tm, t64)
+    err = np.array([np.linalg.norm(ym[a:e] - y64[a:e]) / np.linalg.norm(y64[a:e])
+                    for a, e in zip(bmx.y_offsets[:-1], bmx.y_offsets[1:])])
+    assert err.max() <= 1e-6, np.sort(err)[-5:]
+    b2, _ = engine_batch(w, "mixed", instances=idx)
+    b2.set_state(y)
+    b2.rk_merson_fixed(w.h, 15)
+    b2.rk_merson_fixed(w.h, 15, continue_integration=True)
+    yb, tb = b2.get_state()
+    np.testing.assert_array_equal(yb, ym)
+    np.testing.assert_array_equal(tb, tm)
+    # the states were ill-conditioned: the unrefined FP32 form is far off on some
+    probe, _ = engine_batch(w, "mixed_fast", instances=idx)
+    probe.set_state(y)
+    dfa, _ = probe.realize_acceleration()
+    b64.set_state(y)
+    d64, _ = b64.realize_acceleration()
+    efa = [np.linalg.norm(a - r) / np.linalg.norm(r) for a, r in zip(_udot(dfa, probe), _udot(d64, b64))]
+    assert max(efa) > 1e-4
 
 
 def test_server_continues_ill_conditioned_requests_in_fp64(engine, trees):
@@ -74,10 +103,16 @@ def test_server_continues_ill_conditioned_requests_in_fp64(engine, trees):
     them in FP64 and they match the FP64 batch integration to the mixed
     bar; each is the same alone and in the mix."""
     w, idx, y = trees
-    bmx, _ = engine_batch(w, "mixed", instances=idx)
-    bmx.set_state(y)
-    flagged = np.nonzero(bmx.rk_merson_fixed(w.h, 1) & ILL)[0][:8]
-    assert len(flagged) >= 2
+    bfa, _ = engine_batch(w, "mixed_fast", instances=idx)
+    b64, _ = engine_batch(w, "fp64", instances=idx)
+    bfa.set_state(y)
+    b64.set_state(y)
+    dfa, _ = bfa.realize_acceleration()
+    d64, _ = b64.realize_acceleration()
+    efa = np.array([np.linalg.norm(a - r) / np.linalg.norm(r) for a, r in zip(_udot(dfa, bfa), _udot(d64, b64))])
+    flagged = np.argsort(-efa)[:8]  # the worst-conditioned states (unrefined FP32 error)
+    assert efa[flagged[1]] > 1e-4
+    bmx = bfa
     steps = 20
     srv = Server("mixed", device_budget_bytes=1 << 30, chunk_steps=8)
     topos, ids = {}, {}
