@@ -279,42 +279,73 @@ def time_rk(b, h, nsteps):
     return start.elapsed_time(end), b.launch_count - n0
 
 
+def cpu_trajectory_baseline(w, h, nsteps, seconds: float = 4.0, max_instances: int = 4096):
+    """The oracle (the reference's CPU algorithm restated, -O2) integrating a
+    bounded sample of the same instances on all host threads, for about
+    `seconds`: body-steps/s."""
+    from oracle import oracle as O
+
+    threads = O.hardware_threads()
+    n = min(threads, w.ninst)
+    while True:
+        idx = np.arange(n)
+        t0 = time.perf_counter()
+        O.rk_workload(w, h, nsteps, idx, nthreads=threads)
+        dt = time.perf_counter() - t0
+        if dt >= seconds / 4 or n >= min(max_instances, w.ninst):
+            break
+        n = min(min(max_instances, w.ninst), max(n + 1, int(n * seconds / max(dt, 1e-3) / 2)))
+    return {"value": float(w.nbodies()[:n].sum()) * nsteps / dt, "unit": "body-steps/s", "cores": threads,
+            "kind": "port", "sample": f"{n} instances x {nsteps} steps, {dt:.1f} s wall"}
+
+
 def trajectories():
     """Fixed-step RK-Merson throughput (body-steps/s) on the trajectory
     workloads: the double pendulum (FP64), the random trees and the uneven
-    batch (mixed, FP64 state), with the mixed form's state error after all
-    steps against the FP64 engine on a subset of instances."""
+    batch. The trees run in both precisions: the mixed form (FP32 recursions,
+    FP64 state; steps whose RHS meets an ill-conditioned M taken in FP64) over
+    the full horizon, FP64 over a shorter one for its rate. Beside them: the
+    mixed form's state error after all steps against the FP64 engine on a
+    subset of instances, and the oracle port on the host cores."""
     from simbody_gb300 import Workload, engine_batch
 
     out = {}
-    for cfg, prec, n_inst, n_ref in [(1, "fp64", 1024, 0), (3, "mixed", 16384, 512), (4, "mixed", 10000, 256)]:
+    for cfg, n_inst, n_ref, fp64_steps in [(1, 1024, 0, 0), (3, 16384, 512, 400), (4, 10000, 256, 300)]:
         w = Workload(cfg, n_inst)
-        b, y0 = engine_batch(w, prec)
-        b.set_state(y0)
-        time_rk(b, w.h, 2)  # warm-up (the first call tunes the launch)
-        b.set_state(y0)
-        ms, launches = time_rk(b, w.h, w.nsteps)
-        y, _ = b.get_state()
-        _, st = b.get_ydot()
-        body_steps = int(w.nbodies().sum()) * w.nsteps
-        rec = {"precision": prec, "instances": w.ninst, "steps": w.nsteps, "h": w.h, "ms": ms,
-               "body_steps_per_s": body_steps / (ms * 1e-3), "gpu_launches": launches,
-               # instances that reached a state where the mixed refinement
-               # reported an ill-conditioned M (SBG_INST_ILL_CONDITIONED)
-               "ill_conditioned_instances": int(((st & 32) != 0).sum()),
-               "other_status_nonzero": int(((st & ~32) != 0).sum())}
+        rec = {"instances": w.ninst, "steps": w.nsteps, "h": w.h}
+        body = int(w.nbodies().sum())
+        for prec, steps in ((("fp64", w.nsteps),) if cfg == 1 else (("mixed", w.nsteps), ("fp64", fp64_steps))):
+            b, y0 = engine_batch(w, prec)
+            b.set_state(y0)
+            time_rk(b, w.h, 2)  # warm-up (the first call tunes the launch)
+            b.set_state(y0)
+            f0 = b.fp64_steps()
+            ms, launches = time_rk(b, w.h, steps)
+            y, _ = b.get_state()
+            _, st = b.get_ydot()
+            r = {"steps": steps, "ms": ms, "body_steps_per_s": body * steps / (ms * 1e-3), "gpu_launches": launches,
+                 "status_nonzero": int((st != 0).sum())}
+            if prec == "mixed":
+                # instance steps taken in FP64 (a mixed RHS met an ill-conditioned M)
+                r["fp64_instance_steps_frac"] = (b.fp64_steps() - f0) / float(w.ninst * steps)
+                ymix = y
+            rec[prec] = r
+            b.close()
+        if cfg != 1:
+            rec["mixed_over_fp64"] = rec["mixed"]["body_steps_per_s"] / rec["fp64"]["body_steps_per_s"]
         if n_ref:
             idx = np.arange(n_ref)
             r, yr0 = engine_batch(w, "fp64", instances=idx)
             r.set_state(yr0)
             r.rk_merson_fixed(w.h, w.nsteps)
             yr, _ = r.get_state()
+            offs = w.y_offsets  # the batch's host packing is the workload's, instance order
 
             def rel(a, oa, c, oc):
                 return np.array([np.linalg.norm(a[oa[i]:oa[i + 1]] - c[oc[i]:oc[i + 1]]) /
                                  np.linalg.norm(c[oc[i]:oc[i + 1]]) for i in idx])
 
-            errs = rel(y, b.y_offsets, yr, r.y_offsets)
+            errs = rel(ymix, offs, yr, r.y_offsets)
             # the same FP64 run from a start perturbed by 1e-12 (relative):
             # how far rounding-sized differences grow over the horizon
             rng = np.random.default_rng(0)
@@ -326,8 +357,9 @@ def trajectories():
                                             "max": float(errs.max()),
                                             "fp64_from_1e-12_perturbed_start": {"median": float(np.median(pert)),
                                                                                 "max": float(pert.max())}}
+            r.close()
+        rec["cpu_baseline"] = cpu_trajectory_baseline(w, w.h, w.nsteps)
         out[{1: "double_pendulum", 3: "random_trees", 4: "uneven_batch"}[cfg]] = rec
-        b.close()
     return out
 
 

@@ -271,6 +271,11 @@ int sbg_batch_last_operator_ms(sbg_batch batch, double* ms);
  * FP64 because the refinement reported an ill-conditioned M (see
  * SBG_INST_ILL_CONDITIONED); 0 for other precisions. Synchronous. */
 int sbg_batch_fallback_count(sbg_batch batch, int64_t* n);
+/* Mixed batches: how many instance steps of the batch's integrations so far
+ * were taken in FP64 because a mixed RHS of the step met an ill-conditioned M
+ * (the step itself and the instance's next 15); 0 for other precisions. No
+ * counterpart in the reference. Synchronous. */
+int sbg_batch_fp64_steps(sbg_batch batch, int64_t* n);
 
 /* RungeKuttaMersonIntegrator with setFixedStepSize(h), initialize(state) and
  * exactly nsteps internal steps of h (stepTo looped with

@@ -111,6 +111,7 @@ ENGINE_API = {
     "sbg_calc_composite_body_inertias": (C.c_int, [vp, dp, ip]),
     "sbg_batch_last_operator_ms": (C.c_int, [vp, dp]),
     "sbg_batch_fallback_count": (C.c_int, [vp, i64p]),
+    "sbg_batch_fp64_steps": (C.c_int, [vp, i64p]),
     "sbg_rk_merson_fixed": (C.c_int, [vp, C.c_double, C.c_int32, P(IntegOpts), ip]),
     "sbg_batch_stream": (vp, [vp]),
     "sbg_realize_acceleration_async": (C.c_int, [vp]),

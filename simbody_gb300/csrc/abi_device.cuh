@@ -1280,14 +1280,14 @@ __device__ __noinline__ int stageRhsMixedGroup(const DevTables& T, const Slot& s
     return r;
 }
 
-// Group g of kFbLanes lanes of the FP64 list kernel: the g-th instance in
-// FP64 mode at this launch.
-__device__ __forceinline__ Slot listSlot(const DevTables& T, int launch) {
+// Group g of G lanes of the FP64 list kernel: the g-th instance in FP64
+// mode at this launch.
+template <int G> __device__ __forceinline__ Slot listSlot(const DevTables& T, int launch) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int g = t / kFbLanes, lane = threadIdx.x & 31;
+    const int g = t / G, lane = threadIdx.x & 31;
     const int* list = T.fbList + (int64_t)(launch & 1) * T.ninst;
-    const unsigned mask = ((1u << kFbLanes) - 1u) << (lane & ~(kFbLanes - 1));
-    return Slot{g < T.fbCount[launch & 1] ? list[g] : -1, t % kFbLanes, kFbLanes, mask};
+    const unsigned mask = G == 32 ? 0xffffffffu : ((1u << G) - 1u) << (lane & ~(G - 1));
+    return Slot{g < T.fbCount[launch & 1] ? list[g] : -1, t % G, G, mask};
 }
 
 // One-step launches of a mixed batch integration: the instance's mode at the
@@ -1300,17 +1300,20 @@ __device__ __forceinline__ void fbNext(const DevTables& T, int launch, int inst,
 }
 
 // LIST: the FP64 steps of the instances in FP64 mode during the one-step
-// launches of a mixed batch integration (R = double, kFbLanes lanes per
-// instance through the level-parallel driver, scratch = FP64 records in the
-// level-parallel layout at T.sbase, fbuf = the FP64 stage planes).
+// launches of a mixed batch integration (R = double, fbuf = the FP64 stage
+// planes, scratch = FP64 records at T.sbase per instance). With GROUP,
+// kFbLanes lanes per instance through the level-parallel driver on the
+// field-major layout; without, one thread per instance through the one-thread
+// driver on contiguous records.
 template <class R, int NM, bool REF, bool GROUP, int MINB = 1, bool LOOPS = false, int BS = 128, bool LIST = false>
 __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int first, int count, double* __restrict__ y,
                                                             double* __restrict__ time, R* __restrict__ fbuf,
                                                             int64_t fplane, R* __restrict__ scratch,
                                                             int32_t* __restrict__ status, double h, StepCtl sc,
                                                             double accuracy, double consTol, int projectEveryStep) {
-    static_assert(!LIST || (std::is_same<R, double>::value && !REF && GROUP && !LOOPS), "the FP64 list is level-parallel FP64");
-    const Slot s = LIST ? listSlot(T, sc.launch) : GROUP ? groupSlot(T, first) : chainSlot(T, first, count);
+    static_assert(!LIST || (std::is_same<R, double>::value && !REF && !LOOPS), "the FP64 list is FP64");
+    const Slot s = LIST ? (GROUP ? listSlot<kFbLanes>(T, sc.launch) : listSlot<1>(T, sc.launch))
+                        : GROUP ? groupSlot(T, first) : chainSlot(T, first, count);
     if (s.inst < 0) return;
     const int inst = s.inst;
     // One-step launches of a mixed batch integration: an instance in FP64 mode
@@ -1332,6 +1335,9 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
     int nst = sc.nsteps;
     const double tStop = sc.tStop;
     const int maxSteps = sc.maxSteps > 0 ? sc.maxSteps : kMaxStepsPerCall;
+    // steps this instance still has to take in a fixed-count call of one-step
+    // launches (read before any lane of the group can change it)
+    int left = T.stepsLeft ? T.stepsLeft[inst] : kMaxStepsPerCall;
     bool init = sc.init != 0, pes = projectEveryStep != 0;
     if (T.ictl) {
         const int c = T.ictl[inst];
@@ -1362,7 +1368,9 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
     auto stage = [&](int stg, double c, const R* a, const R* b, R* dst) {
         StageSrc<R> src{y, f0, a, b, base, stride, nq, stg, c};
         FOut<R> o{dst, base, stride, nq};
-        if constexpr (REF && GROUP) {
+        if constexpr (LIST && !GROUP) {
+            st |= rhsChain<R, NM, false>(T, inst, ScrStrided<R>{scratch + T.sbase[inst], 1}, src, o);
+        } else if constexpr (REF && GROUP) {
             bool fin = true;
             st |= stageRhsMixedGroup<NM, R>(T, s, scratch, fallback, &rhs64, y, f0, a, b, base, stride, nq, stg, c,
                                             dst, &fin);
@@ -1404,7 +1412,7 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
         // takeOneStep's choice against tMax = tStop (AbstractIntegratorRep.cpp:536-544)
         double t1;
         if (step >= maxSteps) break;
-        if (T.stepsLeft && T.stepsLeft[inst] <= 0) break;  // one-step launches: this instance is done
+        if (left <= 0) break;  // this instance has taken its steps
         if (nst >= 0) {
             if (step >= nst) break;
             t1 = tc + h;
@@ -1526,9 +1534,13 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
         }
         if constexpr (GROUP) __syncwarp(s.mask);
         tc = t1;
+        --left;
         if (s.gl == 0) {
-            if (T.stepsLeft) --T.stepsLeft[inst];
-            if constexpr (LIST) --T.fbLeft[inst];
+            if (T.stepsLeft) T.stepsLeft[inst] = left;
+            if constexpr (LIST) {
+                --T.fbLeft[inst];
+                atomicAdd(T.fbSteps, 1ULL);
+            }
         }
     }
     if (s.gl == 0) {

@@ -117,8 +117,12 @@ struct sbg_batch_s {
     cudaStream_t stream2 = nullptr;
     cudaEvent_t evFork = nullptr, evJoin = nullptr;
     bool orderIdentity = false;         // launch order = instance order (a one-topology chain batch)
-    cudaStream_t pipe[4] = {};          // streams of the pipelined host realize (pipe[0] = stream)
-    cudaEvent_t pipeEv[4] = {};
+    // pipelined host realize: pipe[0] (= stream) uploads the chunks in order,
+    // pipe[1..3] compute them, pipe[4] downloads them in order; per chunk an
+    // event when its upload and when its gather is done
+    cudaStream_t pipe[5] = {};
+    cudaEvent_t pipeEv[2][16] = {};
+    cudaEvent_t pipeStart = nullptr, pipeEnd = nullptr;
     cudaEvent_t evT0 = nullptr, evT1 = nullptr;
     bool tuned = false;
     cudaGraphExec_t realizeGraph = nullptr;  // captured after tuning
@@ -139,7 +143,10 @@ struct sbg_batch_s {
     int32_t* fbLeft = nullptr;
     int32_t* stepsLeft = nullptr;
     int64_t fbLaunch = 0;             // one-step launches of the integration so far (continued calls go on)
+    bool fbAllFp64 = false;           // the integration switched to the FP64 kernels (too many FP64 steps)
+    unsigned long long fbWindow0 = 0; // FP64 steps counted at the start of the current window
     double* fbuf64 = nullptr;
+    unsigned long long* fbSteps = nullptr;
     int64_t* rowsBase = nullptr;
     double* rows = nullptr;
     cudaStream_t fbStream = nullptr;
@@ -200,10 +207,13 @@ struct sbg_batch_s {
         if (fbJoin) cudaEventDestroy(fbJoin);
         if (fbStream) cudaStreamDestroy(fbStream);
         if (stream2) cudaStreamDestroy(stream2);
-        for (int k = 1; k < 4; ++k)
+        for (int k = 1; k < 5; ++k)
             if (pipe[k]) cudaStreamDestroy(pipe[k]);
-        for (int k = 0; k < 4; ++k)
-            if (pipeEv[k]) cudaEventDestroy(pipeEv[k]);
+        for (auto& row : pipeEv)
+            for (cudaEvent_t e : row)
+                if (e) cudaEventDestroy(e);
+        if (pipeStart) cudaEventDestroy(pipeStart);
+        if (pipeEnd) cudaEventDestroy(pipeEnd);
         if (stream) cudaStreamDestroy(stream);
     }
     int alloc(void** out, size_t bytes, const char* what) {
@@ -904,14 +914,18 @@ int sbg_realize_acceleration(sbg_batch b, double* ydot, int32_t* status) {
 
 // State::updY + realize(Stage::Acceleration) + getYDot from and to host
 // buffers in one call. For a batch whose instances all run the one-thread
-// driver in instance order, the instances are cut into tile-aligned chunks
-// and each chunk's upload, scatter, realize, gather and download go on one
-// of up to four streams, so the copies of one chunk overlap the compute of
-// the others. Other batches take the plain sequence.
+// driver in instance order, the instances are cut into tile-aligned chunks:
+// one stream uploads the chunks in order, three streams scatter, realize and
+// gather them as their uploads land, and one stream downloads them in order
+// as they finish. The copies of one direction thus go one chunk at a time at
+// the link's full rate (concurrent copies would share it, so that the first
+// chunk would arrive no sooner than the last), and a chunk's compute overlaps
+// the other chunks' copies. Other batches take the plain sequence.
 int sbg_realize_acceleration_host(sbg_batch b, const double* y, double* ydot, int32_t* status) {
     if (!b || !y || !ydot) return fail(SBG_ERR_INVALID, "null argument");
     int nchunks = 4;
     if (const char* v = std::getenv("SBG_PIPE_CHUNKS")) nchunks = std::max(1, std::atoi(v));  // tuning override
+    nchunks = std::min(nchunks, 16);
     const bool pipelined = b->orderIdentity && b->nGroupBlocks == 0 && b->nLoop == 0 && b->tuned && nchunks > 1 &&
                            b->ninst >= nchunks * kTile;
     if (!pipelined) {
@@ -928,16 +942,21 @@ int sbg_realize_acceleration_host(sbg_batch b, const double* y, double* ydot, in
     const bool dstPinned = isPinned(ydot);
     double* dst = dstPinned ? ydot : b->hostPinned;
     const bool stPinned = status && isPinned(status);
-    const int nstreams = std::min(nchunks, 4);
     b->pipe[0] = b->stream;
-    for (int k = 0; k < nstreams; ++k) {
-        if (k > 0 && !b->pipe[k]) SBG_CUDA(cudaStreamCreateWithFlags(&b->pipe[k], cudaStreamNonBlocking), "streams");
-        if (!b->pipeEv[k]) SBG_CUDA(cudaEventCreateWithFlags(&b->pipeEv[k], cudaEventDisableTiming), "events");
+    for (int k = 1; k < 5; ++k)
+        if (!b->pipe[k]) SBG_CUDA(cudaStreamCreateWithFlags(&b->pipe[k], cudaStreamNonBlocking), "streams");
+    for (auto& row : b->pipeEv)
+        for (cudaEvent_t& e : row)
+            if (!e) SBG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "events");
+    if (!b->pipeStart) {
+        SBG_CUDA(cudaEventCreateWithFlags(&b->pipeStart, cudaEventDisableTiming), "events");
+        SBG_CUDA(cudaEventCreateWithFlags(&b->pipeEnd, cudaEventDisableTiming), "events");
     }
+    cudaStream_t up = b->pipe[0], down = b->pipe[4];
+    SBG_CUDA(cudaMemsetAsync(b->time, 0, std::max(b->ninst, 1) * sizeof(double), up), "time reset");
     // every stream starts after the work already queued on the batch stream
-    SBG_CUDA(cudaEventRecord(b->pipeEv[0], b->stream), "pipeline");
-    for (int k = 1; k < nstreams; ++k) SBG_CUDA(cudaStreamWaitEvent(b->pipe[k], b->pipeEv[0], 0), "pipeline");
-    SBG_CUDA(cudaMemsetAsync(b->time, 0, std::max(b->ninst, 1) * sizeof(double), b->stream), "time reset");
+    SBG_CUDA(cudaEventRecord(b->pipeStart, up), "pipeline");
+    for (int k = 1; k < 5; ++k) SBG_CUDA(cudaStreamWaitEvent(b->pipe[k], b->pipeStart, 0), "pipeline");
     const int tiles = (b->ninst + kTile - 1) / kTile;
     KArgs a{};
     a.T = &b->T;
@@ -949,10 +968,12 @@ int sbg_realize_acceleration_host(sbg_batch b, const double* y, double* ydot, in
         const int i0 = std::min(b->ninst, (int)((int64_t)tiles * c / nchunks) * kTile);
         const int i1 = std::min(b->ninst, (int)((int64_t)tiles * (c + 1) / nchunks) * kTile);
         if (i1 <= i0) continue;
-        cudaStream_t st = b->pipe[c % nstreams];
         const int64_t o0 = b->hostYOff[i0], o1 = b->hostYOff[i1];
-        SBG_CUDA(cudaMemcpyAsync(b->staging + o0, src + o0, (o1 - o0) * sizeof(double), cudaMemcpyHostToDevice, st),
+        cudaStream_t st = b->pipe[1 + c % 3];
+        SBG_CUDA(cudaMemcpyAsync(b->staging + o0, src + o0, (o1 - o0) * sizeof(double), cudaMemcpyHostToDevice, up),
                  "state upload");
+        SBG_CUDA(cudaEventRecord(b->pipeEv[0][c], up), "pipeline");
+        SBG_CUDA(cudaStreamWaitEvent(st, b->pipeEv[0][c], 0), "pipeline");
         SBG_CUDA(launchScatter(b->T, b->dHostYOff, b->staging, b->y, 0, st, i0, i1 - i0), "state scatter");
         LaunchPlan P = b->plan();
         P.chainFirst = i0;
@@ -962,21 +983,22 @@ int sbg_realize_acceleration_host(sbg_batch b, const double* y, double* ydot, in
         else realize32Chain(a, b->precision == SBG_PRECISION_MIXED, st);
         SBG_CUDA(cudaGetLastError(), "realize launch");
         SBG_CUDA(launchGather(b->T, b->dHostYOff, b->ydot, b->staging, 0, st, i0, i1 - i0), "derivative gather");
-        SBG_CUDA(cudaMemcpyAsync(dst + o0, b->staging + o0, (o1 - o0) * sizeof(double), cudaMemcpyDeviceToHost, st),
+        SBG_CUDA(cudaEventRecord(b->pipeEv[1][c], st), "pipeline");
+        SBG_CUDA(cudaStreamWaitEvent(down, b->pipeEv[1][c], 0), "pipeline");
+        SBG_CUDA(cudaMemcpyAsync(dst + o0, b->staging + o0, (o1 - o0) * sizeof(double), cudaMemcpyDeviceToHost, down),
                  "derivative download");
         if (stPinned)
             SBG_CUDA(cudaMemcpyAsync(status + i0, b->status + i0, (i1 - i0) * sizeof(int32_t), cudaMemcpyDeviceToHost,
-                                     st), "status download");
+                                     down), "status download");
         b->launches += 3 + (b->T.scratch64 ? 1 : 0);
     }
-    for (int k = 1; k < nstreams; ++k) {
-        SBG_CUDA(cudaEventRecord(b->pipeEv[k], b->pipe[k]), "pipeline");
-        SBG_CUDA(cudaStreamWaitEvent(b->stream, b->pipeEv[k], 0), "pipeline");
-    }
     if (status && !stPinned)
-        SBG_CUDA(cudaMemcpyAsync(status, b->status, b->ninst * sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream),
+        SBG_CUDA(cudaMemcpyAsync(status, b->status, b->ninst * sizeof(int32_t), cudaMemcpyDeviceToHost, down),
                  "status download");
-    SBG_CUDA(cudaStreamSynchronize(b->stream), "pipelined realize");
+    // the batch stream continues after the downloads
+    SBG_CUDA(cudaEventRecord(b->pipeEnd, down), "pipeline");
+    SBG_CUDA(cudaStreamWaitEvent(b->stream, b->pipeEnd, 0), "pipeline");
+    SBG_CUDA(cudaStreamSynchronize(down), "pipelined realize");
     if (!dstPinned) std::memcpy(ydot, b->hostPinned, bytes);
     b->stateSet = true;
     b->integrating = false;
@@ -1088,6 +1110,18 @@ int sbg_batch_fallback_count(sbg_batch b, int64_t* n) {
     return SBG_OK;
 }
 
+int sbg_batch_fp64_steps(sbg_batch b, int64_t* n) {
+    if (!b || !n) return fail(SBG_ERR_INVALID, "null argument");
+    *n = 0;
+    if (!b->fbSteps) return SBG_OK;
+    SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    unsigned long long v = 0;
+    SBG_CUDA(cudaStreamSynchronize(b->stream), "FP64 step count");
+    SBG_CUDA(cudaMemcpy(&v, b->fbSteps, sizeof(v), cudaMemcpyDeviceToHost), "FP64 step count");
+    *n = (int64_t)v;
+    return SBG_OK;
+}
+
 int sbg_batch_last_operator_ms(sbg_batch b, double* ms) {
     if (!b || !ms) return fail(SBG_ERR_INVALID, "null argument");
     if (!b->evOp0) return fail(SBG_ERR_STATE, "no tree operator has run");
@@ -1156,6 +1190,9 @@ static int ensureFallbackSteps(sbg_batch b) {
     if ((rc = b->alloc(&p, 4 * std::max<int64_t>(b->colElems, 1) * sizeof(double), "FP64 stage derivatives")))
         return rc;
     b->fbuf64 = static_cast<double*>(p);
+    if ((rc = b->alloc(&p, sizeof(unsigned long long), "FP64 step counter"))) return rc;
+    b->fbSteps = static_cast<unsigned long long*>(p);
+    SBG_CUDA(cudaMemsetAsync(b->fbSteps, 0, sizeof(unsigned long long), b->stream), "FP64 step counter");
     std::vector<int64_t> base(n + 1, 0);
     for (int64_t i = 0; i < n; ++i) base[i + 1] = base[i] + b->rowsElems[i];
     if ((rc = b->alloc(&p, std::max<int64_t>(base[n], 1) * sizeof(double), "FP64 level-parallel records"))) return rc;
@@ -1169,13 +1206,19 @@ static int ensureFallbackSteps(sbg_batch b) {
     return SBG_OK;
 }
 
+// Launches per window of the FP64 share test of a mixed batch integration.
+constexpr int64_t kFp64Window = 64;
+
 // A mixed batch integration as one-step launches. At launch L the mixed
 // kernels step the instances in mixed mode while the FP64 list kernel, on its
 // own stream, steps those in FP64 mode; an instance whose mixed step meets an
 // ill-conditioned M keeps its state and takes that step in FP64 at launch
 // L + 1, so it ends one launch behind the others for each such event.
 // Launches go on until every instance has taken its steps (nsteps >= 0) or
-// reached tStop.
+// reached tStop. Every kFp64Window launches the share of instance steps taken
+// in FP64 is checked; above a quarter, the integration switches for good (its
+// continued calls too) to the FP64 persistent kernels: on chaotic trees the
+// mixed steps then save less than the FP64 ones cost beside them.
 static int rkMersonMixedSteps(sbg_batch b, double h, int32_t nsteps, double tStop, bool cont, double acc, double ctol,
                               int pes) {
     if (int rc = ensureFallbackSteps(b)) return rc;
@@ -1186,12 +1229,18 @@ static int rkMersonMixedSteps(sbg_batch b, double h, int32_t nsteps, double tSto
     Tk.fbLeft = b->fbLeft;
     Tk.stepsLeft = nsteps >= 0 ? b->stepsLeft : nullptr;
     Tk.fbuf64 = b->fbuf64;
+    Tk.fbSteps = b->fbSteps;
     const int n = b->ninst;
     if (!cont) {  // a new integration: every instance starts in mixed mode
         SBG_CUDA(cudaMemsetAsync(b->fbMode, 0, 2 * (size_t)n * sizeof(int32_t), b->stream), "FP64 modes");
         SBG_CUDA(cudaMemsetAsync(b->fbLeft, 0, n * sizeof(int32_t), b->stream), "FP64 modes");
         SBG_CUDA(cudaMemsetAsync(b->fbCount, 0, 2 * sizeof(int32_t), b->stream), "FP64 lists");
         b->fbLaunch = 0;
+        b->fbAllFp64 = false;
+        b->fbWindow0 = 0;
+        SBG_CUDA(cudaStreamSynchronize(b->stream), "FP64 step count");
+        SBG_CUDA(cudaMemcpy(&b->fbWindow0, b->fbSteps, sizeof(unsigned long long), cudaMemcpyDeviceToHost),
+                 "FP64 step count");
     }
     int64_t target = nsteps;
     if (nsteps >= 0) {
@@ -1205,11 +1254,44 @@ static int rkMersonMixedSteps(sbg_batch b, double h, int32_t nsteps, double tSto
         target = stepsToReach(*std::min_element(t0.begin(), t0.end()), tStop, h);
     }
     const LaunchPlan P = b->plan();
+    // FP64 steps: kFbLanes level-parallel lanes per instance (measured faster
+    // than one thread per instance: 2.4x on the uneven trees, 6 % on the
+    // random trees)
+    int fbLanes = kFbLanes;
+    if (const char* v = std::getenv("SBG_FB_LANES")) fbLanes = std::atoi(v) > 1 ? kFbLanes : 1;  // tuning override
     const int64_t limit = 2 * target + 64;
+    // The FP64 persistent kernels, on the FP64 mirror of the records, take
+    // every instance's remaining steps once the integration has switched.
+    auto allFp64 = [&]() -> int {
+        const BatchBufs B64{b->T.scratch64, b->scratchLoop, b->fbuf64, b->fbufLoop ? b->fbufLoop : b->fbuf64,
+                            b->colElems};
+        const StepCtl step{nsteps >= 0 ? nsteps : -1, 0, tStop, 0, 0};
+        SBG_CUDA(launchRKMerson(Tk, P, SBG_PRECISION_FP64, b->y, b->time, B64, b->status, h, step, acc, ctol, pes,
+                                b->streams()),
+                 "RK-Merson kernel launch");
+        b->launches += b->segments();
+        return SBG_OK;
+    };
+    if (b->fbAllFp64) return allFp64();
     int64_t L = 0;
     for (;;) {
         for (; L < target; ++L) {
-            const int li = (int)((b->fbLaunch + L) & ((1 << 30) - 1));  // only its parity matters
+            const int64_t G = b->fbLaunch + L;  // launch index within the whole integration
+            if (G > 0 && G % kFp64Window == 0) {
+                // more than a quarter of the last window's instance steps in FP64:
+                // the FP64 kernels take the rest, without the mixed steps' overhead
+                unsigned long long v = 0;
+                SBG_CUDA(cudaStreamSynchronize(b->stream), "FP64 step count");
+                SBG_CUDA(cudaMemcpy(&v, b->fbSteps, sizeof(v), cudaMemcpyDeviceToHost), "FP64 step count");
+                const unsigned long long d = v - b->fbWindow0;
+                b->fbWindow0 = v;
+                if (4 * d > (unsigned long long)n * kFp64Window) {
+                    b->fbAllFp64 = true;
+                    b->fbLaunch += L;
+                    return allFp64();
+                }
+            }
+            const int li = (int)(G & ((1 << 30) - 1));  // only its parity matters
             SBG_CUDA(cudaMemsetAsync(b->fbCount + ((li + 1) & 1), 0, sizeof(int32_t), b->stream), "FP64 list reset");
             SBG_CUDA(cudaEventRecord(b->fbFork, b->stream), "fork");
             SBG_CUDA(cudaStreamWaitEvent(b->fbStream, b->fbFork, 0), "fork");
@@ -1218,7 +1300,7 @@ static int rkMersonMixedSteps(sbg_batch b, double h, int32_t nsteps, double tSto
                                     b->streams()),
                      "RK-Merson kernel launch");
             SBG_CUDA(launchRKFp64List(Tk, P, b->y, b->time, b->status, h, step, acc, ctol, pes, b->colElems, b->rowsBase,
-                                      b->rows, b->fbStream),
+                                      b->rows, fbLanes, b->fbStream),
                      "FP64 list kernel launch");
             SBG_CUDA(cudaEventRecord(b->fbJoin, b->fbStream), "join");
             SBG_CUDA(cudaStreamWaitEvent(b->stream, b->fbJoin, 0), "join");

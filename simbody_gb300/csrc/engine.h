@@ -147,6 +147,7 @@ struct DevTables {
     int32_t* fbLeft;         // per instance
     int32_t* stepsLeft;      // per instance
     double* fbuf64;          // FP64 stage derivatives of the FP64-mode instances (4 planes)
+    unsigned long long* fbSteps;  // FP64 steps taken by the list kernel (cumulative)
 };
 // FP64 steps an instance takes, from the step whose mixed RHS met an
 // ill-conditioned M, before it tries the mixed form again.

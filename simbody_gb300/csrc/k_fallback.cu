@@ -25,14 +25,28 @@ void realizeFallback(const KArgs& a, bool group, cudaStream_t s) {
 }
 
 // The FP64 steps of the instances in FP64 mode at a one-step launch of a
-// mixed batch integration: rkMersonKernel with LIST, kFbLanes lanes per
-// instance through the level-parallel driver on FP64 records of that layout
-// (rowsBase per instance into rows). The grid covers every instance; groups
-// past the list's length return at once.
-void rkFp64List(const KArgs& a, const int64_t* rowsBase, double* rows, cudaStream_t s) {
+// mixed batch integration: rkMersonKernel with LIST on FP64 records at
+// rowsBase per instance into rows. lanes 1: one thread per instance, the
+// one-thread driver on contiguous records (the batch's record offsets);
+// otherwise kFbLanes lanes per instance, the level-parallel driver on the
+// field-major layout. The grid covers every instance; threads past the list's
+// length return at once.
+void rkFp64List(const KArgs& a, const int64_t* rowsBase, double* rows, int lanes, cudaStream_t s) {
     DevTables T = *a.T;
     if (!T.fbList || T.ninst <= 0) return;
     T.sbase = rowsBase;
+    if (lanes == 1) {
+        const int nb = (T.ninst + 127) / 128;
+        if (a.P->nm == 1)
+            rkMersonKernel<double, 1, false, false, 1, false, 128, true><<<nb, 128, 0, s>>>(
+                T, 0, 0, a.ystate, a.time, T.fbuf64, a.fplane, rows, a.status, a.h, a.step, a.accuracy, a.consTol,
+                a.projectEveryStep);
+        else
+            rkMersonKernel<double, 3, false, false, 1, false, 128, true><<<nb, 128, 0, s>>>(
+                T, 0, 0, a.ystate, a.time, T.fbuf64, a.fplane, rows, a.status, a.h, a.step, a.accuracy, a.consTol,
+                a.projectEveryStep);
+        return;
+    }
     const int nb = (int)(((int64_t)T.ninst * kFbLanes + 127) / 128);
     rkMersonKernel<double, 3, false, true, 1, false, 128, true><<<nb, 128, 0, s>>>(
         T, 0, 0, a.ystate, a.time, T.fbuf64, a.fplane, rows, a.status, a.h, a.step, a.accuracy, a.consTol,

@@ -163,11 +163,11 @@ cudaError_t launchRKMerson(const DevTables& T, const LaunchPlan& P, int precisio
 
 cudaError_t launchRKFp64List(const DevTables& T, const LaunchPlan& P, double* y, double* time, int32_t* status,
                              double h, StepCtl step, double accuracy, double consTol, int projectEveryStep,
-                             int64_t fplane, const int64_t* rowsBase, double* rows, cudaStream_t s) {
+                             int64_t fplane, const int64_t* rowsBase, double* rows, int lanes, cudaStream_t s) {
     KArgs a{};
     a.T = &T; a.P = &P; a.ystate = y; a.time = time; a.status = status; a.h = h; a.step = step;
     a.accuracy = accuracy; a.consTol = consTol; a.projectEveryStep = projectEveryStep; a.fplane = fplane;
-    rkFp64List(a, rowsBase, rows, s);
+    rkFp64List(a, rowsBase, rows, lanes, s);
     return cudaGetLastError();
 }
 

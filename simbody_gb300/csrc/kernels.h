@@ -127,12 +127,12 @@ void rkLoop(const KArgs& a, cudaStream_t s);
 void rkLoopWidth1(const KArgs& a, cudaStream_t s);  // k_rkloops1.cu: rkLoop for batch width 1
 void rkLoopGroup(const KArgs& a, cudaStream_t s);      // loop closures, level-parallel driver
 // One FP64 RK-Merson step for each instance in FP64 mode at this launch
-// (T.fbList[launch & 1]), kFbLanes lanes per instance on FP64 records of the
-// level-parallel layout at rowsBase (k_fallback.cu).
-void rkFp64List(const KArgs& a, const int64_t* rowsBase, double* rows, cudaStream_t s);
+// (T.fbList[launch & 1]) on FP64 records at rowsBase: one thread (lanes 1) or
+// kFbLanes lanes of the level-parallel driver per instance (k_fallback.cu).
+void rkFp64List(const KArgs& a, const int64_t* rowsBase, double* rows, int lanes, cudaStream_t s);
 cudaError_t launchRKFp64List(const DevTables& T, const LaunchPlan& P, double* y, double* time, int32_t* status,
                              double h, StepCtl step, double accuracy, double consTol, int projectEveryStep,
-                             int64_t fplane, const int64_t* rowsBase, double* rows, cudaStream_t s);
+                             int64_t fplane, const int64_t* rowsBase, double* rows, int lanes, cudaStream_t s);
 cudaError_t launchFillInt(int32_t* p, int n, int v, cudaStream_t s);
 // *out = instances with steps left in a one-step integration call
 cudaError_t launchCountUnfinished(int n, const int32_t* stepsLeft, const double* time, const int32_t* status,

@@ -208,6 +208,13 @@ class Batch:
         N.check(N.engine_lib().sbg_batch_fallback_count(self._h, C.byref(n)))
         return n.value
 
+    def fp64_steps(self) -> int:
+        """Mixed batches: instance steps of the integrations so far taken in
+        FP64 (an ill-conditioned M met by a mixed RHS)."""
+        n = C.c_int64()
+        N.check(N.engine_lib().sbg_batch_fp64_steps(self._h, C.byref(n)))
+        return n.value
+
     def last_operator_ms(self) -> float:
         """Device time of the last tree operator's kernels (copies excluded)."""
         ms = C.c_double()

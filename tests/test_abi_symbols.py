@@ -57,6 +57,9 @@ def test_batch_entry_points_refuse_a_null_batch_without_touching_the_device():
         "sbg_calc_composite_body_inertias": (None, d, i32),
         "sbg_multiply_by_minv": (None, d, d),
         "sbg_batch_fallback_count": (None, C.byref(i64)),
+        "sbg_batch_fp64_steps": (None, C.byref(i64)),
+        "sbg_batch_get_qdotdot": (None, d),
+        "sbg_rk_merson_step_to": (None, 1e-3, 1.0, None, i32),
         "sbg_batch_last_operator_ms": (None, d),
     }
     for name, args in calls.items():

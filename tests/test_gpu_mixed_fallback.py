@@ -137,3 +137,29 @@ def test_server_continues_ill_conditioned_requests_in_fp64(engine, trees):
     rid = alone.submit(topos[k], y[bmx.y_offsets[k]:bmx.y_offsets[k + 1]], w.h, steps)
     alone.drain()
     assert np.array_equal(alone.result(rid)[0], srv.result(ids[k])[0])
+
+
+def test_mixed_integration_switches_to_fp64_when_most_steps_need_it(engine, trees):
+    """From the ill-conditioned states a quarter or more of the instance steps
+    need FP64: after its first 64-launch window the integration continues on
+    the FP64 kernels (a few launches instead of two per step), and it stays
+    within the mixed bar of the FP64 integration."""
+    w, idx, y = trees
+    bmx, _ = engine_batch(w, "mixed", instances=idx)
+    b64, _ = engine_batch(w, "fp64", instances=idx)
+    bmx.set_state(y)
+    b64.set_state(y)
+    steps = 256
+    l0, f0 = bmx.launch_count, bmx.fp64_steps()
+    st = bmx.rk_merson_fixed(w.h, steps)
+    launches, fp64 = bmx.launch_count - l0, bmx.fp64_steps() - f0
+    assert (st & ~4 == 0).all()
+    assert fp64 > len(idx) * 64 // 4, fp64  # the first window's share was above a quarter
+    assert launches < steps, launches        # ... so the rest ran on the FP64 kernels
+    b64.rk_merson_fixed(w.h, steps)
+    ym, tm = bmx.get_state()
+    y64, t64 = b64.get_state()
+    np.testing.assert_array_equal(tm, t64)
+    err = np.array([np.linalg.norm(ym[a:e] - y64[a:e]) / np.linalg.norm(y64[a:e])
+                    for a, e in zip(bmx.y_offsets[:-1], bmx.y_offsets[1:])])
+    assert np.median(err) <= 1e-6, np.median(err)
