@@ -11,15 +11,17 @@ void realizeFallback(const KArgs& a, bool group, cudaStream_t s) {
     if (group) {
         const int first = a.P->nChain + a.P->nLoop, count = a.T->ninst - first;
         if (count <= 0) return;
-        realizeFallbackKernel<3, true><<<(count + 127) / 128, 128, 0, s>>>(*a.T, first, count, a.y, a.ydot, a.status);
+        const Launch1D L = spread(count, 128);
+        realizeFallbackKernel<3, true><<<L.grid, L.block, 0, s>>>(*a.T, first, count, a.y, a.ydot, a.status);
     } else {
         const int count = a.P->nChain;
         if (count <= 0) return;
+        const Launch1D L = spread(count, 128);
         if (a.P->nm == 1)
-            realizeFallbackKernel<1, false><<<(count + 127) / 128, 128, 0, s>>>(*a.T, a.P->chainFirst, count, a.y,
+            realizeFallbackKernel<1, false><<<L.grid, L.block, 0, s>>>(*a.T, a.P->chainFirst, count, a.y,
                                                                                a.ydot, a.status);
         else
-            realizeFallbackKernel<3, false><<<(count + 127) / 128, 128, 0, s>>>(*a.T, a.P->chainFirst, count, a.y,
+            realizeFallbackKernel<3, false><<<L.grid, L.block, 0, s>>>(*a.T, a.P->chainFirst, count, a.y,
                                                                                a.ydot, a.status);
     }
 }

@@ -6,24 +6,25 @@
 
 namespace sbg {
 
-static inline int loopBlocks(const LaunchPlan& P) { return (P.nLoop + 127) / 128; }
 
 void realizeLoop(const KArgs& a, cudaStream_t s) {
     double* sc = static_cast<double*>(a.scratchLoop);
-    const int first = a.P->nChain, nb = loopBlocks(*a.P);
+    const int first = a.P->nChain;
+    const Launch1D L = spread(a.P->nLoop, 128);
     if (a.P->nm == 1)
-        realizeKernel<double, 1, false, false, 1, true><<<nb, 128, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.ydot, sc, a.status);
+        realizeKernel<double, 1, false, false, 1, true><<<L.grid, L.block, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.ydot, sc, a.status);
     else
-        realizeKernel<double, 3, false, false, 1, true><<<nb, 128, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.ydot, sc, a.status);
+        realizeKernel<double, 3, false, false, 1, true><<<L.grid, L.block, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.ydot, sc, a.status);
 }
 
 void minvLoop(const KArgs& a, cudaStream_t s) {
     double* sc = static_cast<double*>(a.scratchLoop);
-    const int first = a.P->nChain, nb = loopBlocks(*a.P);
+    const int first = a.P->nChain;
+    const Launch1D L = spread(a.P->nLoop, 128);
     if (a.P->nm == 1)
-        minvKernel<double, 1, false><<<nb, 128, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.f, a.ydot, sc, a.status);
+        minvKernel<double, 1, false><<<L.grid, L.block, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.f, a.ydot, sc, a.status);
     else
-        minvKernel<double, 3, false><<<nb, 128, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.f, a.ydot, sc, a.status);
+        minvKernel<double, 3, false><<<L.grid, L.block, 0, s>>>(*a.T, first, a.P->nLoop, a.y, a.f, a.ydot, sc, a.status);
 }
 
 // Loop-closure instances on the level-parallel driver (FP64): tree passes on

@@ -18,10 +18,10 @@ void realize32Group(const KArgs& a, bool refine, cudaStream_t s) {
 }
 
 void minv32Chain(const KArgs& a, cudaStream_t s) {
-    const int nb = (a.P->nChain + 127) / 128;
+    const Launch1D L = spread(a.P->nChain, 128);
     float* sc = static_cast<float*>(a.scratch);
-    if (a.P->nm == 1) minvKernel<float, 1, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.f, a.ydot, sc, a.status);
-    else minvKernel<float, 3, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.f, a.ydot, sc, a.status);
+    if (a.P->nm == 1) minvKernel<float, 1, false><<<L.grid, L.block, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.f, a.ydot, sc, a.status);
+    else minvKernel<float, 3, false><<<L.grid, L.block, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.f, a.ydot, sc, a.status);
 }
 void minv32Group(const KArgs& a, cudaStream_t s) {
     minvKernel<float, 3, true><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, a.P->groupFirst, 0, a.y, a.f, a.ydot,

@@ -3,23 +3,22 @@
 
 namespace sbg {
 
-static inline int chainBlocks(const LaunchPlan& P) { return (P.nChain + 127) / 128; }
 
 void realize64Chain(const KArgs& a, cudaStream_t s) {
-    const int nb = chainBlocks(*a.P);
+    const Launch1D L = spread(a.P->nChain, 128);
     double* sc = static_cast<double*>(a.scratch);
-    if (a.P->nm == 1) realizeKernel<double, 1, false, false><<<nb, 128, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
-    else realizeKernel<double, 3, false, false><<<nb, 128, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
+    if (a.P->nm == 1) realizeKernel<double, 1, false, false><<<L.grid, L.block, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
+    else realizeKernel<double, 3, false, false><<<L.grid, L.block, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
 }
 void realize64Group(const KArgs& a, cudaStream_t s) {
     realizeKernel<double, 3, false, true><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, a.P->groupFirst, 0, a.y, a.ydot,
                                                                               static_cast<double*>(a.scratch), a.status);
 }
 void minv64Chain(const KArgs& a, cudaStream_t s) {
-    const int nb = chainBlocks(*a.P);
+    const Launch1D L = spread(a.P->nChain, 128);
     double* sc = static_cast<double*>(a.scratch);
-    if (a.P->nm == 1) minvKernel<double, 1, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.f, a.ydot, sc, a.status);
-    else minvKernel<double, 3, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.f, a.ydot, sc, a.status);
+    if (a.P->nm == 1) minvKernel<double, 1, false><<<L.grid, L.block, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.f, a.ydot, sc, a.status);
+    else minvKernel<double, 3, false><<<L.grid, L.block, 0, s>>>(*a.T, 0, a.P->nChain, a.y, a.f, a.ydot, sc, a.status);
 }
 void minv64Group(const KArgs& a, cudaStream_t s) {
     minvKernel<double, 3, true><<<a.P->nGroupBlocks, 128, 0, s>>>(*a.T, a.P->groupFirst, 0, a.y, a.f, a.ydot,

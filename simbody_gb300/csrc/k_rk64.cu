@@ -4,14 +4,14 @@
 namespace sbg {
 
 void rk64Chain(const KArgs& a, cudaStream_t s) {
-    const int nb = (a.P->nChain + 127) / 128;
+    const Launch1D L = spread(a.P->nChain, 128);
     double* fb = static_cast<double*>(a.fbuf);
     double* sc = static_cast<double*>(a.scratch);
     if (a.P->nm == 1)
-        rkMersonKernel<double, 1, false, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.ystate, a.time, fb, a.fplane, sc,
+        rkMersonKernel<double, 1, false, false><<<L.grid, L.block, 0, s>>>(*a.T, 0, a.P->nChain, a.ystate, a.time, fb, a.fplane, sc,
                                                                    a.status, a.h, a.step, a.accuracy, a.consTol, a.projectEveryStep);
     else
-        rkMersonKernel<double, 3, false, false><<<nb, 128, 0, s>>>(*a.T, 0, a.P->nChain, a.ystate, a.time, fb, a.fplane, sc,
+        rkMersonKernel<double, 3, false, false><<<L.grid, L.block, 0, s>>>(*a.T, 0, a.P->nChain, a.ystate, a.time, fb, a.fplane, sc,
                                                                    a.status, a.h, a.step, a.accuracy, a.consTol, a.projectEveryStep);
 }
 void rk64Group(const KArgs& a, cudaStream_t s) {

@@ -5,8 +5,6 @@
 
 namespace sbg {
 
-static inline int loopBlocks(const LaunchPlan& P) { return (P.nLoop + 127) / 128; }
-
 // Batch width 3 here; width 1 (every non-Free body one mobility) in
 // k_rkloops1.cu, so that the two compile in parallel.
 void rkLoop(const KArgs& a, cudaStream_t s) {
@@ -16,8 +14,9 @@ void rkLoop(const KArgs& a, cudaStream_t s) {
     }
     double* sc = static_cast<double*>(a.scratchLoop);
     double* fb = static_cast<double*>(a.fbufLoop);
-    const int first = a.P->nChain, nb = loopBlocks(*a.P);
-    rkMersonKernel<double, 3, false, false, 1, true><<<nb, 128, 0, s>>>(
+    const int first = a.P->nChain;
+    const Launch1D L = spread(a.P->nLoop, 128);
+    rkMersonKernel<double, 3, false, false, 1, true><<<L.grid, L.block, 0, s>>>(
         *a.T, first, a.P->nLoop, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.step, a.accuracy, a.consTol,
         a.projectEveryStep);
 }

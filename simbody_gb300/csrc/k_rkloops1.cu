@@ -8,8 +8,9 @@ namespace sbg {
 void rkLoopWidth1(const KArgs& a, cudaStream_t s) {
     double* sc = static_cast<double*>(a.scratchLoop);
     double* fb = static_cast<double*>(a.fbufLoop);
-    const int first = a.P->nChain, nb = (a.P->nLoop + 127) / 128;
-    rkMersonKernel<double, 1, false, false, 1, true><<<nb, 128, 0, s>>>(
+    const int first = a.P->nChain;
+    const Launch1D L = spread(a.P->nLoop, 128);
+    rkMersonKernel<double, 1, false, false, 1, true><<<L.grid, L.block, 0, s>>>(
         *a.T, first, a.P->nLoop, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.step, a.accuracy, a.consTol,
         a.projectEveryStep);
 }

@@ -86,6 +86,26 @@ cudaError_t launchGather(const DevTables& T, const int64_t* hostOff, const doubl
                          cudaStream_t s, int inst0 = 0, int count = -1);
 
 
+// Grid of a one-thread-per-instance launch of n threads with at most bs per
+// block: blocks shrink (to no fewer than 8 threads) until there are at least
+// two per SM, so that a small batch spreads over every SM (an FP64-bound
+// kernel otherwise leaves most SMs' FP64 units idle).
+struct Launch1D {
+    int grid, block;
+};
+inline Launch1D spread(int64_t n, int bs) {
+    static int sms = 0;
+    if (!sms) {
+        int d = 0, c = 0;
+        if (cudaGetDevice(&d) == cudaSuccess && cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, d) == cudaSuccess)
+            sms = c > 0 ? c : 1;
+        else
+            sms = 1;
+    }
+    while (bs > 8 && (n + bs - 1) / bs < 2 * sms) bs >>= 1;
+    return Launch1D{(int)((n + bs - 1) / bs), bs};
+}
+
 // Per-segment launchers (k_r64.cu, k_r32c.cu, k_r32g.cu, k_rk64.cu,
 // k_rk32c.cu, k_rk32g.cu).
 struct KArgs {

@@ -11,12 +11,12 @@
 namespace sbg {
 
 template <bool REF, int MINB, int BS> static void r32ChainGo(const KArgs& a, cudaStream_t s) {
-    const int nb = (a.P->nChain + BS - 1) / BS;
+    const Launch1D L = spread(a.P->nChain, BS);
     float* sc = static_cast<float*>(a.scratch);
     if (a.P->nm == 1)
-        realizeKernel<float, 1, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
+        realizeKernel<float, 1, REF, false, MINB, false, BS><<<L.grid, L.block, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
     else
-        realizeKernel<float, 3, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
+        realizeKernel<float, 3, REF, false, MINB, false, BS><<<L.grid, L.block, 0, s>>>(*a.T, a.P->chainFirst, a.P->nChain, a.y, a.ydot, sc, a.status);
 }
 
 template <bool REF> static void r32ChainPick(const KArgs& a, cudaStream_t s) {

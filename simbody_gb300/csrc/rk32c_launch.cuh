@@ -8,15 +8,15 @@
 namespace sbg {
 
 template <bool REF, int MINB, int BS> static void rk32ChainGo(const KArgs& a, cudaStream_t s) {
-    const int nb = (a.P->nChain + BS - 1) / BS;
+    const Launch1D L = spread(a.P->nChain, BS);
     float* fb = static_cast<float*>(a.fbuf);
     float* sc = static_cast<float*>(a.scratch);
     if (a.P->nm == 1)
-        rkMersonKernel<float, 1, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(
+        rkMersonKernel<float, 1, REF, false, MINB, false, BS><<<L.grid, L.block, 0, s>>>(
             *a.T, 0, a.P->nChain, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.step, a.accuracy, a.consTol,
             a.projectEveryStep);
     else
-        rkMersonKernel<float, 3, REF, false, MINB, false, BS><<<nb, BS, 0, s>>>(
+        rkMersonKernel<float, 3, REF, false, MINB, false, BS><<<L.grid, L.block, 0, s>>>(
             *a.T, 0, a.P->nChain, a.ystate, a.time, fb, a.fplane, sc, a.status, a.h, a.step, a.accuracy, a.consTol,
             a.projectEveryStep);
 }
