@@ -15,7 +15,7 @@
 //   RungeKuttaMersonBatchIntegrator
 //                                 RungeKuttaMersonIntegrator with setFixedStepSize,
 //                                 setAccuracy, setConstraintTolerance,
-//                                 setProjectEveryStep, initialize, stepTo
+//                                 setProjectEveryStep, initialize, stepTo, stepBy
 #ifndef SIMBODY_GB300_HPP_
 #define SIMBODY_GB300_HPP_
 
@@ -207,12 +207,15 @@ private:
 };
 
 // RungeKuttaMersonIntegrator over every state of a batch, with a fixed step
-// size (Integrator::setFixedStepSize): initialize() sets the common start
-// time; stepTo(t) advances every instance to t, which must be a whole number
-// of steps from the current time. Each stepTo is one sbg_rk_merson_fixed
-// call, which begins with Integrator::initialize's projection (quaternions
-// normalized, loop closures projected) on the batch's current state. Returns
-// one SBG_INST_* word per instance.
+// size (Integrator::setFixedStepSize) and interpolation off
+// (Integrator::setAllowInterpolation(false)): stepTo(t) lands every instance
+// exactly on t, its last step shortened when t is not a whole number of steps
+// away (AbstractIntegratorRep.cpp:536-544). initialize() starts a new
+// integration of the batch's current state: the first stepTo after it does
+// Integrator::initialize's projection (quaternions normalized, loop closures
+// projected); later calls continue the integration, as repeated stepTo calls
+// on one Simbody integrator do. stepTo returns one SBG_INST_* word per
+// instance.
 class RungeKuttaMersonBatchIntegrator {
 public:
     explicit RungeKuttaMersonBatchIntegrator(StateBatch& batch) : b_(batch) {}
@@ -223,24 +226,29 @@ public:
     void setAccuracy(double a) { opts_.accuracy = a; }
     void setConstraintTolerance(double c) { opts_.constraint_tolerance = c; }
     void setProjectEveryStep(bool p) { opts_.project_every_step = p ? 1 : 0; }
-    // Integrator::initialize: records the common start time of the batch.
-    void initialize(double t0 = 0.0) { t_ = t0; }
+    // Integrator::initialize: the next stepTo starts the integration from
+    // the batch's current state, whose time is t0 (StateBatch::setY).
+    void initialize(double t0 = 0.0) {
+        t_ = t0;
+        started_ = false;
+    }
     double getTime() const { return t_; }
-    std::vector<int32_t> stepTo(double tFinal) {
+    std::vector<int32_t> stepTo(double tReport) {
         if (h_ <= 0) throw Error(SBG_ERR_STATE, "setFixedStepSize was not called");
-        const double n = (tFinal - t_) / h_;
-        const double nr = std::round(n);
-        if (nr < 0 || std::fabs(n - nr) > 1e-9 * std::max(1.0, nr))
-            throw Error(SBG_ERR_UNSUPPORTED, "stepTo: the interval is not a whole number of fixed steps");
+        if (!std::isfinite(tReport)) throw Error(SBG_ERR_INVALID, "stepTo: the report time must be finite");
         std::vector<int32_t> st(b_.getNumInstances());
-        check(sbg_rk_merson_fixed(b_.handle(), h_, (int32_t)nr, &opts_, st.data()));
-        t_ = t_ + nr * h_;
+        opts_.continue_integration = started_ ? 1 : 0;
+        check(sbg_rk_merson_step_to(b_.handle(), h_, tReport, &opts_, st.data()));
+        started_ = true;
+        t_ = std::max(t_, tReport);
         return st;
     }
+    std::vector<int32_t> stepBy(double dt) { return stepTo(t_ + dt); }
 
 private:
     StateBatch& b_;
     double h_ = 0, t_ = 0;
+    bool started_ = false;
     sbg_integ_opts opts_{0, 0, 0, 0};
 };
 
