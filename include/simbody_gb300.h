@@ -152,6 +152,18 @@ typedef struct sbg_integ_opts {
     int32_t continue_integration;
 } sbg_integ_opts;
 
+/* Options of the error-controlled integrator (sbg_rk_merson_adaptive); a
+ * value <= 0 takes Simbody's default. */
+typedef struct sbg_adaptive_opts {
+    double  accuracy;              /* Integrator::setAccuracy (1e-3) */
+    double  constraint_tolerance;  /* Integrator::setConstraintTolerance (accuracy/10) */
+    double  initial_step;          /* Integrator::setInitialStepSize (the timescale / 10 = 0.01) */
+    double  min_step;              /* Integrator::setMinimumStepSize (none) */
+    double  max_step;              /* Integrator::setMaximumStepSize (none) */
+    int32_t project_every_step;    /* Integrator::setProjectEveryStep */
+    int32_t max_steps;             /* accepted steps per instance before SBG_INST_TIMEOUT (1e6) */
+} sbg_adaptive_opts;
+
 typedef struct sbg_batch_config {
     int32_t precision;            /* sbg_precision */
     int32_t device;               /* CUDA device ordinal */
@@ -307,6 +319,16 @@ int sbg_rk_merson_step_to(sbg_batch batch, double h, double t_report,
  * instance order. Formed from the state and the udot of the last realize,
  * which must be of the current state (SBG_ERR_STATE otherwise). Synchronous. */
 int sbg_batch_get_qdotdot(sbg_batch batch, double* qdotdot);
+
+/* Error-controlled RungeKuttaMersonIntegrator: setFinalTime(t_final),
+ * initialize(state) (quaternions normalized) and stepTo(t_final) for every
+ * instance of an FP64 batch without loop closures, each with its own step
+ * size (AbstractIntegratorRep.cpp:341-577: takeOneStep, attemptDAEStep's
+ * projection, adjustStepSize :448-502). stats (may be NULL) gets the accepted
+ * and rejected steps of each instance (2 values per instance). Synchronous.
+ * SBG_ERR_UNSUPPORTED for mixed batches and loop closures. */
+int sbg_rk_merson_adaptive(sbg_batch batch, double t_final, const sbg_adaptive_opts* opts, int32_t* status,
+                           int64_t* stats);
 
 /* ------------------------------------------- device-resident (timing) path */
 

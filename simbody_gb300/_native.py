@@ -56,6 +56,12 @@ class IntegOpts(C.Structure):
                 ("project_every_step", C.c_int32), ("continue_integration", C.c_int32)]
 
 
+class AdaptiveOpts(C.Structure):
+    _fields_ = [("accuracy", C.c_double), ("constraint_tolerance", C.c_double), ("initial_step", C.c_double),
+                ("min_step", C.c_double), ("max_step", C.c_double), ("project_every_step", C.c_int32),
+                ("max_steps", C.c_int32)]
+
+
 class BatchConfig(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32), ("device_budget_bytes", C.c_int64)]
 
@@ -120,6 +126,7 @@ ENGINE_API = {
     "sbg_rk_merson_step_to_async": (C.c_int, [vp, C.c_double, C.c_double, P(IntegOpts)]),
     "sbg_batch_get_ydot": (C.c_int, [vp, dp, ip]),
     "sbg_batch_sync": (C.c_int, [vp]),
+    "sbg_rk_merson_adaptive": (C.c_int, [vp, C.c_double, P(AdaptiveOpts), ip, i64p]),
     "sbg_batch_get_qdotdot": (C.c_int, [vp, dp]),
     "sbg_batch_launch_count": (C.c_int64, [vp]),
     "sbg_batch_kernel_variant": (C.c_int, [vp]),

@@ -147,6 +147,7 @@ struct sbg_batch_s {
     unsigned long long fbWindow0 = 0; // FP64 steps counted at the start of the current window
     double* fbuf64 = nullptr;
     unsigned long long* fbSteps = nullptr;
+    long long* adaptStats = nullptr;  // accepted / rejected steps of the error-controlled integrator
     int64_t* rowsBase = nullptr;
     double* rows = nullptr;
     cudaStream_t fbStream = nullptr;
@@ -1399,6 +1400,76 @@ int sbg_batch_get_qdotdot(sbg_batch b, double* qdotdot) {
              "qdotdot download");
     SBG_CUDA(cudaStreamSynchronize(b->stream), "qdotdot");
     std::memcpy(qdotdot, b->hostPinned, nqT * sizeof(double));
+    return SBG_OK;
+}
+
+int sbg_rk_merson_adaptive(sbg_batch b, double t_final, const sbg_adaptive_opts* opts, int32_t* status,
+                           int64_t* stats) {
+    if (!b) return fail(SBG_ERR_INVALID, "null batch");
+    if (!b->stateSet) return fail(SBG_ERR_STATE, "no state has been set");
+    if (!std::isfinite(t_final)) return fail(SBG_ERR_INVALID, "final time must be finite");
+    if (b->precision != SBG_PRECISION_FP64)
+        return fail(SBG_ERR_UNSUPPORTED, "the error-controlled integrator runs on FP64 batches");
+    if (b->nLoop > 0) return fail(SBG_ERR_UNSUPPORTED, "error-controlled integration of loop closures is not supported");
+    AdaptCtl ac{};
+    ac.tFinal = t_final;
+    ac.accuracy = 1e-3;
+    ac.consTol = -1;
+    ac.maxSteps = 1000000;
+    if (opts) {
+        if (opts->accuracy > 0) ac.accuracy = opts->accuracy;
+        if (opts->constraint_tolerance > 0) ac.consTol = opts->constraint_tolerance;
+        ac.hInit = opts->initial_step;
+        ac.hMin = opts->min_step;
+        ac.hMax = opts->max_step;
+        ac.projectEveryStep = opts->project_every_step;
+        if (opts->max_steps > 0) ac.maxSteps = opts->max_steps;
+    }
+    if (ac.consTol <= 0) ac.consTol = ac.accuracy / 10;
+    if (ac.hMin > 0 && ac.hMax > 0 && ac.hMin > ac.hMax) return fail(SBG_ERR_INVALID, "minimum step above maximum step");
+    SBG_CUDA(cudaSetDevice(b->device), "cudaSetDevice");
+    if (b->ninst == 0) return SBG_OK;
+    if (stats && !b->adaptStats) {
+        void* p = nullptr;
+        if (int rc = b->alloc(&p, 2 * (size_t)b->ninst * sizeof(long long), "step statistics")) return rc;
+        b->adaptStats = static_cast<long long*>(p);
+    }
+    ac.stats = stats ? b->adaptStats : nullptr;
+    SBG_CUDA(cudaMemsetAsync(b->status, 0, b->ninst * sizeof(int32_t), b->stream), "status reset");
+    SBG_CUDA(launchNormalizeQuat(b->T, b->y, b->stream), "initialize");  // Integrator::initialize
+    KArgs a{};
+    const LaunchPlan P = b->plan();
+    a.T = &b->T;
+    a.P = &P;
+    a.ystate = b->y;
+    a.time = b->time;
+    a.fbuf = b->fbuf;
+    a.fplane = b->colElems;
+    a.scratch = b->scratch;
+    a.status = b->status;
+    const Streams ss = b->streams();
+    const bool both = P.nChain > 0 && P.nGroupBlocks > 0;
+    if (both) {
+        SBG_CUDA(cudaEventRecord(ss.fork, ss.main), "fork");
+        SBG_CUDA(cudaStreamWaitEvent(ss.side, ss.fork, 0), "fork");
+    }
+    rkAdaptiveChain(a, ac, ss.main);
+    rkAdaptiveGroup(a, ac, both ? ss.side : ss.main);
+    SBG_CUDA(cudaGetLastError(), "error-controlled RK-Merson launch");
+    if (both) {
+        SBG_CUDA(cudaEventRecord(ss.join, ss.side), "join");
+        SBG_CUDA(cudaStreamWaitEvent(ss.main, ss.join, 0), "join");
+    }
+    b->launches += 1 + b->segments();
+    b->integrating = false;  // the fixed-step integrator has nothing to continue
+    b->realized = false;
+    SBG_CUDA(cudaStreamSynchronize(b->stream), "error-controlled RK-Merson");
+    if (status) SBG_CUDA(cudaMemcpy(status, b->status, b->ninst * sizeof(int32_t), cudaMemcpyDeviceToHost), "status download");
+    if (stats) {
+        static_assert(sizeof(long long) == sizeof(int64_t), "statistics are 64-bit");
+        SBG_CUDA(cudaMemcpy(stats, b->adaptStats, 2 * (size_t)b->ninst * sizeof(int64_t), cudaMemcpyDeviceToHost),
+                 "statistics download");
+    }
     return SBG_OK;
 }
 

@@ -106,6 +106,17 @@ inline Launch1D spread(int64_t n, int bs) {
     return Launch1D{(int)((n + bs - 1) / bs), bs};
 }
 
+// Error-controlled RK-Merson (k_rkadapt.cu): Integrator::setFinalTime(tFinal),
+// initialize, stepTo(tFinal) with the given initial, minimum and maximum step
+// sizes (<= 0: the reference's defaults: initial 0.01, no limits) and at most
+// maxSteps accepted steps per instance. stats: accepted and rejected steps per
+// instance (2 values each; null = not wanted).
+struct AdaptCtl {
+    double tFinal, hInit, hMin, hMax, accuracy, consTol;
+    int projectEveryStep, maxSteps;
+    long long* stats;
+};
+
 // Per-segment launchers (k_r64.cu, k_r32c.cu, k_r32g.cu, k_rk64.cu,
 // k_rk32c.cu, k_rk32g.cu).
 struct KArgs {
@@ -146,6 +157,8 @@ void minvLoop(const KArgs& a, cudaStream_t s);
 void rkLoop(const KArgs& a, cudaStream_t s);
 void rkLoopWidth1(const KArgs& a, cudaStream_t s);  // k_rkloops1.cu: rkLoop for batch width 1
 void rkLoopGroup(const KArgs& a, cudaStream_t s);      // loop closures, level-parallel driver
+void rkAdaptiveChain(const KArgs& a, const AdaptCtl& ac, cudaStream_t s);  // k_rkadapt.cu (FP64)
+void rkAdaptiveGroup(const KArgs& a, const AdaptCtl& ac, cudaStream_t s);
 // One FP64 RK-Merson step for each instance in FP64 mode at this launch
 // (T.fbList[launch & 1]) on FP64 records at rowsBase: one thread (lanes 1) or
 // kFbLanes lanes of the level-parallel driver per instance (k_fallback.cu).

@@ -239,6 +239,20 @@ class Batch:
         N.check(N.engine_lib().sbg_rk_merson_step_to(self._h, float(h), float(t_report), C.byref(opts), _iptr(st)))
         return st
 
+    def rk_merson_adaptive(self, t_final: float, accuracy: float = 0.0, constraint_tolerance: float = 0.0,
+                           initial_step: float = 0.0, min_step: float = 0.0, max_step: float = 0.0,
+                           project_every_step: bool = False, max_steps: int = 0):
+        """Error-controlled RK-Merson to t_final (setFinalTime, initialize,
+        stepTo), FP64 batches. Returns (status, stats) with stats[i] =
+        (accepted, rejected) steps of instance i."""
+        opts = N.AdaptiveOpts(accuracy, constraint_tolerance, initial_step, min_step, max_step,
+                              int(project_every_step), int(max_steps))
+        st = np.empty(self.ninst, dtype=np.int32)
+        stats = np.zeros((self.ninst, 2), dtype=np.int64)
+        N.check(N.engine_lib().sbg_rk_merson_adaptive(self._h, float(t_final), C.byref(opts), _iptr(st),
+                                                      stats.ctypes.data_as(C.POINTER(C.c_int64))))
+        return st, stats
+
     # -- device-resident timing path
     @property
     def stream(self) -> int:

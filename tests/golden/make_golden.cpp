@@ -18,6 +18,9 @@
 //   mode 0  stepTo(t_mid); stepTo(t_end)     (a second call continues)
 //   mode 1  stepTo(t_end)
 //   mode 2  stepTo(t_end + 0.3 h)            (a shortened last step)
+// and, into a third file, error-controlled records: a RungeKuttaMersonIntegrator
+// with the given accuracy, setFinalTime(t_final), initialize(s) and stepTo
+// looped until t_final, with the numbers of steps taken and attempted.
 // Reference calls used (paths relative to the Simbody source tree):
 //   MobilizedBody::{Pin,Slider,Universal,Ball,Free} (Simbody/include/simbody/internal/MobilizedBody_*.h)
 //   Force::Gravity, Force::MobilityLinearSpring/Damper (Simbody/include/simbody/internal/Force*.h)
@@ -29,6 +32,9 @@
 //   double y0[ny], ydot[ny], f[nu], minv_f[nu], y_rk[ny], qdd[ny - nu]
 // and a second of continuation records
 //   int64 cfg, inst, ny, mode, status, nsteps_taken   double h, t_mid, t_end, t_out
+//   double y0[ny], y_out[ny]
+// and a third of error-controlled records
+//   int64 cfg, inst, ny, status, steps_taken, steps_attempted   double accuracy, t_final, t_out
 //   double y0[ny], y_out[ny]
 #include "Simbody.h"
 
@@ -103,8 +109,8 @@ void put(FILE* fp, const void* p, size_t bytes) {
 }  // namespace
 
 int main(int argc, char** argv) {
-    if (argc < 3) {
-        fprintf(stderr, "usage: make_golden OUT.bin CONT.bin\n");
+    if (argc < 4) {
+        fprintf(stderr, "usage: make_golden OUT.bin CONT.bin ADAPT.bin\n");
         return 2;
     }
     FILE* fp = fopen(argv[1], "wb");
@@ -263,6 +269,63 @@ int main(int argc, char** argv) {
         sbg_workload_destroy(w);
     }
     fclose(fc);
-    printf("%d records, %d continuation records\n", written, contWritten);
+
+    // error-controlled integration
+    FILE* fa = fopen(argv[3], "wb");
+    if (!fa) return 1;
+    struct AdaptSel { int cfg, ninst; double acc, tFinal; std::vector<int> pick; };
+    const AdaptSel adapt[] = {
+        {1, 8, 1e-3, 1.0, {0, 1}},
+        {1, 8, 1e-6, 0.5, {2}},
+        {2, 4, 1e-3, 0.05, {0, 1}},
+        {3, 6, 1e-3, 0.05, {0, 1, 2}},
+        {3, 6, 1e-5, 0.02, {3}},
+        {4, 8, 1e-3, 0.03, {2, 3}},
+    };
+    int adaptWritten = 0;
+    for (const AdaptSel& c : adapt) {
+        sbg_workload w;
+        if (sbg_workload_create(c.cfg, c.ninst, &w)) {
+            fprintf(stderr, "workload %d: %s\n", c.cfg, sbg_workload_last_error());
+            return 1;
+        }
+        const sbg_system_desc* systems = sbg_workload_systems(w);
+        const int32_t* isys = sbg_workload_instance_system(w);
+        const int64_t* yo = sbg_workload_y_offsets(w);
+        const double* y0 = sbg_workload_y0(w);
+        for (int i : c.pick) {
+            Model m(systems[isys[i]]);
+            const int64_t ny = yo[i + 1] - yo[i];
+            int64_t status = 0, taken = 0, attempted = 0;
+            std::vector<double> yout(ny, 0.0);
+            double tout = 0;
+            try {
+                State s2 = m.sys.getDefaultState();
+                for (int k = 0; k < ny; ++k) s2.updY()[k] = y0[yo[i] + k];
+                RungeKuttaMersonIntegrator integ(m.sys);
+                integ.setAccuracy(c.acc);
+                integ.setFinalTime(c.tFinal);
+                integ.initialize(s2);
+                while (integ.getTime() < c.tFinal) integ.stepTo(c.tFinal);
+                for (int k = 0; k < ny; ++k) yout[k] = integ.getState().getY()[k];
+                tout = integ.getTime();
+                taken = integ.getNumStepsTaken();
+                attempted = integ.getNumStepsAttempted();
+            } catch (const std::exception& e) {
+                fprintf(stderr, "cfg %d inst %d: error-controlled integrator failed: %s\n", c.cfg, i, e.what());
+                status = 1;
+            }
+            const int64_t hdr[6] = {c.cfg, i, ny, status, taken, attempted};
+            const double hd[3] = {c.acc, c.tFinal, tout};
+            put(fa, hdr, sizeof hdr);
+            put(fa, hd, sizeof hd);
+            put(fa, &y0[yo[i]], ny * 8);
+            put(fa, yout.data(), ny * 8);
+            ++adaptWritten;
+        }
+        sbg_workload_destroy(w);
+    }
+    fclose(fa);
+    printf("%d records, %d continuation records, %d error-controlled records\n", written, contWritten, adaptWritten);
     return 0;
 }

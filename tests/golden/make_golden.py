@@ -19,6 +19,12 @@ per instance and mode (0: stepTo(t_mid); stepTo(t_end), 1: stepTo(t_end),
   c_cfg, c_inst, c_ny, c_mode, c_status, c_steps, c_h, c_t_mid, c_t_end,
   c_t_out, c_y_off; c_y0, c_y_out (by c_y_off)
 
+and the error-controlled records (setAccuracy(acc), setFinalTime(t_final),
+stepTo(t_final); steps taken and attempted):
+
+  a_cfg, a_inst, a_ny, a_status, a_taken, a_attempted, a_accuracy, a_t_final,
+  a_t_out, a_y_off; a_y0, a_y_out (by a_y_off)
+
 The vectors are committed; the tests only read the .npz.
 """
 from __future__ import annotations
@@ -94,6 +100,30 @@ def read_continuation(path: Path) -> dict:
     return out
 
 
+def read_adaptive(path: Path) -> dict:
+    raw = path.read_bytes()
+    pos = 0
+    recs = []
+    while pos < len(raw):
+        cfg, inst, ny, status, taken, attempted = (int(v) for v in np.frombuffer(raw, dtype=np.int64, count=6,
+                                                                                  offset=pos))
+        pos += 48
+        acc, tf, tout = np.frombuffer(raw, dtype=np.float64, count=3, offset=pos)
+        pos += 24
+        y0 = np.frombuffer(raw, dtype=np.float64, count=ny, offset=pos).copy()
+        pos += 8 * ny
+        yout = np.frombuffer(raw, dtype=np.float64, count=ny, offset=pos).copy()
+        pos += 8 * ny
+        recs.append(dict(cfg=cfg, inst=inst, ny=ny, status=status, taken=taken, attempted=attempted, accuracy=acc,
+                         t_final=tf, t_out=tout, y0=y0, y_out=yout))
+    out = {"a_" + k: np.array([r[k] for r in recs])
+           for k in ("cfg", "inst", "ny", "status", "taken", "attempted", "accuracy", "t_final", "t_out")}
+    out["a_y_off"] = np.concatenate([[0], np.cumsum(out["a_ny"])]).astype(np.int64)
+    out["a_y0"] = np.concatenate([r["y0"] for r in recs])
+    out["a_y_out"] = np.concatenate([r["y_out"] for r in recs])
+    return out
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--simbody-src", required=True, type=Path)
@@ -114,9 +144,11 @@ def main() -> int:
         subprocess.run(cmd, check=True)
         binf = Path(td) / "records.bin"
         conf = Path(td) / "cont.bin"
-        subprocess.run([str(exe), str(binf), str(conf)], check=True, env={"OPENBLAS_NUM_THREADS": "1"})
+        adaf = Path(td) / "adapt.bin"
+        subprocess.run([str(exe), str(binf), str(conf), str(adaf)], check=True, env={"OPENBLAS_NUM_THREADS": "1"})
         data = read_records(binf)
         data.update(read_continuation(conf))
+        data.update(read_adaptive(adaf))
     np.savez_compressed(a.out, **data)
     print(f"wrote {a.out}: {len(data['cfg'])} records")
     return 0

@@ -60,6 +60,7 @@ def test_batch_entry_points_refuse_a_null_batch_without_touching_the_device():
         "sbg_batch_fp64_steps": (None, C.byref(i64)),
         "sbg_batch_get_qdotdot": (None, d),
         "sbg_rk_merson_step_to": (None, 1e-3, 1.0, None, i32),
+        "sbg_rk_merson_adaptive": (None, 1.0, None, i32, C.byref(i64)),
         "sbg_batch_last_operator_ms": (None, d),
     }
     for name, args in calls.items():

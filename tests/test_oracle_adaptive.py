@@ -105,3 +105,33 @@ def test_loop_closures_are_refused():
     with pytest.raises(RuntimeError, match="loop closures"):
         O.rk_merson_adaptive(w.systems, w.nsys, w.instance_system[[i]], np.array([0, sl.stop - sl.start]),
                              w.y0[sl], 0.1)
+
+
+def _adaptive_records(g):
+    for r in range(len(g["a_cfg"])):
+        ys = slice(int(g["a_y_off"][r]), int(g["a_y_off"][r + 1]))
+        yield r, int(g["a_cfg"][r]), int(g["a_inst"][r]), ys
+
+
+def test_error_controlled_matches_reference_records():
+    """The reference's error-controlled RungeKuttaMersonIntegrator
+    (setAccuracy, setFinalTime, stepTo; default initial step, no step limits)
+    recorded on the seeded workloads, double pendulum to the trees: the oracle
+    takes the same numbers of accepted and rejected steps, ends on the final
+    time and reproduces the final state to 1e-11."""
+    g = dict(np.load(GOLD))
+    sizes = {1: 8, 2: 4, 3: 6, 4: 8}
+    ws = {c: Workload(c, n) for c, n in sizes.items()}
+    for r, cfg, inst, ys in _adaptive_records(g):
+        assert g["a_status"][r] == 0
+        w = ws[cfg]
+        y0 = g["a_y0"][ys]
+        assert np.array_equal(w.y0[w.instance_slice(inst)], y0)
+        y, t, st, stats = O.rk_merson_adaptive(w.systems, w.nsys, w.instance_system[[inst]], np.array([0, len(y0)]),
+                                               y0, float(g["a_t_final"][r]), accuracy=float(g["a_accuracy"][r]))
+        assert st[0] == 0
+        assert t[0] == g["a_t_out"][r]
+        assert stats[0, 0] == g["a_taken"][r], (cfg, inst, stats[0], g["a_taken"][r], g["a_attempted"][r])
+        assert stats[0, 0] + stats[0, 1] == g["a_attempted"][r], (cfg, inst, stats[0], g["a_attempted"][r])
+        rel = np.linalg.norm(y - g["a_y_out"][ys]) / np.linalg.norm(g["a_y_out"][ys])
+        assert rel <= 1e-11, (cfg, inst, rel)
