@@ -45,18 +45,39 @@ typedef enum sbg_status {
 } sbg_status;
 
 /* Mobilizer kinds. Coordinates follow Simbody's defaults:
- *   PIN       nq=1 nu=1  rotation about Fz            (RigidBodyNodeSpec_Pin.h:103-131)
- *   SLIDER    nq=1 nu=1  translation along Fx         (RigidBodyNodeSpec_Slider.h:100-119)
- *   UNIVERSAL nq=2 nu=2  body-fixed X then Y          (RigidBodyNodeSpec_Universal.h:124-189)
- *   BALL      nq=4 nu=3  quaternion, w_FM in F        (RigidBodyNodeSpec_Ball.h:113-214)
- *   FREE      nq=7 nu=6  [quat, p_FM], [w_FM, v_FM]   (RigidBodyNodeSpec_Free.h:142-219) */
+ *   PIN         nq=1 nu=1  rotation about Fz            (RigidBodyNodeSpec_Pin.h:103-131)
+ *   SLIDER      nq=1 nu=1  translation along Fx         (RigidBodyNodeSpec_Slider.h:100-119)
+ *   UNIVERSAL   nq=2 nu=2  body-fixed X then Y          (RigidBodyNodeSpec_Universal.h:124-189)
+ *   BALL        nq=4 nu=3  quaternion, w_FM in F        (RigidBodyNodeSpec_Ball.h:113-214)
+ *   FREE        nq=7 nu=6  [quat, p_FM], [w_FM, v_FM]   (RigidBodyNodeSpec_Free.h:142-219)
+ *   GIMBAL      nq=3 nu=3  body-fixed X-Y-Z angles, u = qdot (RigidBodyNodeSpec_Gimbal.h)
+ *   TRANSLATION nq=3 nu=3  p_FM = q, u = qdot           (RigidBodyNodeSpec_Translation.h)
+ *   CYLINDER    nq=2 nu=2  rotation about and translation along Fz, u = qdot
+ *                                                        (RigidBodyNodeSpec_Cylinder.h)
+ *   PLANAR      nq=3 nu=3  rotation about Fz, translation along Fx, Fy, u = qdot
+ *                                                        (RigidBodyNodeSpec_Planar.h)
+ *   BUSHING     nq=6 nu=6  body-fixed X-Y-Z angles then p_FM, u = qdot
+ *                                                        (RigidBodyNodeSpec_Bushing.h)
+ * With SBG_SYSTEM_EULER_ANGLES a system's BALL and FREE bodies use
+ * body-fixed X-Y-Z angles instead of quaternions (nq = 3 and 6; u is still
+ * w_FM (, v_FM) in F): SimbodyMatterSubsystem::setUseEulerAngles
+ * (RigidBodyNodeSpec_Ball.h:118-127, 198-209). */
 typedef enum sbg_mobilizer {
     SBG_PIN = 0,
     SBG_SLIDER = 1,
     SBG_UNIVERSAL = 2,
     SBG_BALL = 3,
-    SBG_FREE = 4
+    SBG_FREE = 4,
+    SBG_GIMBAL = 5,
+    SBG_TRANSLATION = 6,
+    SBG_CYLINDER = 7,
+    SBG_PLANAR = 8,
+    SBG_BUSHING = 9
 } sbg_mobilizer;
+#define SBG_NUM_MOBILIZERS 10
+
+/* sbg_system_desc.flags */
+#define SBG_SYSTEM_EULER_ANGLES 1  /* SimbodyMatterSubsystem::setUseEulerAngles(true) */
 
 typedef enum sbg_precision {
     SBG_PRECISION_FP64 = 0,   /* every recursion in FP64 */
@@ -129,7 +150,7 @@ typedef struct sbg_system_desc {
     int32_t nbodies;
     int32_t nforces;
     int32_t nconstraints;
-    int32_t reserved;
+    int32_t flags;                /* SBG_SYSTEM_* bits */
     double  gravity[3];
     const sbg_body_desc*            bodies;       /* nbodies entries, body 1 first */
     const sbg_mobility_force_desc*  forces;       /* nforces entries */

@@ -26,14 +26,19 @@ bool buildTopology(const sbg_system_desc& d, Topology& t, const char** err) {
         const sbg_body_desc& bd = d.bodies[i - 1];
         Body& b = t.b[i];
         if (bd.parent < 0 || bd.parent >= i) return fail("body parent must precede the body");
-        if (bd.mobilizer < 0 || bd.mobilizer > 4) return fail("unknown mobilizer");
+        if (bd.mobilizer < 0 || bd.mobilizer >= SBG_NUM_MOBILIZERS) return fail("unknown mobilizer");
         b.parent = bd.parent;
         b.type = bd.mobilizer;
+        const bool ballOrFree = b.type == SBG_BALL || b.type == SBG_FREE;
+        b.euler = ballOrFree && (d.flags & SBG_SYSTEM_EULER_ANGLES);
+        b.quat = ballOrFree && !b.euler;
+        // Euler-angle mode keeps Simbody's q slots (4 and 7) and leaves the
+        // last one unused (RigidBodyNodeSpec_Ball.h:393-395, _Free.h getMaxNQ)
         b.nq = mobNQ(b.type);
         b.nu = mobNU(b.type);
         b.qoff = qn; b.uoff = un;
         qn += b.nq; un += b.nu;
-        if (b.type == SBG_BALL || b.type == SBG_FREE) t.nquat++;
+        if (b.quat) t.nquat++;
         b.level = t.b[b.parent].level + 1;
         t.b[b.parent].children.push_back(i);
         b.mass = bd.mass;
@@ -48,6 +53,8 @@ bool buildTopology(const sbg_system_desc& d, Topology& t, const char** err) {
             b.pMB[r] = -(b.RMB[3 * r + 0] * bd.X_BM[9] + b.RMB[3 * r + 1] * bd.X_BM[10] + b.RMB[3 * r + 2] * bd.X_BM[11]);
     }
     t.nq = qn; t.nu = un;
+    if (d.nconstraints > 0 && (d.flags & SBG_SYSTEM_EULER_ANGLES))
+        return fail("loop closures with Euler-angle Ball or Free bodies are not supported");
     int maxLevel = 0;
     for (int i = 1; i <= t.nb; ++i) maxLevel = std::max(maxLevel, t.b[i].level);
     t.levels.assign(maxLevel, {});
@@ -241,7 +248,7 @@ static double errorNorm(const Topology& t, const double* y1, const double* yerr,
         const double* q = y1 + b.qoff;
         const double* dq = yerr + b.qoff;
         double* o = dqw.data() + b.qoff;
-        if (b.type == SBG_BALL || b.type == SBG_FREE) {
+        if (b.quat) {
             const double e0 = 2 * q[0], e1 = 2 * q[1], e2 = 2 * q[2], e3 = 2 * q[3];
             const double ne1 = -e1, ne2 = -e2, ne3 = -e3;
             const double du0 = ne1 * dq[0] + e0 * dq[1] + ne3 * dq[2] + e2 * dq[3];
@@ -269,7 +276,7 @@ static double errorNorm(const Topology& t, const double* y1, const double* yerr,
 static void normalizeQuaternions(const Topology& t, double* q) {
     for (int bi = 1; bi <= t.nb; ++bi) {
         const Body& b = t.b[bi];
-        if (b.type != SBG_BALL && b.type != SBG_FREE) continue;
+        if (!b.quat) continue;
         double* qq = q + b.qoff;
         const double n = std::sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);
         for (int k = 0; k < 4; ++k) qq[k] = qq[k] / n;
@@ -302,7 +309,7 @@ static void projectionWeightsQ(const Topology& t, const double* q, std::vector<d
     D.assign(t.nu, 1.0);
     for (int bi = 1; bi <= t.nb; ++bi) {
         const Body& b = t.b[bi];
-        if (b.type != SBG_BALL && b.type != SBG_FREE) continue;
+        if (!b.quat) continue;
         const double* qq = q + b.qoff;
         const double n2 = qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3];
         for (int k = 0; k < 3; ++k) D[b.uoff + k] = 4 * n2;
@@ -339,7 +346,7 @@ static void multiplyByN(const Topology& t, const double* q, const double* du, do
         const double* qb = q + b.qoff;
         const double* ub = du + b.uoff;
         double* d = dq + b.qoff;
-        if (b.type == SBG_BALL || b.type == SBG_FREE) {
+        if (b.quat) {
             const double e0 = qb[0] / 2, e1 = qb[1] / 2, e2 = qb[2] / 2, e3 = qb[3] / 2;
             d[0] = -e1 * ub[0] - e2 * ub[1] - e3 * ub[2];
             d[1] = e0 * ub[0] + e3 * ub[1] - e2 * ub[2];
@@ -548,7 +555,7 @@ int rkMersonRun(const Topology& t, double* y, double* time, double h, int nsteps
             int nqt = 0;
             for (int bi = 1; bi <= t.nb; ++bi) {
                 const Body& b = t.b[bi];
-                if (b.type != SBG_BALL && b.type != SBG_FREE) continue;
+                if (!b.quat) continue;
                 const double* qq = y + b.qoff;
                 const double e = std::sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]) - 1;
                 s += e * e;
@@ -679,7 +686,7 @@ int rkMersonAdaptive(const Topology& t, double* y, double* time, double tFinal, 
                 int nqt = 0;
                 for (int bi = 1; bi <= t.nb; ++bi) {
                     const Body& b = t.b[bi];
-                    if (b.type != SBG_BALL && b.type != SBG_FREE) continue;
+                    if (!b.quat) continue;
                     const double* qq = y + b.qoff;
                     const double e = std::sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]) - 1;
                     sq += e * e;
@@ -691,7 +698,7 @@ int rkMersonAdaptive(const Topology& t, double* y, double* time, double tFinal, 
                 } else if (quatNorm > o.consTol || o.projectEveryStep) {
                     for (int bi = 1; bi <= t.nb; ++bi) {
                         const Body& b = t.b[bi];
-                        if (b.type != SBG_BALL && b.type != SBG_FREE) continue;
+                        if (!b.quat) continue;
                         double* qq = y + b.qoff;
                         double* qe = yerr.data() + b.qoff;
                         const double n = std::sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);

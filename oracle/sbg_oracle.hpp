@@ -181,6 +181,8 @@ template <class R> inline void abiAdd(ABI<R>& a, const ABI<R>& b) { a.M = a.M + 
 // ---------------------------------------------------------------- topology
 struct Body {
     int parent = 0, type = 0, nq = 0, nu = 0, qoff = 0, uoff = 0, level = 0;
+    bool quat = false;   // Ball/Free with quaternion coordinates
+    bool euler = false;  // Ball/Free with body-fixed X-Y-Z angles (SimbodyMatterSubsystem::setUseEulerAngles)
     std::vector<int> children;
     double mass = 0, com[3] = {0, 0, 0}, G[6] = {0, 0, 0, 0, 0, 0};  // unit inertia xx yy zz xy xz yz
     double RPF[9], pPF[3], RMB[9], pMB[3];                               // X_PF and X_MB = ~X_BM
@@ -196,8 +198,9 @@ struct Topology {
     std::vector<sbg_ball_constraint_desc> constraints;
 };
 
-inline int mobNQ(int t) { static const int n[5] = {1, 1, 2, 4, 7}; return n[t]; }
-inline int mobNU(int t) { static const int n[5] = {1, 1, 2, 3, 6}; return n[t]; }
+// q and u counts per mobilizer (quaternion mode for Ball and Free)
+inline int mobNQ(int t) { static const int n[10] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6}; return n[t]; }
+inline int mobNU(int t) { static const int n[10] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6}; return n[t]; }
 
 // Node creation and slot assignment (SimbodyMatterSubsystemRep.cpp:256-330,
 // RigidBodyNodeSpec.h:76-86): q/u slots consecutive in body order.
@@ -215,6 +218,7 @@ template <class R> struct BodyCache {
     V3<R> pc;              // Mk mass center offset p_BBc_G
     S33<R> Gi;             // unit inertia about Bo, in G
     R ooNorm;
+    R ca[3], sa[3], ooc1;  // body-fixed X-Y-Z angles: cos, sin, 1/cos(q1)
     // velocity
     V3<R> Vw, Vv, VFw, VFv;
     V3<R> HDw[6], HDv[6];

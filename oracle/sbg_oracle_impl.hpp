@@ -73,6 +73,32 @@ template <class R> inline bool invertD(int n, const R* D, R* DI) {
     return true;
 }
 
+// Body-fixed X-Y-Z angles q[0..2]: cos, sin and 1/cos(q1) into the cache
+// (performQPrecalculations, RigidBodyNodeSpec_Gimbal.h) and R_FM
+// (Rotation::setRotationToBodyFixedXYZ(c, s), Rotation.h:342-349).
+template <class R> inline void bodyFixedXYZ(BodyCache<R>& c, const R* q) {
+    const R cy = cos(q[1]);
+    c.ca[0] = cos(q[0]); c.ca[1] = cy; c.ca[2] = cos(q[2]);
+    c.sa[0] = sin(q[0]); c.sa[1] = sin(q[1]); c.sa[2] = sin(q[2]);
+    c.ooc1 = R(1) / cy;
+    const R* cc = c.ca;
+    const R* ss = c.sa;
+    const R s0s1 = ss[0] * ss[1], s2c0 = ss[2] * cc[0], c0c2 = cc[0] * cc[2], nc1 = -cc[1];
+    c.R_FM(0, 0) = cc[1] * cc[2];           c.R_FM(0, 1) = ss[2] * nc1;           c.R_FM(0, 2) = ss[1];
+    c.R_FM(1, 0) = s2c0 + s0s1 * cc[2];     c.R_FM(1, 1) = c0c2 - s0s1 * ss[2];   c.R_FM(1, 2) = ss[0] * nc1;
+    c.R_FM(2, 0) = ss[0] * ss[2] - ss[1] * c0c2; c.R_FM(2, 1) = ss[0] * cc[2] + ss[1] * s2c0; c.R_FM(2, 2) = cc[0] * cc[1];
+}
+
+// Rotation::multiplyByBodyXYZ_N_P (Rotation.h:395-406): qdot of body-fixed
+// X-Y-Z angles from the angular velocity w in the parent frame.
+template <class R> inline void bodyXYZ_N_P(const R* cc, const R* ss, R ooc1, const R* w, R* qd) {
+    const R s0 = ss[0], c0 = cc[0], s1 = ss[1];
+    const R t = (s0 * w[1] - c0 * w[2]) * ooc1;
+    qd[0] = w[0] + t * s1;
+    qd[1] = c0 * w[1] + s0 * w[2];
+    qd[2] = -t;
+}
+
 // ------------------------------------------------------- position stage
 // RigidBodyNodeSpec::realizePosition (RigidBodyNodeSpec.h:229-288) driven
 // base-to-tip by realizePositionKinematics (SimbodyMatterSubsystemRep.cpp:1112-1144).
@@ -114,7 +140,17 @@ template <class R> void realizePosition(const Topology& t, const R* q, Work<R>& 
                 break;
             }
             case SBG_BALL:
-            case SBG_FREE: {  // RigidBodyNodeSpec_Ball.h:134-180, _Free.h:142-188
+            case SBG_FREE:
+                if (b.euler) {  // RigidBodyNodeSpec_Ball.h:118-127, _Free.h Euler branch
+                    bodyFixedXYZ(c, qb);
+                    for (int j = 0; j < 3; ++j) { V3<R> e = zero3<R>(); e[j] = R(1); c.HFw[j] = e; }
+                    if (b.type == SBG_FREE) {
+                        c.p_FM = v3<R>(qb[3], qb[4], qb[5]);
+                        for (int j = 0; j < 3; ++j) { V3<R> e = zero3<R>(); e[j] = R(1); c.HFv[3 + j] = e; }
+                    }
+                    break;
+                }
+                {  // RigidBodyNodeSpec_Ball.h:134-180, _Free.h:142-188
                 const R len = sqrt(qb[0] * qb[0] + qb[1] * qb[1] + qb[2] * qb[2] + qb[3] * qb[3]);
                 w.qerr[quat++] = len - R(1);
                 c.ooNorm = R(1) / len;
@@ -130,6 +166,38 @@ template <class R> void realizePosition(const Topology& t, const R* q, Work<R>& 
                 if (b.type == SBG_FREE) {
                     c.p_FM = v3<R>(qb[4], qb[5], qb[6]);
                     for (int j = 0; j < 3; ++j) { V3<R> e = zero3<R>(); e[j] = R(1); c.HFv[3 + j] = e; }
+                }
+                break;
+                }
+            case SBG_GIMBAL:
+            case SBG_BUSHING:  // RigidBodyNodeSpec_Gimbal.h, _Bushing.h: calcX_FM, H_FM columns
+                bodyFixedXYZ(c, qb);
+                c.HFw[0] = v3<R>(R(1), R(0), R(0));
+                c.HFw[1] = v3<R>(R(0), c.ca[0], c.sa[0]);
+                c.HFw[2] = v3<R>(c.sa[1], -c.sa[0] * c.ca[1], c.ca[0] * c.ca[1]);
+                if (b.type == SBG_BUSHING) {
+                    c.p_FM = v3<R>(qb[3], qb[4], qb[5]);
+                    for (int j = 0; j < 3; ++j) { V3<R> e = zero3<R>(); e[j] = R(1); c.HFv[3 + j] = e; }
+                }
+                break;
+            case SBG_TRANSLATION:  // RigidBodyNodeSpec_Translation.h
+                c.R_FM = ident33<R>();
+                c.p_FM = v3<R>(qb[0], qb[1], qb[2]);
+                for (int j = 0; j < 3; ++j) { V3<R> e = zero3<R>(); e[j] = R(1); c.HFv[j] = e; }
+                break;
+            case SBG_CYLINDER:  // RigidBodyNodeSpec_Cylinder.h
+            case SBG_PLANAR: {  // RigidBodyNodeSpec_Planar.h
+                const R cq = cos(qb[0]), sq = sin(qb[0]);
+                c.R_FM = ident33<R>();
+                c.R_FM(0, 0) = cq; c.R_FM(1, 1) = cq; c.R_FM(1, 0) = sq; c.R_FM(0, 1) = -sq;
+                c.HFw[0] = v3<R>(R(0), R(0), R(1));
+                if (b.type == SBG_CYLINDER) {
+                    c.p_FM = v3<R>(R(0), R(0), qb[1]);
+                    c.HFv[1] = v3<R>(R(0), R(0), R(1));
+                } else {
+                    c.p_FM = v3<R>(qb[1], qb[2], R(0));
+                    c.HFv[1] = v3<R>(R(1), R(0), R(0));
+                    c.HFv[2] = v3<R>(R(0), R(1), R(0));
                 }
                 break;
             }
@@ -172,7 +240,11 @@ template <class R> void realizeVelocity(const Topology& t, const R* q, const R* 
             const R* ub = u + b.uoff;
             if (qdot) {
                 R* qd = qdot + b.qoff;
-                if (b.type == SBG_BALL || b.type == SBG_FREE) {
+                if (b.euler) {  // RigidBodyNodeSpec_Ball.h:198-209: convertAngVelInParentToBodyXYZDot
+                    bodyXYZ_N_P(c.ca, c.sa, c.ooc1, ub, qd);
+                    if (b.type == SBG_FREE) { qd[3] = ub[3]; qd[4] = ub[4]; qd[5] = ub[5]; qd[6] = R(0); }
+                    else qd[3] = R(0);  // the unused slot
+                } else if (b.quat) {
                     // calcUnnormalizedNForQuaternion: e = q/2 (Rotation.h:712-719)
                     const R e0 = qb[0] / R(2), e1 = qb[1] / R(2), e2 = qb[2] / R(2), e3 = qb[3] / R(2);
                     const R ne1 = -e1, ne2 = -e2, ne3 = -e3;
@@ -196,6 +268,14 @@ template <class R> void realizeVelocity(const Topology& t, const R* q, const R* 
             V3<R> HDFw[6], HDFv[6];
             for (int j = 0; j < 6; ++j) { HDFw[j] = zero3<R>(); HDFv[j] = zero3<R>(); }
             if (b.type == SBG_UNIVERSAL) HDFw[1] = cross(c.VFw, col(c.R_FM, 1));
+            if (b.type == SBG_GIMBAL || b.type == SBG_BUSHING) {  // RigidBodyNodeSpec_Gimbal.h HDot_FM, qdot = u
+                const R c0 = c.ca[0], c1 = c.ca[1], s0 = c.sa[0], s1 = c.sa[1];
+                const R qd0 = ub[0], qd1 = ub[1];
+                const R dc0 = -s0 * qd0, dc1 = -s1 * qd1;
+                const R ds0 = c0 * qd0, ds1 = c1 * qd1;
+                HDFw[1] = v3<R>(R(0), dc0, ds0);
+                HDFw[2] = v3<R>(ds1, -ds0 * c1 - s0 * dc1, dc0 * c1 + c0 * dc1);
+            }
             // calcParentToChildVelocityJacobianInGroundDot (RigidBodyNodeSpec.cpp:82-129)
             const M33<R> RPF = loadR<R>(b.RPF);
             const M33<R> R_GF = pc.R_GB * RPF;
@@ -534,7 +614,28 @@ template <class R> void calcQDotDot(const Topology& t, const R* y, const R* udot
         const R* ub = u + b.uoff;
         const R* bd = udot + b.uoff;
         R* o = qdotdot + b.qoff;
-        if (b.type != SBG_BALL && b.type != SBG_FREE) {
+        if (b.euler) {
+            // Rotation::convertAngAccInParentToBodyXYZDotDot (Rotation.h:1041-1060)
+            // with qdot = N_P(q) w (RigidBodyNodeSpec_Ball.h:355-390 Euler branch)
+            const R cy = cos(qq[1]);
+            const R cc[2] = {cos(qq[0]), cy}, ss[2] = {sin(qq[0]), sin(qq[1])};
+            const R ooc1 = R(1) / cy;
+            R qd[3], Nb[3];
+            bodyXYZ_N_P(cc, ss, ooc1, ub, qd);
+            bodyXYZ_N_P(cc, ss, ooc1, bd, Nb);
+            const R q1oc1 = qd[1] * ooc1;
+            o[0] = Nb[0] + (qd[0] * ss[1] - qd[2]) * q1oc1;
+            o[1] = Nb[1] + qd[0] * qd[2] * cc[1];
+            o[2] = Nb[2] + (qd[2] * ss[1] - qd[0]) * q1oc1;
+            if (b.type == SBG_FREE) {
+                for (int k = 0; k < 3; ++k) o[3 + k] = bd[3 + k];
+                o[6] = R(0);
+            } else {
+                o[3] = R(0);  // the unused slot
+            }
+            continue;
+        }
+        if (!b.quat) {  // u = qdot
             for (int k = 0; k < b.nu; ++k) o[k] = bd[k];
             continue;
         }

@@ -11,9 +11,13 @@ PKG = Path(__file__).resolve().parent
 BUILD = PKG / "_build"
 
 # ----------------------------------------------------------------- structs
-SBG_PIN, SBG_SLIDER, SBG_UNIVERSAL, SBG_BALL, SBG_FREE = range(5)
-NQ = {SBG_PIN: 1, SBG_SLIDER: 1, SBG_UNIVERSAL: 2, SBG_BALL: 4, SBG_FREE: 7}
-NU = {SBG_PIN: 1, SBG_SLIDER: 1, SBG_UNIVERSAL: 2, SBG_BALL: 3, SBG_FREE: 6}
+(SBG_PIN, SBG_SLIDER, SBG_UNIVERSAL, SBG_BALL, SBG_FREE, SBG_GIMBAL, SBG_TRANSLATION, SBG_CYLINDER, SBG_PLANAR,
+ SBG_BUSHING) = range(10)
+NQ = {SBG_PIN: 1, SBG_SLIDER: 1, SBG_UNIVERSAL: 2, SBG_BALL: 4, SBG_FREE: 7, SBG_GIMBAL: 3, SBG_TRANSLATION: 3,
+      SBG_CYLINDER: 2, SBG_PLANAR: 3, SBG_BUSHING: 6}
+NU = {SBG_PIN: 1, SBG_SLIDER: 1, SBG_UNIVERSAL: 2, SBG_BALL: 3, SBG_FREE: 6, SBG_GIMBAL: 3, SBG_TRANSLATION: 3,
+      SBG_CYLINDER: 2, SBG_PLANAR: 3, SBG_BUSHING: 6}
+SYSTEM_EULER_ANGLES = 1
 PRECISION_FP64, PRECISION_MIXED, PRECISION_MIXED_FAST = 0, 1, 2
 
 INST_OK = 0
@@ -46,7 +50,7 @@ class BallConstraintDesc(C.Structure):
 
 class SystemDesc(C.Structure):
     _fields_ = [("nbodies", C.c_int32), ("nforces", C.c_int32), ("nconstraints", C.c_int32),
-                ("reserved", C.c_int32), ("gravity", C.c_double * 3),
+                ("flags", C.c_int32), ("gravity", C.c_double * 3),
                 ("bodies", C.POINTER(BodyDesc)), ("forces", C.POINTER(MobilityForceDesc)),
                 ("constraints", C.POINTER(BallConstraintDesc))]
 

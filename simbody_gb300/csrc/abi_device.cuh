@@ -44,7 +44,8 @@
 
 namespace sbg {
 
-enum { T_PIN = 0, T_SLIDER = 1, T_UNIV = 2, T_BALL = 3, T_FREE = 4 };
+enum { T_PIN = 0, T_SLIDER = 1, T_UNIV = 2, T_BALL = 3, T_FREE = 4, T_GIMBAL = 5, T_TRANSL = 6, T_CYL = 7,
+       T_PLANAR = 8, T_BUSHING = 9 };
 
 // Scratch accessors: S(rec, f) is element f of the record at rec.
 template <class R> struct ScrTiled {
@@ -154,6 +155,22 @@ template <class SC> __device__ __forceinline__ void stDF3(const SC& S, int rec, 
     S(rec, f + 4) = v.z.hi; S(rec, f + 5) = v.z.lo;
 }
 
+// Body-fixed X-Y-Z angles q[0..2]: cos and sin of each and R_FM
+// (Rotation::setRotationToBodyFixedXYZ(c, s), Rotation.h:342-349).
+template <class R> struct XYZ {
+    R c0, c1, s0, s1, ooc1;
+};
+template <class R> __device__ __forceinline__ XYZ<R> bodyXYZ(const R* q, M3<R>& Rm) {
+    R c[3], sn[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) sincosR(q[k], &sn[k], &c[k]);
+    const R s0s1 = sn[0] * sn[1], s2c0 = sn[2] * c[0], c0c2 = c[0] * c[2], nc1 = -c[1];
+    Rm.a[0] = c[1] * c[2];              Rm.a[1] = sn[2] * nc1;               Rm.a[2] = sn[1];
+    Rm.a[3] = s2c0 + s0s1 * c[2];       Rm.a[4] = c0c2 - s0s1 * sn[2];       Rm.a[5] = sn[0] * nc1;
+    Rm.a[6] = sn[0] * sn[2] - sn[1] * c0c2; Rm.a[7] = sn[0] * c[2] + sn[1] * s2c0; Rm.a[8] = c[0] * c[1];
+    return XYZ<R>{c[0], c[1], sn[0], sn[1], R(1) / c[1]};
+}
+
 // ------------------------------------------------------------------ kinematics
 template <class R> struct Kin {
     M3<R> R_;
@@ -203,7 +220,28 @@ __device__ __forceinline__ Kin<R> body1(const DevTables& T, int row, int rec, co
     M3<R> RFM = ident3<R>();
     V3<R> pFM = z3<R>();
     V3<R> y1 = z3<R>();  // Universal: second H_FM column
+    XYZ<R> ea{R(1), R(1), R(0), R(0), R(1)};  // body-fixed X-Y-Z angles
+    const bool quat = (info & F_QUAT) != 0;
     switch (type) {
+    case T_GIMBAL:   // RigidBodyNodeSpec_Gimbal.h: calcX_FM, u = qdot
+    case T_BUSHING:  // RigidBodyNodeSpec_Bushing.h: angles then p_FM, u = qdot
+        ea = bodyXYZ<R>(q, RFM);
+        for (int j = 0; j < n; ++j) out.qdot(qo + j, u[j]);
+        if (type == T_BUSHING) pFM = mk3(q[3], q[4], q[5]);
+        break;
+    case T_TRANSL:  // RigidBodyNodeSpec_Translation.h
+        pFM = mk3(q[0], q[1], q[2]);
+        for (int j = 0; j < 3; ++j) out.qdot(qo + j, u[j]);
+        break;
+    case T_CYL:       // RigidBodyNodeSpec_Cylinder.h: about and along Fz
+    case T_PLANAR: {  // RigidBodyNodeSpec_Planar.h: about Fz, along Fx and Fy
+        R s, c;
+        sincosR(q[0], &s, &c);
+        RFM.a[0] = c; RFM.a[1] = -s; RFM.a[3] = s; RFM.a[4] = c;
+        pFM = type == T_CYL ? mk3(R(0), R(0), q[1]) : mk3(q[1], q[2], R(0));
+        for (int j = 0; j < n; ++j) out.qdot(qo + j, u[j]);
+        break;
+    }
     case T_PIN: {  // RigidBodyNodeSpec_Pin.h:103-122
         R s, c;
         sincosR(q[0], &s, &c);
@@ -227,7 +265,25 @@ __device__ __forceinline__ Kin<R> body1(const DevTables& T, int row, int rec, co
         out.qdot(qo + 1, u[1]);
         break;
     }
-    default: {  // Ball / Free quaternion (RigidBodyNodeSpec_Ball.h:134-214)
+    default: {  // Ball / Free
+        if (!quat) {
+            // body-fixed X-Y-Z angles (RigidBodyNodeSpec_Ball.h:118-127, 198-209):
+            // qdot = N_P(q) w_FM (Rotation.h:395-406); the last q slot is unused
+            ea = bodyXYZ<R>(q, RFM);
+            const R t = (ea.s0 * u[1] - ea.c0 * u[2]) * ea.ooc1;
+            out.qdot(qo + 0, u[0] + t * ea.s1);
+            out.qdot(qo + 1, ea.c0 * u[1] + ea.s0 * u[2]);
+            out.qdot(qo + 2, -t);
+            if (type == T_FREE) {
+                pFM = mk3(q[3], q[4], q[5]);
+                for (int j = 0; j < 3; ++j) out.qdot(qo + 3 + j, u[3 + j]);
+                out.qdot(qo + 6, R(0));
+            } else {
+                out.qdot(qo + 3, R(0));
+            }
+            break;
+        }
+        // quaternion (RigidBodyNodeSpec_Ball.h:134-214)
         const R len = sqrtR(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
         const R oo = R(1) / len;
         const R e0 = q[0] * oo, e1 = q[1] * oo, e2 = q[2] * oo, e3 = q[3] * oo;
@@ -281,11 +337,35 @@ __device__ __forceinline__ Kin<R> body1(const DevTables& T, int row, int rec, co
     };
     // -(r x e_j) for the unit axes
     const V3<R> nrx = mk3(R(0), -r.z, r.y), nry = mk3(r.z, R(0), -r.x), nrz = mk3(-r.y, r.x, R(0));
+    V3<R> hdw = z3<R>();  // sum_j u_j HDot_FM_w_j
     switch (type) {
     case T_PIN:
+    case T_CYL:
+    case T_PLANAR:
         putH(0, col(RGF, 2), mul(RGF, nrz));
         wFM = mk3(R(0), R(0), u[0]);
+        if (type == T_CYL) putH(1, z3<R>(), col(RGF, 2));
+        if (type == T_PLANAR) { putH(1, z3<R>(), col(RGF, 0)); putH(2, z3<R>(), col(RGF, 1)); }
         break;
+    case T_TRANSL:
+        for (int j = 0; j < 3; ++j) putH(j, z3<R>(), col(RGF, j));
+        break;
+    case T_GIMBAL:
+    case T_BUSHING: {
+        // H_FM_w columns (1,0,0), (0,c0,s0), (s1,-s0 c1,c0 c1) and their time
+        // derivatives with qdot = u (RigidBodyNodeSpec_Gimbal.h)
+        const V3<R> h1 = mk3(R(0), ea.c0, ea.s0), h2 = mk3(ea.s1, -ea.s0 * ea.c1, ea.c0 * ea.c1);
+        putH(0, col(RGF, 0), mul(RGF, nrx));
+        putH(1, mul(RGF, h1), mul(RGF, -cross(r, h1)));
+        putH(2, mul(RGF, h2), mul(RGF, -cross(r, h2)));
+        wFM = axpy(axpy(mk3(u[0], R(0), R(0)), u[1], h1), u[2], h2);
+        const R dc0 = -ea.s0 * u[0], dc1 = -ea.s1 * u[1], ds0 = ea.c0 * u[0], ds1 = ea.c1 * u[1];
+        hdw = axpy(u[1] * mk3(R(0), dc0, ds0), u[2],
+                   mk3(ds1, -ds0 * ea.c1 - ea.s0 * dc1, dc0 * ea.c1 + ea.c0 * dc1));
+        if (type == T_BUSHING)
+            for (int j = 0; j < 3; ++j) putH(3 + j, z3<R>(), col(RGF, j));
+        break;
+    }
     case T_SLIDER:
         putH(0, z3<R>(), col(RGF, 0));
         break;
@@ -293,6 +373,7 @@ __device__ __forceinline__ Kin<R> body1(const DevTables& T, int row, int rec, co
         putH(0, col(RGF, 0), mul(RGF, nrx));
         putH(1, mul(RGF, y1), mul(RGF, -cross(r, y1)));
         wFM = axpy(mk3(u[0], R(0), R(0)), u[1], y1);
+        hdw = u[1] * cross(wFM, y1);
         break;
     default:
         putH(0, col(RGF, 0), mul(RGF, nrx));
@@ -310,7 +391,6 @@ __device__ __forceinline__ Kin<R> body1(const DevTables& T, int row, int rec, co
     //   VD_w = R_GF hdw + w_GF x V_w,
     //   VD_v = R_GF(-(r x hdw) - (w_FM x r) x w_FM) + w_GF x V_v
     // with hdw = sum_j u_j HDot_FM_w_j (non-zero for the Universal only).
-    const V3<R> hdw = (type == T_UNIV) ? u[1] * cross(wFM, y1) : z3<R>();
     const V3<R> VDw = mul(RGF, hdw) + cross(P.w, VPw);
     const V3<R> VDv = mul(RGF, -cross(r, hdw) - cross(cross(wFM, r), wFM)) + cross(P.w, VPv);
 
@@ -1351,8 +1431,7 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
         // instances with loop closures project in loopInitialize instead.
         if (init && !(LOOPS && T.incons[inst] > 0)) {
             for (int lb = s.gl; lb < nb; lb += s.G) {
-                const int type = T.info[body0 + lb] & 15;
-                if (type == T_BALL || type == T_FREE) normalizeQuatAt(y, base, stride, T.qoff[body0 + lb]);
+                if (T.info[body0 + lb] & F_QUAT) normalizeQuatAt(y, base, stride, T.qoff[body0 + lb]);
             }
             if constexpr (GROUP) __syncwarp(s.mask);
         }
@@ -1465,7 +1544,7 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
                 y[e] = y1v;
                 fin &= isfinite(y1v);
             }
-            if (type == T_BALL || type == T_FREE) {
+            if (T.info[row] & F_QUAT) {
                 // N * NInv * dq with unnormalized q1 (Rotation.h:712-748)
                 const double e0 = 2 * q1[0], e1 = 2 * q1[1], e2 = 2 * q1[2], e3 = 2 * q1[3];
                 const double du0 = -e1 * dq[0] + e0 * dq[1] - e3 * dq[2] + e2 * dq[3];
@@ -1527,8 +1606,7 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
             else if (quatNorm > consTol || pes) {
                 for (int lb = s.gl; lb < nb; lb += s.G) {
                     const int row = body0 + lb;
-                    const int type = T.info[row] & 15;
-                    if (type == T_BALL || type == T_FREE) normalizeQuatAt(y, base, stride, T.qoff[row]);
+                    if (T.info[row] & F_QUAT) normalizeQuatAt(y, base, stride, T.qoff[row]);
                 }
             }
         }

@@ -35,8 +35,11 @@ int cudaFail(cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return cudaFail(e_, what);      \
     } while (0)
 
-const int kNQ[5] = {1, 1, 2, 4, 7};
-const int kNU[5] = {1, 1, 2, 3, 6};
+// q and u slots per mobilizer (sbg_mobilizer order). Ball and Free keep 4
+// and 7 q slots in Euler-angle mode too, the last one unused, as Simbody's
+// State does (RigidBodyNodeSpec_Ball.h:393-395).
+const int kNQ[SBG_NUM_MOBILIZERS] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6};
+const int kNU[SBG_NUM_MOBILIZERS] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6};
 
 // Host buffers the caller allocated page-locked (cudaMallocHost,
 // cudaHostRegister, a pinned torch tensor) are copied to and from directly;
@@ -266,14 +269,19 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
     if (d->nforces < 0 || (d->nforces > 0 && !d->forces)) return fail(SBG_ERR_INVALID, "bad force list");
     if (d->nconstraints < 0 || (d->nconstraints > 0 && !d->constraints))
         return fail(SBG_ERR_INVALID, "bad constraint list");
+    if (d->flags & ~SBG_SYSTEM_EULER_ANGLES) return fail(SBG_ERR_INVALID, "unknown system flags");
+    const bool euler = (d->flags & SBG_SYSTEM_EULER_ANGLES) != 0;
+    if (euler && d->nconstraints > 0)
+        return fail(SBG_ERR_UNSUPPORTED, "loop closures with Euler-angle Ball or Free bodies are not supported");
     const int nb = d->nbodies;
     std::vector<int> level(nb + 1, 0), qo(nb + 1, 0), uo(nb + 1, 0);
     int nq = 0, nu = 0, nquat = 0, maxnf = 0;
+    auto isQuat = [&](int mob) { return !euler && (mob == SBG_BALL || mob == SBG_FREE); };
     for (int i = 1; i <= nb; ++i) {
         const sbg_body_desc& b = d->bodies[i - 1];
         if (b.parent < 0 || b.parent >= i)
             return fail(SBG_ERR_INVALID, "body " + std::to_string(i) + ": parent must precede the body");
-        if (b.mobilizer < 0 || b.mobilizer > 4)
+        if (b.mobilizer < 0 || b.mobilizer >= SBG_NUM_MOBILIZERS)
             return fail(SBG_ERR_INVALID, "body " + std::to_string(i) + ": unknown mobilizer");
         if (!(b.mass > 0) || !std::isfinite(b.mass))
             return fail(SBG_ERR_INVALID, "body " + std::to_string(i) + ": mass must be positive and finite");
@@ -282,8 +290,8 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
         uo[i] = nu;
         nq += kNQ[b.mobilizer];
         nu += kNU[b.mobilizer];
-        if (b.mobilizer >= SBG_BALL) ++nquat;
-        if (b.mobilizer != SBG_FREE) maxnf = std::max(maxnf, kNU[b.mobilizer]);
+        if (isQuat(b.mobilizer)) ++nquat;
+        if (kNU[b.mobilizer] != 6) maxnf = std::max(maxnf, kNU[b.mobilizer]);  // 6-mobility rows have their own width
     }
     for (int i = 0; i < d->nforces; ++i) {
         const auto& f = d->forces[i];
@@ -339,6 +347,7 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
         for (int i = 0; i < d->nconstraints; ++i)
             if (d->constraints[i].body1 == bi || d->constraints[i].body2 == bi) info |= F_LOOPBODY;
         if (onLoopPath[bi]) info |= F_LOOPPATH;
+        if (isQuat(b.mobilizer)) info |= F_QUAT;
         t->parent.push_back(b.parent == 0 ? -1 : rowOf[b.parent]);
         t->info.push_back(info);
         t->qoff.push_back(qo[bi]);
@@ -389,7 +398,7 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
         if (t->parent[r] != r - 1) t->chain = false;
     t->defaultY.assign(nq + nu, 0.0);
     for (int i = 1; i <= nb; ++i)
-        if (d->bodies[i - 1].mobilizer >= SBG_BALL) t->defaultY[qo[i]] = 1.0;
+        if (isQuat(d->bodies[i - 1].mobilizer)) t->defaultY[qo[i]] = 1.0;
     for (int i = 0; i < d->nconstraints; ++i) t->cons.push_back(d->constraints[i]);
     t->lslot.assign(nb, -1);
     for (int r = 0; r < nb; ++r)

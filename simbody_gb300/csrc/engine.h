@@ -59,6 +59,7 @@ enum : int {
     F_LOOPBODY = 1 << 14,  // body 1 or 2 of a Ball loop closure: keeps a slot record
     F_LOOPPATH = 1 << 15,  // a loop body or an ancestor of one: the only rows a unit
                            // constraint force reaches on its way to the base
+    F_QUAT = 1 << 16,      // Ball or Free with quaternion coordinates (not Euler angles)
 };
 
 // Loop closures (Constraint::Ball), FP64 only. Each body named

@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(128) rkMersonAdaptiveKernel(DevTables T, int f
                 q1[j] = y1At(base + (int64_t)(qo + j) * stride, &ysv);
                 dq[j] = 0.2 * fabs(q1[j] - ysv);
             }
-            if (type == T_BALL || type == T_FREE) {
+            if (T.info[row] & F_QUAT) {
                 sq += quatErrSq(q1, dq);
                 const double len = sqrt(q1[0] * q1[0] + q1[1] * q1[1] + q1[2] * q1[2] + q1[3] * q1[3]);
                 squat += (len - 1) * (len - 1);
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(128) rkMersonAdaptiveKernel(DevTables T, int f
                     double ysv;
                     q1[j] = y1At(base + (int64_t)(qo + j) * stride, &ysv);
                 }
-                if (proj && (type == T_BALL || type == T_FREE)) {
+                if (proj && (T.info[row] & F_QUAT)) {
                     const double len = sqrt(q1[0] * q1[0] + q1[1] * q1[1] + q1[2] * q1[2] + q1[3] * q1[3]);
                     for (int k = 0; k < 4; ++k) q1[k] = q1[k] / len;
                 }

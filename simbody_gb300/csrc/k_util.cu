@@ -15,8 +15,7 @@ __global__ void normalizeQuatKernel(DevTables T, double* __restrict__ y) {
     const int body0 = T.ibody[inst], nb = T.inb[inst];
     for (int lb = 0; lb < nb; ++lb) {
         const int row = body0 + lb;
-        const int type = T.info[row] & 15;
-        if (type == T_BALL || type == T_FREE) normalizeQuatAt(y, base, stride, T.qoff[row]);
+        if (T.info[row] & F_QUAT) normalizeQuatAt(y, base, stride, T.qoff[row]);
     }
 }
 
@@ -40,7 +39,32 @@ __global__ void qdotdotKernel(DevTables T, const int64_t* __restrict__ qHost, co
         const int row = body0 + lb;
         const int type = T.info[row] & 15, n = (T.info[row] >> 4) & 15;
         const int qo = T.qoff[row], uo = T.uoff[row];
-        if (type != T_BALL && type != T_FREE) {
+        if (type == T_BALL || type == T_FREE) {
+            if (!(T.info[row] & F_QUAT)) {
+                // body-fixed X-Y-Z angles: Rotation::convertAngAccInParentToBodyXYZDotDot
+                // (Rotation.h:1041-1060) with qdot = N_P(q) w (Rotation.h:395-406)
+                double c0, s0, c1, s1;
+                sincos(Y(qo), &s0, &c0);
+                sincos(Y(qo + 1), &s1, &c1);
+                const double ooc1 = 1.0 / c1;
+                const double w0 = Y(nq + uo), w1 = Y(nq + uo + 1), w2 = Y(nq + uo + 2);
+                const double b0 = UD(uo), b1 = UD(uo + 1), b2 = UD(uo + 2);
+                const double tw = (s0 * w1 - c0 * w2) * ooc1, tb = (s0 * b1 - c0 * b2) * ooc1;
+                const double qd0 = w0 + tw * s1, qd2 = -tw;
+                const double qd1 = c0 * w1 + s0 * w2;
+                const double q1oc1 = qd1 * ooc1;
+                o[qo + 0] = (b0 + tb * s1) + (qd0 * s1 - qd2) * q1oc1;
+                o[qo + 1] = (c0 * b1 + s0 * b2) + qd0 * qd2 * c1;
+                o[qo + 2] = -tb + (qd2 * s1 - qd0) * q1oc1;
+                if (type == T_FREE) {
+                    for (int k = 0; k < 3; ++k) o[qo + 3 + k] = UD(uo + 3 + k);
+                    o[qo + 6] = 0.0;
+                } else {
+                    o[qo + 3] = 0.0;  // the unused slot
+                }
+                continue;
+            }
+        } else {  // u = qdot
             for (int k = 0; k < n; ++k) o[qo + k] = UD(uo + k);
             continue;
         }

@@ -19,6 +19,13 @@
 //  4  uneven batch: as 3 with body count log-uniform in [4,256]; 1000 steps.
 //  5  serving requests: trees as 4, horizon log-uniform in [100,10000] steps,
 //     20% with 1..4 Constraint::Ball closures to Ground, assembled at t = 0.
+// Test workloads of the wider mobilizer set (no benchmark counterpart):
+//  6  random trees as 3 whose children are uniform over Pin, Slider,
+//     Universal, Ball, Gimbal, Translation, Cylinder, Planar and Bushing, the
+//     root a Free body (even instances) or a Bushing (odd ones); angles
+//     U[-0.5,0.5], displacements U[-0.05,0.05].
+//  7  random trees as 3 in Euler-angle mode (SBG_SYSTEM_EULER_ANGLES): Ball
+//     and Free bodies with body-fixed X-Y-Z angles U[-0.5,0.5].
 #include "../../include/simbody_gb300.h"
 #include "sbg_workloads.h"
 
@@ -37,6 +44,7 @@ struct Sys {
     std::vector<sbg_mobility_force_desc> forces;
     std::vector<sbg_ball_constraint_desc> cons;
     double gravity[3] = {0, -9.8, 0};
+    int32_t flags = 0;
 };
 
 }  // namespace
@@ -63,8 +71,8 @@ void setIdentity(double* X) {
     X[0] = X[4] = X[8] = 1;
 }
 
-int nq_of(int t) { static const int n[5] = {1, 1, 2, 4, 7}; return n[t]; }
-int nu_of(int t) { static const int n[5] = {1, 1, 2, 3, 6}; return n[t]; }
+int nq_of(int t) { static const int n[10] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6}; return n[t]; }
+int nu_of(int t) { static const int n[10] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6}; return n[t]; }
 
 sbg_body_desc makeBody(int parent, int mob, double m, const double G[6], const double pPF[3], const double pBM[3]) {
     sbg_body_desc b;
@@ -97,21 +105,27 @@ void randomUnitQuat(std::mt19937_64& r, double* q) {
     for (int k = 0; k < 4; ++k) q[k] /= n;
 }
 
-// Random tree (workloads 3, 4, 5) and its initial state.
-void randomTree(std::mt19937_64& r, int nb, Sys& s, std::vector<double>& y) {
-    std::uniform_int_distribution<int> typeD(0, 3);
+// Random tree (workloads 3-7) and its initial state. wide: children over
+// all nine non-Free mobilizers and rootType for the root (workload 6);
+// euler: Ball and Free bodies with body-fixed X-Y-Z angles (workload 7).
+// Workloads 3-5 (wide = euler = false) draw exactly the stream they always did.
+void randomTree(std::mt19937_64& r, int nb, Sys& s, std::vector<double>& y, bool wide = false,
+                int rootType = SBG_FREE, bool euler = false) {
+    static const int kWide[9] = {SBG_PIN, SBG_SLIDER, SBG_UNIVERSAL, SBG_BALL, SBG_GIMBAL, SBG_TRANSLATION,
+                                 SBG_CYLINDER, SBG_PLANAR, SBG_BUSHING};
+    std::uniform_int_distribution<int> typeD(0, wide ? 8 : 3);
     std::lognormal_distribution<double> LN(0, 0.5);
     std::uniform_real_distribution<double> US(0.05, 0.3), UK(10, 100), UC(0.1, 1), UP(-0.1, 0.1);
     std::uniform_real_distribution<double> UA(-0.5, 0.5), UL(-0.05, 0.05);
     std::normal_distribution<double> NU(0, 0.5);
     const double pBM[3] = {0, 0.1, 0};
     for (int i = 1; i <= nb; ++i) {
-        int parent = 0, mob = SBG_FREE;
+        int parent = 0, mob = rootType;
         if (i > 1) {
             std::uniform_int_distribution<int> parD(1, i - 1);
             parent = parD(r);
             const int t = typeD(r);
-            mob = t == 0 ? SBG_PIN : t == 1 ? SBG_SLIDER : t == 2 ? SBG_UNIVERSAL : SBG_BALL;
+            mob = wide ? kWide[t] : t == 0 ? SBG_PIN : t == 1 ? SBG_SLIDER : t == 2 ? SBG_UNIVERSAL : SBG_BALL;
         }
         const double m = LN(r);
         const double a = US(r), b = US(r), c = US(r);
@@ -134,7 +148,19 @@ void randomTree(std::mt19937_64& r, int nb, Sys& s, std::vector<double>& y) {
         if (mob == SBG_PIN) q.push_back(UA(r));
         else if (mob == SBG_SLIDER) q.push_back(UL(r));
         else if (mob == SBG_UNIVERSAL) { q.push_back(UA(r)); q.push_back(UA(r)); }
-        else {
+        else if (mob == SBG_GIMBAL || mob == SBG_BUSHING || (euler && (mob == SBG_BALL || mob == SBG_FREE))) {
+            for (int k = 0; k < 3; ++k) q.push_back(UA(r));
+            if (mob == SBG_BUSHING || mob == SBG_FREE)
+                for (int k = 0; k < 3; ++k) q.push_back(i == 1 ? 0.0 : UL(r));
+            // Euler-angle Ball and Free keep the quaternion's slot count; the last is unused
+            if (mob == SBG_BALL || mob == SBG_FREE) q.push_back(0.0);
+        } else if (mob == SBG_TRANSLATION) {
+            for (int k = 0; k < 3; ++k) q.push_back(UL(r));
+        } else if (mob == SBG_CYLINDER) {
+            q.push_back(UA(r)); q.push_back(UL(r));
+        } else if (mob == SBG_PLANAR) {
+            q.push_back(UA(r)); q.push_back(UL(r)); q.push_back(UL(r));
+        } else {
             double qq[4];
             randomUnitQuat(r, qq);
             for (double v : qq) q.push_back(v);
@@ -247,7 +273,7 @@ extern "C" {
 const char* sbg_workload_last_error(void) { return g_wl_err.c_str(); }
 
 int sbg_workload_create(int32_t config, int32_t ninstances, sbg_workload* out) {
-    if (!out || ninstances < 0 || config < 1 || config > 5) { g_wl_err = "bad workload arguments"; return SBG_ERR_INVALID; }
+    if (!out || ninstances < 0 || config < 1 || config > 7) { g_wl_err = "bad workload arguments"; return SBG_ERR_INVALID; }
     auto* w = new sbg_workload_s();
     w->config = config;
     w->y_off.push_back(0);
@@ -298,7 +324,7 @@ int sbg_workload_create(int32_t config, int32_t ninstances, sbg_workload* out) {
         }
     } else {
         w->h = 5e-4;
-        w->nsteps = config == 3 ? 2000 : 1000;
+        w->nsteps = config == 4 || config == 5 ? 1000 : 2000;
         std::uniform_int_distribution<int> n34(20, 40);
         std::uniform_real_distribution<double> ULogN(std::log(4.0), std::log(256.0));
         std::uniform_real_distribution<double> ULogH(std::log(100.0), std::log(10000.0));
@@ -307,12 +333,15 @@ int sbg_workload_create(int32_t config, int32_t ninstances, sbg_workload* out) {
         for (int32_t i = 0; i < ninstances; ++i) {
             std::mt19937_64 r(((uint64_t)config << 32) | (uint64_t)i);
             int nb = 0;
-            if (config == 3) nb = n34(r);
+            if (config == 3 || config >= 6) nb = n34(r);
             else nb = (int)std::lround(std::exp(ULogN(r)));
             nb = std::max(4, std::min(256, nb));
             Sys s;
             std::vector<double> y;
-            randomTree(r, nb, s, y);
+            if (config == 6) randomTree(r, nb, s, y, true, (i & 1) ? SBG_BUSHING : SBG_FREE);
+            else if (config == 7) randomTree(r, nb, s, y, false, SBG_FREE, true);
+            else randomTree(r, nb, s, y);
+            if (config == 7) s.flags = SBG_SYSTEM_EULER_ANGLES;
             if (config == 5) {
                 addLoops(r, s, y.data());
                 w->horizon.push_back((int32_t)std::lround(std::exp(ULogH(r))));
@@ -331,6 +360,7 @@ int sbg_workload_create(int32_t config, int32_t ninstances, sbg_workload* out) {
         d.nbodies = (int32_t)s.bodies.size();
         d.nforces = (int32_t)s.forces.size();
         d.nconstraints = (int32_t)s.cons.size();
+        d.flags = s.flags;
         for (int k = 0; k < 3; ++k) d.gravity[k] = s.gravity[k];
         d.bodies = s.bodies.data();
         d.forces = s.forces.empty() ? nullptr : s.forces.data();

@@ -80,6 +80,11 @@ struct Model {
             case SBG_SLIDER: mobods.push_back(MobilizedBody::Slider(P, X_PF, body, X_BM)); break;
             case SBG_UNIVERSAL: mobods.push_back(MobilizedBody::Universal(P, X_PF, body, X_BM)); break;
             case SBG_BALL: mobods.push_back(MobilizedBody::Ball(P, X_PF, body, X_BM)); break;
+            case SBG_GIMBAL: mobods.push_back(MobilizedBody::Gimbal(P, X_PF, body, X_BM)); break;
+            case SBG_TRANSLATION: mobods.push_back(MobilizedBody::Translation(P, X_PF, body, X_BM)); break;
+            case SBG_CYLINDER: mobods.push_back(MobilizedBody::Cylinder(P, X_PF, body, X_BM)); break;
+            case SBG_PLANAR: mobods.push_back(MobilizedBody::Planar(P, X_PF, body, X_BM)); break;
+            case SBG_BUSHING: mobods.push_back(MobilizedBody::Bushing(P, X_PF, body, X_BM)); break;
             default: mobods.push_back(MobilizedBody::Free(P, X_PF, body, X_BM)); break;
             }
         }
@@ -96,6 +101,18 @@ struct Model {
                              Vec3(c.station2[0], c.station2[1], c.station2[2]));
         }
         sys.realizeTopology();
+        euler = (d.flags & SBG_SYSTEM_EULER_ANGLES) != 0;
+    }
+    bool euler = false;
+    // The default state with the system's model-stage choices applied
+    // (SimbodyMatterSubsystem::setUseEulerAngles).
+    State defaultState() {
+        State st = sys.getDefaultState();
+        if (euler) {
+            matter.setUseEulerAngles(st, true);
+            sys.realizeModel(st);
+        }
+        return st;
     }
 };
 
@@ -128,6 +145,8 @@ int main(int argc, char** argv) {
         {4, 8, 20, 5e-4, {0, 1, 2, 3, 4, 5, 6, 7}, 0},
         {5, 64, 20, 5e-4, {}, 0},
         {5, 64, 200, 5e-4, {}, 1e-9},
+        {6, 8, 20, 5e-4, {0, 1, 2, 3, 4, 5, 6, 7}, 0},
+        {7, 6, 20, 5e-4, {0, 1, 2, 3, 4, 5}, 0},
     };
     int written = 0;
     for (const Sel& s : sels) {
@@ -154,7 +173,7 @@ int main(int argc, char** argv) {
             Model m(d);
             const int64_t ny = yo[i + 1] - yo[i];
             int64_t status = 0;
-            State st = m.sys.getDefaultState();
+            State st = m.defaultState();
             if (st.getNY() != ny) {
                 fprintf(stderr, "cfg %d inst %d: ny %d != %lld\n", s.cfg, i, st.getNY(), (long long)ny);
                 return 1;
@@ -172,7 +191,7 @@ int main(int argc, char** argv) {
             for (int k = 0; k < nu; ++k) minv[k] = out[k];
             double trk = 0;
             try {
-                State s2 = m.sys.getDefaultState();
+                State s2 = m.defaultState();
                 for (int k = 0; k < ny; ++k) s2.updY()[k] = y0[yo[i] + k];
                 RungeKuttaMersonIntegrator integ(m.sys);
                 integ.setFixedStepSize(s.h);
@@ -240,7 +259,7 @@ int main(int argc, char** argv) {
                 std::vector<double> yout(ny, 0.0);
                 double tout = 0;
                 try {
-                    State s2 = m.sys.getDefaultState();
+                    State s2 = m.defaultState();
                     for (int k = 0; k < ny; ++k) s2.updY()[k] = y0[yo[i] + k];
                     RungeKuttaMersonIntegrator integ(m.sys);
                     integ.setFixedStepSize(c.h);
@@ -281,6 +300,8 @@ int main(int argc, char** argv) {
         {3, 6, 1e-3, 0.05, {0, 1, 2}},
         {3, 6, 1e-5, 0.02, {3}},
         {4, 8, 1e-3, 0.03, {2, 3}},
+        {6, 8, 1e-3, 0.03, {0, 1}},
+        {7, 6, 1e-3, 0.03, {0, 1}},
     };
     int adaptWritten = 0;
     for (const AdaptSel& c : adapt) {
@@ -300,7 +321,7 @@ int main(int argc, char** argv) {
             std::vector<double> yout(ny, 0.0);
             double tout = 0;
             try {
-                State s2 = m.sys.getDefaultState();
+                State s2 = m.defaultState();
                 for (int k = 0; k < ny; ++k) s2.updY()[k] = y0[yo[i] + k];
                 RungeKuttaMersonIntegrator integ(m.sys);
                 integ.setAccuracy(c.acc);

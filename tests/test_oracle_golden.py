@@ -21,7 +21,7 @@ from oracle import oracle as O
 from simbody_gb300 import Workload
 
 GOLD = Path(__file__).resolve().parent / "golden" / "reference_vectors.npz"
-WORKLOAD_SIZES = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64}
+WORKLOAD_SIZES = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6}
 
 
 @pytest.fixture(scope="module")
@@ -58,7 +58,10 @@ def test_fixture_covers_every_mobilizer_and_loops(gold, workloads):
         d = workloads[cfg].systems[int(workloads[cfg].instance_system[inst])]
         kinds |= {d.bodies[k].mobilizer for k in range(d.nbodies)}
         loops += d.nconstraints > 0
-    assert kinds == {0, 1, 2, 3, 4} and loops >= 4
+    assert kinds == set(range(10)) and loops >= 4
+    # and the Euler-angle mode of Ball and Free
+    assert any(workloads[cfg].systems[int(workloads[cfg].instance_system[inst])].flags & 1
+               for r, cfg, inst, ys, _ in _records(gold))
 
 
 def test_realize_matches_reference(gold, workloads):

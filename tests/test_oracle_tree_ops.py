@@ -21,9 +21,10 @@ import pytest
 
 from oracle import oracle as O
 from simbody_gb300 import Workload
+from simbody_gb300 import _native as N
 
 GOLD = Path(__file__).resolve().parent / "golden" / "reference_vectors.npz"
-WORKLOAD_SIZES = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64}
+WORKLOAD_SIZES = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6}
 
 
 @pytest.fixture(scope="module")
@@ -137,7 +138,7 @@ def test_composite_inertias_reproduce_the_mass_matrix_diagonal(gold, workloads):
         assert np.isclose(sum(R[b, 0] for b in roots), sum(d.bodies[b].mass for b in range(o.nb)), rtol=1e-13)
         owner = []
         for b in range(o.nb):
-            owner += [b] * {0: 1, 1: 1, 2: 2, 3: 3, 4: 6}[d.bodies[b].mobilizer]
+            owner += [b] * N.NU[d.bodies[b].mobilizer]
         for j in range(o.nu):
             e = np.zeros(o.nu)
             e[j] = 1.0
