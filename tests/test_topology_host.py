@@ -61,7 +61,7 @@ def test_levels_of_a_branched_tree():
 
 
 @pytest.mark.parametrize("field,value,msg", [("parent", 2, "parent must precede"), ("parent", -1, "parent must precede"),
-                                             ("mobilizer", 7, "unknown mobilizer"), ("mass", 0.0, "mass must be positive"),
+                                             ("mobilizer", 10, "unknown mobilizer"), ("mass", 0.0, "mass must be positive"),
                                              ("mass", float("nan"), "mass must be positive")])
 def test_invalid_bodies_are_rejected(field, value, msg):
     b = chain(3)
@@ -91,3 +91,41 @@ def test_largest_serving_tree_flattens():
         b[k].parent = (k * 7919 + 3) % (k + 1)  # any earlier body: a random-looking tree
     t = Topology(make(b, 256), keepalive=b)
     assert t.nbodies == 256 and t.nq == 1024 and t.nu == 768
+
+
+def test_euler_angle_flag_sizes_and_default_state():
+    """SBG_SYSTEM_EULER_ANGLES keeps Ball/Free q slot counts (the last slot
+    unused, as Simbody's State does), drops their quaternions, and refuses
+    loop closures; unknown flags are refused."""
+    import ctypes as C
+
+    from simbody_gb300 import _native as N
+    from simbody_gb300.build import build_engine
+
+    build_engine()
+    lib = N.engine_lib()
+    bodies = (N.BodyDesc * 2)()
+    for k, mob in enumerate((N.SBG_FREE, N.SBG_BALL)):
+        b = bodies[k]
+        b.parent, b.mobilizer, b.mass = k, mob, 1.0
+        b.unit_inertia[0] = b.unit_inertia[1] = b.unit_inertia[2] = 1.0
+        for i in (0, 4, 8):
+            b.X_PF[i] = b.X_BM[i] = 1.0
+    for flags, nquat in ((0, 2), (N.SYSTEM_EULER_ANGLES, 0)):
+        d = N.SystemDesc(2, 0, 0, flags, (C.c_double * 3)(0, -9.8, 0), bodies, None, None)
+        h = C.c_void_p()
+        assert lib.sbg_topology_create(C.byref(d), C.byref(h)) == 0
+        nq, nu, nb, nl, nqt, nc = (C.c_int32() for _ in range(6))
+        lib.sbg_topology_info(h, *(C.byref(v) for v in (nq, nu, nb, nl, nqt, nc)))
+        assert (nq.value, nu.value, nqt.value) == (11, 9, nquat)
+        y = (C.c_double * 20)()
+        lib.sbg_topology_default_state(h, y)
+        assert list(y[:11]) == ([1, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0] if nquat else [0] * 11)
+        lib.sbg_topology_destroy(h)
+    d = N.SystemDesc(2, 0, 0, 4, (C.c_double * 3)(0, -9.8, 0), bodies, None, None)
+    h = C.c_void_p()
+    assert lib.sbg_topology_create(C.byref(d), C.byref(h)) == 1  # unknown flag
+    cons = (N.BallConstraintDesc * 1)()
+    cons[0].body1, cons[0].body2 = 2, 0
+    d = N.SystemDesc(2, 0, 1, N.SYSTEM_EULER_ANGLES, (C.c_double * 3)(0, -9.8, 0), bodies, None, cons)
+    assert lib.sbg_topology_create(C.byref(d), C.byref(h)) == 6  # SBG_ERR_UNSUPPORTED
