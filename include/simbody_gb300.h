@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define SBG_ABI_VERSION 1
+#define SBG_ABI_VERSION 2
 
 typedef enum sbg_status {
     SBG_OK = 0,
@@ -144,8 +144,28 @@ typedef struct sbg_ball_constraint_desc {
     double  station2[3];
 } sbg_ball_constraint_desc;
 
+/* SmoothSphereHalfSpaceForce (SmoothSphereHalfSpaceForce.cpp:252-336)
+ * between a sphere fixed on a body and a half-space fixed in Ground: a
+ * smoothed Hertz normal force with Hunt-Crossley dissipation and a
+ * smoothed static/dynamic/viscous friction, applied at the point midway
+ * through the indentation. The half-space frame is a transform in Ground
+ * (its x axis is the contact normal, pointing into the half-space);
+ * parameters as SmoothSphereHalfSpaceForce::setParameters, with the
+ * reference's defaults when the whole parameter block is zero: stiffness 1,
+ * dissipation 0, frictions 0, transition velocity 0.01, cf 1e-5, bd 300,
+ * bv 50. */
+typedef struct sbg_contact_desc {
+    int32_t body;               /* the sphere's body, 1..nbodies */
+    int32_t reserved;
+    double  station[3];         /* sphere center in the body frame */
+    double  radius;
+    double  halfspace[12];      /* half-space frame in Ground, as the transforms above */
+    double  stiffness, dissipation, static_friction, dynamic_friction, viscous_friction;
+    double  transition_velocity, cf, bd, bv;
+} sbg_contact_desc;
+
 /* A whole System: matter + Force::Gravity (gravity = g * direction) +
- * mobility forces + Ball constraints. */
+ * mobility forces + contact spheres + Ball constraints. */
 typedef struct sbg_system_desc {
     int32_t nbodies;
     int32_t nforces;
@@ -155,6 +175,9 @@ typedef struct sbg_system_desc {
     const sbg_body_desc*            bodies;       /* nbodies entries, body 1 first */
     const sbg_mobility_force_desc*  forces;       /* nforces entries */
     const sbg_ball_constraint_desc* constraints;  /* nconstraints entries */
+    int32_t ncontacts;
+    int32_t reserved2;
+    const sbg_contact_desc*         contacts;     /* ncontacts entries (may be NULL when 0) */
 } sbg_system_desc;
 
 /* Integrator options (SimTKmath Integrator.h:352-383). Zero/negative fields
@@ -447,7 +470,8 @@ int sbg_server_create(const sbg_server_config* config, sbg_server* out);
 int sbg_server_destroy(sbg_server server);
 /* Queue a request (host only, never waits for the GPU; thread-safe). The
  * topology is copied: it may be destroyed after the call. y0 has nq+nu
- * values. SBG_ERR_BUDGET if the request could never fit the server. */
+ * values. SBG_ERR_BUDGET if the request could never fit the server;
+ * SBG_ERR_UNSUPPORTED for a topology with contact spheres. */
 int sbg_server_submit(sbg_server server, sbg_topology topology, const double* y0, double t0, double h,
                       int32_t nsteps, const sbg_integ_opts* opts, int64_t* request_id);
 /* One scheduling round: collect finished ticks, admit, launch one chunk of
@@ -488,7 +512,8 @@ int sbg_serve_simulate(int32_t n, const int64_t* units, const int32_t* horizons,
  * and the per-body scratch lives in a 16 MiB file-scope device array (the
  * topology tables in fixed device arrays: at most 256 bodies and 4096
  * mobility-force elements); larger topologies are rejected with
- * SBG_ERR_INVALID. Runs asynchronously on `stream` (a cudaStream_t, NULL =
+ * SBG_ERR_INVALID, and ones with loop closures or contact spheres with
+ * SBG_ERR_UNSUPPORTED. Runs asynchronously on `stream` (a cudaStream_t, NULL =
  * default stream) of the current device. The first call on a device does the
  * set-up: it looks up the arrays' device addresses (cudaGetSymbolAddress), and
  * with CUDA's lazy module loading that is also when the driver loads this

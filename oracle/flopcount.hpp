@@ -9,7 +9,7 @@ namespace sbgo {
 
 struct CReal {
     double v = 0;
-    static inline thread_local int64_t n[6] = {};  // add, mul, div, sqrt, trig, abs/compare
+    static inline thread_local int64_t n[6] = {};  // add, mul, div, sqrt, trig/tanh/pow, abs/compare
     CReal() = default;
     explicit CReal(double x) : v(x) {}
     static void reset() { for (auto& x : n) x = 0; }
@@ -26,5 +26,8 @@ inline CReal sqrt(CReal a) { ++CReal::n[3]; return CReal(std::sqrt(a.v)); }
 inline CReal sin(CReal a) { ++CReal::n[4]; return CReal(std::sin(a.v)); }
 inline CReal cos(CReal a) { ++CReal::n[4]; return CReal(std::cos(a.v)); }
 inline CReal abs(CReal a) { ++CReal::n[5]; return CReal(std::fabs(a.v)); }
+inline CReal tanh(CReal a) { ++CReal::n[4]; return CReal(std::tanh(a.v)); }
+inline CReal pow(CReal a, CReal b) { ++CReal::n[4]; return CReal(std::pow(a.v, b.v)); }
+inline CReal min(CReal a, CReal b) { ++CReal::n[5]; return a.v < b.v ? a : b; }
 
 }  // namespace sbgo

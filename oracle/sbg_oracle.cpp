@@ -53,6 +53,20 @@ bool buildTopology(const sbg_system_desc& d, Topology& t, const char** err) {
             b.pMB[r] = -(b.RMB[3 * r + 0] * bd.X_BM[9] + b.RMB[3 * r + 1] * bd.X_BM[10] + b.RMB[3 * r + 2] * bd.X_BM[11]);
     }
     t.nq = qn; t.nu = un;
+    if (d.ncontacts < 0 || (d.ncontacts > 0 && !d.contacts)) return fail("bad contact list");
+    for (int i = 0; i < d.ncontacts; ++i) {
+        sbg_contact_desc c = d.contacts[i];
+        if (c.body < 1 || c.body > t.nb) return fail("contact sphere on a bad body");
+        if (!(c.radius > 0)) return fail("contact sphere radius must be positive");
+        const double* par = &c.stiffness;
+        bool zero = true;
+        for (int k = 0; k < 9; ++k) zero &= par[k] == 0;
+        if (zero) {  // SmoothSphereHalfSpaceForceImpl::Parameters() defaults
+            c.stiffness = 1; c.dissipation = 0; c.static_friction = 0; c.dynamic_friction = 0;
+            c.viscous_friction = 0; c.transition_velocity = 0.01; c.cf = 1e-5; c.bd = 300; c.bv = 50;
+        }
+        t.contacts.push_back(c);
+    }
     if (d.nconstraints > 0 && (d.flags & SBG_SYSTEM_EULER_ANGLES))
         return fail("loop closures with Euler-angle Ball or Free bodies are not supported");
     int maxLevel = 0;
@@ -962,6 +976,7 @@ int oracle_system_forces_batch(const sbg_system_desc* systems, int32_t nsys, con
         w.resize(t);
         const double* q = y + y_off[i];
         realizePosition(t, q, w);
+        realizeVelocity(t, q, q + t.nq, w, (double*)nullptr);  // contact forces depend on velocities
         calcForces(t, q, q + t.nq, w);
         for (int k = 0; k < t.nu; ++k) fmob[u_off[i] + k] = w.f[k];
         for (int bi = 1; bi <= t.nb; ++bi)

@@ -196,6 +196,7 @@ struct Topology {
     double gravity[3] = {0, 0, 0};
     std::vector<sbg_mobility_force_desc> forces;
     std::vector<sbg_ball_constraint_desc> constraints;
+    std::vector<sbg_contact_desc> contacts;  // parameters defaulted as the reference's
 };
 
 // q and u counts per mobilizer (quaternion mode for Ball and Free)

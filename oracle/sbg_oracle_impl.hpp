@@ -303,8 +303,46 @@ template <class R> void realizeVelocity(const Topology& t, const R* q, const R* 
 }
 
 // ------------------------------------------------------------ forces
-// Force::Gravity (Force_Gravity.cpp:531-556) and the mobility forces
-// (Force.cpp:339-351, 434-443), accumulated in element order.
+// SmoothSphereHalfSpaceForceImpl::calcForce (SmoothSphereHalfSpaceForce.cpp:
+// 252-336) with the half-space on Ground: the (moment, force) at the body
+// origin of -force applied at the contact point, which is midway through the
+// indentation. Needs the body's position and velocity.
+template <class R> void contactBodyForce(const sbg_contact_desc& k, const BodyCache<R>& c, V3<R>& Mw, V3<R>& Fv) {
+    using std::pow; using std::tanh; using std::min;
+    const V3<R> nrm = v3<R>(R(k.halfspace[0]), R(k.halfspace[3]), R(k.halfspace[6]));  // frame x axis in Ground
+    const V3<R> pH = v3<R>(R(k.halfspace[9]), R(k.halfspace[10]), R(k.halfspace[11]));
+    const R radius = R(k.radius);
+    const V3<R> centre = c.R_GB * loadV<R>(k.station) + c.p_GB;
+    const V3<R> d = centre - pH;
+    const R indentation = -(dot(d, -nrm) - radius);
+    const V3<R> pc = centre + radius * nrm;
+    const V3<R> pa = pc - (R(1) / R(2)) * indentation * nrm;
+    const V3<R> station1 = mulT(c.R_GB, pa - c.p_GB);
+    const V3<R> rG = c.R_GB * station1;
+    const V3<R> v = c.Vv + cross(c.Vw, rG);  // findStationVelocityInGround; Ground's is zero
+    const R vnormal = dot(v, nrm);
+    const V3<R> vtangent = v - vnormal * nrm;
+    const R kk = (R(1) / R(2)) * pow(R(k.stiffness), R(2) / R(3));
+    const R fh_pos = (R(4) / R(3)) * kk * sqrt(radius * kk) * pow(sqrt(indentation * indentation + R(k.cf)), R(3) / R(2));
+    const R fh_smooth = fh_pos * (R(1) / R(2) + (R(1) / R(2)) * tanh(R(k.bd) * indentation));
+    const R cdis = R(k.dissipation);
+    const R fhc_pos = fh_smooth * (R(1) + (R(3) / R(2)) * cdis * vnormal);
+    const R fhc_smooth = fhc_pos * (R(1) / R(2) + (R(1) / R(2)) * tanh(R(k.bv) * (vnormal + (R(2) / (R(3) * cdis)))));
+    V3<R> force = fhc_smooth * nrm;
+    const R aux = dot(vtangent, vtangent) + R(k.cf);
+    const R vslip = pow(aux, R(1) / R(2));
+    const R vrel = vslip / R(k.transition_velocity);
+    const R us = R(k.static_friction), ud = R(k.dynamic_friction), uv = R(k.viscous_friction);
+    const R ff = fhc_smooth * (min(vrel, R(1)) * (ud + R(2) * (us - ud) / (R(1) + vrel * vrel)) + uv * vslip);
+    force = force + (ff / vslip) * vtangent;
+    // applyForceToBodyPoint(station1, -force)
+    Mw = Mw + cross(rG, -force);
+    Fv = Fv - force;
+}
+
+// Force::Gravity (Force_Gravity.cpp:531-556), the mobility forces
+// (Force.cpp:339-351, 434-443) and the contact spheres, accumulated in
+// element order.
 template <class R> void calcForces(const Topology& t, const R* q, const R* u, Work<R>& w) {
     const V3<R> g = loadV<R>(t.gravity);
     for (int bi = 1; bi <= t.nb; ++bi) {
@@ -313,6 +351,7 @@ template <class R> void calcForces(const Topology& t, const R* q, const R* u, Wo
         c.Fw = cross(c.pc, F);
         c.Fv = F;
     }
+    for (const auto& k : t.contacts) contactBodyForce(k, w.c[k.body], w.c[k.body].Fw, w.c[k.body].Fv);
     for (int i = 0; i < t.nu; ++i) w.f[i] = R(0);
     for (const auto& fe : t.forces) {
         const Body& b = t.b[fe.body];

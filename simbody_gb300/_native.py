@@ -48,11 +48,20 @@ class BallConstraintDesc(C.Structure):
                 ("station2", C.c_double * 3)]
 
 
+class ContactDesc(C.Structure):
+    _fields_ = [("body", C.c_int32), ("reserved", C.c_int32), ("station", C.c_double * 3), ("radius", C.c_double),
+                ("halfspace", C.c_double * 12), ("stiffness", C.c_double), ("dissipation", C.c_double),
+                ("static_friction", C.c_double), ("dynamic_friction", C.c_double),
+                ("viscous_friction", C.c_double), ("transition_velocity", C.c_double), ("cf", C.c_double),
+                ("bd", C.c_double), ("bv", C.c_double)]
+
+
 class SystemDesc(C.Structure):
     _fields_ = [("nbodies", C.c_int32), ("nforces", C.c_int32), ("nconstraints", C.c_int32),
                 ("flags", C.c_int32), ("gravity", C.c_double * 3),
                 ("bodies", C.POINTER(BodyDesc)), ("forces", C.POINTER(MobilityForceDesc)),
-                ("constraints", C.POINTER(BallConstraintDesc))]
+                ("constraints", C.POINTER(BallConstraintDesc)), ("ncontacts", C.c_int32),
+                ("reserved2", C.c_int32), ("contacts", C.POINTER(ContactDesc))]
 
 
 class IntegOpts(C.Structure):
@@ -91,7 +100,7 @@ class ServerStats(C.Structure):
 
 
 assert C.sizeof(BodyDesc) == 280 and C.sizeof(MobilityForceDesc) == 32
-assert C.sizeof(BallConstraintDesc) == 56 and C.sizeof(SystemDesc) == 64
+assert C.sizeof(BallConstraintDesc) == 56 and C.sizeof(SystemDesc) == 80 and C.sizeof(ContactDesc) == 208
 
 P = C.POINTER
 dp, ip, i64p, vp = P(C.c_double), P(C.c_int32), P(C.c_int64), C.c_void_p

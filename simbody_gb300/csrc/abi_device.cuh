@@ -89,6 +89,12 @@ template <class R> __device__ __forceinline__ void sincosR(R x, R* s, R* c) {
 template <class R> __device__ __forceinline__ R sqrtR(R x) {
     if constexpr (std::is_same<R, double>::value) return sqrt(x); else return sqrtf(x);
 }
+template <class R> __device__ __forceinline__ R powR(R x, R y) {
+    if constexpr (std::is_same<R, double>::value) return pow(x, y); else return powf(x, y);
+}
+template <class R> __device__ __forceinline__ R tanhR(R x) {
+    if constexpr (std::is_same<R, double>::value) return tanh(x); else return tanhf(x);
+}
 
 // ------------------------------------------------------------- double-float
 // hi + lo pairs of FP32 with error-free transformations (Dekker/Knuth two-sum,
@@ -176,6 +182,43 @@ template <class R> struct Kin {
     M3<R> R_;
     V3<R> p, w, v;
 };
+// SmoothSphereHalfSpaceForceImpl::calcForce (SmoothSphereHalfSpaceForce.cpp:
+// 252-336) for the spheres of one body against half-spaces fixed in Ground:
+// adds to (Mw, Fv) the moment about Bo and the force of -force applied at the
+// contact point, which lies midway through the indentation. K is the body's
+// position and velocity (Ground's velocity is zero, so the contact point's
+// velocity is the sphere body's).
+// Out of line, with everything passed by value, so that the rows without
+// contacts do not pay for its registers.
+template <class R> struct Wrench { V3<R> w, v; };
+template <class R>
+__device__ __noinline__ Wrench<R> contactForces(const R* KP, int kb, int kc, Kin<R> K, Wrench<R> F) {
+    V3<R> Mw = F.w, Fv = F.v;
+    for (int k = 0; k < kc; ++k) {
+        const R* c = KP + (int64_t)(kb + k) * kContactStride;
+        const V3<R> n = mk3(c[4], c[5], c[6]);
+        const V3<R> centre = mul(K.R_, mk3(c[0], c[1], c[2])) + K.p;
+        const R indentation = -(dot(centre - mk3(c[7], c[8], c[9]), -n) - c[3]);
+        const V3<R> r = ((centre + c[3] * n) - (R(0.5) * indentation) * n) - K.p;
+        const V3<R> v = K.v + cross(K.w, r);
+        const R vn = dot(v, n);
+        const V3<R> vt = v - vn * n;
+        // Hertz, smoothed about zero indentation, then Hunt-Crossley
+        const R fh = c[10] * powR(sqrtR(indentation * indentation + c[16]), R(1.5)) *
+                     (R(0.5) + R(0.5) * tanhR(c[17] * indentation));
+        const R fhc = fh * (R(1) + R(1.5) * c[11] * vn) * (R(0.5) + R(0.5) * tanhR(c[18] * (vn + c[19])));
+        // smoothed static / dynamic / viscous friction along the slip
+        const R vslip = sqrtR(dot(vt, vt) + c[16]);
+        const R vrel = vslip / c[15];
+        const R ff = fhc * ((vrel < R(1) ? vrel : R(1)) * (c[13] + R(2) * (c[12] - c[13]) / (R(1) + vrel * vrel)) +
+                            c[14] * vslip);
+        const V3<R> force = fhc * n + (ff / vslip) * vt;
+        Mw = Mw - cross(r, force);
+        Fv = Fv - force;
+    }
+    return Wrench<R>{Mw, Fv};
+}
+
 template <class R> __device__ __forceinline__ Kin<R> groundKin() { return Kin<R>{ident3<R>(), z3<R>(), z3<R>(), z3<R>()}; }
 template <class R, class SC> __device__ __forceinline__ Kin<R> loadKin(const SC& S, int rec) {
     Kin<R> k;
@@ -404,8 +447,16 @@ __device__ __forceinline__ Kin<R> body1(const DevTables& T, int row, int rec, co
     const V3<R> aw = VDw;
     const V3<R> av = VDv + cross(P.w, K.v - P.v);
     // gravity (Force_Gravity.cpp:549-551)
-    const V3<R> Fv = m * g;
-    const V3<R> Fw = cross(pc, Fv);
+    V3<R> Fv = m * g;
+    V3<R> Fw = cross(pc, Fv);
+    if constexpr (!Src::kMInv)
+        if (info & F_CONTACT) {
+            const R* KP;
+            if constexpr (std::is_same<R, double>::value) KP = T.kpar64; else KP = T.kpar32;
+            const Wrench<R> W = contactForces<R>(KP, T.kbeg[row], T.kcnt[row], K, Wrench<R>{Fw, Fv});
+            Fw = W.w;
+            Fv = W.v;
+        }
 
     // mobility forces, in element order (Force.cpp:339-351, 434-443);
     // M^-1 f takes the given f and no body forces instead.
@@ -1209,6 +1260,14 @@ __device__ __forceinline__ int illConditioned(const DevTables& T, const Out& out
         dm = __uint_as_float(__reduce_max_sync(s.mask, __float_as_uint(dm)));
     }
     const float tol = (T.fbList || T.ictl) ? kIllConditionedStep : kIllConditioned;
+    if (T.kcnt) {
+        // Contact spheres: the indentation is a small difference of body
+        // positions, which FP32 kinematics resolve to about 1e-5 of it, so
+        // these instances take the FP64 path of the mixed form.
+        const int b0 = T.ibody[s.inst], nb = T.inb[s.inst];
+        for (int r = 0; r < nb; ++r)
+            if (T.info[b0 + r] & F_CONTACT) return SBG_INST_ILL_CONDITIONED;
+    }
     return dm > tol * um ? SBG_INST_ILL_CONDITIONED : 0;
 }
 

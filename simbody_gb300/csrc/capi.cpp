@@ -305,6 +305,13 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
         if (c.body1 < 0 || c.body1 > nb || c.body2 < 0 || c.body2 > nb || c.body1 == c.body2)
             return fail(SBG_ERR_INVALID, "Ball constraint on bad bodies");
     }
+    if (d->ncontacts < 0 || (d->ncontacts > 0 && !d->contacts)) return fail(SBG_ERR_INVALID, "bad contact list");
+    for (int i = 0; i < d->ncontacts; ++i) {
+        const auto& k = d->contacts[i];
+        if (k.body < 1 || k.body > nb) return fail(SBG_ERR_INVALID, "contact sphere on a bad body");
+        if (!(k.radius > 0) || !std::isfinite(k.radius))
+            return fail(SBG_ERR_INVALID, "contact sphere radius must be positive and finite");
+    }
     auto* t = new (std::nothrow) sbg_topology_s();
     if (!t) return fail(SBG_ERR_NOMEM, "out of host memory");
     t->nb = nb;
@@ -312,6 +319,7 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
     t->nu = nu;
     t->nquat = nquat;
     t->ncons = d->nconstraints;
+    t->ncontacts = d->ncontacts;
     t->maxNonFreeDof = maxnf;
     for (int k = 0; k < 3; ++k) t->gravity[k] = d->gravity[k];
     // level order: stable sort of bodies by level
@@ -324,6 +332,8 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
     // forces grouped by body, application order preserved
     std::vector<std::vector<int>> fOf(nb + 1);
     for (int i = 0; i < d->nforces; ++i) fOf[d->forces[i].body].push_back(i);
+    std::vector<std::vector<int>> kOf(nb + 1);
+    for (int i = 0; i < d->ncontacts; ++i) kOf[d->contacts[i].body].push_back(i);
     std::vector<std::vector<int>> kids(nb + 1);
     for (int i = 1; i <= nb; ++i) kids[d->bodies[i - 1].parent].push_back(i);
     // bodies on the way from a loop body to Ground
@@ -348,6 +358,7 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
             if (d->constraints[i].body1 == bi || d->constraints[i].body2 == bi) info |= F_LOOPBODY;
         if (onLoopPath[bi]) info |= F_LOOPPATH;
         if (isQuat(b.mobilizer)) info |= F_QUAT;
+        if (!kOf[bi].empty()) info |= F_CONTACT;
         t->parent.push_back(b.parent == 0 ? -1 : rowOf[b.parent]);
         t->info.push_back(info);
         t->qoff.push_back(qo[bi]);
@@ -362,6 +373,28 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
             t->fkw.push_back((f.kind << 8) | f.which);
             t->fcoef.push_back(f.coef);
             t->fq0.push_back(f.q0);
+        }
+        t->kbeg.push_back((int32_t)(t->kpar.size() / kContactStride));
+        t->kcnt.push_back((int32_t)kOf[bi].size());
+        for (int ki : kOf[bi]) {
+            const sbg_contact_desc& k = d->contacts[ki];
+            double c[kContactStride];
+            for (int j = 0; j < 3; ++j) c[j] = k.station[j];
+            c[3] = k.radius;
+            for (int j = 0; j < 3; ++j) c[4 + j] = k.halfspace[3 * j];  // x axis of the half-space frame
+            for (int j = 0; j < 3; ++j) c[7 + j] = k.halfspace[9 + j];
+            // parameters, the reference's defaults for an all-zero block
+            // (SmoothSphereHalfSpaceForceImpl::Parameters())
+            double stiff = k.stiffness, diss = k.dissipation, us = k.static_friction, ud = k.dynamic_friction,
+                   uv = k.viscous_friction, vt = k.transition_velocity, cf = k.cf, bd = k.bd, bv = k.bv;
+            if (stiff == 0 && diss == 0 && us == 0 && ud == 0 && uv == 0 && vt == 0 && cf == 0 && bd == 0 && bv == 0) {
+                stiff = 1; vt = 0.01; cf = 1e-5; bd = 300; bv = 50;
+            }
+            const double kk = 0.5 * std::pow(stiff, 2.0 / 3.0);
+            c[10] = (4.0 / 3.0) * kk * std::sqrt(k.radius * kk);
+            c[11] = diss; c[12] = us; c[13] = ud; c[14] = uv; c[15] = vt; c[16] = cf; c[17] = bd; c[18] = bv;
+            c[19] = 2.0 / (3.0 * diss);
+            t->kpar.insert(t->kpar.end(), c, c + kContactStride);
         }
         // params: mass, com, G, R_PF, p_PF, R_MB = ~R_BM, p_MB = -(~R_BM p_BM)
         double p[kParamStride];
@@ -482,8 +515,8 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     // distinct topologies used, concatenated body tables
     std::vector<int> used(ntopo, -1);
     std::vector<int64_t> recTotal(ntopo, 0);
-    std::vector<int32_t> parent, info, qoff, uoff, srec, fbeg, fcnt, fkw, bidx;
-    std::vector<double> par, fcoef, fq0;
+    std::vector<int32_t> parent, info, qoff, uoff, srec, fbeg, fcnt, fkw, bidx, kbeg, kcnt;
+    std::vector<double> par, fcoef, fq0, kpar;
     std::vector<int32_t> rowBase(ntopo, 0);
     for (int i = 0; i < ninst; ++i) {
         const int k = instTopo[i];
@@ -504,6 +537,10 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
         fkw.insert(fkw.end(), t->fkw.begin(), t->fkw.end());
         fcoef.insert(fcoef.end(), t->fcoef.begin(), t->fcoef.end());
         fq0.insert(fq0.end(), t->fq0.begin(), t->fq0.end());
+        const int32_t kOff = (int32_t)(kpar.size() / kContactStride);
+        for (int32_t kb : t->kbeg) kbeg.push_back(kb + kOff);
+        kcnt.insert(kcnt.end(), t->kcnt.begin(), t->kcnt.end());
+        kpar.insert(kpar.end(), t->kpar.begin(), t->kpar.end());
         par.insert(par.end(), t->par.begin(), t->par.end());
     }
     b->nm = nm;
@@ -663,6 +700,13 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     if ((rc = b->upload(&T.fq064, fq0, "force table"))) return bail(rc);
     if ((rc = b->upload(&T.fcoef32, fcoef32, "force table"))) return bail(rc);
     if ((rc = b->upload(&T.fq032, fq032, "force table"))) return bail(rc);
+    if (!kpar.empty()) {
+        const std::vector<float> kpar32(kpar.begin(), kpar.end());
+        if ((rc = b->upload(&T.kbeg, kbeg, "contact table"))) return bail(rc);
+        if ((rc = b->upload(&T.kcnt, kcnt, "contact table"))) return bail(rc);
+        if ((rc = b->upload(&T.kpar64, kpar, "contact table"))) return bail(rc);
+        if ((rc = b->upload(&T.kpar32, kpar32, "contact table"))) return bail(rc);
+    }
     if ((rc = b->upload(&T.ibody, ibody, "instance table"))) return bail(rc);
     if ((rc = b->upload(&T.inb, inb, "instance table"))) return bail(rc);
     if ((rc = b->upload(&T.inq, inq, "instance table"))) return bail(rc);

@@ -60,6 +60,7 @@ enum : int {
     F_LOOPPATH = 1 << 15,  // a loop body or an ancestor of one: the only rows a unit
                            // constraint force reaches on its way to the base
     F_QUAT = 1 << 16,      // Ball or Free with quaternion coordinates (not Euler angles)
+    F_CONTACT = 1 << 17,   // carries SmoothSphereHalfSpaceForce spheres (kbeg/kcnt)
 };
 
 // Loop closures (Constraint::Ball), FP64 only. Each body named
@@ -149,7 +150,20 @@ struct DevTables {
     int32_t* stepsLeft;      // per instance
     double* fbuf64;          // FP64 stage derivatives of the FP64-mode instances (4 planes)
     unsigned long long* fbSteps;  // FP64 steps taken by the list kernel (cumulative)
+    // Contact spheres on a ground half-space (SmoothSphereHalfSpaceForce),
+    // grouped by body row in element order; read only for F_CONTACT rows
+    // (null where no topology has any).
+    const int32_t* kbeg;     // per body row: first contact
+    const int32_t* kcnt;     // per body row: number of contacts
+    const double* kpar64;    // kContactStride per contact
+    const float* kpar32;
 };
+// Per-contact parameters: station[3] (body frame), radius, contact normal
+// n[3] (the half-space frame's x axis in Ground), surface point p_H[3] (its
+// origin in Ground), Hertz factor (4/3) k sqrt(r k) with k = stiffness^(2/3)/2,
+// dissipation c, static, dynamic and viscous friction, transition velocity,
+// cf, bd, bv, 2/(3c) (infinite when c = 0).
+constexpr int kContactStride = 20;
 // FP64 steps an instance takes, from the step whose mixed RHS met an
 // ill-conditioned M, before it tries the mixed form again.
 constexpr int kFp64Steps = 16;

@@ -131,6 +131,7 @@ int sbg_realize_acceleration_noalloc(sbg_topology topo, int32_t ninst, const dou
     if (!topo || ninst < 0 || (ninst > 0 && (!y || !ydot || !status)))
         return naFail(SBG_ERR_INVALID, "null argument or negative instance count");
     if (topo->ncons > 0) return naFail(SBG_ERR_UNSUPPORTED, "loop closures are not supported by the no-alloc path");
+    if (topo->ncontacts > 0) return naFail(SBG_ERR_UNSUPPORTED, "contact spheres are not supported by the no-alloc path");
     if (topo->nb > kNoAllocMaxBodies)
         return naFail(SBG_ERR_INVALID, "topology has " + std::to_string(topo->nb) + " bodies; the no-alloc path takes at most " +
                                            std::to_string(kNoAllocMaxBodies));

@@ -965,6 +965,8 @@ int sbg_server_submit(sbg_server s, sbg_topology topo, const double* y0, double 
     if (nsteps < 0 || nsteps > kCtlSteps) return setError(SBG_ERR_INVALID, "step count out of range");
     if (topo->ncons > kMaxLoopCons)
         return setError(SBG_ERR_UNSUPPORTED, "at most " + std::to_string(kMaxLoopCons) + " Ball loop closures per system");
+    if (topo->ncontacts > 0)
+        return setError(SBG_ERR_UNSUPPORTED, "contact spheres are not supported by the server");
     std::lock_guard<std::mutex> lock(s->mu);
     const bool loops = topo->ncons > 0;
     const int li = loops ? fp64Lane(stepCost(*topo, true, groupLanes(*topo))) : 0;

@@ -26,6 +26,10 @@
 //     U[-0.5,0.5], displacements U[-0.05,0.05].
 //  7  random trees as 3 in Euler-angle mode (SBG_SYSTEM_EULER_ANGLES): Ball
 //     and Free bodies with body-fixed X-Y-Z angles U[-0.5,0.5].
+//  8  random trees as 3 on a ground half-space: a SmoothSphereHalfSpaceForce
+//     sphere on every body (station U[-0.05,0.05]^3, radius U[0.02,0.06]), the
+//     half-space normal tilted U[-0.2,0.2] rad from -Y, the lowest sphere
+//     indented 3 mm at t = 0; 2000 steps of 5e-4.
 #include "../../include/simbody_gb300.h"
 #include "sbg_workloads.h"
 
@@ -43,6 +47,7 @@ struct Sys {
     std::vector<sbg_body_desc> bodies;
     std::vector<sbg_mobility_force_desc> forces;
     std::vector<sbg_ball_constraint_desc> cons;
+    std::vector<sbg_contact_desc> contacts;
     double gravity[3] = {0, -9.8, 0};
     int32_t flags = 0;
 };
@@ -266,6 +271,49 @@ void addLoops(std::mt19937_64& r, Sys& s, const double* q) {
     }
 }
 
+// Workload 8: a contact sphere on every body and a ground half-space,
+// slightly tilted, whose contact normal (the half-space frame's x axis)
+// points down into it and whose surface lies so that the lowest sphere is
+// indented by 3 mm at t = 0. Parameters in the range of gait models (Hertz
+// stiffness 1e6, Hunt-Crossley dissipation 2, static / dynamic / viscous
+// friction 0.8 / 0.5 / 0.1, transition velocity 0.2: with viscous friction
+// 0.5 a few light bodies' friction is too stiff for the fixed step of 5e-4 s);
+// every eighth instance leaves the parameter block zero, which stands for the
+// reference's defaults.
+void addContacts(std::mt19937_64& r, Sys& s, const double* q, bool defaults) {
+    std::uniform_real_distribution<double> UP(-0.05, 0.05), UR(0.02, 0.06), UT(-0.2, 0.2);
+    const int nb = (int)s.bodies.size();
+    const std::vector<Xf> X = bodyTransforms(s, q);
+    const double th = -kPi / 2 + UT(r);
+    const double c = std::cos(th), sn = std::sin(th);
+    const double nrm[3] = {c, sn, 0};
+    double lowest = 1e300;
+    for (int b = 1; b <= nb; ++b) {
+        sbg_contact_desc k;
+        std::memset(&k, 0, sizeof k);
+        k.body = b;
+        for (int j = 0; j < 3; ++j) k.station[j] = UP(r);
+        k.radius = UR(r);
+        const Xf& Xb = X[b];
+        double ctr[3];
+        for (int j = 0; j < 3; ++j)
+            ctr[j] = Xb.R[3 * j] * k.station[0] + Xb.R[3 * j + 1] * k.station[1] + Xb.R[3 * j + 2] * k.station[2] + Xb.p[j];
+        lowest = std::min(lowest, -(ctr[0] * nrm[0] + ctr[1] * nrm[1] + ctr[2] * nrm[2]) - k.radius);
+        if (!defaults) {
+            k.stiffness = 1e6; k.dissipation = 2; k.static_friction = 0.8; k.dynamic_friction = 0.5;
+            k.viscous_friction = 0.1; k.transition_velocity = 0.2; k.cf = 1e-5; k.bd = 300; k.bv = 50;
+        }
+        s.contacts.push_back(k);
+    }
+    // rotation about z by th (row-major), origin at depth d along the normal
+    const double d = -0.003 - lowest;
+    for (auto& k : s.contacts) {
+        const double R[9] = {c, -sn, 0, sn, c, 0, 0, 0, 1};
+        for (int j = 0; j < 9; ++j) k.halfspace[j] = R[j];
+        for (int j = 0; j < 3; ++j) k.halfspace[9 + j] = d * nrm[j];
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -273,7 +321,7 @@ extern "C" {
 const char* sbg_workload_last_error(void) { return g_wl_err.c_str(); }
 
 int sbg_workload_create(int32_t config, int32_t ninstances, sbg_workload* out) {
-    if (!out || ninstances < 0 || config < 1 || config > 7) { g_wl_err = "bad workload arguments"; return SBG_ERR_INVALID; }
+    if (!out || ninstances < 0 || config < 1 || config > 8) { g_wl_err = "bad workload arguments"; return SBG_ERR_INVALID; }
     auto* w = new sbg_workload_s();
     w->config = config;
     w->y_off.push_back(0);
@@ -342,6 +390,7 @@ int sbg_workload_create(int32_t config, int32_t ninstances, sbg_workload* out) {
             else if (config == 7) randomTree(r, nb, s, y, false, SBG_FREE, true);
             else randomTree(r, nb, s, y);
             if (config == 7) s.flags = SBG_SYSTEM_EULER_ANGLES;
+            if (config == 8) addContacts(r, s, y.data(), (i & 7) == 7);
             if (config == 5) {
                 addLoops(r, s, y.data());
                 w->horizon.push_back((int32_t)std::lround(std::exp(ULogH(r))));
@@ -365,6 +414,8 @@ int sbg_workload_create(int32_t config, int32_t ninstances, sbg_workload* out) {
         d.bodies = s.bodies.data();
         d.forces = s.forces.empty() ? nullptr : s.forces.data();
         d.constraints = s.cons.empty() ? nullptr : s.cons.data();
+        d.ncontacts = (int32_t)s.contacts.size();
+        d.contacts = s.contacts.empty() ? nullptr : s.contacts.data();
         w->desc.push_back(d);
     }
     *out = w;

@@ -10,6 +10,9 @@ Python harness see identical inputs).
   4  10,000 trees with body count log-uniform in [4,256], 1000 steps
   5  serving requests: trees as 4, horizons log-uniform in [100,10000] steps,
      20% with 1-4 Ball loop closures
+  6  trees as 3 over all ten mobilizers (Free or Bushing root)
+  7  trees as 3 with Euler-angle Ball and Free bodies
+  8  trees as 3 with a contact sphere on every body over a ground half-space
 """
 from __future__ import annotations
 
@@ -19,7 +22,7 @@ import numpy as np
 
 from . import _native as N
 
-DEFAULT_INSTANCES = {1: 1024, 2: 65536, 3: 16384, 4: 10000, 5: 2000}
+DEFAULT_INSTANCES = {1: 1024, 2: 65536, 3: 16384, 4: 10000, 5: 2000, 6: 16384, 7: 16384, 8: 16384}
 
 
 class Workload:

@@ -3,7 +3,7 @@
 //
 // Built and run by make_golden.py next to this file; it is not part of the
 // library and nothing at test time compiles or runs it. For each selected
-// instance of workload configs 1-5 it records:
+// instance of the workload configs it records:
 //   y0                      the seeded state (from libsbg_workloads)
 //   ydot                    System::realize(s, Stage::Acceleration); s.getYDot()
 //   f, minv_f               SimbodyMatterSubsystem::multiplyByMInv(s, f, out)
@@ -25,6 +25,7 @@
 //   MobilizedBody::{Pin,Slider,Universal,Ball,Free} (Simbody/include/simbody/internal/MobilizedBody_*.h)
 //   Force::Gravity, Force::MobilityLinearSpring/Damper (Simbody/include/simbody/internal/Force*.h)
 //   Constraint::Ball (Simbody/include/simbody/internal/Constraint_Ball.h)
+//   SmoothSphereHalfSpaceForce (Simbody/include/simbody/internal/SmoothSphereHalfSpaceForce.h)
 //   RungeKuttaMersonIntegrator (SimTKmath/Integrators/include/simmath/RungeKuttaMersonIntegrator.h)
 //
 // Output: one binary file of records
@@ -95,6 +96,21 @@ struct Model {
             else
                 Force::MobilityLinearDamper(forces, mobods[f.body], MobilizerUIndex(f.which), f.coef);
         }
+        for (int i = 0; i < d.ncontacts; ++i) {
+            const sbg_contact_desc& k = d.contacts[i];
+            SmoothSphereHalfSpaceForce f(forces);
+            f.setContactSphereBody(mobods[k.body]);
+            f.setContactSphereLocationInBody(Vec3(k.station[0], k.station[1], k.station[2]));
+            f.setContactSphereRadius(k.radius);
+            f.setContactHalfSpaceBody(matter.Ground());
+            f.setContactHalfSpaceFrame(toTransform(k.halfspace));
+            const double* par = &k.stiffness;
+            bool zero = true;
+            for (int j = 0; j < 9; ++j) zero = zero && par[j] == 0;
+            if (!zero)  // a zero block keeps the force's own defaults
+                f.setParameters(k.stiffness, k.dissipation, k.static_friction, k.dynamic_friction, k.viscous_friction,
+                                k.transition_velocity, k.cf, k.bd, k.bv);
+        }
         for (int i = 0; i < d.nconstraints; ++i) {
             const sbg_ball_constraint_desc& c = d.constraints[i];
             Constraint::Ball(mobods[c.body1], Vec3(c.station1[0], c.station1[1], c.station1[2]), mobods[c.body2],
@@ -147,6 +163,8 @@ int main(int argc, char** argv) {
         {5, 64, 200, 5e-4, {}, 1e-9},
         {6, 8, 20, 5e-4, {0, 1, 2, 3, 4, 5, 6, 7}, 0},
         {7, 6, 20, 5e-4, {0, 1, 2, 3, 4, 5}, 0},
+        {8, 8, 20, 5e-4, {0, 1, 2, 3, 4, 5, 6, 7}, 0},
+        {8, 8, 400, 5e-4, {0, 1}, 0},
     };
     int written = 0;
     for (const Sel& s : sels) {
@@ -229,6 +247,7 @@ int main(int argc, char** argv) {
         {3, 6, 5e-4, 0.005, 0.01, {0, 1}},
         {4, 8, 5e-4, 0.005, 0.01, {2, 3}},
         {5, 64, 5e-4, 0.005, 0.01, {}},
+        {8, 8, 5e-4, 0.005, 0.01, {0, 7}},
     };
     int contWritten = 0;
     for (const ContSel& c : cont) {
@@ -302,6 +321,7 @@ int main(int argc, char** argv) {
         {4, 8, 1e-3, 0.03, {2, 3}},
         {6, 8, 1e-3, 0.03, {0, 1}},
         {7, 6, 1e-3, 0.03, {0, 1}},
+        {8, 8, 1e-3, 0.03, {0, 1}},
     };
     int adaptWritten = 0;
     for (const AdaptSel& c : adapt) {

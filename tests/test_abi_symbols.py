@@ -30,13 +30,14 @@ def test_every_declared_symbol_is_exported():
 
 def test_abi_version_and_no_device_here():
     lib = N.engine_lib()
-    assert lib.sbg_abi_version() == 1
+    assert lib.sbg_abi_version() == 2
     assert lib.sbg_device_count() >= 0  # 0 on a machine without a driver; never raises
 
 
 def test_struct_layouts_match_header():
     assert C.sizeof(N.BodyDesc) == 280
-    assert C.sizeof(N.SystemDesc) == 64
+    assert C.sizeof(N.SystemDesc) == 80
+    assert C.sizeof(N.ContactDesc) == 208
 
 
 def test_batch_entry_points_refuse_a_null_batch_without_touching_the_device():

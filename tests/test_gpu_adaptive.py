@@ -29,7 +29,7 @@ def _worst(a, b, off):
 
 def test_adaptive_matches_reference_records(engine):
     g = dict(np.load(GOLD))
-    sizes = {1: 8, 2: 4, 3: 6, 4: 8, 6: 8, 7: 6}
+    sizes = {1: 8, 2: 4, 3: 6, 4: 8, 6: 8, 7: 6, 8: 8}
     for r in range(len(g["a_cfg"])):
         cfg, inst = int(g["a_cfg"][r]), int(g["a_inst"][r])
         w = Workload(cfg, sizes[cfg])
@@ -51,6 +51,7 @@ def test_adaptive_matches_reference_records(engine):
     (3, 256, 0.05, dict(accuracy=1e-4)),
     (3, 128, 0.03, dict(initial_step=1e-3, max_step=4e-3, project_every_step=True)),
     (4, 64, 0.02, dict(min_step=1e-4)),
+    (8, 64, 0.03, dict()),
 ])
 def test_adaptive_matches_oracle(engine, config, n, t_final, kw):
     w = Workload(config, n)

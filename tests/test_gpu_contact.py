@@ -1,0 +1,124 @@
+"""SmoothSphereHalfSpaceForce on the GPU (workload 8: trees of 20-40 bodies,
+a contact sphere on every body, a tilted ground half-space, the lowest
+sphere indented at t = 0), through the C ABI.
+
+  - FP64 integration against the oracle, whose contact force is pinned to
+    the reference's records (test_oracle_golden.py), over 400 steps of
+    5e-4 s, during which the trees land and slide: <= 1e-9 relative, or, for
+    an instance whose landing amplifies rounding (a body that bounces or
+    starts to slip near a smoothing threshold amplifies 1e-15 into 1e-4),
+    within 100 times the oracle's own response to a 1e-14 relative
+    perturbation of the initial state.
+  - The mixed form against FP64 over the same horizon, by the same rule with
+    1e-5. The indentation is a small difference of body positions that FP32
+    kinematics resolve only to about 1e-5 of it, so the mixed form takes
+    instances with contact spheres through its FP64 path.
+  - A zero parameter block stands for the reference's defaults: the engine
+    gives the same accelerations as with the defaults written out.
+  - The server and the allocation-free realize do not take contact spheres
+    (SBG_ERR_UNSUPPORTED) rather than ignore them.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from simbody_gb300 import Server, Workload, engine_batch
+from simbody_gb300 import _native as N
+from simbody_gb300.engine import Topology
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b, off):
+    return np.array([np.linalg.norm(a[off[i]:off[i + 1]] - b[off[i]:off[i + 1]]) /
+                     max(np.linalg.norm(b[off[i]:off[i + 1]]), 1e-300) for i in range(len(off) - 1)])
+
+
+@pytest.fixture(scope="module")
+def w8():
+    return Workload(8, 96)
+
+
+STEPS = 400
+
+
+@pytest.fixture(scope="module")
+def oracle_runs(w8):
+    """The oracle's trajectory and its response to a 1e-14 relative
+    perturbation of y0 (per instance, relative): how much the instance
+    amplifies rounding over the horizon."""
+    ref, rt, rst, _ = O.rk_workload(w8, w8.h, STEPS)
+    rng = np.random.default_rng(8)
+    yp = w8.y0 * (1 + 1e-14 * rng.choice([-1.0, 1.0], size=w8.y0.size))
+    pert, _, _, _ = O.rk_merson(w8.systems, w8.nsys, w8.instance_system, w8.y_offsets, yp, w8.h, STEPS)
+    return ref, rt, rst, _rel(pert, ref, w8.y_offsets)
+
+
+def test_contact_trajectory_fp64_matches_oracle(engine, w8, oracle_runs):
+    ref, rt, rst, sens = oracle_runs
+    b, y0 = engine_batch(w8, "fp64")
+    b.set_state(y0)
+    st = b.rk_merson_fixed(w8.h, STEPS)
+    y, t = b.get_state()
+    np.testing.assert_array_equal(st, rst)
+    assert (st == 0).all()
+    np.testing.assert_array_equal(t, rt)
+    err = _rel(y, ref, b.y_offsets)
+    bound = np.maximum(1e-9, 100 * sens)
+    assert (err <= bound).all(), (err / bound).max()
+    assert (err <= 1e-9).mean() >= 0.9, np.sort(err)[-10:]
+    # the trees moved by more than the tolerance: contact and gravity acted
+    assert _rel(y, y0, b.y_offsets).min() > 1e-3
+
+
+def test_contact_trajectory_mixed_close_to_fp64(engine, w8, oracle_runs):
+    sens = oracle_runs[3]
+    b64, y0 = engine_batch(w8, "fp64")
+    bm, _ = engine_batch(w8, "mixed")
+    b64.set_state(y0)
+    bm.set_state(y0)
+    st64 = b64.rk_merson_fixed(w8.h, STEPS)
+    st = bm.rk_merson_fixed(w8.h, STEPS)
+    np.testing.assert_array_equal(st, st64)
+    assert (st == 0).all()
+    y64, _ = b64.get_state()
+    ym, _ = bm.get_state()
+    err = _rel(ym, y64, b64.y_offsets)
+    bound = np.maximum(1e-5, 100 * sens)
+    assert (err <= bound).all(), (err / bound).max()
+    assert (err <= 1e-5).mean() >= 0.9, np.sort(err)[-10:]
+
+
+def test_zero_parameter_block_is_the_reference_defaults(engine, w8):
+    i = 7  # every eighth instance of workload 8 leaves the block zero
+    d = w8.systems[int(w8.instance_system[i])]
+    assert d.contacts[0].stiffness == 0
+    spelled = (N.ContactDesc * d.ncontacts)()
+    for k in range(d.ncontacts):
+        spelled[k] = N.ContactDesc.from_buffer_copy(d.contacts[k])
+        c = spelled[k]
+        c.stiffness, c.dissipation, c.static_friction, c.dynamic_friction = 1.0, 0.0, 0.0, 0.0
+        c.viscous_friction, c.transition_velocity, c.cf, c.bd, c.bv = 0.0, 0.01, 1e-5, 300.0, 50.0
+    d2 = N.SystemDesc.from_buffer_copy(d)
+    d2.contacts = spelled
+    y0 = w8.y0[w8.instance_slice(i)]
+    out = []
+    for desc in (d, d2):
+        from simbody_gb300.engine import Batch
+        b = Batch([Topology(desc, keepalive=(w8, spelled))], np.zeros(1, np.int32), precision="fp64")
+        b.set_state(y0)
+        ydot, st = b.realize_acceleration()
+        assert st[0] == 0
+        out.append(ydot.copy())
+    np.testing.assert_array_equal(out[0], out[1])
+
+
+def test_server_refuses_contact_spheres(engine, w8):
+    s = Server(precision="fp64", device_budget_bytes=64 << 20)
+    try:
+        topo = Topology(w8.systems[0], keepalive=w8)
+        with pytest.raises(N.EngineError) as e:
+            s.submit(topo, w8.y0[w8.instance_slice(0)], w8.h, 10)
+        assert e.value.code == 6  # SBG_ERR_UNSUPPORTED
+    finally:
+        s.close()

@@ -22,7 +22,7 @@ from simbody_gb300 import Workload, engine_batch
 pytestmark = pytest.mark.gpu
 
 GOLD = Path(__file__).resolve().parent / "golden" / "reference_vectors.npz"
-WORKLOAD_SIZES = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6}
+WORKLOAD_SIZES = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6, 8: 8}
 
 
 @pytest.fixture(scope="module")
@@ -146,7 +146,7 @@ def test_qdotdot_matches_reference_records(engine, gold):
             assert _rel(got, gold["qdd"][qs]) <= 1e-12, (c, i, _rel(got, gold["qdd"][qs]))
 
 
-@pytest.mark.parametrize("config,n", [(2, 256), (3, 256), (4, 64)])
+@pytest.mark.parametrize("config,n", [(2, 256), (3, 256), (4, 64), (8, 64)])
 def test_qdotdot_matches_oracle(engine, config, n):
     import simbody_gb300._native as N
 

@@ -94,7 +94,7 @@ def test_mixed_batch_keeps_loops_in_fp64(engine, w5):
 def test_engine_matches_reference_golden_vectors(engine):
     """Every golden record (configs 1-5) through the engine in FP64."""
     g = dict(np.load(GOLD))
-    sizes = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6}
+    sizes = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6, 8: 8}
     ws = {c: Workload(c, n) for c, n in sizes.items()}
     for r in range(len(g["cfg"])):
         cfg, inst = int(g["cfg"][r]), int(g["inst"][r])

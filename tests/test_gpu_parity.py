@@ -2,7 +2,9 @@
 
 Workloads 6 (trees over all nine non-Free mobilizers: Gimbal, Translation,
 Cylinder, Planar and Bushing beside the benchmark's four, Free or Bushing
-roots) and 7 (trees in Euler-angle mode) cover the wider mobilizer set.
+roots) and 7 (trees in Euler-angle mode) cover the wider mobilizer set, and 8
+(trees with a SmoothSphereHalfSpaceForce sphere on every body, pressing on a
+ground half-space) the contact force.
 
 Tolerances: the plain FP64 form must reproduce realize(Acceleration) to
 <= 1e-12 relative (norm-wise per instance) and short trajectories to <= 1e-12;
@@ -26,7 +28,7 @@ def rel_err_per_instance(a, b, offsets, part=None):
     return np.array(errs)
 
 
-@pytest.mark.parametrize("config,n", [(1, 256), (2, 512), (3, 128), (4, 64), (6, 128), (7, 128)])
+@pytest.mark.parametrize("config,n", [(1, 256), (2, 512), (3, 128), (4, 64), (6, 128), (7, 128), (8, 128)])
 def test_realize_fp64_matches_oracle(engine, config, n):
     w = Workload(config, n)
     b, y0 = engine_batch(w, "fp64")
@@ -42,7 +44,7 @@ def _udot(d, b):
     return np.concatenate([d[b.y_offsets[i] + b.nq[i]:b.y_offsets[i + 1]] for i in range(b.ninst)])
 
 
-@pytest.mark.parametrize("config,n", [(1, 512), (2, 2048), (3, 512), (4, 256), (6, 256), (7, 256)])
+@pytest.mark.parametrize("config,n", [(1, 512), (2, 2048), (3, 512), (4, 256), (6, 256), (7, 256), (8, 256)])
 def test_realize_mixed_udot_error(engine, config, n):
     """Mixed form (FP32 recursions + double-float residual refinement):
     relative udot error per instance <= 1e-5 against FP64."""
@@ -76,7 +78,7 @@ def test_realize_mixed_fast_is_plain_fp32(engine, config, n):
 
 
 @pytest.mark.parametrize("config,n,steps,tol", [(1, 256, 50, 1e-6), (3, 64, 20, 1e-6), (4, 32, 20, 1e-6),
-                                                  (6, 64, 20, 1e-6), (7, 64, 20, 1e-6)])
+                                                  (6, 64, 20, 1e-6), (7, 64, 20, 1e-6), (8, 64, 20, 1e-6)])
 def test_rk_merson_mixed_short_horizon(engine, config, n, steps, tol):
     """FP32 recursions with FP64 state accumulation stay close to the FP64
     trajectory over a short horizon."""
@@ -95,7 +97,8 @@ def test_rk_merson_mixed_short_horizon(engine, config, n, steps, tol):
     assert err.max() <= tol, err.max()
 
 
-@pytest.mark.parametrize("config,n,steps", [(1, 256, 50), (3, 64, 20), (4, 32, 20), (6, 64, 20), (7, 64, 20)])
+@pytest.mark.parametrize("config,n,steps", [(1, 256, 50), (3, 64, 20), (4, 32, 20), (6, 64, 20), (7, 64, 20),
+                                             (8, 64, 20)])
 def test_rk_merson_fp64_short_horizon(engine, config, n, steps):
     w = Workload(config, n)
     b, y0 = engine_batch(w, "fp64")

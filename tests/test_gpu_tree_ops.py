@@ -21,7 +21,7 @@ from simbody_gb300 import Workload, engine_batch
 
 pytestmark = pytest.mark.gpu
 
-CASES = [(1, 64), (2, 96), (3, 64), (4, 48), (5, 64), (6, 64), (7, 64)]
+CASES = [(1, 64), (2, 96), (3, 64), (4, 48), (5, 64), (6, 64), (7, 64), (8, 64)]
 
 
 def _per_instance_rel(a, b, off):

@@ -19,9 +19,10 @@ import pytest
 
 from oracle import oracle as O
 from simbody_gb300 import Workload
+from simbody_gb300 import _native as N
 
 GOLD = Path(__file__).resolve().parent / "golden" / "reference_vectors.npz"
-WORKLOAD_SIZES = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6}
+WORKLOAD_SIZES = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6, 8: 8}
 
 
 @pytest.fixture(scope="module")
@@ -173,3 +174,29 @@ def test_continuation_records_cover_loops_and_quaternions(gold, workloads):
         quats += any(d.bodies[k].mobilizer in (3, 4) for k in range(d.nbodies))
         loops += d.nconstraints > 0
     assert quats >= 6 and loops >= 2
+
+
+def test_contact_records_engage_the_contact_force(gold, workloads):
+    """The records of the ground-contact trees (SmoothSphereHalfSpaceForce)
+    realize with the spheres pressing on the half-space: dropping the contact
+    elements changes the recorded accelerations well beyond the tolerance,
+    and one record uses the force's default parameters (a zero block)."""
+    w = workloads[8]
+    seen_defaults = checked = 0
+    for r, cfg, inst, ys, _ in _records(gold):
+        if cfg != 8:
+            continue
+        d = w.systems[int(w.instance_system[inst])]
+        assert d.ncontacts == d.nbodies
+        seen_defaults += d.contacts[0].stiffness == 0
+        bare = N.SystemDesc.from_buffer_copy(d)
+        bare.ncontacts = 0
+        off = np.array([0, ys.stop - ys.start])
+        ydot, st = O.realize((N.SystemDesc * 1)(bare), 1, np.zeros(1, np.int32), off, gold["y0"][ys])
+        assert st[0] == 0
+        # one indented sphere among 20-40 bodies (the default stiffness, 1,
+        # gives about 1e-4 N): small against the whole ydot, but a hundred
+        # times the agreement of the realize records
+        assert _rel(ydot, gold["ydot"][ys]) > 1e-10, (inst, _rel(ydot, gold["ydot"][ys]))
+        checked += 1
+    assert checked >= 8 and seen_defaults >= 1

@@ -129,3 +129,38 @@ def test_euler_angle_flag_sizes_and_default_state():
     cons[0].body1, cons[0].body2 = 2, 0
     d = N.SystemDesc(2, 0, 1, N.SYSTEM_EULER_ANGLES, (C.c_double * 3)(0, -9.8, 0), bodies, None, cons)
     assert lib.sbg_topology_create(C.byref(d), C.byref(h)) == 6  # SBG_ERR_UNSUPPORTED
+
+
+def test_contact_spheres_are_validated_and_refused_where_unsupported():
+    """SmoothSphereHalfSpaceForce spheres: a bad body or a non-positive
+    radius is SBG_ERR_INVALID; a valid list flattens; the allocation-free
+    realize refuses a topology with spheres (SBG_ERR_UNSUPPORTED) before it
+    touches the device."""
+    b = chain(3)
+    k = (N.ContactDesc * 2)()
+    for j in range(2):
+        k[j].body, k[j].radius = j + 1, 0.05
+        k[j].halfspace[1], k[j].halfspace[3], k[j].halfspace[8] = 1.0, -1.0, 1.0  # normal -Y
+    d = make(b, 3)
+    d.ncontacts, d.contacts = 2, k
+    assert create(d)[0] == 0
+    k[1].body = 4
+    rc, err = create(d)
+    assert rc == 1 and "contact" in err
+    k[1].body, k[1].radius = 2, 0.0
+    rc, err = create(d)
+    assert rc == 1 and "radius" in err
+    d.contacts = None
+    assert create(d)[0] == 1
+    k[1].radius = 0.05
+    d.contacts = k
+    lib = N.engine_lib()
+    h = C.c_void_p()
+    assert lib.sbg_topology_create(C.byref(d), C.byref(h)) == 0
+    try:
+        y = (C.c_double * 6)()
+        st = (C.c_int32 * 1)()
+        assert lib.sbg_realize_acceleration_noalloc(h, 1, y, y, st, None) == 6
+        assert b"contact" in lib.sbg_noalloc_last_error()
+    finally:
+        lib.sbg_topology_destroy(h)
