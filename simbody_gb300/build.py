@@ -24,7 +24,7 @@ ORACLE = ROOT / "oracle"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
-CU_UNITS = ["k_r64.cu", "k_r32c.cu", "k_r32cr.cu", "k_r32g.cu", "k_rk64.cu", "k_rk32c.cu", "k_rk32cr.cu", "k_rk32g.cu",
+CU_UNITS = ["k_r64.cu", "k_r32c.cu", "k_r32cr.cu", "k_r32s.cu", "k_r32g.cu", "k_rk64.cu", "k_rk32c.cu", "k_rk32cr.cu", "k_rk32g.cu",
             "k_util.cu", "k_noalloc.cu", "k_loops.cu", "k_rkloops.cu", "k_rkloops1.cu", "k_ops.cu", "k_fallback.cu",
             "k_rkadapt.cu", "serve.cu"]
 HOST_UNITS = ["capi.cpp"]

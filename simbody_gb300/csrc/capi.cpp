@@ -80,7 +80,8 @@ struct sbg_batch_s {
     int ninst = 0;
     int nm = 3;
     bool tiled = false;
-    int variant = 0;  // kernel occupancy variant: 0 = not tuned yet, 1 or 4
+    int variant = 0;  // kernel variant: 0 = not tuned yet, else 1, 4, 7 or 8 (see LaunchPlan)
+    bool stagedOk = false;  // variant 8 applies: one shared chain topology without Free bodies
     cudaStream_t stream = nullptr;
     std::vector<int32_t> instTopo;
     std::vector<int64_t> hostYOff, hostUOff;  // packed host offsets (n+1)
@@ -675,10 +676,19 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
     b->scratchElems = sOff;
     const int64_t scratchLoopElems = sOffLoop;
     b->tiled = true;
+    {
+        int nUsed = 0, k0 = -1;
+        for (int k = 0; k < ntopo; ++k)
+            if (used[k] >= 0) { ++nUsed; k0 = k; }
+        bool ok = nUsed == 1 && precision != SBG_PRECISION_FP64 && b->nChain == ninst && topos[k0]->chain;
+        for (int r = 0; ok && r < topos[k0]->nb; ++r)
+            if (((topos[k0]->info[r] >> 4) & 15) == 6) ok = false;
+        b->stagedOk = ok;
+    }
     if (precision == SBG_PRECISION_FP64) b->variant = 1;  // FP64 needs every register
     if (const char* v = std::getenv("SBG_VARIANT")) {  // tuning override
         const int want = std::atoi(v);
-        b->variant = want == 4 || want == 7 ? want : 1;
+        b->variant = want == 8 ? (b->stagedOk ? 8 : 7) : want == 4 || want == 7 ? want : 1;
     }
 
     int rc = 0;
@@ -902,8 +912,9 @@ static int tuneVariant(sbg_batch b) {
     }
     if (!fixedVariant && b->precision != SBG_PRECISION_FP64) {
         int bestVariant = 1;
-        for (int v : {4, 7}) {
-            if (v == 7 && b->nChain == 0) continue;  // 64-thread blocks exist for the chain driver only
+        for (int v : {4, 7, 8}) {
+            if (v >= 7 && b->nChain == 0) continue;  // 64-thread blocks exist for the chain driver only
+            if (v == 8 && !b->stagedOk) continue;
             b->variant = v;
             if (int rc = timePlan(b, &ms)) return rc;
             if (ms < best) { best = ms; bestVariant = v; }

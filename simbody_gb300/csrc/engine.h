@@ -191,7 +191,7 @@ struct LaunchPlan {
     int nChain;
     int nGroupBlocks;
     int nm;
-    int variant;  // 1: registers as needed; 4: at most 128 registers (FP32 only)
+    int variant;  // 1: registers as needed; 4: at most 128 registers (FP32 only); 7: 64-thread blocks; 8: 7 staged (realize)
     int nLoop;    // order positions [nChain, nChain + nLoop): instances with loop closures (FP64 chain driver)
     int chainFirst;  // first order position of the chain segment launch (a sub-range of it: pipelined realize)
     int groupFirst;  // first block of the level-parallel launch in the block table

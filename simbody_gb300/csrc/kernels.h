@@ -142,6 +142,10 @@ void realize64Group(const KArgs& a, cudaStream_t s);
 void minv64Chain(const KArgs& a, cudaStream_t s);
 void minv64Group(const KArgs& a, cudaStream_t s);
 void realize32Chain(const KArgs& a, bool refine, cudaStream_t s);
+// Variant 8: the chain driver with record fields staged through shared
+// memory (one shared chain topology, no Free bodies, segment start a
+// multiple of 32).
+void realize32ChainStaged(const KArgs& a, bool refine, cudaStream_t s);
 void realize32Group(const KArgs& a, bool refine, cudaStream_t s);
 void minv32Chain(const KArgs& a, cudaStream_t s);
 void minv32Group(const KArgs& a, cudaStream_t s);

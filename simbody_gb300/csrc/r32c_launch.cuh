@@ -4,7 +4,9 @@
 // variants: 1 = 128-thread blocks with every register the code wants; 4 =
 // 128-thread blocks, at most 128 registers (4 blocks per SM); 7 = 64-thread
 // blocks, at most 144 registers (7 blocks per SM), which keeps a batch of
-// 65,536 one-thread instances in a single balanced wave over 152 SMs.
+// 65,536 one-thread instances in a single balanced wave over 152 SMs; 8 =
+// 7 with the records staged through shared memory (k_r32s.cu), for a batch
+// of one shared chain topology without Free bodies.
 #pragma once
 #include "abi_device.cuh"
 
@@ -21,7 +23,7 @@ template <bool REF, int MINB, int BS> static void r32ChainGo(const KArgs& a, cud
 
 template <bool REF> static void r32ChainPick(const KArgs& a, cudaStream_t s) {
     if (a.P->variant == 4) r32ChainGo<REF, 4, 128>(a, s);
-    else if (a.P->variant == 7) r32ChainGo<REF, 7, 64>(a, s);
+    else if (a.P->variant >= 7) r32ChainGo<REF, 7, 64>(a, s);
     else r32ChainGo<REF, 1, 128>(a, s);
 }
 

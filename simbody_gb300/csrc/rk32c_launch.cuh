@@ -23,7 +23,7 @@ template <bool REF, int MINB, int BS> static void rk32ChainGo(const KArgs& a, cu
 
 template <bool REF> static void rk32ChainPick(const KArgs& a, cudaStream_t s) {
     if (a.P->variant == 4) rk32ChainGo<REF, 4, 128>(a, s);
-    else if (a.P->variant == 7) rk32ChainGo<REF, 7, 64>(a, s);
+    else if (a.P->variant >= 7) rk32ChainGo<REF, 7, 64>(a, s);  // 8: realize only
     else rk32ChainGo<REF, 1, 128>(a, s);
 }
 
