@@ -33,11 +33,12 @@ sys.path.insert(0, str(ROOT))
 
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
-# DRAM bytes (read + write) of one launch of the mixed realize kernel on the
-# 65,536-instance 32-Ball workload, from an ncu capture of that launch
+# DRAM bytes (read + write) of one launch of the mixed realize kernel (the
+# staged chain driver, kernel variant 8) on the 65,536-instance 32-Ball
+# workload, from an ncu capture of that launch
 # (profiles/realize_32ball_65536_ncu.md): the per-body scratch records
 # dominate it, against 235 MB of compulsory state I/O.
-TRAFFIC_BYTES_PER_LAUNCH = 1.807478e9 + 0.905554e9
+TRAFFIC_BYTES_PER_LAUNCH = 1.848917e9 + 0.893990e9
 FP32_LANES = 152 * 128  # SMs x FP32 lanes per SM
 
 
@@ -303,8 +304,11 @@ def cpu_trajectory_baseline(w, h, nsteps, seconds: float = 4.0, max_instances: i
 
 def trajectories():
     """Fixed-step RK-Merson throughput (body-steps/s) on the trajectory
-    workloads: the double pendulum (FP64), the random trees and the uneven
-    batch. The trees run in both precisions: the mixed form (FP32 recursions,
+    workloads: the double pendulum (FP64), the random trees, the uneven
+    batch, and the random trees with a contact sphere on every body over a
+    ground half-space (FP64: the mixed form takes contact instances through
+    FP64, the indentation being beyond FP32 kinematics). The trees run in
+    both precisions: the mixed form (FP32 recursions,
     FP64 state; steps whose RHS meets an ill-conditioned M taken in FP64) over
     the full horizon, FP64 over a shorter one for its rate. Beside them: the
     mixed form's state error after all steps against the FP64 engine on a
@@ -312,11 +316,15 @@ def trajectories():
     from simbody_gb300 import Workload, engine_batch
 
     out = {}
-    for cfg, n_inst, n_ref, fp64_steps in [(1, 1024, 0, 0), (3, 16384, 512, 400), (4, 10000, 256, 300)]:
+    for cfg, n_inst, n_ref, fp64_steps in [(1, 1024, 0, 0), (3, 16384, 512, 400), (4, 10000, 256, 300),
+                                           (8, 16384, 0, 400)]:
         w = Workload(cfg, n_inst)
-        rec = {"instances": w.ninst, "steps": w.nsteps, "h": w.h}
+        horizon = fp64_steps if cfg == 8 else w.nsteps
+        rec = {"instances": w.ninst, "steps": horizon, "h": w.h}
         body = int(w.nbodies().sum())
-        for prec, steps in ((("fp64", w.nsteps),) if cfg == 1 else (("mixed", w.nsteps), ("fp64", fp64_steps))):
+        runs = (("fp64", w.nsteps),) if cfg == 1 else (("fp64", fp64_steps),) if cfg == 8 else \
+            (("mixed", w.nsteps), ("fp64", fp64_steps))
+        for prec, steps in runs:
             b, y0 = engine_batch(w, prec)
             b.set_state(y0)
             time_rk(b, w.h, 2)  # warm-up (the first call tunes the launch)
@@ -333,7 +341,7 @@ def trajectories():
                 ymix = y
             rec[prec] = r
             b.close()
-        if cfg != 1:
+        if cfg in (3, 4):
             rec["mixed_over_fp64"] = rec["mixed"]["body_steps_per_s"] / rec["fp64"]["body_steps_per_s"]
         if n_ref:
             idx = np.arange(n_ref)
@@ -360,8 +368,8 @@ def trajectories():
                                             "fp64_from_1e-12_perturbed_start": {"median": float(np.median(pert)),
                                                                                 "max": float(pert.max())}}
             r.close()
-        rec["cpu_baseline"] = cpu_trajectory_baseline(w, w.h, w.nsteps)
-        out[{1: "double_pendulum", 3: "random_trees", 4: "uneven_batch"}[cfg]] = rec
+        rec["cpu_baseline"] = cpu_trajectory_baseline(w, w.h, horizon)
+        out[{1: "double_pendulum", 3: "random_trees", 4: "uneven_batch", 8: "contact_trees"}[cfg]] = rec
     out["random_trees_error_controlled"] = error_controlled()
     return out
 
