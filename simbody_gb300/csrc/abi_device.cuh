@@ -1280,7 +1280,8 @@ __device__ __forceinline__ int rhs(const DevTables& T, const Slot& s, R* scratch
         double* rec0 = scratch + T.sbase[s.inst];
         if constexpr (GROUP) {
             // tree passes on the group's lanes; the multiplier solve and the
-            // constraint sweeps (loop paths only) on its first lane
+            // constraint sweeps (loop paths only) on its first lane, the
+            // Gram columns on its first three
             // record-major rows (the first lane's serial loop work touches a
             // few records many times: they stay in L1)
             const ScrGen S{rec0, (int)T.sstride[s.inst], 1};
@@ -1288,7 +1289,8 @@ __device__ __forceinline__ int rhs(const DevTables& T, const Slot& s, R* scratch
             if (T.incons[s.inst] > 0) {
                 const LoopState L = loopStateRows(T, s.inst, rec0, nullptr, nullptr, nullptr, 0, 0);
                 int lst = 0;
-                if (s.gl == 0) lst = loopForwardDynamics<NM, true>(L, out);
+                if (s.G >= 3) lst = loopForwardDynamicsLanes<NM>(L, out, s.gl, s.mask);
+                else if (s.gl == 0) lst = loopForwardDynamics<NM, true>(L, out);
                 __syncwarp(s.mask);
                 lst = (int)__reduce_or_sync(s.mask, (unsigned)lst);
                 if (!(lst & SBG_INST_CHOLESKY_FAIL)) loopCorrectionOutRows<NM>(L, out, s.gl, s.G, s.mask);
@@ -1655,7 +1657,10 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
                 if (errNorm <= 16 * accuracy) {
                     const double quatNorm = nquat > 0 ? sqrt(squat / nquat) : 0.0;
                     int lst = 0;
-                    if (s.gl == 0) lst = loopProjectStep<NM>(loopState(), quatNorm, consTol, projLimit, pes);
+                    if (GROUP && s.G >= 3)
+                        lst = loopProjectStepLanes<NM>(loopState(), quatNorm, consTol, projLimit, pes, s.gl, s.mask);
+                    else if (s.gl == 0)
+                        lst = loopProjectStep<NM>(loopState(), quatNorm, consTol, projLimit, pes);
                     st |= loopLeaderOr(lst);
                 }
             }

@@ -609,6 +609,163 @@ __device__ __forceinline__ void loopSweep3(const LoopState& L, const Wt& wt) {
     }
 }
 
+// ----------------------------------------- one Gram column per group lane
+// The same sweep with lane k of a request's group (k < 3) taking column k
+// alone: column k's arithmetic and fields are those of the three-column
+// sweep, and no column reads another's fields, so the three lanes run side
+// by side with the three-column sweep's results bit for bit. An FP64 warp
+// instruction occupies the FP64 pipe alike for one active lane or for three,
+// so on the FP64-poor GB300 this cuts the Gram's time about threefold.
+template <int N, int KIND>
+__device__ __forceinline__ void loopIn1(const LoopState& L, int row, int rec, int n, int info, int k, V3d& zw, V3d& zv) {
+    const SC64& S = L.S;
+    const int eDI = kRecH + 7 * N, eG = eDI + N * N, eEps = eG + 6 * N;
+    const int fE = recEpsK(eEps, k);
+    if (info & F_LOOPBODY) {
+        const int sl = L.slot(row);
+        const V3d tw = ld3<double>(S, sl, slotF(k)), tv = ld3<double>(S, sl, slotF(k) + 3);
+        if (KIND == kMInvSweep) { zw = zw - tw; zv = zv - tv; }
+        else { zw = zw + tw; zv = zv + tv; }
+    }
+    V3d pw = zw, pv = zv;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        if (j < n) {
+            const V3d hw = ld3<double>(S, rec, kRecH + 6 * j), hv = ld3<double>(S, rec, kRecH + 6 * j + 3);
+            const double d = dot(hw, zw) + dot(hv, zv);
+            if (KIND == kMInvSweep) {
+                const V3d gw = ld3<double>(S, rec, eG + 6 * j), gv = ld3<double>(S, rec, eG + 6 * j + 3);
+                const double eps = -d;
+                S(rec, fE + j) = eps;
+                pw = axpy(pw, eps, gw);
+                pv = axpy(pv, eps, gv);
+            } else {
+                S(rec, fE + j) = d;
+            }
+        }
+    }
+    const V3d l = ld3<double>(S, rec, kRecL);
+    zw = pw + cross(l, pv);
+    zv = pv;
+}
+
+template <int N, int KIND>
+__device__ __forceinline__ void loopOut1(const LoopState& L, int rec, int n, bool hasParent, int k, V3d& Aw, V3d& Av) {
+    const SC64& S = L.S;
+    const int eDI = kRecH + 7 * N, eG = eDI + N * N, eEps = eG + 6 * N;
+    const int fE = recEpsK(eEps, k);
+    const V3d l = ld3<double>(S, rec, kRecL);
+    const V3d Apw = hasParent ? Aw : z3<double>();
+    const V3d Apv = hasParent ? Av + cross(Aw, l) : z3<double>();
+    double eps[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) eps[j] = j < n ? S(rec, fE + j) : 0.0;
+    Aw = Apw;
+    Av = Apv;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        if (i < n) {
+            const V3d hw = ld3<double>(S, rec, kRecH + 6 * i), hv = ld3<double>(S, rec, kRecH + 6 * i + 3);
+            double sv;
+            if (KIND == kMInvSweep) {
+                const V3d gw = ld3<double>(S, rec, eG + 6 * i), gv = ld3<double>(S, rec, eG + 6 * i + 3);
+                sv = 0.0;
+#pragma unroll
+                for (int c = 0; c < N; ++c)
+                    if (c < n) sv = sv + S(rec, eDI + i * N + c) * eps[c];
+                sv = sv - (dot(gw, Apw) + dot(gv, Apv));
+            } else {
+                sv = eps[i];
+            }
+            Aw = axpy(Aw, sv, hw);
+            Av = axpy(Av, sv, hv);
+        }
+    }
+}
+
+template <int KIND>
+__device__ __noinline__ void loopIn16(const LoopState& L, int row, int rec, int info, int k, V3d& zw, V3d& zv) {
+    loopIn1<6, KIND>(L, row, rec, 6, info, k, zw, zv);
+}
+template <int KIND>
+__device__ __noinline__ void loopOut16(const LoopState& L, int rec, bool hasParent, int k, V3d& Aw, V3d& Av) {
+    loopOut1<6, KIND>(L, rec, 6, hasParent, k, Aw, Av);
+}
+
+// Column k of the three-column sweep (loopSweep3), on one lane.
+template <int NM, int KIND, class Wt>
+__device__ __forceinline__ void loopSweepColumn(const LoopState& L, const Wt& wt, int k) {
+    const DevTables& T = L.T;
+    const SC64& S = L.S;
+    const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
+    const int fZ = recZaccK(k);
+    {
+        V3d cw = z3<double>(), cv = z3<double>();
+        bool have = false;
+        for (int lb = nb - 1; lb >= 0; --lb) {
+            const int row = body0 + lb;
+            const int info = T.info[row];
+            if (!(info & F_LOOPPATH)) {
+                have = false;
+                continue;
+            }
+            const int n = (info >> 4) & 15;
+            const int rec = L.rec(row);
+            V3d zw = z3<double>(), zv = z3<double>();
+            if (info & F_MEMCHILD) {
+                zw = ld3<double>(S, rec, fZ);
+                zv = ld3<double>(S, rec, fZ + 3);
+                st3<double>(S, rec, fZ, z3<double>());
+                st3<double>(S, rec, fZ + 3, z3<double>());
+            }
+            if (have) { zw = zw + cw; zv = zv + cv; }
+            if (n == 6) loopIn16<KIND>(L, row, rec, info, k, zw, zv);
+            else loopIn1<NM, KIND>(L, row, rec, n, info, k, zw, zv);
+            if (KIND == kJacSweep) {
+                const int fE = recEpsK(recEps(recN(n, NM)), k);
+                for (int j = 0; j < n; ++j) S(rec, fE + j) = S(rec, fE + j) * wt(row, j);
+            }
+            const int parent = T.parent[row];
+            have = (info & F_CARRY) != 0;
+            if (have) {
+                cw = zw;
+                cv = zv;
+            } else if (parent >= 0) {
+                const int pr = L.rec(body0 + parent);
+                st3<double>(S, pr, fZ, ld3<double>(S, pr, fZ) + zw);
+                st3<double>(S, pr, fZ + 3, ld3<double>(S, pr, fZ + 3) + zv);
+            }
+        }
+    }
+    {
+        V3d aw = z3<double>(), av = z3<double>();
+        for (int lb = 0; lb < nb; ++lb) {
+            const int row = body0 + lb;
+            const int info = T.info[row];
+            if (!(info & F_LOOPPATH)) continue;
+            const int n = (info >> 4) & 15;
+            const int rec = L.rec(row);
+            const int parent = T.parent[row];
+            const bool hp = parent >= 0;
+            V3d pw = aw, pv = av;
+            if (hp && !(info & F_CARRY)) {
+                const int pr = L.rec(body0 + parent);
+                pw = ld3<double>(S, pr, 6 * k);
+                pv = ld3<double>(S, pr, 6 * k + 3);
+            }
+            if (n == 6) loopOut16<KIND>(L, rec, hp, k, pw, pv);
+            else loopOut1<NM, KIND>(L, rec, n, hp, k, pw, pv);
+            if (info & F_LOOPBODY) {
+                st3<double>(S, L.slot(row), slotB(k), pw);
+                st3<double>(S, L.slot(row), slotB(k) + 3, pv);
+            }
+            if (info & F_MEMCHILD) { st3<double>(S, rec, 6 * k, pw); st3<double>(S, rec, 6 * k + 3, pv); }
+            aw = pw;
+            av = pv;
+        }
+    }
+}
+
 // Cholesky of the leading m x m block (row stride kMaxLoopEq), lower factor
 // in place; then the two triangular solves.
 __device__ __forceinline__ bool loopCholFactor(int m, double* A) {
@@ -667,6 +824,62 @@ __device__ __forceinline__ void loopGram(const LoopState& L, const Wt& wt, doubl
     }
 }
 
+// loopGram with lane k < 3 of the group (gl, mask: the lane's index in the
+// group and the group's lanes; absolute lane = the warp lane) sweeping
+// column k of every constraint. A is filled on the group's first lane only;
+// every lane of the group must call.
+template <int NM, int KIND, class Wt>
+__device__ __forceinline__ void loopGramLanes(const LoopState& L, const Wt& wt, double* A, int gl, unsigned mask) {
+    const DevTables& T = L.T;
+    const int nc = T.incons[L.inst];
+    const int base = (int)(threadIdx.x & 31) - gl;
+    const bool act = gl < 3;
+    const int k = act ? gl : 0;
+    if (act) {  // this column's accumulators held tree-pass values
+        const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
+        for (int lb = 0; lb < nb; ++lb) {
+            const int row = body0 + lb;
+            if ((T.info[row] & (F_MEMCHILD | F_LOOPPATH)) == (F_MEMCHILD | F_LOOPPATH)) {
+                st3<double>(L.S, L.rec(row), recZaccK(k), z3<double>());
+                st3<double>(L.S, L.rec(row), recZaccK(k) + 3, z3<double>());
+            }
+        }
+    }
+    for (int c = 0; c < nc; ++c) {
+        if (act) {
+            for (int c2 = 0; c2 < nc; ++c2) {
+                int s1, s2;
+                loopSlots(L, c2, s1, s2);
+                if (s1 >= 0) { st3<double>(L.S, s1, slotF(k), z3<double>()); st3<double>(L.S, s1, slotF(k) + 3, z3<double>()); }
+                if (s2 >= 0) { st3<double>(L.S, s2, slotF(k), z3<double>()); st3<double>(L.S, s2, slotF(k) + 3, z3<double>()); }
+            }
+            const LoopGeom Gc = loopGeom(L, c);
+            V3d e = z3<double>();
+            if (k == 0) e.x = 1.0; else if (k == 1) e.y = 1.0; else e.z = 1.0;
+            loopAddForceK(L.S, Gc.s2, Gc.r2, e, k);
+            loopAddForceK(L.S, Gc.s1, Gc.r1, -e, k);
+            loopSweepColumn<NM, KIND>(L, wt, k);
+        }
+        for (int i = 0; i < nc; ++i) {
+            V3d d = z3<double>();
+            if (act) {
+                const LoopGeom G = loopGeom(L, i);
+                d = slotPoint(L.S, G.s2, slotB(k), G.r2) - slotPoint(L.S, G.s1, slotB(k), G.r1);
+            }
+            const double v[3] = {d.x, d.y, d.z};
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                const double v1 = __shfl_sync(mask, v[r], base + 1), v2 = __shfl_sync(mask, v[r], base + 2);
+                if (gl == 0) {
+                    A[(3 * i + r) * kMaxLoopEq + 3 * c] = v[r];
+                    A[(3 * i + r) * kMaxLoopEq + 3 * c + 1] = v1;
+                    A[(3 * i + r) * kMaxLoopEq + 3 * c + 2] = v2;
+                }
+            }
+        }
+    }
+}
+
 // Loop forward dynamics after the tree RHS (which left the tree udot in out
 // and A_GB in the slots). Returns SBG_INST_* bits. With DEFER_OUT the
 // outward half of the final correction (udot -= M^-1 G^T lambda, every body)
@@ -702,6 +915,40 @@ __device__ __noinline__ int loopForwardDynamics(const LoopState& L, Out& out) {
             for (int i = 0; i < n; ++i) out.udot(uo + i, out.udotGet(uo + i) - ud[i]);
         });
     }
+    return 0;
+}
+
+// loopForwardDynamics<NM, true> on a group of at least three lanes, the Gram
+// columns spread over lanes 0-2 (loopGramLanes); the rest runs on the first
+// lane as before, with the same results bit for bit. Every lane of the group
+// calls; the status is the first lane's.
+template <int NM, class Out>
+__device__ __noinline__ int loopForwardDynamicsLanes(const LoopState& L, Out& out, int gl, unsigned mask) {
+    const DevTables& T = L.T;
+    const int inst = L.inst;
+    const SC64& S = L.S;
+    const int nc = T.incons[inst], m = 3 * nc;
+    double lam[kMaxLoopEq];
+    if (gl == 0) {
+        loopZeroAcc(L);
+        for (int c = 0; c < nc; ++c) {
+            const LoopGeom G = loopGeom(L, c);
+            const V3d aS = slotPoint(S, G.s2, kSlotA, G.r2) + slotCentripetal(S, G.s2, G.r2);
+            const V3d aC = slotPoint(S, G.s1, kSlotA, G.r1) + slotCentripetal(S, G.s1, G.r1);
+            const V3d d = aS - aC;
+            lam[3 * c] = d.x; lam[3 * c + 1] = d.y; lam[3 * c + 2] = d.z;
+        }
+    }
+    __syncwarp(mask);
+    double A[kMaxLoopEq * kMaxLoopEq];
+    auto one = [](int, int) { return 1.0; };
+    loopGramLanes<NM, kMInvSweep>(L, one, A, gl, mask);
+    if (gl != 0) return 0;
+    if (!loopCholFactor(m, A)) return SBG_INST_CHOLESKY_FAIL;
+    loopCholSolve(m, A, lam);
+    loopClearForces(L);
+    for (int c = 0; c < nc; ++c) loopAddConstraintForce(L, loopGeom(L, c), mk3(lam[3 * c], lam[3 * c + 1], lam[3 * c + 2]));
+    loopSweepIn<NM, kMInvSweep>(L, one);
     return 0;
 }
 
@@ -915,6 +1162,204 @@ __device__ __noinline__ bool loopProjectU(const LoopState& L, double tol, bool f
         return false;
     }
     return true;
+}
+
+// ------------------------------- projections with the Gram over the lanes
+// loopProjectQ / loopProjectU / loopProjectStep for a group of at least three
+// lanes: the Gram (loopGramLanes) on lanes 0-2, everything else on the first
+// lane, whose decisions (norms, failures) every lane takes by shuffle so that
+// all of them run the same iterations. Same results bit for bit.
+__device__ __forceinline__ double laneBcast(double v, int base, unsigned mask) { return __shfl_sync(mask, v, base); }
+__device__ __forceinline__ int laneBcast(int v, int base, unsigned mask) { return __shfl_sync(mask, v, base); }
+
+template <int NM>
+__device__ __noinline__ bool loopProjectQLanes(const LoopState& L, double tol, bool localOnly, int gl, unsigned mask) {
+    const DevTables& T = L.T;
+    const int nq = T.inq[L.inst], m = 3 * T.incons[L.inst];
+    const int base = (int)(threadIdx.x & 31) - gl;
+    const bool lead = gl == 0;
+    double perr[kMaxLoopEq], A[kMaxLoopEq * kMaxLoopEq];
+    double normOnEntry = 0;
+    if (lead) {
+        normOnEntry = loopPerr(L, perr);
+        for (int k = 0; k < nq; ++k) {
+            saveAt(L, k) = yAt(L, k);
+            deltaAt(L, k) = 0.0;  // rows off the loop paths never move
+        }
+    }
+    normOnEntry = laneBcast(normOnEntry, base, mask);
+    const double tryFor = loopTryFor(tol);
+    double achieved = normOnEntry, prev = normOnEntry;
+    int its = 0;
+    auto wq = [&](int row, int j) -> double {
+        const int type = T.info[row] & 15;
+        if ((type == T_BALL || type == T_FREE) && j < 3) {
+            const int qo = T.qoff[row];
+            const double q0 = yAt(L, qo), q1 = yAt(L, qo + 1), q2 = yAt(L, qo + 2), q3 = yAt(L, qo + 3);
+            return 4 * (q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
+        }
+        return 1.0;
+    };
+    do {
+        __syncwarp(mask);  // the first lane's q and kinematics, before the Gram reads them
+        loopGramLanes<NM, kJacSweep>(L, wq, A, gl, mask);
+        int fail = 0;
+        if (lead) {
+            if (!loopCholFactor(m, A)) {
+                fail = 1;
+            } else {
+                loopCholSolve(m, A, perr);
+                loopClearForces(L);
+                for (int c = 0; c < m / 3; ++c)
+                    loopAddConstraintForce(L, loopGeom(L, c), mk3(perr[3 * c], perr[3 * c + 1], perr[3 * c + 2]));
+                loopSweep<NM, kJacSweep>(L, wq, [&](int row, int n, const double* du) {
+                    const int type = T.info[row] & 15, qo = T.qoff[row];
+                    double dq[7];
+                    int nqb = n;
+                    if (type == T_BALL || type == T_FREE) {
+                        const double e0 = yAt(L, qo) / 2, e1 = yAt(L, qo + 1) / 2, e2 = yAt(L, qo + 2) / 2,
+                                     e3 = yAt(L, qo + 3) / 2;
+                        dq[0] = -e1 * du[0] - e2 * du[1] - e3 * du[2];
+                        dq[1] = e0 * du[0] + e3 * du[1] - e2 * du[2];
+                        dq[2] = -e3 * du[0] + e0 * du[1] + e1 * du[2];
+                        dq[3] = e2 * du[0] - e1 * du[1] + e0 * du[2];
+                        nqb = 4;
+                        if (type == T_FREE) { dq[4] = du[3]; dq[5] = du[4]; dq[6] = du[5]; nqb = 7; }
+                    } else {
+                        for (int j = 0; j < n; ++j) dq[j] = du[j];
+                    }
+                    for (int j = 0; j < nqb; ++j) {
+                        deltaAt(L, qo + j) = dq[j];
+                        yAt(L, qo + j) -= dq[j];
+                    }
+                });
+                loopKinematics<NM>(L);
+                achieved = loopPerr(L, perr);
+            }
+        }
+        if (laneBcast(fail, base, mask)) return false;
+        achieved = laneBcast(achieved, base, mask);
+        ++its;
+        if (localOnly && its >= 2 && achieved > prev) {
+            if (lead) {
+                for (int k = 0; k < nq; ++k) yAt(L, k) += deltaAt(L, k);
+                loopKinematics<NM>(L);
+                achieved = loopPerr(L, perr);
+            }
+            achieved = laneBcast(achieved, base, mask);
+            break;
+        }
+        prev = achieved;
+    } while (achieved > tryFor && its < 20);
+    if (achieved > tol) {
+        if (lead && achieved >= normOnEntry) {
+            for (int k = 0; k < nq; ++k) yAt(L, k) = saveAt(L, k);
+            loopKinematics<NM>(L);
+        }
+        return false;
+    }
+    if (lead) {
+        loopNormalizeQuats(L);
+        loopKinematics<NM>(L);
+    }
+    return true;
+}
+
+template <int NM>
+__device__ __noinline__ bool loopProjectULanes(const LoopState& L, double tol, bool force, double limit, bool localOnly,
+                                               int gl, unsigned mask) {
+    const DevTables& T = L.T;
+    const int nq = T.inq[L.inst], nu = T.inu[L.inst], m = 3 * T.incons[L.inst];
+    const int base = (int)(threadIdx.x & 31) - gl;
+    const bool lead = gl == 0;
+    double verr[kMaxLoopEq], A[kMaxLoopEq * kMaxLoopEq];
+    double normOnEntry = 0;
+    if (lead) {
+        loopKinematics<NM>(L);
+        normOnEntry = loopVerr(L, verr);
+    }
+    normOnEntry = laneBcast(normOnEntry, base, mask);
+    if (normOnEntry > limit) return false;
+    if (normOnEntry == 0 || (normOnEntry <= tol && !force)) return true;
+    if (lead)
+        for (int k = 0; k < nu; ++k) {
+            saveAt(L, nq + k) = yAt(L, nq + k);
+            deltaAt(L, nq + k) = 0.0;  // rows off the loop paths never move
+        }
+    __syncwarp(mask);  // the saved u, before the Gram's weights read it
+    auto wu = [&](int row, int j) -> double {
+        const double a = fabs(saveAt(L, nq + T.uoff[row] + j));
+        const double e = a > 1 ? a : 1.0;
+        return e * e;
+    };
+    loopGramLanes<NM, kJacSweep>(L, wu, A, gl, mask);
+    int fail = lead ? (loopCholFactor(m, A) ? 0 : 1) : 0;
+    if (laneBcast(fail, base, mask)) return false;
+    const double tryFor = loopTryFor(tol);
+    double achieved = normOnEntry, prev = normOnEntry;
+    int its = 0;
+    do {
+        if (lead) {
+            loopCholSolve(m, A, verr);
+            loopClearForces(L);
+            for (int c = 0; c < m / 3; ++c)
+                loopAddConstraintForce(L, loopGeom(L, c), mk3(verr[3 * c], verr[3 * c + 1], verr[3 * c + 2]));
+            loopSweep<NM, kJacSweep>(L, wu, [&](int row, int n, const double* du) {
+                const int uo = nq + T.uoff[row];
+                for (int j = 0; j < n; ++j) {
+                    deltaAt(L, uo + j) = du[j];
+                    yAt(L, uo + j) -= du[j];
+                }
+            });
+            loopKinematics<NM>(L);
+            achieved = loopVerr(L, verr);
+        }
+        achieved = laneBcast(achieved, base, mask);
+        ++its;
+        if (localOnly && its >= 2 && achieved > prev) {
+            if (lead) {
+                for (int k = 0; k < nu; ++k) yAt(L, nq + k) += deltaAt(L, nq + k);
+                loopKinematics<NM>(L);
+                achieved = loopVerr(L, verr);
+            }
+            achieved = laneBcast(achieved, base, mask);
+            break;
+        }
+        prev = achieved;
+    } while (achieved > tryFor && its < 7);
+    if (achieved > tol) {
+        if (lead && achieved >= normOnEntry)
+            for (int k = 0; k < nu; ++k) yAt(L, nq + k) = saveAt(L, nq + k);
+        return false;
+    }
+    return true;
+}
+
+template <int NM>
+__device__ __noinline__ int loopProjectStepLanes(const LoopState& L, double quatNorm, double tol, double limit, bool force,
+                                                 int gl, unsigned mask) {
+    const int base = (int)(threadIdx.x & 31) - gl;
+    const bool lead = gl == 0;
+    double perr[kMaxLoopEq];
+    double perrNorm = 0;
+    if (lead) {
+        loopZeroAcc(L);
+        loopKinematics<NM>(L);
+        perrNorm = loopPerr(L, perr);
+    }
+    perrNorm = laneBcast(perrNorm, base, mask);
+    const double normOnEntry = fmax(perrNorm, quatNorm);
+    bool ok = true;
+    if (normOnEntry > limit) {
+        ok = false;
+    } else if (perrNorm == 0 || (perrNorm <= tol && !force)) {
+        if (lead && (quatNorm > tol || force)) loopNormalizeQuats(L);
+    } else {
+        ok = loopProjectQLanes<NM>(L, tol, true, gl, mask);
+    }
+    __syncwarp(mask);
+    if (ok) ok = loopProjectULanes<NM>(L, tol, force, limit, true, gl, mask);
+    return ok ? 0 : SBG_INST_PROJECTION_FAILED;
 }
 
 // Integrator::initialize: ProjectOptions::ForceProjection, no projection

@@ -142,3 +142,25 @@ def test_failed_mixed_request_is_rerun_in_fp64(engine, w5, topos):
     assert ib["attempts"] == 2 and ib["status"] & N.INST_NONFINITE
     assert io["attempts"] == 1 and io["status"] == 0 and np.isfinite(yo).all()
     assert srv.stats()["submitted"] == 2
+
+
+def test_loop_requests_with_tight_tolerance_match_batch_integration(engine, w5, topos):
+    """A constraint tolerance of 1e-9 makes the position and velocity
+    projections run at every step. In the server they spread the Gram over
+    the request's first three lanes; the batch path runs them on one thread.
+    Both integrate to the same states (1e-10)."""
+    loops = [i for i in range(NREQ) if w5.systems[int(w5.instance_system[i])].nconstraints > 0][:4]
+    assert loops
+    srv = Server("fp64", device_budget_bytes=1 << 30, chunk_steps=16)
+    ids = {i: srv.submit(topos[i], w5.y0[w5.instance_slice(i)], w5.h, 60, constraint_tolerance=1e-9) for i in loops}
+    srv.drain()
+    for i in loops:
+        y, inf = srv.result(ids[i])
+        b, y0 = engine_batch(w5, "fp64", instances=[i])
+        b.set_state(y0)
+        st = b.rk_merson_fixed(w5.h, 60, constraint_tolerance=1e-9)
+        yb, _ = b.get_state()
+        assert st[0] == 0 and inf["status"] == 0
+        err = np.linalg.norm(y - yb) / np.linalg.norm(yb)
+        assert err <= 1e-10, (i, err)
+    srv.close()
