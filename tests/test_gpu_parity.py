@@ -145,6 +145,16 @@ def test_pipelined_host_realize_equals_separate_calls(engine, precision):
     sp = torch.empty(b.ninst, dtype=torch.int32).pin_memory().numpy()
     got1, st1 = b.realize_acceleration_from(yp, dp, sp)
     assert (st1 == 0).all() and np.array_equal(got1, ref1)
+    # the same buffers again: from the second such call on, the call replays
+    # a captured graph, which must read the buffers' new contents each time
+    for k, (yin, want) in enumerate([(y0, ref), (y1, ref1), (y0, ref)]):
+        yp[:] = yin
+        got2, st2 = b.realize_acceleration_from(yp, dp, sp)
+        assert (st2 == 0).all() and np.array_equal(got2, want), k
+    # pageable buffers go through the batch's own staging: the same holds
+    for yin, want in [(y1, ref1), (y0, ref), (y1, ref1)]:
+        got3, _ = b.realize_acceleration_from(yin.copy())
+        assert np.array_equal(got3, want)
 
 
 def test_full_size_ball_chain_fp64_matches_oracle(engine):
