@@ -518,8 +518,10 @@ int sbg_serve_simulate(int32_t n, const int64_t* units, const int32_t* horizons,
  * set-up: it looks up the arrays' device addresses (cudaGetSymbolAddress), and
  * with CUDA's lazy module loading that is also when the driver loads this
  * module and creates its fixed arrays (about 16.3 MiB), so that first call can
- * fail with SBG_ERR_CUDA if the device has no memory left. Make it at start-up,
- * before any stream capture; later calls allocate nothing. All calls share
+ * fail with SBG_ERR_CUDA if the device has no memory left. Make it at start-up;
+ * later calls allocate nothing. Each call uploads the topology tables from
+ * host memory that ends with the call, so a call on a stream that is being
+ * captured returns SBG_ERR_UNSUPPORTED. All calls share
  * the arrays, which keep the last call's contents: calls that overlap on the
  * GPU race. Message of the last failure: sbg_noalloc_last_error(). */
 int sbg_realize_acceleration_noalloc(sbg_topology topology, int32_t ninstances,

@@ -147,6 +147,16 @@ int sbg_realize_acceleration_noalloc(sbg_topology topo, int32_t ninst, const dou
                                            " bytes of scratch, above the no-alloc capacity of " +
                                            std::to_string(kNoAllocScratchBytes) + " bytes");
     if (ninst == 0) return SBG_OK;
+    {   // the per-call table uploads read host memory that ends with the call:
+        // a capturing stream would record copies that replay from freed memory
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cs) != cudaSuccess) {
+            cudaGetLastError();
+            return naFail(SBG_ERR_CUDA, "cudaStreamIsCapturing failed");
+        }
+        if (cs != cudaStreamCaptureStatusNone)
+            return naFail(SBG_ERR_UNSUPPORTED, "the no-alloc realize cannot run on a capturing stream");
+    }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess || dev < 0 || dev >= 64) return naFail(SBG_ERR_CUDA, "no current CUDA device");

@@ -133,3 +133,32 @@ def test_noalloc_rejects_oversized_topology(engine):
                                               C.c_void_p(st.data_ptr()), None)
     assert rc == 1
     assert b"at most 256" in lib.sbg_noalloc_last_error()
+
+
+def test_noalloc_refuses_a_capturing_stream(engine):
+    """Its table uploads read host memory that ends with the call, so on a
+    stream that is being captured it returns SBG_ERR_UNSUPPORTED before it
+    enqueues anything, and the capture stays valid."""
+    torch = pytest.importorskip("torch")
+    w = Workload(2, 64)
+    topo = Topology(w.systems[0], keepalive=w)
+    ny = w.y0.size // w.ninst
+    y = torch.from_numpy(w.y0.copy()).cuda()
+    ydot = torch.zeros(w.ninst * ny, dtype=torch.float64, device="cuda")
+    st = torch.zeros(w.ninst, dtype=torch.int32, device="cuda")
+    _noalloc(topo, w.ninst, w.y0.copy())  # the first call's set-up, outside any capture
+    lib = N.engine_lib()
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    x = torch.zeros(4, device="cuda")
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=s):
+        rc = lib.sbg_realize_acceleration_noalloc(topo.handle, w.ninst, C.c_void_p(y.data_ptr()),
+                                                  C.c_void_p(ydot.data_ptr()), C.c_void_p(st.data_ptr()),
+                                                  C.c_void_p(s.cuda_stream))
+        x += 1
+    assert rc == 6, rc  # SBG_ERR_UNSUPPORTED
+    assert b"capturing" in lib.sbg_noalloc_last_error()
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(x[0]) == 2.0  # the capture held the other work
