@@ -72,9 +72,10 @@ typedef enum sbg_mobilizer {
     SBG_TRANSLATION = 6,
     SBG_CYLINDER = 7,
     SBG_PLANAR = 8,
-    SBG_BUSHING = 9
+    SBG_BUSHING = 9,
+    SBG_WELD = 10               /* no mobilities: X_FM = identity (RigidBodyNode_Weld.cpp:369-470) */
 } sbg_mobilizer;
-#define SBG_NUM_MOBILIZERS 10
+#define SBG_NUM_MOBILIZERS 11
 
 /* sbg_system_desc.flags */
 #define SBG_SYSTEM_EULER_ANGLES 1  /* SimbodyMatterSubsystem::setUseEulerAngles(true) */

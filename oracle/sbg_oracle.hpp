@@ -200,8 +200,8 @@ struct Topology {
 };
 
 // q and u counts per mobilizer (quaternion mode for Ball and Free)
-inline int mobNQ(int t) { static const int n[10] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6}; return n[t]; }
-inline int mobNU(int t) { static const int n[10] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6}; return n[t]; }
+inline int mobNQ(int t) { static const int n[11] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6, 0}; return n[t]; }
+inline int mobNU(int t) { static const int n[11] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6, 0}; return n[t]; }
 
 // Node creation and slot assignment (SimbodyMatterSubsystemRep.cpp:256-330,
 // RigidBodyNodeSpec.h:76-86): q/u slots consecutive in body order.

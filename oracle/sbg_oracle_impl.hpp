@@ -118,6 +118,9 @@ template <class R> void realizePosition(const Topology& t, const R* q, Work<R>& 
             for (int j = 0; j < 6; ++j) { c.HFw[j] = zero3<R>(); c.HFv[j] = zero3<R>(); }
             c.p_FM = zero3<R>();
             switch (b.type) {
+            case SBG_WELD:  // RigidBodyNode_Weld.cpp:389-396: X_FM = identity, no q
+                c.R_FM = ident33<R>();
+                break;
             case SBG_PIN: {  // RigidBodyNodeSpec_Pin.h:103-131; Rotation.h:210-213
                 const R cq = cos(qb[0]), sq = sin(qb[0]);
                 c.R_FM = ident33<R>();

@@ -12,11 +12,11 @@ BUILD = PKG / "_build"
 
 # ----------------------------------------------------------------- structs
 (SBG_PIN, SBG_SLIDER, SBG_UNIVERSAL, SBG_BALL, SBG_FREE, SBG_GIMBAL, SBG_TRANSLATION, SBG_CYLINDER, SBG_PLANAR,
- SBG_BUSHING) = range(10)
+ SBG_BUSHING, SBG_WELD) = range(11)
 NQ = {SBG_PIN: 1, SBG_SLIDER: 1, SBG_UNIVERSAL: 2, SBG_BALL: 4, SBG_FREE: 7, SBG_GIMBAL: 3, SBG_TRANSLATION: 3,
-      SBG_CYLINDER: 2, SBG_PLANAR: 3, SBG_BUSHING: 6}
+      SBG_CYLINDER: 2, SBG_PLANAR: 3, SBG_BUSHING: 6, SBG_WELD: 0}
 NU = {SBG_PIN: 1, SBG_SLIDER: 1, SBG_UNIVERSAL: 2, SBG_BALL: 3, SBG_FREE: 6, SBG_GIMBAL: 3, SBG_TRANSLATION: 3,
-      SBG_CYLINDER: 2, SBG_PLANAR: 3, SBG_BUSHING: 6}
+      SBG_CYLINDER: 2, SBG_PLANAR: 3, SBG_BUSHING: 6, SBG_WELD: 0}
 SYSTEM_EULER_ANGLES = 1
 PRECISION_FP64, PRECISION_MIXED, PRECISION_MIXED_FAST = 0, 1, 2
 

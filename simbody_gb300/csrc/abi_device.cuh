@@ -45,7 +45,7 @@
 namespace sbg {
 
 enum { T_PIN = 0, T_SLIDER = 1, T_UNIV = 2, T_BALL = 3, T_FREE = 4, T_GIMBAL = 5, T_TRANSL = 6, T_CYL = 7,
-       T_PLANAR = 8, T_BUSHING = 9 };
+       T_PLANAR = 8, T_BUSHING = 9, T_WELD = 10 };
 
 // Scratch accessors: S(rec, f) is element f of the record at rec.
 template <class R> struct ScrTiled {
@@ -266,6 +266,8 @@ __device__ __forceinline__ Kin<R> body1(const DevTables& T, int row, int rec, co
     XYZ<R> ea{R(1), R(1), R(0), R(0), R(1)};  // body-fixed X-Y-Z angles
     const bool quat = (info & F_QUAT) != 0;
     switch (type) {
+    case T_WELD:  // RigidBodyNode_Weld.cpp:389-396: X_FM = identity, no q
+        break;
     case T_GIMBAL:   // RigidBodyNodeSpec_Gimbal.h: calcX_FM, u = qdot
     case T_BUSHING:  // RigidBodyNodeSpec_Bushing.h: angles then p_FM, u = qdot
         ea = bodyXYZ<R>(q, RFM);
@@ -417,6 +419,8 @@ __device__ __forceinline__ Kin<R> body1(const DevTables& T, int row, int rec, co
         putH(1, mul(RGF, y1), mul(RGF, -cross(r, y1)));
         wFM = axpy(mk3(u[0], R(0), R(0)), u[1], y1);
         hdw = u[1] * cross(wFM, y1);
+        break;
+    case T_WELD:  // no mobilities: V_PB_G = VD_PB_G = 0 (RigidBodyNode_Weld.cpp:378-386)
         break;
     default:
         putH(0, col(RGF, 0), mul(RGF, nrx));

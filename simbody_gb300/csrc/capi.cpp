@@ -38,8 +38,8 @@ int cudaFail(cudaError_t e, const char* what) {
 // q and u slots per mobilizer (sbg_mobilizer order). Ball and Free keep 4
 // and 7 q slots in Euler-angle mode too, the last one unused, as Simbody's
 // State does (RigidBodyNodeSpec_Ball.h:393-395).
-const int kNQ[SBG_NUM_MOBILIZERS] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6};
-const int kNU[SBG_NUM_MOBILIZERS] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6};
+const int kNQ[SBG_NUM_MOBILIZERS] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6, 0};
+const int kNU[SBG_NUM_MOBILIZERS] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6, 0};
 
 // Host buffers the caller allocated page-locked (cudaMallocHost,
 // cudaHostRegister, a pinned torch tensor) are copied to and from directly;

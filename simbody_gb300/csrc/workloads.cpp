@@ -21,7 +21,7 @@
 //     20% with 1..4 Constraint::Ball closures to Ground, assembled at t = 0.
 // Test workloads of the wider mobilizer set (no benchmark counterpart):
 //  6  random trees as 3 whose children are uniform over Pin, Slider,
-//     Universal, Ball, Gimbal, Translation, Cylinder, Planar and Bushing, the
+//     Universal, Ball, Gimbal, Translation, Cylinder, Planar, Bushing and Weld, the
 //     root a Free body (even instances) or a Bushing (odd ones); angles
 //     U[-0.5,0.5], displacements U[-0.05,0.05].
 //  7  random trees as 3 in Euler-angle mode (SBG_SYSTEM_EULER_ANGLES): Ball
@@ -76,8 +76,8 @@ void setIdentity(double* X) {
     X[0] = X[4] = X[8] = 1;
 }
 
-int nq_of(int t) { static const int n[10] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6}; return n[t]; }
-int nu_of(int t) { static const int n[10] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6}; return n[t]; }
+int nq_of(int t) { static const int n[11] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6, 0}; return n[t]; }
+int nu_of(int t) { static const int n[11] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6, 0}; return n[t]; }
 
 sbg_body_desc makeBody(int parent, int mob, double m, const double G[6], const double pPF[3], const double pBM[3]) {
     sbg_body_desc b;
@@ -110,15 +110,15 @@ void randomUnitQuat(std::mt19937_64& r, double* q) {
     for (int k = 0; k < 4; ++k) q[k] /= n;
 }
 
-// Random tree (workloads 3-7) and its initial state. wide: children over
-// all nine non-Free mobilizers and rootType for the root (workload 6);
+// Random tree (workloads 3-8) and its initial state. wide: children over
+// all ten non-Free mobilizers and rootType for the root (workload 6);
 // euler: Ball and Free bodies with body-fixed X-Y-Z angles (workload 7).
 // Workloads 3-5 (wide = euler = false) draw exactly the stream they always did.
 void randomTree(std::mt19937_64& r, int nb, Sys& s, std::vector<double>& y, bool wide = false,
                 int rootType = SBG_FREE, bool euler = false) {
-    static const int kWide[9] = {SBG_PIN, SBG_SLIDER, SBG_UNIVERSAL, SBG_BALL, SBG_GIMBAL, SBG_TRANSLATION,
-                                 SBG_CYLINDER, SBG_PLANAR, SBG_BUSHING};
-    std::uniform_int_distribution<int> typeD(0, wide ? 8 : 3);
+    static const int kWide[10] = {SBG_PIN, SBG_SLIDER, SBG_UNIVERSAL, SBG_BALL, SBG_GIMBAL, SBG_TRANSLATION,
+                                  SBG_CYLINDER, SBG_PLANAR, SBG_BUSHING, SBG_WELD};
+    std::uniform_int_distribution<int> typeD(0, wide ? 9 : 3);
     std::lognormal_distribution<double> LN(0, 0.5);
     std::uniform_real_distribution<double> US(0.05, 0.3), UK(10, 100), UC(0.1, 1), UP(-0.1, 0.1);
     std::uniform_real_distribution<double> UA(-0.5, 0.5), UL(-0.05, 0.05);
@@ -165,6 +165,8 @@ void randomTree(std::mt19937_64& r, int nb, Sys& s, std::vector<double>& y, bool
             q.push_back(UA(r)); q.push_back(UL(r));
         } else if (mob == SBG_PLANAR) {
             q.push_back(UA(r)); q.push_back(UL(r)); q.push_back(UL(r));
+        } else if (mob == SBG_WELD) {
+            // no coordinates
         } else {
             double qq[4];
             randomUnitQuat(r, qq);

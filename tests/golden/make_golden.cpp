@@ -86,6 +86,7 @@ struct Model {
             case SBG_CYLINDER: mobods.push_back(MobilizedBody::Cylinder(P, X_PF, body, X_BM)); break;
             case SBG_PLANAR: mobods.push_back(MobilizedBody::Planar(P, X_PF, body, X_BM)); break;
             case SBG_BUSHING: mobods.push_back(MobilizedBody::Bushing(P, X_PF, body, X_BM)); break;
+            case SBG_WELD: mobods.push_back(MobilizedBody::Weld(P, X_PF, body, X_BM)); break;
             default: mobods.push_back(MobilizedBody::Free(P, X_PF, body, X_BM)); break;
             }
         }
