@@ -73,9 +73,11 @@ typedef enum sbg_mobilizer {
     SBG_CYLINDER = 7,
     SBG_PLANAR = 8,
     SBG_BUSHING = 9,
-    SBG_WELD = 10               /* no mobilities: X_FM = identity (RigidBodyNode_Weld.cpp:369-470) */
+    SBG_WELD = 10,              /* no mobilities: X_FM = identity (RigidBodyNode_Weld.cpp:369-470) */
+    SBG_SCREW = 11              /* 1: rotation q about Fz with translation pitch*q along it
+                                   (RigidBodyNodeSpec_Screw.h:121-140) */
 } sbg_mobilizer;
-#define SBG_NUM_MOBILIZERS 11
+#define SBG_NUM_MOBILIZERS 12
 
 /* sbg_system_desc.flags */
 #define SBG_SYSTEM_EULER_ANGLES 1  /* SimbodyMatterSubsystem::setUseEulerAngles(true) */
@@ -119,6 +121,7 @@ typedef struct sbg_body_desc {
     double  unit_inertia[6];    /* xx yy zz xy xz yz */
     double  X_PF[12];           /* inboard frame F on parent P */
     double  X_BM[12];           /* outboard frame M on body B */
+    double  pitch;              /* SBG_SCREW: translation along Fz per radian about Fz (else unused) */
 } sbg_body_desc;
 
 /* Mobility force elements, applied in array order (Force.cpp:339-351, 434-443).

@@ -42,6 +42,7 @@ bool buildTopology(const sbg_system_desc& d, Topology& t, const char** err) {
         b.level = t.b[b.parent].level + 1;
         t.b[b.parent].children.push_back(i);
         b.mass = bd.mass;
+        b.pitch = bd.pitch;
         for (int k = 0; k < 3; ++k) b.com[k] = bd.com[k];
         for (int k = 0; k < 6; ++k) b.G[k] = bd.unit_inertia[k];
         for (int k = 0; k < 9; ++k) b.RPF[k] = bd.X_PF[k];

@@ -186,6 +186,7 @@ struct Body {
     std::vector<int> children;
     double mass = 0, com[3] = {0, 0, 0}, G[6] = {0, 0, 0, 0, 0, 0};  // unit inertia xx yy zz xy xz yz
     double RPF[9], pPF[3], RMB[9], pMB[3];                               // X_PF and X_MB = ~X_BM
+    double pitch = 0;                                                    // Screw
 };
 
 struct Topology {
@@ -200,8 +201,8 @@ struct Topology {
 };
 
 // q and u counts per mobilizer (quaternion mode for Ball and Free)
-inline int mobNQ(int t) { static const int n[11] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6, 0}; return n[t]; }
-inline int mobNU(int t) { static const int n[11] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6, 0}; return n[t]; }
+inline int mobNQ(int t) { static const int n[12] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6, 0, 1}; return n[t]; }
+inline int mobNU(int t) { static const int n[12] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6, 0, 1}; return n[t]; }
 
 // Node creation and slot assignment (SimbodyMatterSubsystemRep.cpp:256-330,
 // RigidBodyNodeSpec.h:76-86): q/u slots consecutive in body order.

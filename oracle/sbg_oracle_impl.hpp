@@ -121,6 +121,15 @@ template <class R> void realizePosition(const Topology& t, const R* q, Work<R>& 
             case SBG_WELD:  // RigidBodyNode_Weld.cpp:389-396: X_FM = identity, no q
                 c.R_FM = ident33<R>();
                 break;
+            case SBG_SCREW: {  // RigidBodyNodeSpec_Screw.h:121-140: about Fz, p_FM = (0, 0, q pitch)
+                const R cq = cos(qb[0]), sq = sin(qb[0]);
+                c.R_FM = ident33<R>();
+                c.R_FM(0, 0) = cq; c.R_FM(1, 1) = cq; c.R_FM(1, 0) = sq; c.R_FM(0, 1) = -sq;
+                c.p_FM = v3<R>(R(0), R(0), qb[0] * R(b.pitch));
+                c.HFw[0] = v3<R>(R(0), R(0), R(1));
+                c.HFv[0] = v3<R>(R(0), R(0), R(b.pitch));
+                break;
+            }
             case SBG_PIN: {  // RigidBodyNodeSpec_Pin.h:103-131; Rotation.h:210-213
                 const R cq = cos(qb[0]), sq = sin(qb[0]);
                 c.R_FM = ident33<R>();

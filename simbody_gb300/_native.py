@@ -12,11 +12,11 @@ BUILD = PKG / "_build"
 
 # ----------------------------------------------------------------- structs
 (SBG_PIN, SBG_SLIDER, SBG_UNIVERSAL, SBG_BALL, SBG_FREE, SBG_GIMBAL, SBG_TRANSLATION, SBG_CYLINDER, SBG_PLANAR,
- SBG_BUSHING, SBG_WELD) = range(11)
+ SBG_BUSHING, SBG_WELD, SBG_SCREW) = range(12)
 NQ = {SBG_PIN: 1, SBG_SLIDER: 1, SBG_UNIVERSAL: 2, SBG_BALL: 4, SBG_FREE: 7, SBG_GIMBAL: 3, SBG_TRANSLATION: 3,
-      SBG_CYLINDER: 2, SBG_PLANAR: 3, SBG_BUSHING: 6, SBG_WELD: 0}
+      SBG_CYLINDER: 2, SBG_PLANAR: 3, SBG_BUSHING: 6, SBG_WELD: 0, SBG_SCREW: 1}
 NU = {SBG_PIN: 1, SBG_SLIDER: 1, SBG_UNIVERSAL: 2, SBG_BALL: 3, SBG_FREE: 6, SBG_GIMBAL: 3, SBG_TRANSLATION: 3,
-      SBG_CYLINDER: 2, SBG_PLANAR: 3, SBG_BUSHING: 6, SBG_WELD: 0}
+      SBG_CYLINDER: 2, SBG_PLANAR: 3, SBG_BUSHING: 6, SBG_WELD: 0, SBG_SCREW: 1}
 SYSTEM_EULER_ANGLES = 1
 PRECISION_FP64, PRECISION_MIXED, PRECISION_MIXED_FAST = 0, 1, 2
 
@@ -35,7 +35,7 @@ STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "BUDGET", 5: "S
 class BodyDesc(C.Structure):
     _fields_ = [("parent", C.c_int32), ("mobilizer", C.c_int32), ("mass", C.c_double),
                 ("com", C.c_double * 3), ("unit_inertia", C.c_double * 6),
-                ("X_PF", C.c_double * 12), ("X_BM", C.c_double * 12)]
+                ("X_PF", C.c_double * 12), ("X_BM", C.c_double * 12), ("pitch", C.c_double)]
 
 
 class MobilityForceDesc(C.Structure):
@@ -99,7 +99,7 @@ class ServerStats(C.Structure):
                 ("gpu_seconds", C.c_double), ("host_seconds", C.c_double)]
 
 
-assert C.sizeof(BodyDesc) == 280 and C.sizeof(MobilityForceDesc) == 32
+assert C.sizeof(BodyDesc) == 288 and C.sizeof(MobilityForceDesc) == 32
 assert C.sizeof(BallConstraintDesc) == 56 and C.sizeof(SystemDesc) == 80 and C.sizeof(ContactDesc) == 208
 
 P = C.POINTER

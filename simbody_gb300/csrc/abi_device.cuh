@@ -45,7 +45,7 @@
 namespace sbg {
 
 enum { T_PIN = 0, T_SLIDER = 1, T_UNIV = 2, T_BALL = 3, T_FREE = 4, T_GIMBAL = 5, T_TRANSL = 6, T_CYL = 7,
-       T_PLANAR = 8, T_BUSHING = 9, T_WELD = 10 };
+       T_PLANAR = 8, T_BUSHING = 9, T_WELD = 10, T_SCREW = 11 };
 
 // Scratch accessors: S(rec, f) is element f of the record at rec.
 template <class R> struct ScrTiled {
@@ -287,10 +287,12 @@ __device__ __forceinline__ Kin<R> body1(const DevTables& T, int row, int rec, co
         for (int j = 0; j < n; ++j) out.qdot(qo + j, u[j]);
         break;
     }
-    case T_PIN: {  // RigidBodyNodeSpec_Pin.h:103-122
+    case T_PIN:      // RigidBodyNodeSpec_Pin.h:103-122
+    case T_SCREW: {  // RigidBodyNodeSpec_Screw.h:121-132: about Fz, p_FM = (0, 0, q pitch)
         R s, c;
         sincosR(q[0], &s, &c);
         RFM.a[0] = c; RFM.a[1] = -s; RFM.a[3] = s; RFM.a[4] = c;
+        if (type == T_SCREW) pFM = mk3(R(0), R(0), q[0] * pr[34]);
         out.qdot(qo, u[0]);
         break;
     }
@@ -421,6 +423,10 @@ __device__ __forceinline__ Kin<R> body1(const DevTables& T, int row, int rec, co
         hdw = u[1] * cross(wFM, y1);
         break;
     case T_WELD:  // no mobilities: V_PB_G = VD_PB_G = 0 (RigidBodyNode_Weld.cpp:378-386)
+        break;
+    case T_SCREW:  // H_FM = [(0,0,1); (0,0,pitch)] (RigidBodyNodeSpec_Screw.h:134-140), constant in F
+        putH(0, col(RGF, 2), mul(RGF, mk3(R(0), R(0), pr[34]) + nrz));
+        wFM = mk3(R(0), R(0), u[0]);
         break;
     default:
         putH(0, col(RGF, 0), mul(RGF, nrx));

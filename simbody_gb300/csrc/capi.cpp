@@ -38,8 +38,8 @@ int cudaFail(cudaError_t e, const char* what) {
 // q and u slots per mobilizer (sbg_mobilizer order). Ball and Free keep 4
 // and 7 q slots in Euler-angle mode too, the last one unused, as Simbody's
 // State does (RigidBodyNodeSpec_Ball.h:393-395).
-const int kNQ[SBG_NUM_MOBILIZERS] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6, 0};
-const int kNU[SBG_NUM_MOBILIZERS] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6, 0};
+const int kNQ[SBG_NUM_MOBILIZERS] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6, 0, 1};
+const int kNU[SBG_NUM_MOBILIZERS] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6, 0, 1};
 
 // Host buffers the caller allocated page-locked (cudaMallocHost,
 // cudaHostRegister, a pinned torch tensor) are copied to and from directly;
@@ -397,7 +397,7 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
             c[19] = 2.0 / (3.0 * diss);
             t->kpar.insert(t->kpar.end(), c, c + kContactStride);
         }
-        // params: mass, com, G, R_PF, p_PF, R_MB = ~R_BM, p_MB = -(~R_BM p_BM)
+        // params: mass, com, G, R_PF, p_PF, R_MB = ~R_BM, p_MB = -(~R_BM p_BM), pitch
         double p[kParamStride];
         p[0] = b.mass;
         for (int k = 0; k < 3; ++k) p[1 + k] = b.com[k];
@@ -408,6 +408,7 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
             for (int c = 0; c < 3; ++c) p[22 + 3 * r2 + c] = b.X_BM[3 * c + r2];
         for (int r2 = 0; r2 < 3; ++r2)
             p[31 + r2] = -(p[22 + 3 * r2] * b.X_BM[9] + p[22 + 3 * r2 + 1] * b.X_BM[10] + p[22 + 3 * r2 + 2] * b.X_BM[11]);
+        p[34] = b.mobilizer == SBG_SCREW ? b.pitch : 0.0;
         t->par.insert(t->par.end(), p, p + kParamStride);
     }
     t->recSize = rec;

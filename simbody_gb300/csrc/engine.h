@@ -12,7 +12,8 @@
 //     fbeg/fcnt  mobility-force elements of this body, in application order
 //     par     kParamStride parameters per body (AoS): mass, com[3],
 //             unit inertia[6] (xx yy zz xy xz yz), R_PF[9], p_PF[3],
-//             R_MB[9], p_MB[3]; stored in FP64 and, for the mixed form, FP32.
+//             R_MB[9], p_MB[3], screw pitch; stored in FP64 and, for the
+//             mixed form, FP32.
 //   Instance table: first body row, body count, q/u sizes, addressing of its
 //   state column and scratch record, gravity index.
 //   State y, derivatives and scratch are "columns": element k of instance i
@@ -25,7 +26,7 @@
 
 namespace sbg {
 
-constexpr int kParamStride = 34;
+constexpr int kParamStride = 35;
 constexpr int kMaxDof = 6;
 
 // Scratch record of one body (elements of the arithmetic type R), n = ndof:

@@ -21,7 +21,8 @@
 //     20% with 1..4 Constraint::Ball closures to Ground, assembled at t = 0.
 // Test workloads of the wider mobilizer set (no benchmark counterpart):
 //  6  random trees as 3 whose children are uniform over Pin, Slider,
-//     Universal, Ball, Gimbal, Translation, Cylinder, Planar, Bushing and Weld, the
+//     Universal, Ball, Gimbal, Translation, Cylinder, Planar, Bushing, Weld and
+//     Screw (pitch U[-0.05,0.05]), the
 //     root a Free body (even instances) or a Bushing (odd ones); angles
 //     U[-0.5,0.5], displacements U[-0.05,0.05].
 //  7  random trees as 3 in Euler-angle mode (SBG_SYSTEM_EULER_ANGLES): Ball
@@ -76,8 +77,8 @@ void setIdentity(double* X) {
     X[0] = X[4] = X[8] = 1;
 }
 
-int nq_of(int t) { static const int n[11] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6, 0}; return n[t]; }
-int nu_of(int t) { static const int n[11] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6, 0}; return n[t]; }
+int nq_of(int t) { static const int n[12] = {1, 1, 2, 4, 7, 3, 3, 2, 3, 6, 0, 1}; return n[t]; }
+int nu_of(int t) { static const int n[12] = {1, 1, 2, 3, 6, 3, 3, 2, 3, 6, 0, 1}; return n[t]; }
 
 sbg_body_desc makeBody(int parent, int mob, double m, const double G[6], const double pPF[3], const double pBM[3]) {
     sbg_body_desc b;
@@ -111,14 +112,14 @@ void randomUnitQuat(std::mt19937_64& r, double* q) {
 }
 
 // Random tree (workloads 3-8) and its initial state. wide: children over
-// all ten non-Free mobilizers and rootType for the root (workload 6);
+// all eleven non-Free mobilizers and rootType for the root (workload 6);
 // euler: Ball and Free bodies with body-fixed X-Y-Z angles (workload 7).
 // Workloads 3-5 (wide = euler = false) draw exactly the stream they always did.
 void randomTree(std::mt19937_64& r, int nb, Sys& s, std::vector<double>& y, bool wide = false,
                 int rootType = SBG_FREE, bool euler = false) {
-    static const int kWide[10] = {SBG_PIN, SBG_SLIDER, SBG_UNIVERSAL, SBG_BALL, SBG_GIMBAL, SBG_TRANSLATION,
-                                  SBG_CYLINDER, SBG_PLANAR, SBG_BUSHING, SBG_WELD};
-    std::uniform_int_distribution<int> typeD(0, wide ? 9 : 3);
+    static const int kWide[11] = {SBG_PIN, SBG_SLIDER, SBG_UNIVERSAL, SBG_BALL, SBG_GIMBAL, SBG_TRANSLATION,
+                                  SBG_CYLINDER, SBG_PLANAR, SBG_BUSHING, SBG_WELD, SBG_SCREW};
+    std::uniform_int_distribution<int> typeD(0, wide ? 10 : 3);
     std::lognormal_distribution<double> LN(0, 0.5);
     std::uniform_real_distribution<double> US(0.05, 0.3), UK(10, 100), UC(0.1, 1), UP(-0.1, 0.1);
     std::uniform_real_distribution<double> UA(-0.5, 0.5), UL(-0.05, 0.05);
@@ -139,6 +140,7 @@ void randomTree(std::mt19937_64& r, int nb, Sys& s, std::vector<double>& y, bool
         double pPF[3] = {0, 0, 0};
         if (i > 1) { pPF[0] = UP(r); pPF[1] = UP(r); pPF[2] = UP(r); }
         s.bodies.push_back(makeBody(parent, mob, m, G, pPF, pBM));
+        if (mob == SBG_SCREW) s.bodies.back().pitch = UL(r);  // U[-0.05, 0.05] per radian
         for (int j = 0; j < nu_of(mob); ++j) {
             sbg_mobility_force_desc sp{0, i, j, 0, UK(r), 0.0};
             sbg_mobility_force_desc dp{1, i, j, 0, UC(r), 0.0};
@@ -150,7 +152,7 @@ void randomTree(std::mt19937_64& r, int nb, Sys& s, std::vector<double>& y, bool
     std::vector<double> q, u;
     for (int i = 1; i <= nb; ++i) {
         const int mob = s.bodies[i - 1].mobilizer;
-        if (mob == SBG_PIN) q.push_back(UA(r));
+        if (mob == SBG_PIN || mob == SBG_SCREW) q.push_back(UA(r));
         else if (mob == SBG_SLIDER) q.push_back(UL(r));
         else if (mob == SBG_UNIVERSAL) { q.push_back(UA(r)); q.push_back(UA(r)); }
         else if (mob == SBG_GIMBAL || mob == SBG_BUSHING || (euler && (mob == SBG_BALL || mob == SBG_FREE))) {

@@ -10,7 +10,7 @@ Python harness see identical inputs).
   4  10,000 trees with body count log-uniform in [4,256], 1000 steps
   5  serving requests: trees as 4, horizons log-uniform in [100,10000] steps,
      20% with 1-4 Ball loop closures
-  6  trees as 3 over all eleven mobilizers (Free or Bushing root)
+  6  trees as 3 over all twelve mobilizers (Free or Bushing root)
   7  trees as 3 with Euler-angle Ball and Free bodies
   8  trees as 3 with a contact sphere on every body over a ground half-space
 """

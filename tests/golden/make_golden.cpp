@@ -87,6 +87,7 @@ struct Model {
             case SBG_PLANAR: mobods.push_back(MobilizedBody::Planar(P, X_PF, body, X_BM)); break;
             case SBG_BUSHING: mobods.push_back(MobilizedBody::Bushing(P, X_PF, body, X_BM)); break;
             case SBG_WELD: mobods.push_back(MobilizedBody::Weld(P, X_PF, body, X_BM)); break;
+            case SBG_SCREW: mobods.push_back(MobilizedBody::Screw(P, X_PF, body, X_BM, b.pitch)); break;
             default: mobods.push_back(MobilizedBody::Free(P, X_PF, body, X_BM)); break;
             }
         }

@@ -35,7 +35,7 @@ def test_abi_version_and_no_device_here():
 
 
 def test_struct_layouts_match_header():
-    assert C.sizeof(N.BodyDesc) == 280
+    assert C.sizeof(N.BodyDesc) == 288
     assert C.sizeof(N.SystemDesc) == 80
     assert C.sizeof(N.ContactDesc) == 208
 

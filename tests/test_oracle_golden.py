@@ -59,7 +59,7 @@ def test_fixture_covers_every_mobilizer_and_loops(gold, workloads):
         d = workloads[cfg].systems[int(workloads[cfg].instance_system[inst])]
         kinds |= {d.bodies[k].mobilizer for k in range(d.nbodies)}
         loops += d.nconstraints > 0
-    assert kinds == set(range(11)) and loops >= 4
+    assert kinds == set(range(12)) and loops >= 4
     # and the Euler-angle mode of Ball and Free
     assert any(workloads[cfg].systems[int(workloads[cfg].instance_system[inst])].flags & 1
                for r, cfg, inst, ys, _ in _records(gold))

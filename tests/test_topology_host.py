@@ -37,7 +37,8 @@ def create(desc):
 
 @pytest.mark.parametrize("mob,nq,nu,nquat", [(N.SBG_PIN, 1, 1, 0), (N.SBG_SLIDER, 1, 1, 0),
                                               (N.SBG_UNIVERSAL, 2, 2, 0), (N.SBG_BALL, 4, 3, 1),
-                                              (N.SBG_FREE, 7, 6, 1), (N.SBG_WELD, 0, 0, 0)])
+                                              (N.SBG_FREE, 7, 6, 1), (N.SBG_WELD, 0, 0, 0),
+                                              (N.SBG_SCREW, 1, 1, 0)])
 def test_sizes_and_default_state(mob, nq, nu, nquat):
     b = chain(3, mob)
     t = Topology(make(b, 3), keepalive=b)
@@ -61,7 +62,7 @@ def test_levels_of_a_branched_tree():
 
 
 @pytest.mark.parametrize("field,value,msg", [("parent", 2, "parent must precede"), ("parent", -1, "parent must precede"),
-                                             ("mobilizer", 11, "unknown mobilizer"), ("mass", 0.0, "mass must be positive"),
+                                             ("mobilizer", 12, "unknown mobilizer"), ("mass", 0.0, "mass must be positive"),
                                              ("mass", float("nan"), "mass must be positive")])
 def test_invalid_bodies_are_rejected(field, value, msg):
     b = chain(3)
