@@ -122,3 +122,51 @@ def test_server_refuses_contact_spheres(engine, w8):
         assert e.value.code == 6  # SBG_ERR_UNSUPPORTED
     finally:
         s.close()
+
+
+def _with_spheres(w, every=2, seed=3):
+    """Put a contact sphere on each body of every `every`-th system of
+    workload w (in place), over a ground half-space whose surface lies at
+    y = -0.1, so that the lower bodies of about half of those trees press
+    into it; returns the arrays to keep alive."""
+    rng = np.random.default_rng(seed)
+    keep = []
+    for k in range(0, w.nsys, every):
+        d = w.systems[k]
+        arr = (N.ContactDesc * d.nbodies)()
+        for j in range(d.nbodies):
+            c = arr[j]
+            c.body, c.radius = j + 1, 0.05
+            c.station[0], c.station[1], c.station[2] = rng.uniform(-0.05, 0.05, 3)
+            c.halfspace[1], c.halfspace[3], c.halfspace[8] = 1.0, -1.0, 1.0  # x axis (the normal) = -Y
+            c.halfspace[10] = -0.1  # surface at y = -0.1: the lower bodies start below it
+            c.stiffness, c.dissipation, c.static_friction, c.dynamic_friction = 1e5, 1.0, 0.6, 0.4
+            c.viscous_friction, c.transition_velocity, c.cf, c.bd, c.bv = 0.1, 0.2, 1e-5, 300.0, 50.0
+        d.ncontacts, d.contacts = d.nbodies, arr
+        keep.append(arr)
+    return keep
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_contacts_with_loop_closures_and_mixed_batches(engine, precision):
+    """Contact spheres on every other system of the serving mix (trees with
+    and without Ball loop closures) in one batch: realize against the
+    oracle (FP64 1e-12; mixed 1e-5), and a short integration (1e-9)."""
+    w = Workload(5, 48)
+    keep = _with_spheres(w)
+    assert any(w.systems[k].nconstraints > 0 and w.systems[k].ncontacts > 0 for k in range(w.nsys))
+    b, y0 = engine_batch(w, precision)
+    b.set_state(y0)
+    ydot, st = b.realize_acceleration()
+    ref, rst = O.realize_workload(w)
+    assert (st == 0).all() and (rst == 0).all()
+    err = _rel(ydot, ref, b.y_offsets)
+    assert err.max() <= (1e-12 if precision == "fp64" else 1e-5), err.max()
+    if precision == "fp64":
+        b.set_state(y0)
+        st = b.rk_merson_fixed(w.h, 20)
+        y, _ = b.get_state()
+        ry, _, rst, _ = O.rk_workload(w, w.h, 20)
+        assert (st == 0).all() and (rst == 0).all()
+        assert _rel(y, ry, b.y_offsets).max() <= 1e-9
+    del keep
