@@ -474,8 +474,7 @@ int sbg_server_create(const sbg_server_config* config, sbg_server* out);
 int sbg_server_destroy(sbg_server server);
 /* Queue a request (host only, never waits for the GPU; thread-safe). The
  * topology is copied: it may be destroyed after the call. y0 has nq+nu
- * values. SBG_ERR_BUDGET if the request could never fit the server;
- * SBG_ERR_UNSUPPORTED for a topology with contact spheres. */
+ * values. SBG_ERR_BUDGET if the request could never fit the server. */
 int sbg_server_submit(sbg_server server, sbg_topology topology, const double* y0, double t0, double h,
                       int32_t nsteps, const sbg_integ_opts* opts, int64_t* request_id);
 /* One scheduling round: collect finished ticks, admit, launch one chunk of

@@ -195,7 +195,7 @@ template <class R>
 __device__ __noinline__ Wrench<R> contactForces(const R* KP, int kb, int kc, Kin<R> K, Wrench<R> F) {
     V3<R> Mw = F.w, Fv = F.v;
     for (int k = 0; k < kc; ++k) {
-        const R* c = KP + (int64_t)(kb + k) * kContactStride;
+        const R* c = KP + (int64_t)kb + (int64_t)k * kContactStride;
         const V3<R> n = mk3(c[4], c[5], c[6]);
         const V3<R> centre = mul(K.R_, mk3(c[0], c[1], c[2])) + K.p;
         const R indentation = -(dot(centre - mk3(c[7], c[8], c[9]), -n) - c[3]);

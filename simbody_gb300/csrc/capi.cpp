@@ -375,7 +375,7 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
             t->fcoef.push_back(f.coef);
             t->fq0.push_back(f.q0);
         }
-        t->kbeg.push_back((int32_t)(t->kpar.size() / kContactStride));
+        t->kbeg.push_back((int32_t)t->kpar.size());
         t->kcnt.push_back((int32_t)kOf[bi].size());
         for (int ki : kOf[bi]) {
             const sbg_contact_desc& k = d->contacts[ki];
@@ -539,7 +539,7 @@ int sbg_batch_create(const sbg_topology* topos, int32_t ntopo, const int32_t* in
         fkw.insert(fkw.end(), t->fkw.begin(), t->fkw.end());
         fcoef.insert(fcoef.end(), t->fcoef.begin(), t->fcoef.end());
         fq0.insert(fq0.end(), t->fq0.begin(), t->fq0.end());
-        const int32_t kOff = (int32_t)(kpar.size() / kContactStride);
+        const int32_t kOff = (int32_t)kpar.size();
         for (int32_t kb : t->kbeg) kbeg.push_back(kb + kOff);
         kcnt.insert(kcnt.end(), t->kcnt.begin(), t->kcnt.end());
         kpar.insert(kpar.end(), t->kpar.begin(), t->kpar.end());

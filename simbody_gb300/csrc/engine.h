@@ -154,7 +154,7 @@ struct DevTables {
     // Contact spheres on a ground half-space (SmoothSphereHalfSpaceForce),
     // grouped by body row in element order; read only for F_CONTACT rows
     // (null where no topology has any).
-    const int32_t* kbeg;     // per body row: first contact
+    const int32_t* kbeg;     // per body row: offset of its first contact's values in kpar
     const int32_t* kcnt;     // per body row: number of contacts
     const double* kpar64;    // kContactStride per contact
     const float* kpar32;

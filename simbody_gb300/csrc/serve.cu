@@ -145,6 +145,7 @@ struct ServeReq {
     std::vector<double> par64;   // kParamStride x nb
     std::vector<int32_t> fkw;
     std::vector<double> fcoef, fq0;
+    std::vector<double> kpar;    // contact spheres: kContactStride values each, after the forces in the force pool
     std::vector<int32_t> lcons;  // 2 per constraint (local rows)
     std::vector<double> lst;     // 6 per constraint
     std::vector<double> y0;
@@ -162,7 +163,7 @@ struct ServeReq {
 };
 
 enum RowTable { R_PARENT = 0, R_INFO, R_QOFF, R_UOFF, R_SREC, R_FBEG, R_FCNT, R_LREC, R_CBEG, R_CCNT, R_CLIST, R_LEV,
-                R_LSLOT, kRowTables };
+                R_LSLOT, R_KBEG, R_KCNT, kRowTables };
 
 struct TickRec {
     int parity = 0;
@@ -307,6 +308,8 @@ void buildImage(const sbg_topology_s& t, ServeReq& r, Footprint& fp) {
         at(R_LSLOT, i) = t.lslot[i];
         at(R_CBEG, i) = t.cbeg[i];  // request-relative: + row base at admission
         at(R_CCNT, i) = t.ccnt[i];
+        at(R_KBEG, i) = t.kbeg[i];  // request-relative: + force base + nf at admission
+        at(R_KCNT, i) = t.kcnt[i];
     }
     for (size_t i = 0; i < t.clist.size(); ++i) at(R_CLIST, (int)i) = t.clist[i];
     for (int L = 0; L <= t.nlevels; ++L) at(R_LEV, L) = t.levStart[L];
@@ -314,10 +317,11 @@ void buildImage(const sbg_topology_s& t, ServeReq& r, Footprint& fp) {
     r.fkw = t.fkw;
     r.fcoef = t.fcoef;
     r.fq0 = t.fq0;
+    r.kpar = t.kpar;
     r.lcons = t.lcons;
     r.lst = t.lst;
     fp.units[kPoolRows] = rows;
-    fp.units[kPoolForces] = r.nf;
+    fp.units[kPoolForces] = r.nf + (int64_t)r.kpar.size();  // a contact takes kContactStride force units
     fp.units[kPoolState] = t.nq + t.nu;
     // level-parallel records: one row per body (loop closures: then the
     // slot rows, 2 per constraint), FP64 for loop closures
@@ -372,11 +376,13 @@ int64_t imageBytes(const ServeReq& r, size_t rsz, int* ndesc) {
     add(r.nf * 4);
     add(r.nf * 16);
     add(r.nf * 8);
+    add((int64_t)r.kpar.size() * 8);
+    add((int64_t)r.kpar.size() * 4);
     add((int64_t)r.y0.size() * 8);
     add(r.ncons * 2 * 4);
     add(r.ncons * 6 * 8);
     add(16 * 8);  // the slot's instance entries
-    *ndesc = kRowTables + 2 + 5 + 1 + 2 + 16;
+    *ndesc = kRowTables + 2 + 5 + 2 + 1 + 2 + 16;
     return b;
 }
 
@@ -390,6 +396,7 @@ void stageRequest(ServeLane* s, Stager& st, ServeReq& r, const SchedRequest& sr)
     for (int i = 0; i < r.nb; ++i) {
         tab[(size_t)R_FBEG * rows + i] += (int32_t)f0;
         tab[(size_t)R_CBEG * rows + i] += (int32_t)row0;
+        tab[(size_t)R_KBEG * rows + i] += (int32_t)(f0 + r.nf);
     }
     for (int k = 0; k < kRowTables; ++k) st.put(tab.data() + (size_t)k * rows, rows * 4, s->rowsI[k] + row0);
     st.put(r.par64.data(), (int64_t)r.par64.size() * 8, s->par64 + row0 * kParamStride);
@@ -404,6 +411,11 @@ void stageRequest(ServeLane* s, Stager& st, ServeReq& r, const SchedRequest& sr)
         st.put(r.fq0.data(), r.nf * 8, s->fq064 + f0);
         st.put(c32.data(), r.nf * 4, s->fcoef32 + f0);
         st.put(q32.data(), r.nf * 4, s->fq032 + f0);
+    }
+    if (!r.kpar.empty()) {  // contact values in the force pool after the forces
+        const std::vector<float> k32(r.kpar.begin(), r.kpar.end());
+        st.put(r.kpar.data(), (int64_t)r.kpar.size() * 8, s->fcoef64 + f0 + r.nf);
+        st.put(k32.data(), (int64_t)k32.size() * 4, s->fcoef32 + f0 + r.nf);
     }
     st.put(r.y0.data(), (int64_t)r.y0.size() * 8, s->y + y0);
     if (r.ncons > 0) {
@@ -605,6 +617,10 @@ int laneCreate(const sbg_server_config* cfg, int64_t budget, std::chrono::steady
     T.fq064 = s->fq064;
     T.fcoef32 = s->fcoef32;
     T.fq032 = s->fq032;
+    T.kbeg = s->rowsI[R_KBEG];
+    T.kcnt = s->rowsI[R_KCNT];
+    T.kpar64 = s->fcoef64;
+    T.kpar32 = s->fcoef32;
     T.ibody = s->ibody;
     T.inb = s->inb;
     T.inq = s->inq;
@@ -893,7 +909,7 @@ int moveRetries(sbg_server_s* s) {
         r.recW = a.recW;
         r.t0 = a.t0; r.h = a.h; r.acc = a.acc; r.ctol = a.ctol; r.pes = a.pes;
         for (int k = 0; k < 3; ++k) r.grav[k] = a.grav[k];
-        r.rowsI = a.rowsI; r.par64 = a.par64; r.fkw = a.fkw; r.fcoef = a.fcoef; r.fq0 = a.fq0;
+        r.rowsI = a.rowsI; r.par64 = a.par64; r.fkw = a.fkw; r.fcoef = a.fcoef; r.fq0 = a.fq0; r.kpar = a.kpar;
         r.lcons = a.lcons; r.lst = a.lst; r.y0 = a.y0;
         r.steps = a.steps;
         r.submitS = a.submitS;
@@ -965,8 +981,6 @@ int sbg_server_submit(sbg_server s, sbg_topology topo, const double* y0, double 
     if (nsteps < 0 || nsteps > kCtlSteps) return setError(SBG_ERR_INVALID, "step count out of range");
     if (topo->ncons > kMaxLoopCons)
         return setError(SBG_ERR_UNSUPPORTED, "at most " + std::to_string(kMaxLoopCons) + " Ball loop closures per system");
-    if (topo->ncontacts > 0)
-        return setError(SBG_ERR_UNSUPPORTED, "contact spheres are not supported by the server");
     std::lock_guard<std::mutex> lock(s->mu);
     const bool loops = topo->ncons > 0;
     const int li = loops ? fp64Lane(stepCost(*topo, true, groupLanes(*topo))) : 0;

@@ -22,7 +22,7 @@ struct sbg_topology_s {
     std::vector<double> par;             // kParamStride per row
     std::vector<int32_t> fkw;            // force elements, grouped by row
     std::vector<double> fcoef, fq0;
-    std::vector<int32_t> kbeg, kcnt;     // contact spheres per row (grouped by row)
+    std::vector<int32_t> kbeg, kcnt;     // contact spheres per row: offset in kpar, count
     std::vector<double> kpar;            // kContactStride per contact
     int ncontacts = 0;
     double gravity[3] = {0, 0, 0};

@@ -15,8 +15,9 @@ sphere indented at t = 0), through the C ABI.
     instances with contact spheres through its FP64 path.
   - A zero parameter block stands for the reference's defaults: the engine
     gives the same accelerations as with the defaults written out.
-  - The server and the allocation-free realize do not take contact spheres
-    (SBG_ERR_UNSUPPORTED) rather than ignore them.
+  - The server integrates contact requests like the batch path, the same
+    alone and in a mix; the allocation-free realize refuses them
+    (test_topology_host.py).
 """
 import numpy as np
 import pytest
@@ -113,15 +114,53 @@ def test_zero_parameter_block_is_the_reference_defaults(engine, w8):
     np.testing.assert_array_equal(out[0], out[1])
 
 
-def test_server_refuses_contact_spheres(engine, w8):
-    s = Server(precision="fp64", device_budget_bytes=64 << 20)
-    try:
-        topo = Topology(w8.systems[0], keepalive=w8)
-        with pytest.raises(N.EngineError) as e:
-            s.submit(topo, w8.y0[w8.instance_slice(0)], w8.h, 10)
-        assert e.value.code == 6  # SBG_ERR_UNSUPPORTED
-    finally:
-        s.close()
+def test_server_integrates_contact_spheres(engine, w8):
+    """Contact requests in the server: FP64 results match the batch path
+    (1e-9: the server's level-parallel driver sums children in another
+    order over 40 steps of landing trees); in a mixed server they switch to
+    FP64 within their first step (the indentation is beyond FP32) and match
+    to 1e-8; and a
+    request's result is the same alone and among tree requests without
+    spheres (bit for bit)."""
+    idx = list(range(8))
+    topos = {i: Topology(w8.systems[int(w8.instance_system[i])], keepalive=w8) for i in idx}
+    steps = 40
+    ref = {}
+    for i in idx:
+        b, y0 = engine_batch(w8, "fp64", instances=[i])
+        b.set_state(y0)
+        st = b.rk_merson_fixed(w8.h, steps)
+        assert st[0] == 0
+        ref[i] = b.get_state()[0]
+    w5 = Workload(5, 24)
+    t5 = [Topology(w5.systems[int(w5.instance_system[i])], keepalive=w5) for i in range(24)]
+    for precision in ("fp64", "mixed"):
+        srv = Server(precision, device_budget_bytes=1 << 30, chunk_steps=16)
+        ids = {i: srv.submit(topos[i], w8.y0[w8.instance_slice(i)], w8.h, steps) for i in idx}
+        srv.drain()
+        alone = {}
+        for i in idx:
+            y, inf = srv.result(ids[i])
+            assert inf["status"] == 0, (precision, i, inf["status"])
+            if precision == "mixed":
+                assert inf["fp64_steps"] == 1
+            err = np.linalg.norm(y - ref[i]) / np.linalg.norm(ref[i])
+            # mixed: the switch to FP64 comes within the request's first step
+            assert err <= (1e-9 if precision == "fp64" else 1e-8), (precision, i, err)
+            alone[i] = y
+        srv.close()
+        srv = Server(precision, device_budget_bytes=1 << 30, chunk_steps=16)
+        mix = {}
+        for k, i in enumerate(idx):
+            mix[i] = srv.submit(topos[i], w8.y0[w8.instance_slice(i)], w8.h, steps)
+            for j in range(3 * k, 3 * k + 3):
+                srv.submit(t5[j], w5.y0[w5.instance_slice(j)], w5.h, 30)
+            srv.tick()
+        srv.drain()
+        for i in idx:
+            y, _ = srv.result(mix[i])
+            assert np.array_equal(y, alone[i]), (precision, i)
+        srv.close()
 
 
 def _with_spheres(w, every=2, seed=3):
