@@ -454,8 +454,9 @@ typedef struct sbg_request_info {
                            from its initial state in FP64 */
     int32_t fp64_steps; /* 1: a mixed-precision request reached a state where
                            the mixed form's refinement could not meet its bar
-                           (SBG_INST_ILL_CONDITIONED) and took its remaining
-                           steps in FP64 */
+                           (SBG_INST_ILL_CONDITIONED): that RHS and the next
+                           16 steps ran in FP64, then the mixed form was
+                           tried again */
 } sbg_request_info;
 
 typedef struct sbg_server_stats {

@@ -1510,9 +1510,9 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
     const double projLimit = fmax(2 * consTol, sqrt(consTol));
     // Mixed form in the server's lane: once the refinement reports an
     // ill-conditioned M, the instance's RHS runs in FP64 on the FP64 mirror of
-    // its records for the rest of the request (kStFp64 in its status word
-    // keeps that across launches). A batch has no per-instance control: it
-    // keeps SBG_INST_ILL_CONDITIONED in the status and stays mixed.
+    // its records (that stage's RHS included) for kFp64Steps steps, then the
+    // mixed form is tried again (kStFp64 and the step count in its status
+    // word keep that across launches).
     const bool fallback = REF && GROUP && T.ictl && T.scratch64;
     bool rhs64 = fallback && (st & kStFp64);
     auto stage = [&](int stg, double c, const R* a, const R* b, R* dst) {
@@ -1522,8 +1522,11 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
             st |= rhsChain<R, NM, false>(T, inst, ScrStrided<R>{scratch + T.sbase[inst], 1}, src, o);
         } else if constexpr (REF && GROUP) {
             bool fin = true;
+            const bool was64 = rhs64;
             st |= stageRhsMixedGroup<NM, R>(T, s, scratch, fallback, &rhs64, y, f0, a, b, base, stride, nq, stg, c,
                                             dst, &fin);
+            if (rhs64 && !was64)  // switched at this stage: this step and the next kFp64Steps - 1
+                st = (st & ~kStFp64LeftMask) | kStWasFp64 | (kFp64Steps << kStFp64LeftShift);
             o.finite = fin;
         } else {
             st |= rhs<R, NM, REF, GROUP, LOOPS>(T, s, scratch, src, o);
@@ -1685,6 +1688,16 @@ __global__ void __launch_bounds__(BS, MINB) rkMersonKernel(DevTables T, int firs
             }
         }
         if constexpr (GROUP) __syncwarp(s.mask);
+        if (fallback && rhs64) {  // one FP64 step taken: back to the mixed form after kFp64Steps
+            const int n64 = ((st & kStFp64LeftMask) >> kStFp64LeftShift) - 1;
+            st &= ~kStFp64LeftMask;
+            if (n64 > 0) {
+                st |= n64 << kStFp64LeftShift;
+            } else {
+                rhs64 = false;
+                st &= ~kStFp64;
+            }
+        }
         tc = t1;
         --left;
         if (s.gl == 0) {

@@ -173,9 +173,14 @@ constexpr int kFbLanes = 8;
 constexpr int kCtlSteps = (1 << 24) - 1;
 constexpr int kCtlInit = 1 << 30;                // first launch: Integrator::initialize projections
 constexpr int kCtlProjectEveryStep = 1 << 29;    // Integrator::setProjectEveryStep(true)
-// Status-word bit kept across a request's launches in the server: its RHS
-// runs in FP64 from now on (stripped before the status is reported).
+// Status-word bits kept across a request's launches in the server
+// (stripped before the status is reported): its RHS runs in FP64 for the
+// next kStFp64Left steps (a count in bits 20-27), after which it tries the
+// mixed form again; kStWasFp64 records that it ever switched.
 constexpr int kStFp64 = 1 << 30;
+constexpr int kStWasFp64 = 1 << 29;
+constexpr int kStFp64LeftShift = 20;
+constexpr int kStFp64LeftMask = 0xFF << kStFp64LeftShift;
 // The mixed form's refinement trusts its FP32 factorisation while the
 // correction stays within this fraction of udot (max-norms): 1e-4 in a
 // realize, where a flagged instance costs an FP64 recomputation after the

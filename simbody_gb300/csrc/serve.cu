@@ -459,8 +459,8 @@ void harvest(ServeLane* s, const TickRec& tr) {
         std::memcpy(r.y.data(), p, r.y.size() * 8);
         std::memcpy(&r.t, p + r.y.size() * 8, 8);
         std::memcpy(&r.status, p + r.y.size() * 8 + 8, 4);
-        if (r.status & kStFp64) r.fp64Steps = 1;
-        r.status &= ~kStFp64;
+        if (r.status & (kStFp64 | kStWasFp64)) r.fp64Steps = 1;
+        r.status &= ~(kStFp64 | kStWasFp64 | kStFp64LeftMask);
         if (s->retryFailed && (r.status & (SBG_INST_NONFINITE | SBG_INST_SINGULAR_D | SBG_INST_PROJECTION_FAILED))) {
             s->retry.push_back(s->byId[pr.first]);  // rerun from y0 in FP64; not done yet
             continue;
