@@ -9,13 +9,17 @@
 //   StateBatch                    a device-resident batch of States
 //     setY / getY / setTime       State::updY / getY / setTime (State.h:962-1034)
 //     realizeAcceleration         System::realize(s, Stage::Acceleration) + getYDot
+//     getQDotDot                  State::getQDotDot after that realize
 //     multiplyByMInv / multiplyByM / calcResidualForceIgnoringConstraints /
 //     multiplyBySystemJacobian(Transpose) / calcCompositeBodyInertias
 //                                 SimbodyMatterSubsystem operators (.h:1262-2323)
 //   RungeKuttaMersonBatchIntegrator
 //                                 RungeKuttaMersonIntegrator with setFixedStepSize,
 //                                 setAccuracy, setConstraintTolerance,
-//                                 setProjectEveryStep, initialize, stepTo, stepBy
+//                                 setProjectEveryStep, initialize, stepTo, stepBy;
+//                                 without a fixed step size, error-controlled
+//                                 (setInitial/Minimum/MaximumStepSize,
+//                                 getNumStepsTaken/Attempted per instance)
 #ifndef SIMBODY_GB300_HPP_
 #define SIMBODY_GB300_HPP_
 
@@ -106,10 +110,12 @@ public:
         check(sbg_batch_layout(h_, yOff_.data(), &ny));
         uOff_.assign(n_ + 1, 0);
         bOff_.assign(n_ + 1, 0);
+        qOff_.assign(n_ + 1, 0);
         for (int i = 0; i < n_; ++i) {
             const Topology* t = topologies[instanceTopology[i]];
             uOff_[i + 1] = uOff_[i] + t->getNU();
             bOff_[i + 1] = bOff_[i] + t->getNumBodies();
+            qOff_[i + 1] = qOff_[i] + t->getNQ();
         }
     }
     ~StateBatch() {
@@ -148,6 +154,15 @@ public:
         if (status) *status = std::move(st);
         return ydot;
     }
+
+    // State::getQDotDot() of every instance after realizeAcceleration() of
+    // the current state (nq values per instance, back to back: getQOffsets).
+    std::vector<double> getQDotDot() const {
+        std::vector<double> qdd(qOff_[n_]);
+        check(sbg_batch_get_qdotdot(h_, qdd.data()));
+        return qdd;
+    }
+    const std::vector<int64_t>& getQOffsets() const { return qOff_; }
 
     // SimbodyMatterSubsystem operators (u-like vectors packed like the u
     // parts of y; body vectors 6 values per body, inertias 10).
@@ -203,7 +218,7 @@ private:
 
     sbg_batch h_ = nullptr;
     int n_ = 0;
-    std::vector<int64_t> yOff_, uOff_, bOff_;
+    std::vector<int64_t> yOff_, uOff_, bOff_, qOff_;
 };
 
 // RungeKuttaMersonIntegrator over every state of a batch, with a fixed step
@@ -216,6 +231,13 @@ private:
 // projected); later calls continue the integration, as repeated stepTo calls
 // on one Simbody integrator do. stepTo returns one SBG_INST_* word per
 // instance.
+//
+// Without setFixedStepSize the integrator is error-controlled, as Simbody's
+// is by default: each instance takes its own steps (accuracy, initial,
+// minimum and maximum step size as set), and stepTo(t) brings every instance
+// to exactly t (Integrator::setFinalTime(t) + stepTo(t); FP64 batches
+// without loop closures). Each such stepTo starts the step-size control anew
+// from the initial step size.
 class RungeKuttaMersonBatchIntegrator {
 public:
     explicit RungeKuttaMersonBatchIntegrator(StateBatch& batch) : b_(batch) {}
@@ -223,9 +245,16 @@ public:
         if (!(h > 0) || !std::isfinite(h)) throw Error(SBG_ERR_INVALID, "step size must be positive");
         h_ = h;
     }
-    void setAccuracy(double a) { opts_.accuracy = a; }
-    void setConstraintTolerance(double c) { opts_.constraint_tolerance = c; }
-    void setProjectEveryStep(bool p) { opts_.project_every_step = p ? 1 : 0; }
+    void setAccuracy(double a) { opts_.accuracy = a; aopts_.accuracy = a; }
+    void setConstraintTolerance(double c) { opts_.constraint_tolerance = c; aopts_.constraint_tolerance = c; }
+    void setProjectEveryStep(bool p) { opts_.project_every_step = p ? 1 : 0; aopts_.project_every_step = p ? 1 : 0; }
+    void setInitialStepSize(double h) { aopts_.initial_step = h; }
+    void setMinimumStepSize(double h) { aopts_.min_step = h; }
+    void setMaximumStepSize(double h) { aopts_.max_step = h; }
+    // Accepted and attempted steps of each instance in the last
+    // error-controlled stepTo (Integrator::getNumStepsTaken / Attempted).
+    const std::vector<int64_t>& getNumStepsTaken() const { return taken_; }
+    const std::vector<int64_t>& getNumStepsAttempted() const { return attempted_; }
     // Integrator::initialize: the next stepTo starts the integration from
     // the batch's current state, whose time is t0 (StateBatch::setY).
     void initialize(double t0 = 0.0) {
@@ -234,9 +263,20 @@ public:
     }
     double getTime() const { return t_; }
     std::vector<int32_t> stepTo(double tReport) {
-        if (h_ <= 0) throw Error(SBG_ERR_STATE, "setFixedStepSize was not called");
         if (!std::isfinite(tReport)) throw Error(SBG_ERR_INVALID, "stepTo: the report time must be finite");
         std::vector<int32_t> st(b_.getNumInstances());
+        if (h_ <= 0) {  // error-controlled
+            std::vector<int64_t> stats(2 * st.size());
+            check(sbg_rk_merson_adaptive(b_.handle(), tReport, &aopts_, st.data(), stats.data()));
+            taken_.resize(st.size());
+            attempted_.resize(st.size());
+            for (size_t i = 0; i < st.size(); ++i) {
+                taken_[i] = stats[2 * i];
+                attempted_[i] = stats[2 * i] + stats[2 * i + 1];
+            }
+            t_ = std::max(t_, tReport);
+            return st;
+        }
         opts_.continue_integration = started_ ? 1 : 0;
         check(sbg_rk_merson_step_to(b_.handle(), h_, tReport, &opts_, st.data()));
         started_ = true;
@@ -250,6 +290,8 @@ private:
     double h_ = 0, t_ = 0;
     bool started_ = false;
     sbg_integ_opts opts_{0, 0, 0, 0};
+    sbg_adaptive_opts aopts_{0, 0, 0, 0, 0, 0, 0};
+    std::vector<int64_t> taken_, attempted_;
 };
 
 }  // namespace sbg
