@@ -68,8 +68,6 @@ bool buildTopology(const sbg_system_desc& d, Topology& t, const char** err) {
         }
         t.contacts.push_back(c);
     }
-    if (d.nconstraints > 0 && (d.flags & SBG_SYSTEM_EULER_ANGLES))
-        return fail("loop closures with Euler-angle Ball or Free bodies are not supported");
     int maxLevel = 0;
     for (int i = 1; i <= t.nb; ++i) maxLevel = std::max(maxLevel, t.b[i].level);
     t.levels.assign(maxLevel, {});
@@ -306,7 +304,9 @@ static void normalizeQuaternions(const Topology& t, double* q) {
 // Position (projectQ, SimbodyMatterSubsystemRep.cpp:4096-4442): the reference
 // solves (P NInv) x = perr for the minimum-norm x and steps q -= N NInv x
 // (Wu = 1, Tp = 1; :4271-4300). With D = NInv NInv^T, which is 4|q|^2 I on
-// the rotational mobilities of a quaternion joint (Rotation.h:742-748) and 1
+// the rotational mobilities of a quaternion joint (Rotation.h:742-748), the
+// 3x3 block NInv NInv^T on those of a joint in body-fixed X-Y-Z angles
+// (NInv = [x, Rx y, Rx Ry z], RigidBodyNodeSpec_Ball.h:266-300) and 1
 // elsewhere, that is du = D G^T (G D G^T)^-1 perr, q -= N(q) du. Full Newton
 // until RMS(perr) <= 0.1 tol, at most 20 iterations; with localOnly the
 // iteration stops when the norm grows (:4310-4321); the entry q is restored
@@ -319,39 +319,76 @@ static void normalizeQuaternions(const Topology& t, double* q) {
 
 static double normRMSv(const std::vector<double>& v) { return normRMS(v.data(), (int)v.size()); }
 
-// D = diag(NInv NInv^T) per mobility for the current (unnormalized) q.
-static void projectionWeightsQ(const Topology& t, const double* q, std::vector<double>& D) {
+// The 3x3 weight blocks of the joints in body-fixed X-Y-Z angles: u offset
+// and NInv NInv^T (row-major); their mobilities' diagonal weights are 0.
+struct WeightBlocks {
+    std::vector<int> uoff;
+    std::vector<double> B;  // 9 per block
+};
+
+// D = diag(NInv NInv^T) per mobility for the current (unnormalized) q, and
+// the full blocks of the Euler-angle joints.
+static void projectionWeightsQ(const Topology& t, const double* q, std::vector<double>& D, WeightBlocks& blk) {
     D.assign(t.nu, 1.0);
+    blk.uoff.clear();
+    blk.B.clear();
     for (int bi = 1; bi <= t.nb; ++bi) {
         const Body& b = t.b[bi];
-        if (!b.quat) continue;
         const double* qq = q + b.qoff;
+        if (b.euler) {
+            const double c0 = std::cos(qq[0]), s0 = std::sin(qq[0]), c1 = std::cos(qq[1]), s1 = std::sin(qq[1]);
+            // NInv columns: (1,0,0), (0,c0,s0), (s1,-s0 c1,c0 c1)
+            const double N[9] = {1, 0, s1, 0, c0, -s0 * c1, 0, s0, c0 * c1};
+            double B[9];
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) B[3 * r + c] = N[3 * r] * N[3 * c] + N[3 * r + 1] * N[3 * c + 1] + N[3 * r + 2] * N[3 * c + 2];
+            blk.uoff.push_back(b.uoff);
+            blk.B.insert(blk.B.end(), B, B + 9);
+            for (int k = 0; k < 3; ++k) D[b.uoff + k] = 0.0;
+            continue;
+        }
+        if (!b.quat) continue;
         const double n2 = qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3];
         for (int k = 0; k < 3; ++k) D[b.uoff + k] = 4 * n2;
     }
 }
 
-// A = G diag(Wt) G^T (m x m).
+// A = G D G^T (m x m), D = diag(Wt) plus the blocks.
 static void weightedGram(int m, int nu, const std::vector<double>& G, const std::vector<double>& Wt,
-                         std::vector<double>& A) {
+                         std::vector<double>& A, const WeightBlocks* blk = nullptr) {
     A.assign((size_t)m * m, 0.0);
     for (int i = 0; i < m; ++i)
         for (int j = 0; j < m; ++j) {
             double s = 0;
             for (int k = 0; k < nu; ++k) s += G[(size_t)i * nu + k] * Wt[k] * G[(size_t)j * nu + k];
+            if (blk)
+                for (size_t bk = 0; bk < blk->uoff.size(); ++bk) {
+                    const int u = blk->uoff[bk];
+                    const double* B = &blk->B[9 * bk];
+                    for (int a = 0; a < 3; ++a)
+                        for (int c = 0; c < 3; ++c) s += G[(size_t)i * nu + u + a] * B[3 * a + c] * G[(size_t)j * nu + u + c];
+                }
             A[(size_t)i * m + j] = s;
         }
 }
 
-// du = diag(Wt) G^T lambda.
+// du = D G^T lambda.
 static void weightedGT(int m, int nu, const std::vector<double>& G, const std::vector<double>& Wt,
-                       const std::vector<double>& lam, std::vector<double>& du) {
+                       const std::vector<double>& lam, std::vector<double>& du, const WeightBlocks* blk = nullptr) {
     du.assign(nu, 0.0);
+    std::vector<double> g(nu);
     for (int k = 0; k < nu; ++k) {
         double s = 0;
         for (int i = 0; i < m; ++i) s += G[(size_t)i * nu + k] * lam[i];
+        g[k] = s;
         du[k] = Wt[k] * s;
     }
+    if (blk)
+        for (size_t bk = 0; bk < blk->uoff.size(); ++bk) {
+            const int u = blk->uoff[bk];
+            const double* B = &blk->B[9 * bk];
+            for (int a = 0; a < 3; ++a) du[u + a] = B[3 * a] * g[u] + B[3 * a + 1] * g[u + 1] + B[3 * a + 2] * g[u + 2];
+        }
 }
 
 // dq = N(q) du with the unnormalized N of Rotation.h:712-719.
@@ -368,6 +405,11 @@ static void multiplyByN(const Topology& t, const double* q, const double* du, do
             d[2] = -e3 * ub[0] + e0 * ub[1] + e1 * ub[2];
             d[3] = e2 * ub[0] - e1 * ub[1] + e0 * ub[2];
             if (b.type == SBG_FREE) { d[4] = ub[3]; d[5] = ub[4]; d[6] = ub[5]; }
+        } else if (b.euler) {  // N_P of body-fixed X-Y-Z angles; the last q slot is unused
+            const double cc[2] = {std::cos(qb[0]), std::cos(qb[1])}, ss[2] = {std::sin(qb[0]), std::sin(qb[1])};
+            bodyXYZ_N_P(cc, ss, 1.0 / cc[1], ub, d);
+            if (b.type == SBG_FREE) { d[3] = ub[3]; d[4] = ub[4]; d[5] = ub[5]; d[6] = 0; }
+            else d[3] = 0;
         } else {
             for (int j = 0; j < b.nq; ++j) d[j] = ub[j];
         }
@@ -399,6 +441,7 @@ static void verrAt(const Topology& t, const double* q, const double* u, Work<dou
 static bool projectQNewton(const Topology& t, double* q, Work<double>& w, double tol, bool localOnly) {
     const int m = 3 * (int)t.constraints.size();
     std::vector<double> perr, G, D, A, lam, du, dq(t.nq);
+    WeightBlocks blk;
     perrAt(t, q, w, perr);
     const double normOnEntry = normRMSv(perr);
     const std::vector<double> saveQ(q, q + t.nq);
@@ -407,11 +450,11 @@ static bool projectQNewton(const Topology& t, double* q, Work<double>& w, double
     int its = 0;
     do {
         constraintJacobian(t, w, G);
-        projectionWeightsQ(t, q, D);
-        weightedGram(m, t.nu, G, D, A);
+        projectionWeightsQ(t, q, D, blk);
+        weightedGram(m, t.nu, G, D, A, &blk);
         lam = perr;
         if (!cholSolve(m, A, lam)) return false;
-        weightedGT(m, t.nu, G, D, lam, du);
+        weightedGT(m, t.nu, G, D, lam, du, &blk);
         multiplyByN(t, q, du.data(), dq.data());
         for (int k = 0; k < t.nq; ++k) q[k] -= dq[k];
         perrAt(t, q, w, perr);

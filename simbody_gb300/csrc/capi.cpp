@@ -272,8 +272,6 @@ int sbg_topology_create(const sbg_system_desc* d, sbg_topology* out) {
         return fail(SBG_ERR_INVALID, "bad constraint list");
     if (d->flags & ~SBG_SYSTEM_EULER_ANGLES) return fail(SBG_ERR_INVALID, "unknown system flags");
     const bool euler = (d->flags & SBG_SYSTEM_EULER_ANGLES) != 0;
-    if (euler && d->nconstraints > 0)
-        return fail(SBG_ERR_UNSUPPORTED, "loop closures with Euler-angle Ball or Free bodies are not supported");
     const int nb = d->nbodies;
     std::vector<int> level(nb + 1, 0), qo(nb + 1, 0), uo(nb + 1, 0);
     int nq = 0, nu = 0, nquat = 0, maxnf = 0;

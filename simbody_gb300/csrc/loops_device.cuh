@@ -86,6 +86,11 @@ __device__ __forceinline__ LoopState loopStateRows(const DevTables& T, int inst,
                      T.ibody[inst], T.inb[inst]};
 }
 
+// The weights of a sweep that applies none (kMInvSweep; see PosWeights).
+struct NoWeights {
+    __device__ __forceinline__ void apply(int, int, double*) const {}
+};
+
 struct NullOut {
     template <class R> __device__ __forceinline__ void qdot(int, R) {}
     template <class R> __device__ __forceinline__ void udot(int, R) {}
@@ -318,9 +323,12 @@ __device__ __forceinline__ void loopSweepIn(const LoopState& L, const Wt& wt) {
         if (have) { zw = zw + cw; zv = zv + cv; }
         if (n == 6) loopIn6<KIND>(L, row, rec, info, zw, zv);
         else loopIn<NM, KIND>(L, row, rec, n, info, zw, zv);
-        if (KIND == kJacSweep) {
+        if constexpr (KIND == kJacSweep) {
             const int eEps = recEps(recN(n, NM));
-            for (int j = 0; j < n; ++j) S(rec, eEps + j) = S(rec, eEps + j) * wt(row, j);
+            double g[6];
+            for (int j = 0; j < n; ++j) g[j] = S(rec, eEps + j);
+            wt.apply(row, n, g);
+            for (int j = 0; j < n; ++j) S(rec, eEps + j) = g[j];
         }
         const int parent = T.parent[row];
         have = (info & F_CARRY) != 0;
@@ -552,11 +560,14 @@ __device__ __forceinline__ void loopSweep3(const LoopState& L, const Wt& wt) {
             }
             if (n == 6) loopIn36<KIND>(L, row, rec, info, zw, zv);
             else loopIn3<NM, KIND>(L, row, rec, n, info, zw, zv);
-            if (KIND == kJacSweep) {
+            if constexpr (KIND == kJacSweep) {
                 const int eEps = recEps(recN(n, NM));
-                for (int k = 0; k < 3; ++k)
-                    for (int j = 0; j < n; ++j)
-                        S(rec, recEpsK(eEps, k) + j) = S(rec, recEpsK(eEps, k) + j) * wt(row, j);
+                for (int k = 0; k < 3; ++k) {
+                    double g[6];
+                    for (int j = 0; j < n; ++j) g[j] = S(rec, recEpsK(eEps, k) + j);
+                    wt.apply(row, n, g);
+                    for (int j = 0; j < n; ++j) S(rec, recEpsK(eEps, k) + j) = g[j];
+                }
             }
             const int parent = T.parent[row];
             have = (info & F_CARRY) != 0;
@@ -721,9 +732,12 @@ __device__ __forceinline__ void loopSweepColumn(const LoopState& L, const Wt& wt
             if (have) { zw = zw + cw; zv = zv + cv; }
             if (n == 6) loopIn16<KIND>(L, row, rec, info, k, zw, zv);
             else loopIn1<NM, KIND>(L, row, rec, n, info, k, zw, zv);
-            if (KIND == kJacSweep) {
+            if constexpr (KIND == kJacSweep) {
                 const int fE = recEpsK(recEps(recN(n, NM)), k);
-                for (int j = 0; j < n; ++j) S(rec, fE + j) = S(rec, fE + j) * wt(row, j);
+                double g[6];
+                for (int j = 0; j < n; ++j) g[j] = S(rec, fE + j);
+                wt.apply(row, n, g);
+                for (int j = 0; j < n; ++j) S(rec, fE + j) = g[j];
             }
             const int parent = T.parent[row];
             have = (info & F_CARRY) != 0;
@@ -901,7 +915,7 @@ __device__ __noinline__ int loopForwardDynamics(const LoopState& L, Out& out) {
         lam[3 * c] = d.x; lam[3 * c + 1] = d.y; lam[3 * c + 2] = d.z;
     }
     double A[kMaxLoopEq * kMaxLoopEq];
-    auto one = [](int, int) { return 1.0; };
+    const NoWeights one{};
     loopGram<NM, kMInvSweep>(L, one, A);
     if (!loopCholFactor(m, A)) return SBG_INST_CHOLESKY_FAIL;
     loopCholSolve(m, A, lam);
@@ -941,7 +955,7 @@ __device__ __noinline__ int loopForwardDynamicsLanes(const LoopState& L, Out& ou
     }
     __syncwarp(mask);
     double A[kMaxLoopEq * kMaxLoopEq];
-    auto one = [](int, int) { return 1.0; };
+    const NoWeights one{};
     loopGramLanes<NM, kMInvSweep>(L, one, A, gl, mask);
     if (gl != 0) return 0;
     if (!loopCholFactor(m, A)) return SBG_INST_CHOLESKY_FAIL;
@@ -1019,12 +1033,92 @@ __device__ __forceinline__ void loopNormalizeQuats(const LoopState& L) {
     const int body0 = T.ibody[L.inst], nb = T.inb[L.inst];
     for (int lb = 0; lb < nb; ++lb) {
         const int row = body0 + lb;
-        const int type = T.info[row] & 15;
-        if (type != T_BALL && type != T_FREE) continue;
+        if (!(T.info[row] & F_QUAT)) continue;
         const int qo = T.qoff[row];
         const double q0 = yAt(L, qo), q1 = yAt(L, qo + 1), q2 = yAt(L, qo + 2), q3 = yAt(L, qo + 3);
         const double len = sqrt(q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
         yAt(L, qo) = q0 / len; yAt(L, qo + 1) = q1 / len; yAt(L, qo + 2) = q2 / len; yAt(L, qo + 3) = q3 / len;
+    }
+}
+
+// Projection weights applied to the n values g = ~H F of a row in the
+// inward half of a kJacSweep (du = D ~G lambda).
+//   PosWeights (projectQ): D = NInv NInv^T of the current q: 4|q|^2 on the
+//     rotational mobilities of a quaternion joint (Rotation.h:742-748); for a
+//     joint in body-fixed X-Y-Z angles the 3x3 block NInv NInv^T with
+//     NInv = [x, Rx y, Rx Ry z] (RigidBodyNodeSpec_Ball.h:266-300); 1 elsewhere
+//   VelWeights (projectU): E^2, E = max(|u|, 1) of the entry u (saved)
+// The Gram of the forward dynamics (kMInvSweep) applies none (NoWeights,
+// defined with the sweeps).
+struct PosWeights {
+    const LoopState* L;
+    __device__ __forceinline__ void apply(int row, int n, double* g) const {
+        const DevTables& T = L->T;
+        const int info = T.info[row], type = info & 15;
+        const int qo = T.qoff[row];
+        if (info & F_QUAT) {
+            const double q0 = yAt(*L, qo), q1 = yAt(*L, qo + 1), q2 = yAt(*L, qo + 2), q3 = yAt(*L, qo + 3);
+            const double w = 4 * (q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
+            for (int j = 0; j < 3 && j < n; ++j) g[j] = g[j] * w;
+        } else if (type == T_BALL || type == T_FREE) {
+            double s0, c0, s1, c1;
+            sincos(yAt(*L, qo), &s0, &c0);
+            sincos(yAt(*L, qo + 1), &s1, &c1);
+            const double N[9] = {1, 0, s1, 0, c0, -s0 * c1, 0, s0, c0 * c1};
+            double B[9];
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c)
+                    B[3 * r + c] = N[3 * r] * N[3 * c] + N[3 * r + 1] * N[3 * c + 1] + N[3 * r + 2] * N[3 * c + 2];
+            const double a0 = g[0], a1 = g[1], a2 = g[2];
+            for (int r = 0; r < 3; ++r) g[r] = B[3 * r] * a0 + B[3 * r + 1] * a1 + B[3 * r + 2] * a2;
+        }
+    }
+};
+struct VelWeights {
+    const LoopState* L;
+    int nq;
+    __device__ __forceinline__ void apply(int row, int n, double* g) const {
+        const int uo = L->T.uoff[row];
+        for (int j = 0; j < n; ++j) {
+            const double a = fabs(saveAt(*L, nq + uo + j));
+            const double e = a > 1 ? a : 1.0;
+            g[j] = g[j] * (e * e);
+        }
+    }
+};
+
+// q -= N(q) du for one row's du (the unnormalized N of a quaternion,
+// Rotation.h:712-719; N_P of body-fixed X-Y-Z angles, Rotation.h:395-406,
+// the last q slot unused; the identity otherwise). Records du in delta.
+__device__ __forceinline__ void loopStepQ(const LoopState& L, int row, int n, const double* du) {
+    const DevTables& T = L.T;
+    const int info = T.info[row], type = info & 15, qo = T.qoff[row];
+    double dq[7];
+    int nqb = n;
+    if (info & F_QUAT) {
+        const double e0 = yAt(L, qo) / 2, e1 = yAt(L, qo + 1) / 2, e2 = yAt(L, qo + 2) / 2, e3 = yAt(L, qo + 3) / 2;
+        dq[0] = -e1 * du[0] - e2 * du[1] - e3 * du[2];
+        dq[1] = e0 * du[0] + e3 * du[1] - e2 * du[2];
+        dq[2] = -e3 * du[0] + e0 * du[1] + e1 * du[2];
+        dq[3] = e2 * du[0] - e1 * du[1] + e0 * du[2];
+        nqb = 4;
+        if (type == T_FREE) { dq[4] = du[3]; dq[5] = du[4]; dq[6] = du[5]; nqb = 7; }
+    } else if (type == T_BALL || type == T_FREE) {
+        double s0, c0, s1, c1;
+        sincos(yAt(L, qo), &s0, &c0);
+        sincos(yAt(L, qo + 1), &s1, &c1);
+        const double t = (s0 * du[1] - c0 * du[2]) * (1.0 / c1);
+        dq[0] = du[0] + t * s1;
+        dq[1] = c0 * du[1] + s0 * du[2];
+        dq[2] = -t;
+        if (type == T_FREE) { dq[3] = du[3]; dq[4] = du[4]; dq[5] = du[5]; dq[6] = 0; nqb = 7; }
+        else { dq[3] = 0; nqb = 4; }
+    } else {
+        for (int j = 0; j < n; ++j) dq[j] = du[j];
+    }
+    for (int j = 0; j < nqb; ++j) {
+        deltaAt(L, qo + j) = dq[j];
+        yAt(L, qo + j) -= dq[j];
     }
 }
 
@@ -1046,16 +1140,7 @@ __device__ __noinline__ bool loopProjectQ(const LoopState& L, double tol, bool l
     const double tryFor = loopTryFor(tol);
     double achieved = normOnEntry, prev = normOnEntry;
     int its = 0;
-    // D = diag(NInv NInv^T) of the current q
-    auto wq = [&](int row, int j) -> double {
-        const int type = T.info[row] & 15;
-        if ((type == T_BALL || type == T_FREE) && j < 3) {
-            const int qo = T.qoff[row];
-            const double q0 = yAt(L, qo), q1 = yAt(L, qo + 1), q2 = yAt(L, qo + 2), q3 = yAt(L, qo + 3);
-            return 4 * (q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
-        }
-        return 1.0;
-    };
+    const PosWeights wq{&L};  // D = NInv NInv^T of the current q
     do {
         loopGram<NM, kJacSweep>(L, wq, A);
         if (!loopCholFactor(m, A)) return false;
@@ -1063,27 +1148,8 @@ __device__ __noinline__ bool loopProjectQ(const LoopState& L, double tol, bool l
         loopClearForces(L);
         for (int c = 0; c < m / 3; ++c)
             loopAddConstraintForce(L, loopGeom(L, c), mk3(perr[3 * c], perr[3 * c + 1], perr[3 * c + 2]));
-        // q -= N(q) du with the unnormalized N (Rotation.h:712-719)
-        loopSweep<NM, kJacSweep>(L, wq, [&](int row, int n, const double* du) {
-            const int type = T.info[row] & 15, qo = T.qoff[row];
-            double dq[7];
-            int nqb = n;
-            if (type == T_BALL || type == T_FREE) {
-                const double e0 = yAt(L, qo) / 2, e1 = yAt(L, qo + 1) / 2, e2 = yAt(L, qo + 2) / 2, e3 = yAt(L, qo + 3) / 2;
-                dq[0] = -e1 * du[0] - e2 * du[1] - e3 * du[2];
-                dq[1] = e0 * du[0] + e3 * du[1] - e2 * du[2];
-                dq[2] = -e3 * du[0] + e0 * du[1] + e1 * du[2];
-                dq[3] = e2 * du[0] - e1 * du[1] + e0 * du[2];
-                nqb = 4;
-                if (type == T_FREE) { dq[4] = du[3]; dq[5] = du[4]; dq[6] = du[5]; nqb = 7; }
-            } else {
-                for (int j = 0; j < n; ++j) dq[j] = du[j];
-            }
-            for (int j = 0; j < nqb; ++j) {
-                deltaAt(L, qo + j) = dq[j];
-                yAt(L, qo + j) -= dq[j];
-            }
-        });
+        // q -= N(q) du (loopStepQ)
+        loopSweep<NM, kJacSweep>(L, wq, [&](int row, int n, const double* du) { loopStepQ(L, row, n, du); });
         loopKinematics<NM>(L);
         achieved = loopPerr(L, perr);
         ++its;
@@ -1123,11 +1189,7 @@ __device__ __noinline__ bool loopProjectU(const LoopState& L, double tol, bool f
         deltaAt(L, nq + k) = 0.0;  // rows off the loop paths never move
     }
     // E^2 with E = max(|u|, 1) frozen at entry
-    auto wu = [&](int row, int j) -> double {
-        const double a = fabs(saveAt(L, nq + T.uoff[row] + j));
-        const double e = a > 1 ? a : 1.0;
-        return e * e;
-    };
+    const VelWeights wu{&L, nq};
     loopGram<NM, kJacSweep>(L, wu, A);
     if (!loopCholFactor(m, A)) return false;
     const double tryFor = loopTryFor(tol);
@@ -1191,15 +1253,7 @@ __device__ __noinline__ bool loopProjectQLanes(const LoopState& L, double tol, b
     const double tryFor = loopTryFor(tol);
     double achieved = normOnEntry, prev = normOnEntry;
     int its = 0;
-    auto wq = [&](int row, int j) -> double {
-        const int type = T.info[row] & 15;
-        if ((type == T_BALL || type == T_FREE) && j < 3) {
-            const int qo = T.qoff[row];
-            const double q0 = yAt(L, qo), q1 = yAt(L, qo + 1), q2 = yAt(L, qo + 2), q3 = yAt(L, qo + 3);
-            return 4 * (q0 * q0 + q1 * q1 + q2 * q2 + q3 * q3);
-        }
-        return 1.0;
-    };
+    const PosWeights wq{&L};  // D = NInv NInv^T of the current q
     do {
         __syncwarp(mask);  // the first lane's q and kinematics, before the Gram reads them
         loopGramLanes<NM, kJacSweep>(L, wq, A, gl, mask);
@@ -1212,27 +1266,7 @@ __device__ __noinline__ bool loopProjectQLanes(const LoopState& L, double tol, b
                 loopClearForces(L);
                 for (int c = 0; c < m / 3; ++c)
                     loopAddConstraintForce(L, loopGeom(L, c), mk3(perr[3 * c], perr[3 * c + 1], perr[3 * c + 2]));
-                loopSweep<NM, kJacSweep>(L, wq, [&](int row, int n, const double* du) {
-                    const int type = T.info[row] & 15, qo = T.qoff[row];
-                    double dq[7];
-                    int nqb = n;
-                    if (type == T_BALL || type == T_FREE) {
-                        const double e0 = yAt(L, qo) / 2, e1 = yAt(L, qo + 1) / 2, e2 = yAt(L, qo + 2) / 2,
-                                     e3 = yAt(L, qo + 3) / 2;
-                        dq[0] = -e1 * du[0] - e2 * du[1] - e3 * du[2];
-                        dq[1] = e0 * du[0] + e3 * du[1] - e2 * du[2];
-                        dq[2] = -e3 * du[0] + e0 * du[1] + e1 * du[2];
-                        dq[3] = e2 * du[0] - e1 * du[1] + e0 * du[2];
-                        nqb = 4;
-                        if (type == T_FREE) { dq[4] = du[3]; dq[5] = du[4]; dq[6] = du[5]; nqb = 7; }
-                    } else {
-                        for (int j = 0; j < n; ++j) dq[j] = du[j];
-                    }
-                    for (int j = 0; j < nqb; ++j) {
-                        deltaAt(L, qo + j) = dq[j];
-                        yAt(L, qo + j) -= dq[j];
-                    }
-                });
+                loopSweep<NM, kJacSweep>(L, wq, [&](int row, int n, const double* du) { loopStepQ(L, row, n, du); });
                 loopKinematics<NM>(L);
                 achieved = loopPerr(L, perr);
             }
@@ -1287,11 +1321,7 @@ __device__ __noinline__ bool loopProjectULanes(const LoopState& L, double tol, b
             deltaAt(L, nq + k) = 0.0;  // rows off the loop paths never move
         }
     __syncwarp(mask);  // the saved u, before the Gram's weights read it
-    auto wu = [&](int row, int j) -> double {
-        const double a = fabs(saveAt(L, nq + T.uoff[row] + j));
-        const double e = a > 1 ? a : 1.0;
-        return e * e;
-    };
+    const VelWeights wu{&L, nq};
     loopGramLanes<NM, kJacSweep>(L, wu, A, gl, mask);
     int fail = lead ? (loopCholFactor(m, A) ? 0 : 1) : 0;
     if (laneBcast(fail, base, mask)) return false;

@@ -27,6 +27,8 @@
 //     U[-0.5,0.5], displacements U[-0.05,0.05].
 //  7  random trees as 3 in Euler-angle mode (SBG_SYSTEM_EULER_ANGLES): Ball
 //     and Free bodies with body-fixed X-Y-Z angles U[-0.5,0.5].
+//  9  random trees as 7 (Euler-angle mode) where 20% get 1..4 Ball loop
+//     closures to Ground as in 5, assembled at t = 0.
 //  8  random trees as 3 on a ground half-space: a SmoothSphereHalfSpaceForce
 //     sphere on every body (station U[-0.05,0.05]^3, radius U[0.02,0.06]), the
 //     half-space normal tilted U[-0.2,0.2] rad from -Y, the lowest sphere
@@ -45,6 +47,7 @@ namespace {
 const double kPi = 3.14159265358979323846;
 
 struct Sys {
+    bool euler = false;  // Ball and Free bodies in body-fixed X-Y-Z angles
     std::vector<sbg_body_desc> bodies;
     std::vector<sbg_mobility_force_desc> forces;
     std::vector<sbg_ball_constraint_desc> cons;
@@ -199,11 +202,20 @@ Xf inverse(const Xf& A) {
     for (int i = 0; i < 3; ++i) B.p[i] = -(B.R[3 * i] * A.p[0] + B.R[3 * i + 1] * A.p[1] + B.R[3 * i + 2] * A.p[2]);
     return B;
 }
-Xf jointX(int mob, const double* q) {
+Xf jointX(int mob, const double* q, bool euler) {
     Xf X;
     std::memset(&X, 0, sizeof X);
     X.R[0] = X.R[4] = X.R[8] = 1;
-    if (mob == SBG_PIN) {
+    if (euler && (mob == SBG_BALL || mob == SBG_FREE)) {
+        // body-fixed X-Y-Z angles: R = Rx(q0) Ry(q1) Rz(q2)
+        const double c0 = std::cos(q[0]), s0 = std::sin(q[0]), c1 = std::cos(q[1]), s1 = std::sin(q[1]),
+                     c2 = std::cos(q[2]), s2 = std::sin(q[2]);
+        const double R[9] = {c1 * c2, -c1 * s2, s1,
+                             c0 * s2 + s0 * s1 * c2, c0 * c2 - s0 * s1 * s2, -s0 * c1,
+                             s0 * s2 - c0 * s1 * c2, s0 * c2 + c0 * s1 * s2, c0 * c1};
+        std::memcpy(X.R, R, sizeof R);
+        if (mob == SBG_FREE) { X.p[0] = q[3]; X.p[1] = q[4]; X.p[2] = q[5]; }
+    } else if (mob == SBG_PIN) {
         const double c = std::cos(q[0]), s = std::sin(q[0]);
         X.R[0] = c; X.R[1] = -s; X.R[3] = s; X.R[4] = c;
     } else if (mob == SBG_SLIDER) {
@@ -230,7 +242,7 @@ std::vector<Xf> bodyTransforms(const Sys& s, const double* q) {
     int qo = 0;
     for (int i = 1; i <= nb; ++i) {
         const sbg_body_desc& b = s.bodies[i - 1];
-        const Xf X_PB = compose(compose(fromArr(b.X_PF), jointX(b.mobilizer, q + qo)), inverse(fromArr(b.X_BM)));
+        const Xf X_PB = compose(compose(fromArr(b.X_PF), jointX(b.mobilizer, q + qo, s.euler)), inverse(fromArr(b.X_BM)));
         X[i] = compose(X[b.parent], X_PB);
         qo += nq_of(b.mobilizer);
     }
@@ -325,7 +337,7 @@ extern "C" {
 const char* sbg_workload_last_error(void) { return g_wl_err.c_str(); }
 
 int sbg_workload_create(int32_t config, int32_t ninstances, sbg_workload* out) {
-    if (!out || ninstances < 0 || config < 1 || config > 8) { g_wl_err = "bad workload arguments"; return SBG_ERR_INVALID; }
+    if (!out || ninstances < 0 || config < 1 || config > 9) { g_wl_err = "bad workload arguments"; return SBG_ERR_INVALID; }
     auto* w = new sbg_workload_s();
     w->config = config;
     w->y_off.push_back(0);
@@ -391,9 +403,13 @@ int sbg_workload_create(int32_t config, int32_t ninstances, sbg_workload* out) {
             Sys s;
             std::vector<double> y;
             if (config == 6) randomTree(r, nb, s, y, true, (i & 1) ? SBG_BUSHING : SBG_FREE);
-            else if (config == 7) randomTree(r, nb, s, y, false, SBG_FREE, true);
+            else if (config == 7 || config == 9) randomTree(r, nb, s, y, false, SBG_FREE, true);
             else randomTree(r, nb, s, y);
-            if (config == 7) s.flags = SBG_SYSTEM_EULER_ANGLES;
+            if (config == 7 || config == 9) {
+                s.flags = SBG_SYSTEM_EULER_ANGLES;
+                s.euler = true;
+            }
+            if (config == 9) addLoops(r, s, y.data());
             if (config == 8) addContacts(r, s, y.data(), (i & 7) == 7);
             if (config == 5) {
                 addLoops(r, s, y.data());

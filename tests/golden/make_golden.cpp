@@ -153,8 +153,8 @@ int main(int argc, char** argv) {
     FILE* fc = fopen(argv[2], "wb");
     if (!fc) return 1;
     struct Sel { int cfg, ninst, nsteps; double h; std::vector<int> pick; double consTol; };
-    // cfg 5 draws 1-4 Ball loops for about one request in five; the
-    // instances listed are ones that carry loops and ones that do not.
+    // cfgs 5 and 9 draw 1-4 Ball loops for about one tree in five; for an
+    // empty list, four instances that carry loops and two that do not.
     const Sel sels[] = {
         {1, 8, 1000, 1e-3, {0, 1, 2, 3}, 0},
         {1, 8, 20, 1e-3, {4, 5, 6, 7}, 0},
@@ -167,6 +167,8 @@ int main(int argc, char** argv) {
         {7, 6, 20, 5e-4, {0, 1, 2, 3, 4, 5}, 0},
         {8, 8, 20, 5e-4, {0, 1, 2, 3, 4, 5, 6, 7}, 0},
         {8, 8, 400, 5e-4, {0, 1}, 0},
+        {9, 64, 20, 5e-4, {}, 0},
+        {9, 64, 100, 2e-3, {}, 1e-9},
     };
     int written = 0;
     for (const Sel& s : sels) {
@@ -180,7 +182,7 @@ int main(int argc, char** argv) {
         const int64_t* yo = sbg_workload_y_offsets(w);
         const double* y0 = sbg_workload_y0(w);
         std::vector<int> pick = s.pick;
-        if (pick.empty()) {  // config 5: four constrained requests and two free ones
+        if (pick.empty()) {  // configs 5 and 9: four instances with loops and two without
             int withLoops = 0, without = 0;
             for (int i = 0; i < s.ninst; ++i) {
                 const bool loops = systems[isys[i]].nconstraints > 0;

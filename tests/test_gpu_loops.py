@@ -94,7 +94,7 @@ def test_mixed_batch_keeps_loops_in_fp64(engine, w5):
 def test_engine_matches_reference_golden_vectors(engine):
     """Every golden record (configs 1-5) through the engine in FP64."""
     g = dict(np.load(GOLD))
-    sizes = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6, 8: 8}
+    sizes = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6, 8: 8, 9: 64}
     ws = {c: Workload(c, n) for c, n in sizes.items()}
     for r in range(len(g["cfg"])):
         cfg, inst = int(g["cfg"][r]), int(g["inst"][r])
@@ -113,3 +113,48 @@ def test_engine_matches_reference_golden_vectors(engine):
         assert st[0] == 0, (cfg, inst, int(st[0]))
         assert t[0] == g["t_rk"][r]
         assert np.linalg.norm(y - g["y_rk"][ys]) <= 1e-10 * np.linalg.norm(g["y_rk"][ys]), (cfg, inst)
+
+
+@pytest.mark.parametrize("path", ["batch", "server"])
+def test_euler_angle_trees_with_loops_project_like_the_oracle(engine, path):
+    """Workload 9: Ball and Free bodies in body-fixed X-Y-Z angles with Ball
+    loop closures. Their position projection weighs each such joint with
+    the 3x3 block NInv NInv^T and steps q by N_P(q) du (the oracle restates
+    it and matches the reference's records of workload 9). A 1e-9
+    tolerance at h = 2e-3 makes the projections run inside the steps (at
+    5e-4 the drift stays under it); through the batch
+    path and through the server's FP64 lanes (the Gram on three lanes) the
+    states match the oracle to 1e-10 / 1e-9."""
+    from simbody_gb300 import Server
+    from simbody_gb300.engine import Topology
+
+    w9 = Workload(9, 64)
+    idx = np.array(loop_instances(w9, 12))
+    # Instance 38 diverges at this step size (the oracle flags it
+    # NONFINITE | CHOLESKY_FAIL); the comparison keeps the ones that stay finite.
+    _, _, rst, _ = O.rk_workload(w9, 2e-3, 100, idx, cons_tol=1e-9)
+    idx = idx[rst == 0]
+    assert len(idx) >= 10
+    ref, _, rst, nproj = O.rk_workload(w9, 2e-3, 100, idx, cons_tol=1e-9)
+    assert nproj > 0 and (rst == 0).all()
+    if path == "batch":
+        b, y0 = engine_batch(w9, "fp64", instances=idx)
+        b.set_state(y0)
+        st = b.rk_merson_fixed(2e-3, 100, constraint_tolerance=1e-9)
+        y, _ = b.get_state()
+        assert (st == 0).all()
+        assert rel(y, ref, b.y_offsets).max() <= 1e-10
+    else:
+        srv = Server("fp64", device_budget_bytes=1 << 30, chunk_steps=16)
+        ids = {}
+        for i in idx:
+            t = Topology(w9.systems[int(w9.instance_system[i])], keepalive=w9)
+            ids[int(i)] = srv.submit(t, w9.y0[w9.instance_slice(int(i))], 2e-3, 100, constraint_tolerance=1e-9)
+        srv.drain()
+        off = np.concatenate([[0], np.cumsum([int(w9.y_offsets[i + 1] - w9.y_offsets[i]) for i in idx])])
+        for k, i in enumerate(idx):
+            y, inf = srv.result(ids[int(i)])
+            assert inf["status"] == 0
+            r = ref[off[k]:off[k + 1]]
+            assert np.linalg.norm(y - r) / np.linalg.norm(r) <= 1e-9, int(i)
+        srv.close()

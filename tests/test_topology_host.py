@@ -96,7 +96,7 @@ def test_largest_serving_tree_flattens():
 
 def test_euler_angle_flag_sizes_and_default_state():
     """SBG_SYSTEM_EULER_ANGLES keeps Ball/Free q slot counts (the last slot
-    unused, as Simbody's State does), drops their quaternions, and refuses
+    unused, as Simbody's State does), drops their quaternions, and takes
     loop closures; unknown flags are refused."""
     import ctypes as C
 
@@ -129,7 +129,8 @@ def test_euler_angle_flag_sizes_and_default_state():
     cons = (N.BallConstraintDesc * 1)()
     cons[0].body1, cons[0].body2 = 2, 0
     d = N.SystemDesc(2, 0, 1, N.SYSTEM_EULER_ANGLES, (C.c_double * 3)(0, -9.8, 0), bodies, None, cons)
-    assert lib.sbg_topology_create(C.byref(d), C.byref(h)) == 6  # SBG_ERR_UNSUPPORTED
+    assert lib.sbg_topology_create(C.byref(d), C.byref(h)) == 0  # loop closures in Euler-angle mode
+    lib.sbg_topology_destroy(h)
 
 
 def test_contact_spheres_are_validated_and_refused_where_unsupported():
