@@ -92,9 +92,9 @@ bool buildTopology(const sbg_system_desc& d, Topology& t, const char** err) {
 // Constraint::Ball (ConstraintImpl.h:1835-1993). Station S1 on body1 and S2
 // on body2 must coincide: perr = p_G(S2) - p_G(S1) (3 equations each).
 // The loop forward dynamics (SimbodyMatterSubsystemRep.cpp:5076-5152) solves
-// (G M^-1 G^T) lambda = aerr(udot_tree); the reference factors with
-// rank-revealing QTZ, this restatement (and the engine) with Cholesky, which
-// agree for a full-rank G.
+// (G M^-1 G^T) lambda = aerr(udot_tree) by the rank-revealing QTZ at
+// conditioning tolerance m Eps^(3/4) (:5116-5135), restated in qtzSolve
+// below, so redundant closures (G rank-deficient) solve as well.
 template <class R> struct LoopWork {
     std::vector<R> G;  // m x nu constraint Jacobian (rows)
 };
@@ -167,31 +167,165 @@ template <class R> static void perrAll(const Topology& t, const Work<R>& w, R* p
     }
 }
 
-// Cholesky of an m x m SPD matrix in place (lower), then solve.
-static bool cholSolve(int m, std::vector<double>& A, std::vector<double>& b) {
-    for (int j = 0; j < m; ++j) {
-        double s = A[j * m + j];
-        for (int k = 0; k < j; ++k) s -= A[j * m + k] * A[j * m + k];
-        if (!(s > 0)) return false;
-        const double d = std::sqrt(s);
-        A[j * m + j] = d;
-        for (int i = j + 1; i < m; ++i) {
-            double v = A[i * m + j];
-            for (int k = 0; k < j; ++k) v -= A[i * m + k] * A[j * m + k];
-            A[i * m + j] = v / d;
+// ------------------------------------------------- rank-revealing solve
+// The minimum-norm least-squares solution x of A x = b (A nr x nc, row-major)
+// through a complete orthogonal factorization, as FactorQTZ does
+// (SimTKmath/LinearAlgebra/src/FactorQTZ.cpp:355-430 factor, :225-290 solve;
+// it calls LAPACK's dgeqp3, dlaic1, dtzrzf, dormqr and dormrz the way dgelsy
+// does, LAPACK 3.x, not part of the reference's sources):
+//  1. A P = Q R by Householder QR with column pivoting, the remaining column
+//     of largest norm first;
+//  2. the rank r: 0 if R00 = 0, else the leading blocks R[0:k,0:k] are taken
+//     in turn while smin/smax > rcond, stopping at the first that fails;
+//  3. x = P [R11 R12]^+ (Q^T b)[0:r], the minimum-norm solution of the kept
+//     rows (R22 is dropped).
+// LAPACK estimates smin and smax incrementally; this restatement takes them
+// exactly (one-sided Jacobi on the leading block), so the two can decide
+// differently only for a block whose condition lies within the estimate's
+// error of 1/rcond. LAPACK reduces [R11 R12] to [T 0] Z by right-side
+// reflections; here [R11 R12]^+ c comes from a QR of its transpose, which is
+// the same minimum-norm solution. Returns r.
+
+// Householder reflector of (alpha, x[0..n)) in the convention of dlarfg:
+// H = I - tau v v^T with v = (1, x'), H (alpha, x) = (beta, 0).
+static void householder(double& alpha, double* x, int n, int stride, double& tau) {
+    double xn = 0;
+    for (int i = 0; i < n; ++i) xn += x[i * stride] * x[i * stride];
+    xn = std::sqrt(xn);
+    if (xn == 0) { tau = 0; return; }
+    const double beta = -std::copysign(std::hypot(alpha, xn), alpha);
+    tau = (beta - alpha) / beta;
+    const double sc = 1.0 / (alpha - beta);
+    for (int i = 0; i < n; ++i) x[i * stride] *= sc;
+    alpha = beta;
+}
+
+// Extreme singular values of the leading k x k block of an upper-triangular
+// matrix (row stride ld), by one-sided Jacobi rotations (Hestenes).
+static void extremeSingularValues(const std::vector<double>& R, int ld, int k, double& smin, double& smax) {
+    std::vector<double> B((size_t)k * k);
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < k; ++j) B[(size_t)j * k + i] = j >= i ? R[(size_t)i * ld + j] : 0.0;  // column j
+    const double eps = std::numeric_limits<double>::epsilon();
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        bool rotated = false;
+        for (int i = 0; i < k - 1; ++i)
+            for (int j = i + 1; j < k; ++j) {
+                double a = 0, b = 0, g = 0;
+                double* ci = &B[(size_t)i * k];
+                double* cj = &B[(size_t)j * k];
+                for (int r = 0; r < k; ++r) { a += ci[r] * ci[r]; b += cj[r] * cj[r]; g += ci[r] * cj[r]; }
+                if (!(std::abs(g) > eps * std::sqrt(a * b))) continue;
+                rotated = true;
+                const double zeta = (b - a) / (2 * g);
+                const double t = std::copysign(1.0, zeta) / (std::abs(zeta) + std::sqrt(1 + zeta * zeta));
+                const double c = 1 / std::sqrt(1 + t * t), sn = c * t;
+                for (int r = 0; r < k; ++r) {
+                    const double u = ci[r], v = cj[r];
+                    ci[r] = c * u - sn * v;
+                    cj[r] = sn * u + c * v;
+                }
+            }
+        if (!rotated) break;
+    }
+    smin = std::numeric_limits<double>::infinity();
+    smax = 0;
+    for (int j = 0; j < k; ++j) {
+        double n = 0;
+        for (int r = 0; r < k; ++r) n += B[(size_t)j * k + r] * B[(size_t)j * k + r];
+        n = std::sqrt(n);
+        smin = std::min(smin, n);
+        smax = std::max(smax, n);
+    }
+}
+
+static int qtzSolve(int nr, int nc, std::vector<double> A, double rcond, const double* b, double* x) {
+    const int mn = std::min(nr, nc);
+    std::vector<int> piv(nc);
+    for (int j = 0; j < nc; ++j) piv[j] = j;
+    std::vector<double> tau(mn, 0.0);
+    for (int k = 0; k < mn; ++k) {
+        int jmax = k;
+        double best = -1;
+        for (int j = k; j < nc; ++j) {
+            double n = 0;
+            for (int i = k; i < nr; ++i) n += A[(size_t)i * nc + j] * A[(size_t)i * nc + j];
+            if (n > best) { best = n; jmax = j; }
+        }
+        if (jmax != k) {
+            for (int i = 0; i < nr; ++i) std::swap(A[(size_t)i * nc + k], A[(size_t)i * nc + jmax]);
+            std::swap(piv[k], piv[jmax]);
+        }
+        householder(A[(size_t)k * nc + k], &A[(size_t)(k + 1) * nc + k], nr - k - 1, nc, tau[k]);
+        if (tau[k] == 0) continue;
+        for (int j = k + 1; j < nc; ++j) {
+            double w = A[(size_t)k * nc + j];
+            for (int i = k + 1; i < nr; ++i) w += A[(size_t)i * nc + k] * A[(size_t)i * nc + j];
+            w *= tau[k];
+            A[(size_t)k * nc + j] -= w;
+            for (int i = k + 1; i < nr; ++i) A[(size_t)i * nc + j] -= w * A[(size_t)i * nc + k];
         }
     }
-    for (int i = 0; i < m; ++i) {
-        double v = b[i];
-        for (int k = 0; k < i; ++k) v -= A[i * m + k] * b[k];
-        b[i] = v / A[i * m + i];
+    int r = 0;
+    if (mn > 0 && A[0] != 0) {
+        r = 1;
+        while (r < mn) {
+            double smin, smax;
+            extremeSingularValues(A, nc, r + 1, smin, smax);
+            if (!(smax * rcond < smin)) break;
+            ++r;
+        }
     }
-    for (int i = m - 1; i >= 0; --i) {
-        double v = b[i];
-        for (int k = i + 1; k < m; ++k) v -= A[k * m + i] * b[k];
-        b[i] = v / A[i * m + i];
+    // c = Q^T b
+    std::vector<double> c(b, b + nr);
+    for (int k = 0; k < mn; ++k) {
+        if (tau[k] == 0) continue;
+        double w = c[k];
+        for (int i = k + 1; i < nr; ++i) w += A[(size_t)i * nc + k] * c[i];
+        w *= tau[k];
+        c[k] -= w;
+        for (int i = k + 1; i < nr; ++i) c[i] -= w * A[(size_t)i * nc + k];
     }
-    return true;
+    std::vector<double> z(nc, 0.0);
+    if (r == nc) {
+        for (int i = r - 1; i >= 0; --i) {
+            double v = c[i];
+            for (int j = i + 1; j < r; ++j) v -= A[(size_t)i * nc + j] * z[j];
+            z[i] = v / A[(size_t)i * nc + i];
+        }
+    } else if (r > 0) {
+        // T^T = [R11 R12]^T (nc x r) = Q2 R2; z = Q2 [R2^-T c; 0].
+        std::vector<double> Tt((size_t)nc * r);
+        for (int i = 0; i < r; ++i)
+            for (int j = 0; j < nc; ++j) Tt[(size_t)j * r + i] = j >= i ? A[(size_t)i * nc + j] : 0.0;
+        std::vector<double> tau2(r, 0.0);
+        for (int k = 0; k < r; ++k) {
+            householder(Tt[(size_t)k * r + k], &Tt[(size_t)(k + 1) * r + k], nc - k - 1, r, tau2[k]);
+            if (tau2[k] == 0) continue;
+            for (int j = k + 1; j < r; ++j) {
+                double w = Tt[(size_t)k * r + j];
+                for (int i = k + 1; i < nc; ++i) w += Tt[(size_t)i * r + k] * Tt[(size_t)i * r + j];
+                w *= tau2[k];
+                Tt[(size_t)k * r + j] -= w;
+                for (int i = k + 1; i < nc; ++i) Tt[(size_t)i * r + j] -= w * Tt[(size_t)i * r + k];
+            }
+        }
+        for (int i = 0; i < r; ++i) {  // R2^T w = c, R2 upper
+            double v = c[i];
+            for (int j = 0; j < i; ++j) v -= Tt[(size_t)j * r + i] * z[j];
+            z[i] = v / Tt[(size_t)i * r + i];
+        }
+        for (int k = r - 1; k >= 0; --k) {  // z = Q2 z
+            if (tau2[k] == 0) continue;
+            double w = z[k];
+            for (int i = k + 1; i < nc; ++i) w += Tt[(size_t)i * r + k] * z[i];
+            w *= tau2[k];
+            z[k] -= w;
+            for (int i = k + 1; i < nc; ++i) z[i] -= w * Tt[(size_t)i * r + k];
+        }
+    }
+    for (int j = 0; j < nc; ++j) x[piv[j]] = z[j];
+    return r;
 }
 
 // realize(Acceleration) with Ball loop closures (double only). Returns
@@ -227,8 +361,12 @@ static int realizeAccelerationLoops(const Topology& t, const double* y, Work<dou
             A[(size_t)i * m + j] = s;
         }
     }
-    std::vector<double> lam = aerr;
-    if (!cholSolve(m, A, lam)) return st | SBG_INST_CHOLESKY_FAIL;
+    // FactorQTZ(GMInvGt, m Eps^(3/4)) and solve (:5116-5135).
+    for (double v : A)
+        if (!std::isfinite(v)) return st | SBG_INST_CHOLESKY_FAIL;
+    std::vector<double> lam(m);
+    const double eps = std::numeric_limits<double>::epsilon();
+    qtzSolve(m, m, A, m * std::sqrt(eps) * std::sqrt(std::sqrt(eps)), aerr.data(), lam.data());
     // udot -= M^-1 G^T lambda
     std::vector<double> gtl(nu, 0.0);
     for (int i = 0; i < m; ++i)
@@ -297,41 +435,44 @@ static void normalizeQuaternions(const Topology& t, double* q) {
 }
 
 // ---------------------------------------------------------- projection
-// Both projections solve a weighted minimum-norm correction through the
-// normal equations, factored by Cholesky (the reference factors the
-// weighted Jacobian with rank-revealing QTZ; the two agree for full-rank G).
+// Both projections take the minimum-norm solution of a scaled constraint
+// Jacobian through FactorQTZ (qtzSolve above), as the reference does.
 //
 // Position (projectQ, SimbodyMatterSubsystemRep.cpp:4096-4442): the reference
-// solves (P NInv) x = perr for the minimum-norm x and steps q -= N NInv x
-// (Wu = 1, Tp = 1; :4271-4300). With D = NInv NInv^T, which is 4|q|^2 I on
-// the rotational mobilities of a quaternion joint (Rotation.h:742-748), the
-// 3x3 block NInv NInv^T on those of a joint in body-fixed X-Y-Z angles
-// (NInv = [x, Rx y, Rx Ry z], RigidBodyNodeSpec_Ball.h:266-300) and 1
-// elsewhere, that is du = D G^T (G D G^T)^-1 perr, q -= N(q) du. Full Newton
-// until RMS(perr) <= 0.1 tol, at most 20 iterations; with localOnly the
-// iteration stops when the norm grows (:4310-4321); the entry q is restored
-// if the result is worse than on entry (:4336-4341); then quaternions are
-// normalized (:4411-4413).
+// solves (P NInv) x = perr for the minimum-norm x, at conditioning tolerance
+// m Eps^(1/2) (:4256-4281), and steps q -= N NInv x (Wu = 1, Tp = 1;
+// :4282-4300). Here the same solution is taken in u space: with S
+// any square factor of NInv NInv^T (S S^T = NInv NInv^T), the minimum-norm x'
+// of (G S) x' = perr gives du = S x' = NInv x, and G S has the singular values
+// of P NInv. S is 2|q| I on the rotational mobilities of a quaternion joint
+// (NInv NInv^T = 4|q|^2 I for the unnormalized NInv, Rotation.h:742-748), the
+// 3x3 NInv itself on those of a joint in body-fixed X-Y-Z angles (NInv =
+// [x, Rx y, Rx Ry z], RigidBodyNodeSpec_Ball.h:266-300) and 1 elsewhere. Full
+// Newton until RMS(perr) <= 0.1 tol, at most 20 iterations; with localOnly
+// the iteration stops when the norm grows (:4310-4321); the entry q is
+// restored if the result is worse than on entry (:4336-4341); then
+// quaternions are normalized (:4411-4413).
 //
-// Velocity (projectU, :4664-4943): weights uRelScale_i = max(|u_i|, 1)
-// taken at entry (:4760-4765), du = E^2 G^T (G E^2 G^T)^-1 verr with the
-// factorization made once (:4806-4808), at most 7 iterations.
+// Velocity (projectU, :4664-4943): E = diag(uRelScale), uRelScale_i =
+// max(|u_i|, 1) taken at entry (:4778-4784); the minimum-norm x of (G E) x =
+// verr at tolerance m Eps^(1/2) (:4793-4812), du = E x, the factorization
+// made once; at most 7 iterations.
 
 static double normRMSv(const std::vector<double>& v) { return normRMS(v.data(), (int)v.size()); }
 
-// The 3x3 weight blocks of the joints in body-fixed X-Y-Z angles: u offset
-// and NInv NInv^T (row-major); their mobilities' diagonal weights are 0.
-struct WeightBlocks {
+// Block-diagonal nu x nu scale: diag, overridden by 3x3 blocks (row-major)
+// at the u offsets in uoff.
+struct ScaleFactor {
+    std::vector<double> diag;
     std::vector<int> uoff;
     std::vector<double> B;  // 9 per block
 };
 
-// D = diag(NInv NInv^T) per mobility for the current (unnormalized) q, and
-// the full blocks of the Euler-angle joints.
-static void projectionWeightsQ(const Topology& t, const double* q, std::vector<double>& D, WeightBlocks& blk) {
-    D.assign(t.nu, 1.0);
-    blk.uoff.clear();
-    blk.B.clear();
+// S with S S^T = NInv NInv^T for the current (unnormalized) q.
+static void projectionFactorQ(const Topology& t, const double* q, ScaleFactor& S) {
+    S.diag.assign(t.nu, 1.0);
+    S.uoff.clear();
+    S.B.clear();
     for (int bi = 1; bi <= t.nb; ++bi) {
         const Body& b = t.b[bi];
         const double* qq = q + b.qoff;
@@ -339,56 +480,52 @@ static void projectionWeightsQ(const Topology& t, const double* q, std::vector<d
             const double c0 = std::cos(qq[0]), s0 = std::sin(qq[0]), c1 = std::cos(qq[1]), s1 = std::sin(qq[1]);
             // NInv columns: (1,0,0), (0,c0,s0), (s1,-s0 c1,c0 c1)
             const double N[9] = {1, 0, s1, 0, c0, -s0 * c1, 0, s0, c0 * c1};
-            double B[9];
-            for (int r = 0; r < 3; ++r)
-                for (int c = 0; c < 3; ++c) B[3 * r + c] = N[3 * r] * N[3 * c] + N[3 * r + 1] * N[3 * c + 1] + N[3 * r + 2] * N[3 * c + 2];
-            blk.uoff.push_back(b.uoff);
-            blk.B.insert(blk.B.end(), B, B + 9);
-            for (int k = 0; k < 3; ++k) D[b.uoff + k] = 0.0;
+            S.uoff.push_back(b.uoff);
+            S.B.insert(S.B.end(), N, N + 9);
             continue;
         }
         if (!b.quat) continue;
-        const double n2 = qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3];
-        for (int k = 0; k < 3; ++k) D[b.uoff + k] = 4 * n2;
+        const double n = std::sqrt(qq[0] * qq[0] + qq[1] * qq[1] + qq[2] * qq[2] + qq[3] * qq[3]);
+        for (int k = 0; k < 3; ++k) S.diag[b.uoff + k] = 2 * n;
     }
 }
 
-// A = G D G^T (m x m), D = diag(Wt) plus the blocks.
-static void weightedGram(int m, int nu, const std::vector<double>& G, const std::vector<double>& Wt,
-                         std::vector<double>& A, const WeightBlocks* blk = nullptr) {
-    A.assign((size_t)m * m, 0.0);
+// A = G S (m x nu).
+static void scaledJacobian(int m, int nu, const std::vector<double>& G, const ScaleFactor& S, std::vector<double>& A) {
+    A.assign((size_t)m * nu, 0.0);
     for (int i = 0; i < m; ++i)
-        for (int j = 0; j < m; ++j) {
-            double s = 0;
-            for (int k = 0; k < nu; ++k) s += G[(size_t)i * nu + k] * Wt[k] * G[(size_t)j * nu + k];
-            if (blk)
-                for (size_t bk = 0; bk < blk->uoff.size(); ++bk) {
-                    const int u = blk->uoff[bk];
-                    const double* B = &blk->B[9 * bk];
-                    for (int a = 0; a < 3; ++a)
-                        for (int c = 0; c < 3; ++c) s += G[(size_t)i * nu + u + a] * B[3 * a + c] * G[(size_t)j * nu + u + c];
-                }
-            A[(size_t)i * m + j] = s;
+        for (int k = 0; k < nu; ++k) A[(size_t)i * nu + k] = G[(size_t)i * nu + k] * S.diag[k];
+    for (size_t bk = 0; bk < S.uoff.size(); ++bk) {
+        const int u = S.uoff[bk];
+        const double* B = &S.B[9 * bk];
+        for (int i = 0; i < m; ++i) {
+            const double* g = &G[(size_t)i * nu + u];
+            for (int c = 0; c < 3; ++c) A[(size_t)i * nu + u + c] = g[0] * B[c] + g[1] * B[3 + c] + g[2] * B[6 + c];
         }
+    }
 }
 
-// du = D G^T lambda.
-static void weightedGT(int m, int nu, const std::vector<double>& G, const std::vector<double>& Wt,
-                       const std::vector<double>& lam, std::vector<double>& du, const WeightBlocks* blk = nullptr) {
+// du = S x.
+static void applyScale(int nu, const ScaleFactor& S, const std::vector<double>& x, std::vector<double>& du) {
     du.assign(nu, 0.0);
-    std::vector<double> g(nu);
-    for (int k = 0; k < nu; ++k) {
-        double s = 0;
-        for (int i = 0; i < m; ++i) s += G[(size_t)i * nu + k] * lam[i];
-        g[k] = s;
-        du[k] = Wt[k] * s;
+    for (int k = 0; k < nu; ++k) du[k] = S.diag[k] * x[k];
+    for (size_t bk = 0; bk < S.uoff.size(); ++bk) {
+        const int u = S.uoff[bk];
+        const double* B = &S.B[9 * bk];
+        for (int a = 0; a < 3; ++a) du[u + a] = B[3 * a] * x[u] + B[3 * a + 1] * x[u + 1] + B[3 * a + 2] * x[u + 2];
     }
-    if (blk)
-        for (size_t bk = 0; bk < blk->uoff.size(); ++bk) {
-            const int u = blk->uoff[bk];
-            const double* B = &blk->B[9 * bk];
-            for (int a = 0; a < 3; ++a) du[u + a] = B[3 * a] * g[u] + B[3 * a + 1] * g[u + 1] + B[3 * a + 2] * g[u + 2];
-        }
+}
+
+// qtzSolve of a finite system; false (the projection fails) otherwise.
+static bool qtzSolveFinite(int m, int nu, const std::vector<double>& A, double rcond, const double* b,
+                           std::vector<double>& x) {
+    for (double v : A)
+        if (!std::isfinite(v)) return false;
+    for (int i = 0; i < m; ++i)
+        if (!std::isfinite(b[i])) return false;
+    x.assign(nu, 0.0);
+    qtzSolve(m, nu, A, rcond, b, x.data());
+    return true;
 }
 
 // dq = N(q) du with the unnormalized N of Rotation.h:712-719.
@@ -440,21 +577,21 @@ static void verrAt(const Topology& t, const double* q, const double* u, Work<dou
 // Newton iteration of projectQ (loops present, perr not yet acceptable).
 static bool projectQNewton(const Topology& t, double* q, Work<double>& w, double tol, bool localOnly) {
     const int m = 3 * (int)t.constraints.size();
-    std::vector<double> perr, G, D, A, lam, du, dq(t.nq);
-    WeightBlocks blk;
+    std::vector<double> perr, G, A, x(t.nu), du, dq(t.nq);
+    ScaleFactor S;
     perrAt(t, q, w, perr);
     const double normOnEntry = normRMSv(perr);
     const std::vector<double> saveQ(q, q + t.nq);
     const double tryFor = std::max(0.1 * tol, std::pow(std::numeric_limits<double>::epsilon(), 0.875));
     double achieved = normOnEntry, prev = normOnEntry;
     int its = 0;
+    const double condTol = m * std::sqrt(std::numeric_limits<double>::epsilon());
     do {
         constraintJacobian(t, w, G);
-        projectionWeightsQ(t, q, D, blk);
-        weightedGram(m, t.nu, G, D, A, &blk);
-        lam = perr;
-        if (!cholSolve(m, A, lam)) return false;
-        weightedGT(m, t.nu, G, D, lam, du, &blk);
+        projectionFactorQ(t, q, S);
+        scaledJacobian(m, t.nu, G, S, A);
+        if (!qtzSolveFinite(m, t.nu, A, condTol, perr.data(), x)) return false;
+        applyScale(t.nu, S, x, du);
         multiplyByN(t, q, du.data(), dq.data());
         for (int k = 0; k < t.nq; ++k) q[k] -= dq[k];
         perrAt(t, q, w, perr);
@@ -480,7 +617,7 @@ static bool projectQNewton(const Topology& t, double* q, Work<double>& w, double
 static bool projectULoops(const Topology& t, const double* q, double* u, Work<double>& w, double tol, bool force,
                           double limit, bool localOnly) {
     const int m = 3 * (int)t.constraints.size();
-    std::vector<double> verr, G, E2(t.nu), A, lam, du;
+    std::vector<double> verr, G, E2(t.nu), A, du;
     realizePosition(t, q, w);
     verrAt(t, q, u, w, verr);
     const double normOnEntry = normRMSv(verr);
@@ -491,18 +628,19 @@ static bool projectULoops(const Topology& t, const double* q, double* u, Work<do
         E2[k] = e * e;
     }
     constraintJacobian(t, w, G);
-    weightedGram(m, t.nu, G, E2, A);
-    // factor once: cholSolve factors in place, so keep the factor for reuse
-    const std::vector<double> A0 = A;
+    ScaleFactor E;
+    E.diag = E2;
+    for (double& e : E.diag) e = std::sqrt(e);
+    scaledJacobian(m, t.nu, G, E, A);
+    const double condTol = m * std::sqrt(std::numeric_limits<double>::epsilon());
+    std::vector<double> x(t.nu);
     const std::vector<double> saveU(u, u + t.nu);
     const double tryFor = std::max(0.1 * tol, std::pow(std::numeric_limits<double>::epsilon(), 0.875));
     double achieved = normOnEntry, prev = normOnEntry;
     int its = 0;
     do {
-        A = A0;
-        lam = verr;
-        if (!cholSolve(m, A, lam)) return false;
-        weightedGT(m, t.nu, G, E2, lam, du);
+        if (!qtzSolveFinite(m, t.nu, A, condTol, verr.data(), x)) return false;
+        applyScale(t.nu, E, x, du);
         for (int k = 0; k < t.nu; ++k) u[k] -= du[k];
         verrAt(t, q, u, w, verr);
         achieved = normRMSv(verr);

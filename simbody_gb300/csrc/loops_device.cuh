@@ -16,8 +16,10 @@
 // with the tree solution udot_t,  (G M^-1 G^T) lambda = aerr(udot_t),
 // udot = udot_t - M^-1 G^T lambda. Column j of G M^-1 G^T is the point
 // acceleration difference of an M^-1 sweep driven by unit forces of
-// equation j. The m x m system (m <= 12) is factored by Cholesky in FP64;
-// the reference uses rank-revealing QTZ, which agrees for a full-rank G.
+// equation j. The m x m system (m <= 12) is factored in FP64 by a Cholesky
+// with symmetric pivoting that drops the equations a redundant closure
+// repeats (loopCholFactor); the reference's rank-revealing QTZ gives the same
+// constraint forces.
 //
 // Projections (SimbodyMatterSubsystemRep.cpp:4096-4442 and 4664-4943):
 //   position  du = D G^T (G D G^T)^-1 perr, q -= N(q) du, full Newton until
@@ -780,33 +782,132 @@ __device__ __forceinline__ void loopSweepColumn(const LoopState& L, const Wt& wt
     }
 }
 
-// Cholesky of the leading m x m block (row stride kMaxLoopEq), lower factor
-// in place; then the two triangular solves.
-__device__ __forceinline__ bool loopCholFactor(int m, double* A) {
-    for (int j = 0; j < m; ++j) {
-        double s = A[j * kMaxLoopEq + j];
-        for (int k = 0; k < j; ++k) s -= A[j * kMaxLoopEq + k] * A[j * kMaxLoopEq + k];
-        if (!(s > 0)) return false;
-        const double d = sqrt(s);
-        A[j * kMaxLoopEq + j] = d;
-        for (int i = j + 1; i < m; ++i) {
-            double v = A[i * kMaxLoopEq + j];
-            for (int k = 0; k < j; ++k) v -= A[i * kMaxLoopEq + k] * A[j * kMaxLoopEq + k];
-            A[i * kMaxLoopEq + j] = v / d;
+// Rank-revealing Cholesky of the leading m x m block of a positive
+// semidefinite Gram (row stride kMaxLoopEq; its lower triangle is the matrix):
+// symmetric pivoting, the largest remaining diagonal first, stopping at the
+// first pivot not above relTol times the first. F.r is the rank kept and
+// F.piv the order of the equations: A = W W^T with W = P [L11; L21] (m x r).
+// loopCholSolve gives the least-squares solution lambda = W (W^T W)^-2 W^T b
+// (A^-1 b at full rank). The reference's QTZ factorization takes the
+// minimum-norm least-squares solution; the two differ by a null vector of A,
+// which is one of G^T, so the constraint forces and the projections'
+// corrections agree, also where the equations of redundant closures do not
+// (the centripetal accelerations of two pinned points of one body spinning
+// about another axis). relTol is the reference's conditioning tolerance for
+// the matrix the Gram squares: kAccRelTol for G M^-1 G^T, whose own
+// condition the reference tests, kProjRelTol for G D G^T, the square of the
+// weighted Jacobian whose condition it tests. false when the block is not
+// finite or its largest diagonal is not positive.
+struct LoopFactor {
+    int r;
+    signed char piv[kMaxLoopEq];
+};
+__device__ __forceinline__ double kAccRelTol(int m) { return m * 1.8189894035458565e-12; }  // m Eps^(3/4)
+__device__ __forceinline__ double kProjRelTol(int m) { return (double)(m * m) * 2.220446049250313e-16; }  // (m Eps^(1/2))^2
+
+__device__ __forceinline__ bool loopCholFactor(int m, double* A, double relTol, LoopFactor& F) {
+    F.r = 0;
+    for (int i = 0; i < m; ++i) {
+        F.piv[i] = (signed char)i;
+        for (int k = 0; k <= i; ++k) {
+            const double v = A[i * kMaxLoopEq + k];
+            if (!isfinite(v)) return false;
+            A[k * kMaxLoopEq + i] = v;
         }
+    }
+    double d0 = 0;
+    for (int j = 0; j < m; ++j) {
+        int p = j;
+        double best = A[j * kMaxLoopEq + j];
+        for (int i = j + 1; i < m; ++i)
+            if (A[i * kMaxLoopEq + i] > best) { best = A[i * kMaxLoopEq + i]; p = i; }
+        if (j == 0) {
+            if (!(best > 0)) return false;
+            d0 = best;
+        }
+        if (!(best > relTol * d0)) break;
+        if (p != j) {
+            for (int k = 0; k < m; ++k) {
+                const double t = A[j * kMaxLoopEq + k];
+                A[j * kMaxLoopEq + k] = A[p * kMaxLoopEq + k];
+                A[p * kMaxLoopEq + k] = t;
+            }
+            for (int k = 0; k < m; ++k) {
+                const double t = A[k * kMaxLoopEq + j];
+                A[k * kMaxLoopEq + j] = A[k * kMaxLoopEq + p];
+                A[k * kMaxLoopEq + p] = t;
+            }
+            const signed char t = F.piv[j];
+            F.piv[j] = F.piv[p];
+            F.piv[p] = t;
+        }
+        const double d = sqrt(best);
+        A[j * kMaxLoopEq + j] = d;
+        for (int i = j + 1; i < m; ++i) A[i * kMaxLoopEq + j] /= d;
+        for (int i = j + 1; i < m; ++i)
+            for (int k = j + 1; k < m; ++k) A[i * kMaxLoopEq + k] -= A[i * kMaxLoopEq + j] * A[k * kMaxLoopEq + j];
+        F.r = j + 1;
     }
     return true;
 }
-__device__ __forceinline__ void loopCholSolve(int m, const double* A, double* b) {
-    for (int i = 0; i < m; ++i) {
-        double v = b[i];
-        for (int k = 0; k < i; ++k) v -= A[i * kMaxLoopEq + k] * b[k];
-        b[i] = v / A[i * kMaxLoopEq + i];
+__device__ __forceinline__ void loopCholSolve(int m, const double* A, const LoopFactor& F, double* b) {
+    double w[kMaxLoopEq];
+    for (int i = 0; i < m; ++i) w[i] = b[F.piv[i]];
+    const int r = F.r;
+    if (r == m) {
+        for (int i = 0; i < r; ++i) {
+            double v = w[i];
+            for (int k = 0; k < i; ++k) v -= A[i * kMaxLoopEq + k] * w[k];
+            w[i] = v / A[i * kMaxLoopEq + i];
+        }
+        for (int i = r - 1; i >= 0; --i) {
+            double v = w[i];
+            for (int k = i + 1; k < r; ++k) v -= A[k * kMaxLoopEq + i] * w[k];
+            w[i] = v / A[i * kMaxLoopEq + i];
+        }
+        for (int i = 0; i < m; ++i) b[F.piv[i]] = w[i];
+        return;
     }
-    for (int i = m - 1; i >= 0; --i) {
-        double v = b[i];
-        for (int k = i + 1; k < m; ++k) v -= A[k * kMaxLoopEq + i] * b[k];
-        b[i] = v / A[i * kMaxLoopEq + i];
+    // W[i][j] = A[i][j] for i >= j, j < r. C = W^T W = R R^T (lower R);
+    // y = C^-1 C^-1 W^T w; lambda = W y.
+    double C[kMaxLoopEq * kMaxLoopEq], y[kMaxLoopEq];
+    for (int j = 0; j < r; ++j) {
+        double t = 0;
+        for (int i = j; i < m; ++i) t += A[i * kMaxLoopEq + j] * w[i];
+        y[j] = t;
+        for (int k = 0; k <= j; ++k) {
+            double c = 0;
+            for (int i = j; i < m; ++i) c += A[i * kMaxLoopEq + j] * A[i * kMaxLoopEq + k];
+            C[j * kMaxLoopEq + k] = c;
+        }
+    }
+    for (int j = 0; j < r; ++j) {
+        double d = C[j * kMaxLoopEq + j];
+        for (int k = 0; k < j; ++k) d -= C[j * kMaxLoopEq + k] * C[j * kMaxLoopEq + k];
+        d = sqrt(d);
+        C[j * kMaxLoopEq + j] = d;
+        for (int i = j + 1; i < r; ++i) {
+            double v = C[i * kMaxLoopEq + j];
+            for (int k = 0; k < j; ++k) v -= C[i * kMaxLoopEq + k] * C[j * kMaxLoopEq + k];
+            C[i * kMaxLoopEq + j] = v / d;
+        }
+    }
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int i = 0; i < r; ++i) {
+            double v = y[i];
+            for (int k = 0; k < i; ++k) v -= C[i * kMaxLoopEq + k] * y[k];
+            y[i] = v / C[i * kMaxLoopEq + i];
+        }
+        for (int i = r - 1; i >= 0; --i) {
+            double v = y[i];
+            for (int k = i + 1; k < r; ++k) v -= C[k * kMaxLoopEq + i] * y[k];
+            y[i] = v / C[i * kMaxLoopEq + i];
+        }
+    }
+    for (int i = 0; i < m; ++i) {
+        double v = 0;
+        for (int j = 0; j <= i && j < r; ++j) v += A[i * kMaxLoopEq + j] * y[j];
+        b[F.piv[i]] = v;
     }
 }
 
@@ -917,8 +1018,9 @@ __device__ __noinline__ int loopForwardDynamics(const LoopState& L, Out& out) {
     double A[kMaxLoopEq * kMaxLoopEq];
     const NoWeights one{};
     loopGram<NM, kMInvSweep>(L, one, A);
-    if (!loopCholFactor(m, A)) return SBG_INST_CHOLESKY_FAIL;
-    loopCholSolve(m, A, lam);
+    LoopFactor F;
+    if (!loopCholFactor(m, A, kAccRelTol(m), F)) return SBG_INST_CHOLESKY_FAIL;
+    loopCholSolve(m, A, F, lam);
     loopClearForces(L);
     for (int c = 0; c < nc; ++c) loopAddConstraintForce(L, loopGeom(L, c), mk3(lam[3 * c], lam[3 * c + 1], lam[3 * c + 2]));
     if constexpr (DEFER_OUT) {
@@ -958,8 +1060,9 @@ __device__ __noinline__ int loopForwardDynamicsLanes(const LoopState& L, Out& ou
     const NoWeights one{};
     loopGramLanes<NM, kMInvSweep>(L, one, A, gl, mask);
     if (gl != 0) return 0;
-    if (!loopCholFactor(m, A)) return SBG_INST_CHOLESKY_FAIL;
-    loopCholSolve(m, A, lam);
+    LoopFactor F;
+    if (!loopCholFactor(m, A, kAccRelTol(m), F)) return SBG_INST_CHOLESKY_FAIL;
+    loopCholSolve(m, A, F, lam);
     loopClearForces(L);
     for (int c = 0; c < nc; ++c) loopAddConstraintForce(L, loopGeom(L, c), mk3(lam[3 * c], lam[3 * c + 1], lam[3 * c + 2]));
     loopSweepIn<NM, kMInvSweep>(L, one);
@@ -1143,8 +1246,9 @@ __device__ __noinline__ bool loopProjectQ(const LoopState& L, double tol, bool l
     const PosWeights wq{&L};  // D = NInv NInv^T of the current q
     do {
         loopGram<NM, kJacSweep>(L, wq, A);
-        if (!loopCholFactor(m, A)) return false;
-        loopCholSolve(m, A, perr);
+        LoopFactor F;
+        if (!loopCholFactor(m, A, kProjRelTol(m), F)) return false;
+        loopCholSolve(m, A, F, perr);
         loopClearForces(L);
         for (int c = 0; c < m / 3; ++c)
             loopAddConstraintForce(L, loopGeom(L, c), mk3(perr[3 * c], perr[3 * c + 1], perr[3 * c + 2]));
@@ -1191,12 +1295,13 @@ __device__ __noinline__ bool loopProjectU(const LoopState& L, double tol, bool f
     // E^2 with E = max(|u|, 1) frozen at entry
     const VelWeights wu{&L, nq};
     loopGram<NM, kJacSweep>(L, wu, A);
-    if (!loopCholFactor(m, A)) return false;
+    LoopFactor F;
+    if (!loopCholFactor(m, A, kProjRelTol(m), F)) return false;
     const double tryFor = loopTryFor(tol);
     double achieved = normOnEntry, prev = normOnEntry;
     int its = 0;
     do {
-        loopCholSolve(m, A, verr);
+        loopCholSolve(m, A, F, verr);
         loopClearForces(L);
         for (int c = 0; c < m / 3; ++c)
             loopAddConstraintForce(L, loopGeom(L, c), mk3(verr[3 * c], verr[3 * c + 1], verr[3 * c + 2]));
@@ -1259,10 +1364,11 @@ __device__ __noinline__ bool loopProjectQLanes(const LoopState& L, double tol, b
         loopGramLanes<NM, kJacSweep>(L, wq, A, gl, mask);
         int fail = 0;
         if (lead) {
-            if (!loopCholFactor(m, A)) {
+            LoopFactor F;
+            if (!loopCholFactor(m, A, kProjRelTol(m), F)) {
                 fail = 1;
             } else {
-                loopCholSolve(m, A, perr);
+                loopCholSolve(m, A, F, perr);
                 loopClearForces(L);
                 for (int c = 0; c < m / 3; ++c)
                     loopAddConstraintForce(L, loopGeom(L, c), mk3(perr[3 * c], perr[3 * c + 1], perr[3 * c + 2]));
@@ -1323,14 +1429,15 @@ __device__ __noinline__ bool loopProjectULanes(const LoopState& L, double tol, b
     __syncwarp(mask);  // the saved u, before the Gram's weights read it
     const VelWeights wu{&L, nq};
     loopGramLanes<NM, kJacSweep>(L, wu, A, gl, mask);
-    int fail = lead ? (loopCholFactor(m, A) ? 0 : 1) : 0;
+    LoopFactor F;
+    int fail = lead ? (loopCholFactor(m, A, kProjRelTol(m), F) ? 0 : 1) : 0;
     if (laneBcast(fail, base, mask)) return false;
     const double tryFor = loopTryFor(tol);
     double achieved = normOnEntry, prev = normOnEntry;
     int its = 0;
     do {
         if (lead) {
-            loopCholSolve(m, A, verr);
+            loopCholSolve(m, A, F, verr);
             loopClearForces(L);
             for (int c = 0; c < m / 3; ++c)
                 loopAddConstraintForce(L, loopGeom(L, c), mk3(verr[3 * c], verr[3 * c + 1], verr[3 * c + 2]));

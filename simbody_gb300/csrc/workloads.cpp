@@ -33,6 +33,9 @@
 //     sphere on every body (station U[-0.05,0.05]^3, radius U[0.02,0.06]), the
 //     half-space normal tilted U[-0.2,0.2] rad from -Y, the lowest sphere
 //     indented 3 mm at t = 0; 2000 steps of 5e-4.
+// 10  random trees as 3, each closed by 1..2 Ball closures to Ground and made
+//     redundant: a repeated closure, a second pinned point of the same body,
+//     or both (instance % 3), so G M^-1 G^T is rank-deficient.
 #include "../../include/simbody_gb300.h"
 #include "sbg_workloads.h"
 
@@ -251,10 +254,10 @@ std::vector<Xf> bodyTransforms(const Sys& s, const double* q) {
 
 // 20% of serving requests get 1..4 Ball closures from a deep body to Ground,
 // with the Ground station at the body station's t = 0 location.
-void addLoops(std::mt19937_64& r, Sys& s, const double* q) {
+void addLoops(std::mt19937_64& r, Sys& s, const double* q, bool always = false, int maxLoops = 4) {
     std::uniform_real_distribution<double> U01(0, 1), UP(-0.05, 0.05);
-    if (U01(r) >= 0.2) return;
-    std::uniform_int_distribution<int> nl(1, 4);
+    if (!always && U01(r) >= 0.2) return;
+    std::uniform_int_distribution<int> nl(1, maxLoops);
     int want = nl(r);
     const int nb = (int)s.bodies.size();
     // depth and dofs along the path from Ground
@@ -281,6 +284,31 @@ void addLoops(std::mt19937_64& r, Sys& s, const double* q) {
         c.body2 = 0;
         for (int j = 0; j < 3; ++j) c.station1[j] = UP(r);
         const Xf& Xb = X[b];
+        for (int j = 0; j < 3; ++j)
+            c.station2[j] = Xb.R[3 * j] * c.station1[0] + Xb.R[3 * j + 1] * c.station1[1] + Xb.R[3 * j + 2] * c.station1[2] + Xb.p[j];
+        s.cons.push_back(c);
+    }
+}
+
+// Workload 10: every tree closed by one or two Ball closures to Ground, then
+// made redundant (kind = instance % 3): 0 repeats the first closure exactly
+// (G M^-1 G^T loses rank 3), 1 pins a second point of the first closure's body
+// (two points fix all but the rotation about the line through them: 6
+// equations of rank 5), 2 does both. The added closures hold at t = 0.
+void addRedundantLoops(std::mt19937_64& r, Sys& s, const double* q, int kind) {
+    addLoops(r, s, q, true, 2);
+    if (s.cons.empty()) return;
+    const sbg_ball_constraint_desc c0 = s.cons[0];
+    if (kind != 1) s.cons.push_back(c0);
+    if (kind != 0) {
+        std::uniform_real_distribution<double> UA(0.1, 0.2), US(-1, 1);
+        sbg_ball_constraint_desc c = c0;
+        double dir[3], n = 0;
+        for (int j = 0; j < 3; ++j) { dir[j] = US(r); n += dir[j] * dir[j]; }
+        n = std::sqrt(n);
+        const double len = UA(r);
+        for (int j = 0; j < 3; ++j) c.station1[j] = c0.station1[j] + len * dir[j] / n;
+        const Xf& Xb = bodyTransforms(s, q)[c0.body1];
         for (int j = 0; j < 3; ++j)
             c.station2[j] = Xb.R[3 * j] * c.station1[0] + Xb.R[3 * j + 1] * c.station1[1] + Xb.R[3 * j + 2] * c.station1[2] + Xb.p[j];
         s.cons.push_back(c);
@@ -337,7 +365,7 @@ extern "C" {
 const char* sbg_workload_last_error(void) { return g_wl_err.c_str(); }
 
 int sbg_workload_create(int32_t config, int32_t ninstances, sbg_workload* out) {
-    if (!out || ninstances < 0 || config < 1 || config > 9) { g_wl_err = "bad workload arguments"; return SBG_ERR_INVALID; }
+    if (!out || ninstances < 0 || config < 1 || config > 10) { g_wl_err = "bad workload arguments"; return SBG_ERR_INVALID; }
     auto* w = new sbg_workload_s();
     w->config = config;
     w->y_off.push_back(0);
@@ -410,6 +438,7 @@ int sbg_workload_create(int32_t config, int32_t ninstances, sbg_workload* out) {
                 s.euler = true;
             }
             if (config == 9) addLoops(r, s, y.data());
+            if (config == 10) addRedundantLoops(r, s, y.data(), (int)(i % 3));
             if (config == 8) addContacts(r, s, y.data(), (i & 7) == 7);
             if (config == 5) {
                 addLoops(r, s, y.data());

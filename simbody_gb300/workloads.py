@@ -14,6 +14,8 @@ Python harness see identical inputs).
   7  trees as 3 with Euler-angle Ball and Free bodies
   8  trees as 3 with a contact sphere on every body over a ground half-space
   9  trees as 7 (Euler-angle mode), 20% with 1-4 Ball loop closures
+ 10  trees as 3 with redundant Ball closures: a repeated closure, a second
+     pinned point of a closed body, or both (rank-deficient G M^-1 G^T)
 """
 from __future__ import annotations
 
@@ -23,7 +25,7 @@ import numpy as np
 
 from . import _native as N
 
-DEFAULT_INSTANCES = {1: 1024, 2: 65536, 3: 16384, 4: 10000, 5: 2000, 6: 16384, 7: 16384, 8: 16384, 9: 1000}
+DEFAULT_INSTANCES = {1: 1024, 2: 65536, 3: 16384, 4: 10000, 5: 2000, 6: 16384, 7: 16384, 8: 16384, 9: 1000, 10: 300}
 
 
 class Workload:

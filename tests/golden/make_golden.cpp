@@ -169,6 +169,8 @@ int main(int argc, char** argv) {
         {8, 8, 400, 5e-4, {0, 1}, 0},
         {9, 64, 20, 5e-4, {}, 0},
         {9, 64, 100, 2e-3, {}, 1e-9},
+        {10, 6, 20, 5e-4, {0, 1, 2, 3, 4, 5}, 0},
+        {10, 6, 100, 2e-3, {0, 1, 2, 3, 4, 5}, 1e-9},
     };
     int written = 0;
     for (const Sel& s : sels) {

@@ -29,7 +29,7 @@ def _worst(a, b, off):
 
 def test_adaptive_matches_reference_records(engine):
     g = dict(np.load(GOLD))
-    sizes = {1: 8, 2: 4, 3: 6, 4: 8, 6: 8, 7: 6, 8: 8, 9: 64}
+    sizes = {1: 8, 2: 4, 3: 6, 4: 8, 6: 8, 7: 6, 8: 8, 9: 64, 10: 6}
     for r in range(len(g["a_cfg"])):
         cfg, inst = int(g["a_cfg"][r]), int(g["a_inst"][r])
         w = Workload(cfg, sizes[cfg])

@@ -5,7 +5,8 @@ Instances with loop closures run the FP64 chain driver in every precision
 (the multiplier solve and the projections are FP64), so they are held to the
 FP64 tolerances: realize <= 1e-12 relative, trajectories <= 1e-10 relative
 (projections are Newton solves stopped at a tolerance; roundoff differences
-between the Cholesky paths shift the iterates slightly).
+between the engine's pivoted Cholesky of the Gram and the oracle's QTZ
+factorization of the Jacobian shift the iterates slightly).
 """
 from pathlib import Path
 
@@ -94,7 +95,7 @@ def test_mixed_batch_keeps_loops_in_fp64(engine, w5):
 def test_engine_matches_reference_golden_vectors(engine):
     """Every golden record (configs 1-5) through the engine in FP64."""
     g = dict(np.load(GOLD))
-    sizes = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6, 8: 8, 9: 64}
+    sizes = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6, 8: 8, 9: 64, 10: 6}
     ws = {c: Workload(c, n) for c, n in sizes.items()}
     for r in range(len(g["cfg"])):
         cfg, inst = int(g["cfg"][r]), int(g["inst"][r])
@@ -125,9 +126,6 @@ def test_euler_angle_trees_with_loops_project_like_the_oracle(engine, path):
     5e-4 the drift stays under it); through the batch
     path and through the server's FP64 lanes (the Gram on three lanes) the
     states match the oracle to 1e-10 / 1e-9."""
-    from simbody_gb300 import Server
-    from simbody_gb300.engine import Topology
-
     w9 = Workload(9, 64)
     idx = np.array(loop_instances(w9, 12))
     # Instance 38 diverges at this step size (the oracle flags it
@@ -145,16 +143,58 @@ def test_euler_angle_trees_with_loops_project_like_the_oracle(engine, path):
         assert (st == 0).all()
         assert rel(y, ref, b.y_offsets).max() <= 1e-10
     else:
-        srv = Server("fp64", device_budget_bytes=1 << 30, chunk_steps=16)
-        ids = {}
-        for i in idx:
-            t = Topology(w9.systems[int(w9.instance_system[i])], keepalive=w9)
-            ids[int(i)] = srv.submit(t, w9.y0[w9.instance_slice(int(i))], 2e-3, 100, constraint_tolerance=1e-9)
-        srv.drain()
-        off = np.concatenate([[0], np.cumsum([int(w9.y_offsets[i + 1] - w9.y_offsets[i]) for i in idx])])
-        for k, i in enumerate(idx):
-            y, inf = srv.result(ids[int(i)])
-            assert inf["status"] == 0
-            r = ref[off[k]:off[k + 1]]
-            assert np.linalg.norm(y - r) / np.linalg.norm(r) <= 1e-9, int(i)
-        srv.close()
+        server_vs_oracle(w9, idx, 2e-3, 100, ref)
+
+
+def server_vs_oracle(w, idx, h, nsteps, ref, bound=1e-9):
+    """Each instance as an FP64 server request with a 1e-9 constraint
+    tolerance, against the oracle's states ref (concatenated over idx)."""
+    from simbody_gb300 import Server
+    from simbody_gb300.engine import Topology
+
+    srv = Server("fp64", device_budget_bytes=1 << 30, chunk_steps=16)
+    ids = {}
+    for i in idx:
+        t = Topology(w.systems[int(w.instance_system[i])], keepalive=w)
+        ids[int(i)] = srv.submit(t, w.y0[w.instance_slice(int(i))], h, nsteps, constraint_tolerance=1e-9)
+    srv.drain()
+    off = np.concatenate([[0], np.cumsum([int(w.y_offsets[i + 1] - w.y_offsets[i]) for i in idx])])
+    for k, i in enumerate(idx):
+        y, inf = srv.result(ids[int(i)])
+        assert inf["status"] == 0
+        r = ref[off[k]:off[k + 1]]
+        assert np.linalg.norm(y - r) / np.linalg.norm(r) <= bound, int(i)
+    srv.close()
+
+
+@pytest.mark.parametrize("path", ["batch", "server"])
+def test_redundant_closures_match_oracle(engine, path):
+    """Workload 10: every tree closed to Ground and made redundant (a repeated
+    closure, a second pinned point of the same body, or both), so G M^-1 G^T
+    and the projections' Gram lose rank. The engine's pivoted Cholesky drops
+    the equations that repeat others; the oracle restates the reference's
+    QTZ minimum-norm solve, and matches the reference's records of this
+    workload to 1e-14. Realize (FP64 and mixed batches) <= 1e-12; 100 steps
+    of 1e-3 at a 1e-9 constraint tolerance, where the projections run in
+    the steps, <= 1e-10 on the batch path and 1e-9 through the server."""
+    w = Workload(10, 48)
+    idx = np.arange(48)
+    ref, _, rst, nproj = O.rk_workload(w, 1e-3, 100, idx, cons_tol=1e-9)
+    assert nproj > 0 and (rst == 0).all()
+    if path == "server":
+        server_vs_oracle(w, idx, 1e-3, 100, ref)
+        return
+    rd, rdst = O.realize_workload(w, idx)
+    assert (rdst == 0).all()
+    for precision in ("fp64", "mixed"):
+        b, y0 = engine_batch(w, precision, instances=idx)
+        b.set_state(y0)
+        ydot, st = b.realize_acceleration()
+        assert (st == 0).all()
+        assert rel(ydot, rd, b.y_offsets).max() <= 1e-12, precision
+    b, y0 = engine_batch(w, "fp64", instances=idx)
+    b.set_state(y0)
+    st = b.rk_merson_fixed(1e-3, 100, constraint_tolerance=1e-9)
+    y, _ = b.get_state()
+    assert (st == 0).all()
+    assert rel(y, ref, b.y_offsets).max() <= 1e-10

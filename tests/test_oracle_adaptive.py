@@ -53,7 +53,7 @@ def test_step_size_controller(err, limited, h_min, h_max, ok, factor):
 
 def test_fixed_limits_reproduce_the_reference_fixed_step_states():
     g = dict(np.load(GOLD))
-    w_all = {c: Workload(c, n) for c, n in {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6, 8: 8, 9: 64}.items()}
+    w_all = {c: Workload(c, n) for c, n in {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6, 8: 8, 9: 64, 10: 6}.items()}
     checked = 0
     for r in range(len(g["cfg"])):
         cfg, inst = int(g["cfg"][r]), int(g["inst"][r])
@@ -120,7 +120,7 @@ def test_error_controlled_matches_reference_records():
     takes the same numbers of accepted and rejected steps, ends on the final
     time and reproduces the final state to 1e-11."""
     g = dict(np.load(GOLD))
-    sizes = {1: 8, 2: 4, 3: 6, 4: 8, 6: 8, 7: 6, 8: 8, 9: 64}
+    sizes = {1: 8, 2: 4, 3: 6, 4: 8, 6: 8, 7: 6, 8: 8, 9: 64, 10: 6}
     ws = {c: Workload(c, n) for c, n in sizes.items()}
     for r, cfg, inst, ys in _adaptive_records(g):
         assert g["a_status"][r] == 0

@@ -22,7 +22,7 @@ from simbody_gb300 import Workload
 from simbody_gb300 import _native as N
 
 GOLD = Path(__file__).resolve().parent / "golden" / "reference_vectors.npz"
-WORKLOAD_SIZES = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6, 8: 8, 9: 64}
+WORKLOAD_SIZES = {1: 8, 2: 4, 3: 6, 4: 8, 5: 64, 6: 8, 7: 6, 8: 8, 9: 64, 10: 6}
 
 
 @pytest.fixture(scope="module")
@@ -114,6 +114,35 @@ def test_tight_tolerance_records_project_in_steps(gold, workloads):
                                        cons_tol=float(gold["cons_tol"][r]))
         done += nproj > 0
     assert done >= 3
+
+
+def test_redundant_closures_solve_like_reference(gold, workloads):
+    """Workload 10 repeats a closure or pins a second point of a closed body,
+    so G M^-1 G^T is rank-deficient. The oracle's QTZ minimum-norm solve (the reference's FactorQTZ) matches the
+    reference's records, the tight-tolerance ones with projections in every
+    few steps."""
+    w = workloads[10]
+    kinds = set()
+    projected = 0
+    for r, cfg, inst, ys, _ in _records(gold):
+        if cfg != 10:
+            continue
+        s = w.systems[int(w.instance_system[inst])]
+        cons = [(s.constraints[k].body1, tuple(s.constraints[k].station1)) for k in range(s.nconstraints)]
+        repeated = len(set(cons)) < len(cons)
+        two_points = len({b for b, _ in cons}) < len(set(cons))
+        kinds.add((repeated, two_points))
+        ydot, st = O.realize_workload(w, [inst])
+        assert st[0] == 0 and gold["status"][r] == 0
+        ref = gold["ydot"][ys]
+        assert np.linalg.norm(ydot - ref) / np.linalg.norm(ref) <= 1e-12
+        y, _, st, nproj = O.rk_workload(w, float(gold["h"][r]), int(gold["nsteps"][r]), [inst],
+                                        cons_tol=float(gold["cons_tol"][r]))
+        ref = gold["y_rk"][ys]
+        assert st[0] == 0 and np.linalg.norm(y - ref) / np.linalg.norm(ref) <= 1e-11
+        projected += nproj > 0
+    assert kinds == {(True, False), (False, True), (True, True)}
+    assert projected >= 6
 
 
 def test_qdotdot_matches_reference(gold, workloads):
