@@ -13,6 +13,10 @@
 //                           make the in-step projections run), stepped for
 //                           exactly nsteps steps
 //   qdd                     s.getQDotDot() after the realize above
+//   adapter_gdev            the Simbody-side adapter (simbody_gb300_simtk.hpp)
+//                           reads the built system back into descriptors: all
+//                           fields equal the workload's bit for bit (else the
+//                           run stops), gravity to this relative deviation
 // and, into a second file, integrator continuation records: with
 // setFixedStepSize(h) and setAllowInterpolation(false), after initialize(s)
 //   mode 0  stepTo(t_mid); stepTo(t_end)     (a second call continues)
@@ -29,7 +33,7 @@
 //   RungeKuttaMersonIntegrator (SimTKmath/Integrators/include/simmath/RungeKuttaMersonIntegrator.h)
 //
 // Output: one binary file of records
-//   int64 cfg, inst, ny, nu, nsteps, status   double h, t_rk, cons_tol
+//   int64 cfg, inst, ny, nu, nsteps, status   double h, t_rk, cons_tol, adapter_gdev
 //   double y0[ny], ydot[ny], f[nu], minv_f[nu], y_rk[ny], qdd[ny - nu]
 // and a second of continuation records
 //   int64 cfg, inst, ny, mode, status, nsteps_taken   double h, t_mid, t_end, t_out
@@ -46,16 +50,13 @@
 #include <vector>
 
 #include "sbg_workloads.h"
+#include "simbody_gb300_simtk.hpp"
 
 using namespace SimTK;
 
 namespace {
 
-Transform toTransform(const double* x) {
-    // x = row-major 3x3 rotation followed by the translation
-    const Mat33 R(x[0], x[1], x[2], x[3], x[4], x[5], x[6], x[7], x[8]);
-    return Transform(Rotation(R, true), Vec3(x[9], x[10], x[11]));
-}
+Transform toTransform(const double* x) { return sbg::simtk::unpackTransform(x); }
 
 // One MultibodySystem per described system; body index 0 is Ground and body
 // k >= 1 is desc.bodies[k-1].
@@ -64,6 +65,7 @@ struct Model {
     SimbodyMatterSubsystem matter;
     GeneralForceSubsystem forces;
     std::vector<MobilizedBody> mobods;
+    sbg::simtk::ForceLog log;  // the elements whose parameters Simbody does not expose
 
     explicit Model(const sbg_system_desc& d) : matter(sys), forces(sys) {
         const Vec3 g(d.gravity[0], d.gravity[1], d.gravity[2]);
@@ -94,24 +96,22 @@ struct Model {
         for (int i = 0; i < d.nforces; ++i) {
             const sbg_mobility_force_desc& f = d.forces[i];
             if (f.kind == 0)
-                Force::MobilityLinearSpring(forces, mobods[f.body], MobilizerQIndex(f.which), f.coef, f.q0);
+                log.addMobilityLinearSpring(forces, mobods[f.body], MobilizerQIndex(f.which), f.coef, f.q0);
             else
-                Force::MobilityLinearDamper(forces, mobods[f.body], MobilizerUIndex(f.which), f.coef);
+                log.addMobilityLinearDamper(forces, mobods[f.body], MobilizerUIndex(f.which), f.coef);
         }
         for (int i = 0; i < d.ncontacts; ++i) {
             const sbg_contact_desc& k = d.contacts[i];
-            SmoothSphereHalfSpaceForce f(forces);
-            f.setContactSphereBody(mobods[k.body]);
-            f.setContactSphereLocationInBody(Vec3(k.station[0], k.station[1], k.station[2]));
-            f.setContactSphereRadius(k.radius);
-            f.setContactHalfSpaceBody(matter.Ground());
-            f.setContactHalfSpaceFrame(toTransform(k.halfspace));
             const double* par = &k.stiffness;
+            sbg::simtk::ContactParameters p;
             bool zero = true;
-            for (int j = 0; j < 9; ++j) zero = zero && par[j] == 0;
-            if (!zero)  // a zero block keeps the force's own defaults
-                f.setParameters(k.stiffness, k.dissipation, k.static_friction, k.dynamic_friction, k.viscous_friction,
-                                k.transition_velocity, k.cf, k.bd, k.bv);
+            for (int j = 0; j < 9; ++j) {
+                p[j] = par[j];
+                zero = zero && par[j] == 0;
+            }
+            // a zero block keeps the force's own defaults
+            log.addSmoothSphereHalfSpaceForce(forces, mobods[k.body], Vec3(k.station[0], k.station[1], k.station[2]),
+                                              k.radius, matter.Ground(), toTransform(k.halfspace), zero ? nullptr : &p);
         }
         for (int i = 0; i < d.nconstraints; ++i) {
             const sbg_ball_constraint_desc& c = d.constraints[i];
@@ -133,6 +133,62 @@ struct Model {
         return st;
     }
 };
+
+// The Simbody-side adapter (include/simbody_gb300_simtk.hpp) reads the
+// built system back into descriptors; they must equal the ones it was built
+// from, every field bit for bit except gravity, which Force::Gravity keeps as
+// a unit direction and a magnitude. Returns gravity's relative deviation;
+// exits on any other difference.
+double adapterRoundTrip(const sbg_system_desc& d, Model& m, int cfg, int inst) {
+    const State st = m.defaultState();
+    const sbg::simtk::SystemDescription a = sbg::simtk::describe(m.matter, m.forces, m.log, st);
+    const sbg_system_desc& e = a.desc;
+    int bad = 0;
+    auto same = [&](const double* x, const double* y, int n) {
+        for (int k = 0; k < n; ++k) bad += x[k] != y[k];
+    };
+    bad += e.nbodies != d.nbodies || e.nforces != d.nforces || e.nconstraints != d.nconstraints ||
+           e.ncontacts != d.ncontacts || e.flags != d.flags;
+    if (!bad) {
+        for (int i = 0; i < d.nbodies; ++i) {
+            const sbg_body_desc &x = e.bodies[i], &y = d.bodies[i];
+            bad += x.parent != y.parent || x.mobilizer != y.mobilizer || x.mass != y.mass;
+            same(x.com, y.com, 3);
+            same(x.unit_inertia, y.unit_inertia, 6);
+            same(x.X_PF, y.X_PF, 12);
+            same(x.X_BM, y.X_BM, 12);
+            if (y.mobilizer == SBG_SCREW) bad += x.pitch != y.pitch;
+        }
+        for (int i = 0; i < d.nforces; ++i) {
+            const sbg_mobility_force_desc &x = e.forces[i], &y = d.forces[i];
+            bad += x.kind != y.kind || x.body != y.body || x.which != y.which || x.coef != y.coef;
+            if (y.kind == 0) bad += x.q0 != y.q0;
+        }
+        for (int i = 0; i < d.nconstraints; ++i) {
+            const sbg_ball_constraint_desc &x = e.constraints[i], &y = d.constraints[i];
+            bad += x.body1 != y.body1 || x.body2 != y.body2;
+            same(x.station1, y.station1, 3);
+            same(x.station2, y.station2, 3);
+        }
+        for (int i = 0; i < d.ncontacts; ++i) {
+            const sbg_contact_desc &x = e.contacts[i], &y = d.contacts[i];
+            bad += x.body != y.body || x.radius != y.radius;
+            same(x.station, y.station, 3);
+            same(x.halfspace, y.halfspace, 12);
+            same(&x.stiffness, &y.stiffness, 9);
+        }
+    }
+    if (bad) {
+        fprintf(stderr, "cfg %d inst %d: the adapter's descriptors differ in %d fields\n", cfg, inst, bad);
+        std::exit(1);
+    }
+    double gn = 0, dn = 0;
+    for (int k = 0; k < 3; ++k) {
+        gn += d.gravity[k] * d.gravity[k];
+        dn += (e.gravity[k] - d.gravity[k]) * (e.gravity[k] - d.gravity[k]);
+    }
+    return gn > 0 ? std::sqrt(dn / gn) : std::sqrt(dn);
+}
 
 void put(FILE* fp, const void* p, size_t bytes) {
     if (fwrite(p, 1, bytes, fp) != bytes) {
@@ -195,6 +251,7 @@ int main(int argc, char** argv) {
         for (int i : pick) {
             const sbg_system_desc& d = systems[isys[i]];
             Model m(d);
+            const double gdev = adapterRoundTrip(d, m, s.cfg, i);
             const int64_t ny = yo[i + 1] - yo[i];
             int64_t status = 0;
             State st = m.defaultState();
@@ -203,7 +260,7 @@ int main(int argc, char** argv) {
                 return 1;
             }
             const int64_t nu = st.getNU();
-            for (int k = 0; k < ny; ++k) st.updY()[k] = y0[yo[i] + k];
+            sbg::simtk::setY(&y0[yo[i]], st);
             std::vector<double> ydot(ny), f(nu), minv(nu), yrk(ny);
             m.sys.realize(st, Stage::Acceleration);
             for (int k = 0; k < ny; ++k) ydot[k] = st.getYDot()[k];
@@ -216,21 +273,21 @@ int main(int argc, char** argv) {
             double trk = 0;
             try {
                 State s2 = m.defaultState();
-                for (int k = 0; k < ny; ++k) s2.updY()[k] = y0[yo[i] + k];
+                sbg::simtk::setY(&y0[yo[i]], s2);
                 RungeKuttaMersonIntegrator integ(m.sys);
                 integ.setFixedStepSize(s.h);
                 integ.setReturnEveryInternalStep(true);
                 if (s.consTol > 0) integ.setConstraintTolerance(s.consTol);
                 integ.initialize(s2);
                 while (integ.getNumStepsTaken() < s.nsteps) integ.stepTo(1e9);
-                for (int k = 0; k < ny; ++k) yrk[k] = integ.getState().getY()[k];
+                sbg::simtk::getY(integ.getState(), yrk.data());
                 trk = integ.getTime();
             } catch (const std::exception& e) {
                 fprintf(stderr, "cfg %d inst %d: integrator failed: %s\n", s.cfg, i, e.what());
                 status = 1;
             }
             const int64_t hdr[6] = {s.cfg, i, ny, nu, s.nsteps, status};
-            const double hd[3] = {s.h, trk, s.consTol};
+            const double hd[4] = {s.h, trk, s.consTol, gdev};
             put(fp, hdr, sizeof hdr);
             put(fp, hd, sizeof hd);
             put(fp, &y0[yo[i]], ny * 8);
@@ -285,7 +342,7 @@ int main(int argc, char** argv) {
                 double tout = 0;
                 try {
                     State s2 = m.defaultState();
-                    for (int k = 0; k < ny; ++k) s2.updY()[k] = y0[yo[i] + k];
+                    sbg::simtk::setY(&y0[yo[i]], s2);
                     RungeKuttaMersonIntegrator integ(m.sys);
                     integ.setFixedStepSize(c.h);
                     integ.setAllowInterpolation(false);
@@ -294,7 +351,7 @@ int main(int argc, char** argv) {
                     if (mode == 0) { to(c.tMid); to(c.tEnd); }
                     else if (mode == 1) to(c.tEnd);
                     else to(c.tEnd + 0.3 * c.h);
-                    for (int k = 0; k < ny; ++k) yout[k] = integ.getState().getY()[k];
+                    sbg::simtk::getY(integ.getState(), yout.data());
                     tout = integ.getTime();
                     taken = integ.getNumStepsTaken();
                 } catch (const std::exception& e) {
@@ -348,13 +405,13 @@ int main(int argc, char** argv) {
             double tout = 0;
             try {
                 State s2 = m.defaultState();
-                for (int k = 0; k < ny; ++k) s2.updY()[k] = y0[yo[i] + k];
+                sbg::simtk::setY(&y0[yo[i]], s2);
                 RungeKuttaMersonIntegrator integ(m.sys);
                 integ.setAccuracy(c.acc);
                 integ.setFinalTime(c.tFinal);
                 integ.initialize(s2);
                 while (integ.getTime() < c.tFinal) integ.stepTo(c.tFinal);
-                for (int k = 0; k < ny; ++k) yout[k] = integ.getState().getY()[k];
+                sbg::simtk::getY(integ.getState(), yout.data());
                 tout = integ.getTime();
                 taken = integ.getNumStepsTaken();
                 attempted = integ.getNumStepsAttempted();

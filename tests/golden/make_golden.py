@@ -9,6 +9,9 @@ driver make_golden.cpp is compiled against them, run on the seeded workloads
 
   cfg, inst, ny, nu, nsteps, status, h, t_rk,    one entry per record
   cons_tol (0 = the integrator's default)
+  adapter_gdev (include/simbody_gb300_simtk.hpp read the built system back
+                into descriptors equal to the workload's; gravity's relative
+                deviation, the only field not kept bit for bit)
   y_off, u_off, q_off                            offsets into the flat arrays
   y0, ydot, y_rk (by y_off); f, minv_f (by u_off); qdd (by q_off)
 
@@ -57,16 +60,17 @@ def read_records(path: Path) -> dict:
     while pos < len(raw):
         hdr = np.frombuffer(raw, dtype=np.int64, count=6, offset=pos)
         pos += 48
-        h, t, ctol = np.frombuffer(raw, dtype=np.float64, count=3, offset=pos)
-        pos += 24
+        h, t, ctol, gdev = np.frombuffer(raw, dtype=np.float64, count=4, offset=pos)
+        pos += 32
         cfg, inst, ny, nu, nsteps, status = (int(v) for v in hdr)
         arrs = {}
         for name, n in (("y0", ny), ("ydot", ny), ("f", nu), ("minv_f", nu), ("y_rk", ny), ("qdd", ny - nu)):
             arrs[name] = np.frombuffer(raw, dtype=np.float64, count=n, offset=pos).copy()
             pos += 8 * n
-        recs.append(dict(cfg=cfg, inst=inst, ny=ny, nu=nu, nsteps=nsteps, status=status, h=h, t_rk=t, cons_tol=ctol, **arrs))
+        recs.append(dict(cfg=cfg, inst=inst, ny=ny, nu=nu, nsteps=nsteps, status=status, h=h, t_rk=t, cons_tol=ctol,
+                         adapter_gdev=gdev, **arrs))
     out = {k: np.array([r[k] for r in recs]) for k in ("cfg", "inst", "ny", "nu", "nsteps", "status", "h", "t_rk",
-                                                 "cons_tol")}
+                                                 "cons_tol", "adapter_gdev")}
     out["y_off"] = np.concatenate([[0], np.cumsum(out["ny"])]).astype(np.int64)
     out["u_off"] = np.concatenate([[0], np.cumsum(out["nu"])]).astype(np.int64)
     out["q_off"] = np.concatenate([[0], np.cumsum(out["ny"] - out["nu"])]).astype(np.int64)

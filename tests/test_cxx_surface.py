@@ -64,3 +64,19 @@ def test_cxx_surface_on_the_host(tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == "ok", (r.returncode, r.stdout, r.stderr)
+
+
+def test_simtk_adapter_round_trips_every_recorded_system():
+    """include/simbody_gb300_simtk.hpp is compiled against Simbody by the
+    golden-vector generator (tests/golden/make_golden.{py,cpp}), which builds
+    each recorded system through its ForceLog, reads it back with describe()
+    and stops unless every descriptor field equals the workload's bit for bit;
+    gravity, kept by Force::Gravity as a direction and a magnitude, is
+    recorded as a relative deviation. Every record carries one, and all are
+    within rounding."""
+    import numpy as np
+
+    g = np.load(ROOT / "tests" / "golden" / "reference_vectors.npz")
+    assert len(g["adapter_gdev"]) == len(g["cfg"]) > 0
+    assert set(np.unique(g["cfg"])) == set(range(1, 11))
+    assert g["adapter_gdev"].max() <= 1e-15
