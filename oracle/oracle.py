@@ -41,6 +41,7 @@ def lib() -> C.CDLL:
         L.oracle_rk_merson_adaptive_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, dp, C.c_double,
                                                       C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                                       C.c_int32, C.c_int32, ip, i64p, C.c_int32]
+        L.oracle_qtz_solve.argtypes = [C.c_int32, C.c_int32, dp, C.c_double, dp, dp]
         L.oracle_adjust_step_size.argtypes = [C.c_double, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double,
                                               dp]
         L.oracle_count_realize.argtypes = [sd, dp, i64p]
@@ -199,6 +200,16 @@ def adjust_step_size(err, h, accuracy=1e-3, err_order=4, limited=False, h_min=0.
     ok = lib().oracle_adjust_step_size(float(err), int(err_order), int(limited), float(accuracy), float(h_min),
                                        float(h_max), C.byref(hh))
     return bool(ok), hh.value
+
+
+def qtz_solve(A, b, rcond):
+    """The rank-revealing solve of the loop closures alone: (minimum-norm
+    least-squares x of A x = b at conditioning tolerance rcond, rank)."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(A.shape[1])
+    r = lib().oracle_qtz_solve(A.shape[0], A.shape[1], _d(A), float(rcond), _d(b), _d(x))
+    return x, r
 
 
 def count_realize(system_ptr, y):

@@ -1210,6 +1210,13 @@ int oracle_adjust_step_size(double err, int32_t errOrder, int32_t limited, doubl
     return adjustStepSize(err, errOrder, limited != 0, accuracy, hMin, hMax, *h) ? 1 : 0;
 }
 
+// The rank-revealing minimum-norm solve alone (qtzSolve), for its unit tests:
+// A nr x nc row-major, x gets nc values; returns the rank.
+int oracle_qtz_solve(int32_t nr, int32_t nc, const double* A, double rcond, const double* b, double* x) {
+    if (nr < 0 || nc < 0) return setErr("negative size");
+    return qtzSolve(nr, nc, std::vector<double>(A, A + (size_t)nr * nc), rcond, b, x);
+}
+
 // Exact operation counts of one realize(Acceleration) of one instance with
 // the counting scalar: counts[0]=add/sub, [1]=mul, [2]=div, [3]=sqrt,
 // [4]=sin/cos, [5]=abs/compare.
