@@ -96,7 +96,8 @@ typedef enum sbg_precision {
 #define SBG_INST_NONFINITE          1   /* NaN/Inf in a derivative or state */
 #define SBG_INST_SINGULAR_D         2   /* zero pivot in a D = H^T P H inverse */
 #define SBG_INST_PROJECTION_FAILED  4   /* quaternion/constraint projection refused */
-#define SBG_INST_CHOLESKY_FAIL      8   /* loop-closure Gram not finite (redundant closures solve) */
+#define SBG_INST_CHOLESKY_FAIL      8   /* loop-closure Gram not finite, or all zero (closures no
+                                               mobility can move); redundant closures solve */
 #define SBG_INST_TIMEOUT           16   /* persistent kernel hit its iteration budget */
 /* Mixed form, internal: at some RHS of this instance the refinement
  * correction was larger than a set fraction of udot (1e-4 in a realize, 1e-5
