@@ -1,8 +1,9 @@
 // simbody_gb300_simtk.hpp -- Simbody (SimTK) side of the drop-in: reads a
 // MultibodySystem into the C ABI's descriptors and moves State y vectors to
 // and from the ABI's packing. Header-only C++17; include after "Simbody.h"
-// and link Simbody as usual. The batch calls themselves go through
-// simbody_gb300.hpp (sbg::Topology, sbg::StateBatch, ...) or the C ABI.
+// and link Simbody as usual. The batch calls go through simbody_gb300.hpp
+// (sbg::Topology, sbg::StateBatch, ...), which this header includes; the
+// helpers at the end move batches of States through them.
 //
 //   sbg::simtk::ForceLog log;                          // next to the GeneralForceSubsystem
 //   log.addMobilityLinearSpring(forces, mobod, MobilizerQIndex(0), k, q0);
@@ -36,7 +37,7 @@
 #include <string>
 #include <vector>
 
-#include "simbody_gb300.h"
+#include "simbody_gb300.hpp"
 
 namespace sbg {
 namespace simtk {
@@ -282,6 +283,65 @@ inline void setY(const double* y, SimTK::State& s) {
     SimTK::Vector& Y = s.updY();
     const int n = ny(s);
     for (int k = 0; k < n; ++k) Y[k] = y[k];
+}
+
+// ------------------------------------------------- batches of States
+// Instance i of the batch is states[i]; each State's system must be the
+// instance's topology (the batch's instanceTopology).
+
+// State::getY and getTime of every State into the batch.
+inline void loadStates(StateBatch& batch, const std::vector<const SimTK::State*>& states) {
+    const std::vector<int64_t>& off = batch.getYOffsets();
+    if ((int)states.size() != batch.getNumInstances()) throw Error(SBG_ERR_INVALID, "one State per instance");
+    std::vector<double> y((size_t)off.back()), t(states.size());
+    for (size_t i = 0; i < states.size(); ++i) {
+        if (ny(*states[i]) != off[i + 1] - off[i]) throw Error(SBG_ERR_INVALID, "State size differs from its topology");
+        getY(*states[i], y.data() + off[i]);
+        t[i] = states[i]->getTime();
+    }
+    batch.setY(y, t);
+}
+
+// The batch's y and times back into the States (after an integration).
+inline void storeStates(const StateBatch& batch, const std::vector<SimTK::State*>& states) {
+    const std::vector<int64_t>& off = batch.getYOffsets();
+    if ((int)states.size() != batch.getNumInstances()) throw Error(SBG_ERR_INVALID, "one State per instance");
+    const std::vector<double> y = batch.getY(), t = batch.getTime();
+    for (size_t i = 0; i < states.size(); ++i) {
+        if (ny(*states[i]) != off[i + 1] - off[i]) throw Error(SBG_ERR_INVALID, "State size differs from its topology");
+        setY(y.data() + off[i], *states[i]);
+        states[i]->setTime(t[i]);
+    }
+}
+
+// System::realize(s, Stage::Acceleration) and s.getYDot() for every State:
+// ydot[i] of states[i]; status (may be null) gets the SBG_INST_* words.
+inline std::vector<SimTK::Vector> realizeAcceleration(StateBatch& batch, const std::vector<const SimTK::State*>& states,
+                                                      std::vector<int32_t>* status = nullptr) {
+    loadStates(batch, states);
+    const std::vector<double> yd = batch.realizeAcceleration(status);
+    const std::vector<int64_t>& off = batch.getYOffsets();
+    std::vector<SimTK::Vector> out(states.size());
+    for (size_t i = 0; i < states.size(); ++i) {
+        const int n = (int)(off[i + 1] - off[i]);
+        out[i].resize(n);
+        for (int k = 0; k < n; ++k) out[i][k] = yd[off[i] + k];
+    }
+    return out;
+}
+
+// RungeKuttaMersonIntegrator::initialize(s) and stepTo(tReport) for every
+// State, the results written back into the States. Configure integ
+// (setFixedStepSize, setAccuracy, ...) before; the States' common time is the
+// start. Returns the SBG_INST_* word of each (Integrator::StepFailed analogue).
+inline std::vector<int32_t> integrateTo(RungeKuttaMersonBatchIntegrator& integ, StateBatch& batch,
+                                        const std::vector<SimTK::State*>& states, double tReport) {
+    const std::vector<const SimTK::State*> in(states.begin(), states.end());
+    loadStates(batch, in);
+    integ.initialize(states.empty() ? 0.0 : states[0]->getTime());
+    std::vector<int32_t> st = integ.stepTo(tReport);
+    storeStates(batch, states);
+    return st;
 }
 
 }  // namespace simtk
