@@ -166,3 +166,26 @@ def test_contact_spheres_are_validated_and_refused_where_unsupported():
         assert b"contact" in lib.sbg_noalloc_last_error()
     finally:
         lib.sbg_topology_destroy(h)
+
+
+def test_closure_counts_and_redundant_closures():
+    """Redundant closures are taken as Simbody builds them: a repeated
+    closure and a second pinned point of the same body. Batches hold up to
+    four closures per system (12 equations, the multiplier solve's fixed
+    size); a batch of a system with five is refused SBG_ERR_UNSUPPORTED
+    before any device is touched (the server refuses it at submit)."""
+    lib = N.engine_lib()
+    b = chain(8, N.SBG_BALL)
+    c = (N.BallConstraintDesc * 5)()
+    for k, (body, s) in enumerate([(8, 0.0), (8, 0.0), (8, 0.1), (6, 0.0), (4, 0.0)]):
+        c[k].body1, c[k].body2 = body, 0
+        c[k].station1[0] = s
+    t4 = Topology(make(b, 8, None, 0, c, 4), keepalive=(b, c))
+    assert t4.nbodies == 8
+    t5 = Topology(make(b, 8, None, 0, c, 5), keepalive=(b, c))
+    which = (C.c_int32 * 1)(0)
+    cfg = N.BatchConfig(N.PRECISION_FP64, 0, 0)
+    h = C.c_void_p()
+    topos = (C.c_void_p * 1)(t5.handle)
+    assert lib.sbg_batch_create(topos, 1, which, 1, C.byref(cfg), C.byref(h)) == 6  # SBG_ERR_UNSUPPORTED
+    assert b"at most 4" in lib.sbg_last_error()
