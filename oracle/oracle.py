@@ -41,6 +41,7 @@ def lib() -> C.CDLL:
         L.oracle_rk_merson_adaptive_batch.argtypes = [sd, C.c_int32, ip, C.c_int32, i64p, dp, dp, C.c_double,
                                                       C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                                       C.c_int32, C.c_int32, ip, i64p, C.c_int32]
+        L.oracle_instance_invariants.argtypes = [C.POINTER(N.SystemDesc), dp, dp, dp, dp, dp]
         L.oracle_qtz_solve.argtypes = [C.c_int32, C.c_int32, dp, C.c_double, dp, dp]
         L.oracle_adjust_step_size.argtypes = [C.c_double, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double,
                                               dp]
@@ -200,6 +201,21 @@ def adjust_step_size(err, h, accuracy=1e-3, err_order=4, limited=False, h_min=0.
     ok = lib().oracle_adjust_step_size(float(err), int(err_order), int(limited), float(accuracy), float(h_min),
                                        float(h_max), C.byref(hh))
     return bool(ok), hh.value
+
+
+def invariants(system, y):
+    """Kinetic, gravity and spring energies and the Ball closures' position,
+    velocity and acceleration errors (after the constrained realize) of one
+    instance: dict(ke, pe_gravity, pe_springs, perr, verr, aerr, status)."""
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    m = 3 * int(system.nconstraints)
+    en = np.zeros(3)
+    perr, verr, aerr = np.zeros(max(m, 1)), np.zeros(max(m, 1)), np.zeros(max(m, 1))
+    st = lib().oracle_instance_invariants(C.byref(system), _d(y), _d(en), _d(perr), _d(verr), _d(aerr))
+    if st < 0:
+        raise RuntimeError(lib().oracle_last_error().decode())
+    return dict(ke=en[0], pe_gravity=en[1], pe_springs=en[2], perr=perr[:m], verr=verr[:m], aerr=aerr[:m],
+                status=st)
 
 
 def qtz_solve(A, b, rcond):

@@ -1210,6 +1210,71 @@ int oracle_adjust_step_size(double err, int32_t errOrder, int32_t limited, doubl
     return adjustStepSize(err, errOrder, limited != 0, accuracy, hMin, hMax, *h) ? 1 : 0;
 }
 
+// Invariants of one instance at y, for the restated known-answer tests:
+// energy[0] kinetic energy u.M u / 2 (multiplyByM, as above); energy[1]
+// gravity's potential energy -sum m g.p_C (Force_Gravity.cpp:531-556, zero
+// height 0); energy[2] the mobility springs' sum k (q[which] - q0)^2 / 2
+// (Force.cpp:353-360). perr, verr, aerr (3 per Ball closure; may be null when
+// there are none): the closure errors of ConstraintImpl.h:1896-1960 at y, the
+// accelerations those of the constrained realize(Acceleration). Returns the
+// realize's SBG_INST_* bits.
+int oracle_instance_invariants(const sbg_system_desc* d, const double* y, double* energy, double* perr, double* verr,
+                               double* aerr) {
+    Topology t;
+    const char* e = nullptr;
+    if (!buildTopology(*d, t, &e)) return -setErr(e);
+    Work<double> w;
+    w.resize(t);
+    const double* q = y;
+    const double* u = y + t.nq;
+    std::vector<double> ydot(t.nq + t.nu), Mu(t.nu);
+    const int st = t.constraints.empty() ? (realizeAcceleration(t, y, w, ydot.data()) ? 0 : SBG_INST_SINGULAR_D)
+                                         : realizeAccelerationLoops(t, y, w, ydot.data());
+    realizePosition(t, q, w);
+    realizeVelocity(t, q, u, w, (double*)nullptr);
+    accelerationsOutward(t, w, u, false);
+    forcesInward(t, w, 1, (const double*)nullptr, (const double*)nullptr, Mu.data());
+    double ke = 0;
+    for (int k = 0; k < t.nu; ++k) ke += u[k] * Mu[k];
+    energy[0] = ke / 2;
+    // accelerationsOutward overwrote the body accelerations; positions and
+    // velocities are unchanged.
+    double pe = 0;
+    const V3<double> g = loadV<double>(d->gravity);
+    for (int bi = 1; bi <= t.nb; ++bi) {
+        const BodyCache<double>& c = w.c[bi];
+        const V3<double> pC = c.p_GB + c.R_GB * loadV<double>(d->bodies[bi - 1].com);
+        pe -= d->bodies[bi - 1].mass * dot(g, pC);
+    }
+    energy[1] = pe;
+    double ps = 0;
+    for (int i = 0; i < d->nforces; ++i) {
+        const sbg_mobility_force_desc& f = d->forces[i];
+        if (f.kind != 0) continue;
+        const double dq = q[t.b[f.body].qoff + f.which] - f.q0;
+        ps += f.coef * dq * dq / 2;
+    }
+    energy[2] = ps;
+    if (!t.constraints.empty()) {
+        accelerationsOutward(t, w, ydot.data() + t.nq, true);
+        std::vector<V3<double>> Aw(t.nb + 1), Av(t.nb + 1);
+        for (int b = 0; b <= t.nb; ++b) { Aw[b] = w.c[b].Aw; Av[b] = w.c[b].Av; }
+        perrAll(t, w, perr);
+        for (size_t ci = 0; ci < t.constraints.size(); ++ci) {
+            const auto& c = t.constraints[ci];
+            const V3<double> pS = pointS(w, c);
+            V3<double> v1, a1, v2, a2;
+            pointKin(w, c.body1, pS, v1, &a1, Aw.data(), Av.data());
+            pointKin(w, c.body2, pS, v2, &a2, Aw.data(), Av.data());
+            for (int k = 0; k < 3; ++k) {
+                verr[3 * ci + k] = v2[k] - v1[k];
+                aerr[3 * ci + k] = a2[k] - a1[k];
+            }
+        }
+    }
+    return st;
+}
+
 // The rank-revealing minimum-norm solve alone (qtzSolve), for its unit tests:
 // A nr x nc row-major, x gets nc values; returns the rank.
 int oracle_qtz_solve(int32_t nr, int32_t nc, const double* A, double rcond, const double* b, double* x) {

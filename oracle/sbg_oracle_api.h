@@ -36,6 +36,8 @@ int oracle_rk_merson_adaptive_batch(const sbg_system_desc* systems, int32_t nsys
                                     double hInit, double hMin, double hMax, double accuracy, double consTol,
                                     int32_t projectEveryStep, int32_t maxSteps, int32_t* status, int64_t* stats,
                                     int32_t nthreads);
+int oracle_instance_invariants(const sbg_system_desc* d, const double* y, double* energy, double* perr, double* verr,
+                               double* aerr);
 int oracle_qtz_solve(int32_t nr, int32_t nc, const double* A, double rcond, const double* b, double* x);
 int oracle_adjust_step_size(double err, int32_t errOrder, int32_t limited, double accuracy, double hMin, double hMax,
                             double* h);

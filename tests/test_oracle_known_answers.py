@@ -6,6 +6,11 @@
                              M^-1 f reproduced by the forward dynamics
   Force.cpp:339-351          the spring reads q[which] and writes u[which],
                              also for quaternion joints
+  TestForces.cpp:244-290     energy conservation under RK Merson (Gimbal
+                             chain, mobility spring, gravity)
+  TestConstraints.cpp:49-127 Ball closure errors after projection: position
+                             and velocity within the tolerance, acceleration
+                             to machine precision
 """
 import ctypes as C
 
@@ -100,3 +105,94 @@ def test_forward_dynamics_is_minv_of_applied_forces():
     minv = O.multiply_by_minv(arr, 1, np.zeros(1, np.int32), np.array([0, 2]), np.array([0.75, 0.0]),
                               np.array([0, 1]), f)
     assert abs(ydot[1] - minv[0]) <= 1e-14
+
+
+def rotation(angle, axis):
+    """Rotation(angle, UnitVec3(axis)): right-handed about the unit axis,
+    row-major."""
+    a = np.asarray(axis, dtype=np.float64)
+    a = a / np.linalg.norm(a)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) * np.cos(angle) + (1 - np.cos(angle)) * np.outer(a, a) + np.sin(angle) * K
+
+
+def chain_system(mobilizers, mass, com, unit_inertia, X_PF, X_BM, gravity=(0.0, 0.0, 0.0), forces=(), balls=()):
+    """A chain, body k+1 on body k, every body alike; X_* = (R 3x3, p)."""
+    n = len(mobilizers)
+    bodies = (N.BodyDesc * n)()
+    for k, mob in enumerate(mobilizers):
+        b = bodies[k]
+        b.parent, b.mobilizer, b.mass = k, mob, mass
+        b.com[:] = list(com)
+        b.unit_inertia[:] = list(unit_inertia)
+        b.X_PF[:] = list(np.ravel(X_PF[0])) + list(X_PF[1])
+        b.X_BM[:] = list(np.ravel(X_BM[0])) + list(X_BM[1])
+    fs = (N.MobilityForceDesc * max(1, len(forces)))()
+    for i, (kind, body, which, coef, q0) in enumerate(forces):
+        fs[i].kind, fs[i].body, fs[i].which, fs[i].coef, fs[i].q0 = kind, body, which, coef, q0
+    cs = (N.BallConstraintDesc * max(1, len(balls)))()
+    for i, (b1, s1, b2, s2) in enumerate(balls):
+        cs[i].body1, cs[i].body2 = b1, b2
+        cs[i].station1[:] = list(s1)
+        cs[i].station2[:] = list(s2)
+    d = N.SystemDesc()
+    d.nbodies, d.nforces, d.nconstraints = n, len(forces), len(balls)
+    d.gravity[:] = list(gravity)
+    d.bodies = C.cast(bodies, C.POINTER(N.BodyDesc))
+    d.forces = C.cast(fs, C.POINTER(N.MobilityForceDesc)) if forces else None
+    d.constraints = C.cast(cs, C.POINTER(N.BallConstraintDesc)) if balls else None
+    return (N.SystemDesc * 1)(d), (bodies, fs, cs)
+
+
+def test_conservative_forces_conserve_energy_under_rk_merson():
+    """TestForces.cpp:244-290: a chain of ten unit Gimbal bodies (bond 0.5)
+    with a MobilityLinearSpring (body 1, q 1, k 0.1, q0 1) and gravity
+    (0, -1, 0), from a random state, keeps its energy within 0.5 % over
+    10 s of RK Merson at accuracy 1e-4. (The reference adds a
+    TwoPointLinearSpring, which is not on this path.)"""
+    I3 = np.eye(3)
+    arr, keep = chain_system([N.SBG_GIMBAL] * 10, 1.0, (0, 0, 0), (1, 1, 1, 0, 0, 0), (I3, (0, 0, 0)),
+                             (I3, (0.5, 0, 0)), gravity=(0, -1.0, 0), forces=[(0, 1, 1, 0.1, 1.0)])
+    ny = 60
+    y0 = np.random.default_rng(244).uniform(0, 1, ny)
+
+    def energy(y):
+        e = O.invariants(arr[0], y)
+        assert e["status"] == 0
+        return e["ke"] + e["pe_gravity"] + e["pe_springs"]
+
+    y, t, st, stats = O.rk_merson_adaptive(arr, 1, np.zeros(1, np.int32), np.array([0, ny], np.int64), y0, 10.0,
+                                           accuracy=1e-4)
+    assert st[0] == 0 and t[0] == 10.0 and stats[0, 0] > 100
+    e0, e1 = energy(y0), energy(y)
+    assert abs(e0 / e1 - 1) < 0.005, (e0, e1)
+
+
+def test_ball_constraint_errors_after_projection():
+    """TestConstraints.cpp:49-127: a chain of ten bodies (Gimbal, with a
+    Universal at 5 and a Ball at 7; mass 1.23, COM (.1,.2,-.03), rotated
+    inboard and outboard frames) closed by a Ball between the origins of
+    bodies 1 and 10. From a random state, projection to 1e-10 leaves
+    position and velocity errors within 1e-10, and the accelerations of
+    the constrained realize meet the closure to machine precision times
+    the problem size (10 nu SignificantReal)."""
+    mobs = [N.SBG_GIMBAL] * 10
+    mobs[5], mobs[7] = N.SBG_UNIVERSAL, N.SBG_BALL
+    X_PF = (rotation(np.pi / 20, (1, 2, 3)), (-0.1, 0.3, 0.2))
+    X_BM = (rotation(-np.pi / 17, (2, 0.2, 3)), (0.5, 0, 0))
+    arr, keep = chain_system(mobs, 1.23, (0.1, 0.2, -0.03), (1.1, 1.2, 1.3, 0.01, -0.02, 0.07), X_PF, X_BM,
+                             balls=[(1, (0, 0, 0), 10, (0, 0, 0))])
+    nq, nu = 8 * 3 + 2 + 4, 8 * 3 + 2 + 3
+    y0 = np.random.default_rng(100).uniform(0, 1, nq + nu)
+    before = O.invariants(arr[0], y0)
+    assert np.abs(before["perr"]).max() > 0.1  # the random state violates the closure
+    y, _, st = O.rk_merson_run(arr, 1, np.zeros(1, np.int32), np.array([0, nq + nu], np.int64), y0, 1e-3,
+                               nsteps=0, initialize=True, cons_tol=1e-10)
+    assert st[0] == 0
+    inv = O.invariants(arr[0], y)
+    assert inv["status"] == 0
+    assert np.linalg.norm(inv["perr"]) <= 1e-10
+    assert np.linalg.norm(inv["verr"]) <= 1e-10
+    ydot = realize_one(arr, y)
+    scale = max(1.0, np.abs(ydot[nq:]).max())
+    assert np.linalg.norm(inv["aerr"]) <= 10 * nu * np.finfo(float).eps ** 0.875 * scale, inv["aerr"]
