@@ -24,7 +24,9 @@
 //   mode 2  stepTo(t_end + 0.3 h)            (a shortened last step)
 // and, into a third file, error-controlled records: a RungeKuttaMersonIntegrator
 // with the given accuracy, setFinalTime(t_final), initialize(s) and stepTo
-// looped until t_final, with the numbers of steps taken and attempted.
+// looped until t_final, with the numbers of steps taken and attempted;
+// and, into a fourth, the number of systems outside the GPU path (one
+// unsupported element each) that the Simbody-side adapter refused.
 // Reference calls used (paths relative to the Simbody source tree):
 //   MobilizedBody::{Pin,Slider,Universal,Ball,Free} (Simbody/include/simbody/internal/MobilizedBody_*.h)
 //   Force::Gravity, Force::MobilityLinearSpring/Damper (Simbody/include/simbody/internal/Force*.h)
@@ -190,6 +192,43 @@ double adapterRoundTrip(const sbg_system_desc& d, Model& m, int cfg, int inst) {
     return gn > 0 ? std::sqrt(dn / gn) : std::sqrt(dn);
 }
 
+// describe() must refuse what the GPU path does not cover. Each case is a
+// two-Pin pendulum plus one such element; returns how many were refused
+// (exits if one is not).
+int adapterRefusals() {
+    int refused = 0;
+    for (int c = 0; c < 6; ++c) {
+        MultibodySystem sys;
+        SimbodyMatterSubsystem matter(sys);
+        GeneralForceSubsystem forces(sys);
+        sbg::simtk::ForceLog log;
+        Force::Gravity gravity(forces, matter, -YAxis, 9.8);
+        Body::Rigid body(MassProperties(1.0, Vec3(0), UnitInertia(1)));
+        MobilizedBody::Pin b1(matter.Ground(), Transform(), body, Transform(Vec3(0, 1, 0)));
+        MobilizedBody::Pin b2(b1, Transform(), body, Transform(Vec3(0, 1, 0)));
+        const char* what = "";
+        switch (c) {
+        case 0: Force::TwoPointLinearSpring(forces, b1, Vec3(0), b2, Vec3(0), 1.0, 0.5); what = "a two-point spring"; break;
+        case 1: Force::MobilityLinearSpring(forces, b1, MobilizerQIndex(0), 1.0, 0.0); what = "a spring outside the log"; break;
+        case 2: gravity.setDefaultBodyIsExcluded(b2, true); what = "gravity excluding a body"; break;
+        case 3: log.addSmoothSphereHalfSpaceForce(forces, b2, Vec3(0), 0.1, b1, Transform()); what = "a moving half-space"; break;
+        case 4: Constraint::Rod(b1, Vec3(0), b2, Vec3(0.1, 0, 0), 1.0); what = "a Rod constraint"; break;
+        default: MobilizedBody::Ellipsoid(b2, Transform(), body, Transform()); what = "an Ellipsoid mobilizer"; break;
+        }
+        sys.realizeTopology();
+        const State st = sys.getDefaultState();
+        try {
+            sbg::simtk::describe(matter, forces, log, st);
+        } catch (const std::runtime_error&) {
+            ++refused;
+            continue;
+        }
+        fprintf(stderr, "the adapter took %s\n", what);
+        std::exit(1);
+    }
+    return refused;
+}
+
 void put(FILE* fp, const void* p, size_t bytes) {
     if (fwrite(p, 1, bytes, fp) != bytes) {
         fprintf(stderr, "write failed\n");
@@ -200,8 +239,8 @@ void put(FILE* fp, const void* p, size_t bytes) {
 }  // namespace
 
 int main(int argc, char** argv) {
-    if (argc < 4) {
-        fprintf(stderr, "usage: make_golden OUT.bin CONT.bin ADAPT.bin\n");
+    if (argc < 5) {
+        fprintf(stderr, "usage: make_golden OUT.bin CONT.bin ADAPT.bin REFUSALS.txt\n");
         return 2;
     }
     FILE* fp = fopen(argv[1], "wb");
@@ -430,6 +469,12 @@ int main(int argc, char** argv) {
         sbg_workload_destroy(w);
     }
     fclose(fa);
-    printf("%d records, %d continuation records, %d error-controlled records\n", written, contWritten, adaptWritten);
+    const int refusals = adapterRefusals();
+    FILE* fr = fopen(argv[4], "w");
+    if (!fr) return 1;
+    fprintf(fr, "%d\n", refusals);
+    fclose(fr);
+    printf("%d records, %d continuation records, %d error-controlled records, %d adapter refusals\n", written,
+           contWritten, adaptWritten, refusals);
     return 0;
 }

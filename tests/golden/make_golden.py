@@ -9,6 +9,11 @@ driver make_golden.cpp is compiled against them, run on the seeded workloads
 
   cfg, inst, ny, nu, nsteps, status, h, t_rk,    one entry per record
   cons_tol (0 = the integrator's default)
+  adapter_refusals (how many systems with one element outside the GPU path
+                    -- a two-point spring, a spring created outside the
+                    log, gravity excluding a body, a moving half-space, a
+                    Rod constraint, an Ellipsoid mobilizer -- describe()
+                    refused; the run stops if it takes one)
   adapter_gdev (include/simbody_gb300_simtk.hpp read the built system back
                 into descriptors equal to the workload's; gravity's relative
                 deviation, the only field not kept bit for bit)
@@ -149,10 +154,13 @@ def main() -> int:
         binf = Path(td) / "records.bin"
         conf = Path(td) / "cont.bin"
         adaf = Path(td) / "adapt.bin"
-        subprocess.run([str(exe), str(binf), str(conf), str(adaf)], check=True, env={"OPENBLAS_NUM_THREADS": "1"})
+        reff = Path(td) / "refusals.txt"
+        subprocess.run([str(exe), str(binf), str(conf), str(adaf), str(reff)], check=True,
+                       env={"OPENBLAS_NUM_THREADS": "1"})
         data = read_records(binf)
         data.update(read_continuation(conf))
         data.update(read_adaptive(adaf))
+        data["adapter_refusals"] = np.array(int(reff.read_text().strip()), dtype=np.int64)
     np.savez_compressed(a.out, **data)
     print(f"wrote {a.out}: {len(data['cfg'])} records")
     return 0

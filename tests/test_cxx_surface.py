@@ -80,3 +80,7 @@ def test_simtk_adapter_round_trips_every_recorded_system():
     assert len(g["adapter_gdev"]) == len(g["cfg"]) > 0
     assert set(np.unique(g["cfg"])) == set(range(1, 11))
     assert g["adapter_gdev"].max() <= 1e-15
+    # and it refused each of six systems with one element outside the GPU
+    # path (a two-point spring, a spring created outside its log, gravity
+    # excluding a body, a moving half-space, a Rod constraint, an Ellipsoid)
+    assert int(g["adapter_refusals"]) == 6
